@@ -1,0 +1,316 @@
+"""Regenerates the golden fixtures in tests/golden/fixtures/ from the reference PGMax code itself.
+
+Run from the repository root:  python tests/golden/make_golden.py [--reference PATH]
+
+The reference (google-deepmind/PGMax 0.6.1, pure Python over JAX) is imported unmodified from its
+source tree, with `jax_shim` standing in for jax/numba (neither is installed here). Every call to
+`BP(...).run / run_with_diffs / run_bp` made while this script runs is intercepted and saved with
+the flat wiring that `InfererContext` compiled (pgmax/infer/inferer.py:65-118), the input BPArrays,
+the run parameters and the reference's outputs (messages, per-iteration deltas, flat beliefs and
+the MAP decode). Two sources of runs are captured:
+  1. the reference's own tests (tests/test_pgmax.py, tests/test_clipping.py,
+     tests/factor/test_{or,and,pool}.py, tests/fgraph/test_fgraph.py), executed as-is; the
+     84-message golden vector of tests/test_pgmax.py:63-152 is captured from its `jnp.allclose`;
+  2. the seeded graphs of `cases.py` (Ising 50x50 at 1000 iterations, small RBM, Potts,
+     deconvolution, a mixed Enum/OR/AND/Pool graph), which the tests rebuild with pgmax_gb300 to
+     check that the host-side wiring is identical.
+It also records single factor-update calls (`FAC_TO_VAR_UPDATES[type](...)`, normalize True and
+False, several temperatures) on the mixed graph.
+"""
+
+import argparse
+import importlib
+import json
+import os
+import sys
+import traceback
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "fixtures")
+TYPE_NAMES = ("enum", "or", "and", "pool")
+
+
+def _np(x, dtype=None):
+  a = np.asarray(x)
+  return a.astype(dtype) if dtype is not None else a
+
+
+def wiring_arrays(ctx, fg_state):
+  """Flat wiring exactly as the reference's InfererContext holds it."""
+  from pgmax.factor import FAC_TO_VAR_UPDATES  # pylint: disable=g-import-not-at-top
+  d = {
+      "var_states_for_edge_states": _np(ctx.var_states_for_edge_states, np.int32),
+      "edge_indices_for_edge_states": _np(ctx.edge_indices_for_edge_states, np.int32),
+      "factor_indices_for_edge_states": _np(ctx.factor_indices_for_edge_states, np.int32),
+      "num_edges": np.int64(ctx.num_edges),
+      "num_factors": np.int64(ctx.num_factors),
+      "num_var_states": np.int64(fg_state.num_var_states),
+      "evidence_to_vars": _np(fg_state.evidence_to_vars, np.int32),
+  }
+  msgs_ranges, pot_ranges = [], []
+  for ftype, name in zip(FAC_TO_VAR_UPDATES, TYPE_NAMES):
+    msgs_ranges.append(ctx.factor_type_to_msgs_range[ftype])
+    pot_ranges.append(ctx.factor_type_to_potentials_range[ftype])
+    args = ctx.inference_arguments[ftype]
+    for k, v in args.items():
+      if isinstance(v, (int, np.integer)):
+        d[f"{name}.{k}"] = np.int64(v)
+      else:
+        d[f"{name}.{k}"] = _np(v, np.int32)
+  d["msgs_ranges"] = np.array(msgs_ranges, dtype=np.int64).reshape(4, 2)
+  d["potentials_ranges"] = np.array(pot_ranges, dtype=np.int64).reshape(4, 2)
+  return d
+
+
+class Recorder:
+
+  def __init__(self):
+    self.runs = []
+    self.allclose_args = []
+    self.current = "unnamed"
+    self.meta = {}
+
+
+REC = Recorder()
+
+
+def install_capture(pgmax):
+  """Wraps pgmax.infer.BP so that every run is recorded."""
+  bp_mod = importlib.import_module("pgmax.infer.bp")
+  inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  orig_bp = bp_mod.BP
+
+  def BP(bp_state, temperature=0.0):  # pylint: disable=invalid-name
+    bp = orig_bp(bp_state, temperature)
+    ctx = inferer_mod.InfererContext(bp_state)
+    wiring = wiring_arrays(ctx, bp_state.fg_state)
+    groups = bp_state.fg_state.variable_groups
+
+    def run_with_diffs(bp_arrays, num_iters, damping=0.5, temperature=temperature):
+      out, deltas = bp.run_with_diffs(bp_arrays, num_iters, damping, temperature)
+      flat_beliefs = np.asarray(
+          importlib.import_module("jax").numpy.array(bp_arrays.evidence)
+          .at[ctx.var_states_for_edge_states].add(out.ftov_msgs), dtype=np.float32)
+      beliefs = bp.get_beliefs(out)
+      decoded = inferer_mod.decode_map_states(beliefs)
+      map_flat = []
+      for vg in groups:
+        m = decoded[vg]
+        if isinstance(m, dict):
+          map_flat += [int(np.asarray(m[n]).reshape(-1)[0]) for n in vg.variable_names]
+        else:
+          map_flat += list(np.asarray(m).reshape(-1).astype(np.int64))
+      REC.runs.append({
+          "source": REC.current,
+          "meta": dict(REC.meta),
+          "wiring": wiring,
+          "log_potentials": _np(bp_arrays.log_potentials, np.float32),
+          "evidence": _np(bp_arrays.evidence, np.float32),
+          "ftov_msgs_in": _np(bp_arrays.ftov_msgs, np.float32),
+          "num_iters": np.int64(num_iters),
+          "damping": np.float64(damping),
+          "temperature": np.float64(temperature),
+          "ftov_msgs_out": _np(out.ftov_msgs, np.float32),
+          "deltas": _np(deltas, np.float32),
+          "flat_beliefs": flat_beliefs,
+          "map_flat": np.array(map_flat, dtype=np.int32),
+      })
+      return out, deltas
+
+    def run(bp_arrays, num_iters, damping=0.5, temperature=temperature):
+      return run_with_diffs(bp_arrays, num_iters, damping, temperature)[0]
+
+    def run_bp(bp_arrays, num_iters, damping=0.5):
+      return run(bp_arrays, num_iters, damping, temperature)
+
+    return bp_mod.BeliefPropagation(
+        init=bp.init, update=bp.update, to_bp_state=bp.to_bp_state,
+        get_beliefs=bp.get_beliefs, run=run, run_bp=run_bp, run_with_diffs=run_with_diffs)
+
+  bp_mod.BP = BP
+  infer_pkg = importlib.import_module("pgmax.infer")
+  infer_pkg.BP = BP
+
+  jnp = importlib.import_module("jax.numpy")
+  orig_allclose = jnp.allclose
+
+  def allclose(a, b, *args, **kwargs):
+    REC.allclose_args.append((REC.current, np.asarray(a), np.asarray(b), kwargs))
+    return orig_allclose(a, b, *args, **kwargs)
+
+  jnp.allclose = allclose
+
+
+def save_run(path, run, extra=None):
+  arrays = {}
+  for k, v in run["wiring"].items():
+    arrays["w." + k] = v
+  for k in ("log_potentials", "evidence", "ftov_msgs_in", "num_iters", "damping", "temperature",
+            "ftov_msgs_out", "deltas", "flat_beliefs", "map_flat"):
+    arrays[k] = run[k]
+  meta = {"source": run["source"], **run["meta"]}
+  arrays["meta"] = np.array(json.dumps(meta))
+  if extra:
+    arrays.update(extra)
+  np.savez_compressed(path, **arrays)
+
+
+def run_reference_tests(ref):
+  """Runs selected reference test functions unmodified; returns {name: error or None}."""
+  status = {}
+  modules = {
+      "test_pgmax": ["test_e2e_sanity_check", "test_e2e_heretic"],
+      "test_clipping": None,
+      "factor.test_or": None,
+      "factor.test_and": None,
+      "factor.test_pool": None,
+      "fgraph.test_fgraph": ["test_bp_state", "test_bp", "test_bp_different_num_states"],
+  }
+  for mod_name, fns in modules.items():
+    mod = importlib.import_module("tests." + mod_name)
+    names = fns or [n for n in dir(mod) if n.startswith("test_")]
+    for n in names:
+      if not hasattr(mod, n):
+        continue
+      REC.current = f"{mod_name}::{n}"
+      REC.meta = {}
+      try:
+        getattr(mod, n)()
+        status[REC.current] = None
+      except Exception as e:  # pylint: disable=broad-except
+        status[REC.current] = f"{type(e).__name__}: {e}"[:300]
+        traceback.print_exc()
+  return status
+
+
+def run_cases(api):
+  sys.path.insert(0, HERE)
+  import cases  # pylint: disable=g-import-not-at-top
+  plans = [
+      ("ising50_T1", "ising", dict(n=50, seed=0), dict(num_iters=1000, damping=0.5, temperature=1.0)),
+      ("ising50_T0", "ising", dict(n=50, seed=0), dict(num_iters=1000, damping=0.5, temperature=0.0)),
+      ("ising12_T1", "ising", dict(n=12, seed=3), dict(num_iters=50, damping=0.5, temperature=1.0)),
+      ("rbm_s0", "rbm", dict(nh=20, nv=30, seed=0, sample=0), dict(num_iters=100, damping=0.5, temperature=0.0)),
+      ("rbm_s1", "rbm", dict(nh=20, nv=30, seed=0, sample=1), dict(num_iters=100, damping=0.5, temperature=0.0)),
+      ("potts_K4", "potts", dict(L=8, K=4, seed=1), dict(num_iters=30, damping=0.5, temperature=1.0)),
+      ("potts_K8", "potts", dict(L=6, K=8, seed=2), dict(num_iters=30, damping=0.5, temperature=1.0)),
+      ("potts_K16", "potts", dict(L=4, K=16, seed=3), dict(num_iters=20, damping=0.5, temperature=0.5)),
+      ("deconv_T1", "deconv", dict(seed=0), dict(num_iters=40, damping=0.5, temperature=1.0)),
+      ("deconv_T0", "deconv", dict(seed=0), dict(num_iters=40, damping=0.5, temperature=0.0)),
+      ("mixed_T0", "mixed", dict(seed=0), dict(num_iters=7, damping=0.5, temperature=0.0)),
+      ("mixed_T1", "mixed", dict(seed=0), dict(num_iters=7, damping=0.5, temperature=1.0)),
+      ("mixed_T0.3", "mixed", dict(seed=1), dict(num_iters=7, damping=0.3, temperature=0.3)),
+      ("mixed_T0.001", "mixed", dict(seed=2), dict(num_iters=5, damping=0.5, temperature=0.001)),
+      ("mixed_iters0", "mixed", dict(seed=3), dict(num_iters=0, damping=0.5, temperature=1.0)),
+      ("mixed_iters1", "mixed", dict(seed=3), dict(num_iters=1, damping=0.9, temperature=0.7)),
+  ]
+  saved = []
+  for name, builder, bkw, rkw in plans:
+    fg, groups, ev = cases.BUILDERS[builder](api, **bkw)
+    bp = api.infer.BP(fg.bp_state, temperature=rkw["temperature"])
+    init_kw = {"evidence_updates": ev}
+    if builder == "mixed":
+      init_kw["ftov_msgs_updates"] = cases.mixed_ftov_updates(api, groups, seed=bkw["seed"])
+    bp_arrays = bp.init(**init_kw)
+    REC.current = f"case::{name}"
+    REC.meta = {"case": name, "builder": builder, "builder_kwargs": bkw, "run_kwargs": rkw}
+    bp.run_with_diffs(bp_arrays, **rkw)
+    saved.append(name)
+  return saved
+
+
+def factor_update_fixtures(api):
+  """Direct calls of each factor-type update on the mixed graph."""
+  sys.path.insert(0, HERE)
+  import cases  # pylint: disable=g-import-not-at-top
+  from pgmax.factor import FAC_TO_VAR_UPDATES  # pylint: disable=g-import-not-at-top
+  inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  fg, _, _ = cases.mixed(api, seed=5)
+  bp_state = fg.bp_state
+  ctx = inferer_mod.InfererContext(bp_state)
+  wiring = wiring_arrays(ctx, bp_state.fg_state)
+  lp = np.asarray(bp_state.log_potentials.value, dtype=np.float32)
+  rng = np.random.RandomState(7)
+  n_es = wiring["var_states_for_edge_states"].shape[0]
+  out = {}
+  idx = 0
+  for temperature in (0.0, 0.001, 0.05, 0.3, 1.0, 2.5):
+    for normalize in (True, False):
+      vtof = rng.normal(size=(n_es,)).astype(np.float32) * 2.0
+      out[f"upd{idx}.vtof"] = vtof
+      out[f"upd{idx}.temperature"] = np.float64(temperature)
+      out[f"upd{idx}.normalize"] = np.int64(normalize)
+      for t, (ftype, tname) in enumerate(zip(FAC_TO_VAR_UPDATES, TYPE_NAMES)):
+        ms, me = ctx.factor_type_to_msgs_range[ftype]
+        ps, pe = ctx.factor_type_to_potentials_range[ftype]
+        if ms == me:
+          continue
+        res = FAC_TO_VAR_UPDATES[ftype](
+            vtof_msgs=vtof[ms:me], log_potentials=lp[ps:pe], temperature=temperature,
+            normalize=normalize, **ctx.inference_arguments[ftype])
+        out[f"upd{idx}.{tname}"] = np.asarray(res, dtype=np.float32)
+      idx += 1
+  arrays = {"w." + k: v for k, v in wiring.items()}
+  arrays.update(out)
+  arrays["log_potentials"] = lp
+  arrays["num_updates"] = np.int64(idx)
+  arrays["meta"] = np.array(json.dumps({"source": "factor_updates", "case": "mixed", "seed": 5}))
+  np.savez_compressed(os.path.join(OUT, "factor_updates_mixed.npz"), **arrays)
+
+
+def main():
+  ap = argparse.ArgumentParser()
+  ap.add_argument("--reference", default=os.environ.get("PGMAX_REFERENCE", "/root/reference"))
+  args = ap.parse_args()
+  sys.path.insert(0, HERE)
+  import jax_shim  # pylint: disable=g-import-not-at-top
+  jax_shim.install()
+  sys.path.insert(0, args.reference)
+  import pgmax  # pylint: disable=g-import-not-at-top
+  from pgmax import factor, fgraph, fgroup, infer, vgroup  # pylint: disable=g-import-not-at-top
+  install_capture(pgmax)
+  api = types.SimpleNamespace(factor=factor, fgraph=fgraph, fgroup=fgroup, infer=infer,
+                              vgroup=vgroup)
+  os.makedirs(OUT, exist_ok=True)
+  for f in os.listdir(OUT):
+    if f.endswith(".npz"):
+      os.remove(os.path.join(OUT, f))
+
+  status = run_reference_tests(args.reference)
+  n_ref = len(REC.runs)
+  run_cases(api)
+  factor_update_fixtures(api)
+
+  # Golden vector of tests/test_pgmax.py: the (messages, expected) pair of its allclose call.
+  golden = [a for a in REC.allclose_args if a[0] == "test_pgmax::test_e2e_sanity_check"]
+  extra_golden = {}
+  if golden:
+    extra_golden = {"golden_expected": golden[0][2].astype(np.float32),
+                    "golden_atol": np.float64(golden[0][3].get("atol", 1e-8))}
+
+  counts = {}
+  for i, run in enumerate(REC.runs):
+    src = run["source"].replace("::", "__").replace(".", "_")
+    if run["meta"].get("case"):
+      fname = f"case_{run['meta']['case']}.npz"
+    else:
+      counts[src] = counts.get(src, 0) + 1
+      fname = f"ref_{src}_{counts[src]:02d}.npz"
+    extra = extra_golden if run["source"] == "test_pgmax::test_e2e_sanity_check" else None
+    save_run(os.path.join(OUT, fname), run, extra)
+  manifest = {
+      "reference_tests": status,
+      "captured_runs_from_reference_tests": n_ref,
+      "captured_runs_total": len(REC.runs),
+      "golden_vector_captured": bool(golden),
+  }
+  with open(os.path.join(OUT, "MANIFEST.json"), "w") as f:
+    json.dump(manifest, f, indent=1, sort_keys=True)
+  print(json.dumps(manifest, indent=1))
+
+
+if __name__ == "__main__":
+  main()
