@@ -1,0 +1,388 @@
+"""Benchmark: RBM perturb-and-MAP, the headline BP workload, on the pgbp CUDA engine.
+
+Workload (one "step"): a 784-visible x 500-hidden binary RBM - unary EnumFactorGroups with biases
+N(0, 0.5^2), a PairwiseFactorGroup of 392,000 2x2 tables [[0, 0], [0, W_ij]] with W ~ N(0, 0.1^2)
+(built like the reference's benchmark/rbm_lib.py:135-171) - and a batch of 128 perturb-and-MAP
+samples, each with fresh Gumbel(0, 1) evidence on every unary state. One step runs BP for 200
+iterations at temperature 0, damping 0.5 over the whole batch, then computes beliefs and MAP-decodes
+every sample (the reference benchmark's timed region, rbm_lib.py:180-187, minus JAX compilation).
+Data are synthetic and seeded (the reference's own numbers are for other RBM sizes on a V100).
+
+Metric: edge-message updates per second = batch x num_edges x iterations / time, num_edges =
+2*392,000 + 1,284 = 785,284.
+  value  device-resident inputs; CUDA events on the launching stream around K steps.
+  e2e    the public API (pgmax_gb300.infer.BP) with host buffers: every step copies the step's
+         Gumbel evidence from pinned host memory, runs BP, decodes, and copies the MAP states back.
+Roofline: the dense pairwise Enum kernel dominates; its per-launch algorithmic bytes are
+  B*4*(2*E_pairwise) message reads + writes + B*4*N_vs variable sums + 4*P_pairwise shared potentials,
+timed per launch with CUDA events (pgbp_profile_*) inside the timed region.
+`--impl reference` times the reference algorithm on the host CPU (the C oracle, a float32
+restatement of PGMax's run_with_diffs: PGMax itself needs jax, which is not installed) on a bounded
+sample of the same workload with all host cores.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NH, NV, BATCH, ITERS, DAMPING, TEMPERATURE = 500, 784, 128, 200, 0.5, 0.0
+NUM_EDGES = 2 * NH * NV + NH + NV
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "pairwise_kernel_rbm_b128.md")
+
+
+def rbm_params(seed=0):
+  rng = np.random.default_rng(seed)
+  W = rng.normal(0.0, 0.1, size=(NH, NV)).astype(np.float32)
+  bh = rng.normal(0.0, 0.5, size=(NH,)).astype(np.float32)
+  bv = rng.normal(0.0, 0.5, size=(NV,)).astype(np.float32)
+  return W, bh, bv
+
+
+def build_rbm(seed=0):
+  from pgmax_gb300 import fgraph, fgroup, vgroup  # pylint: disable=g-import-not-at-top
+  W, bh, bv = rbm_params(seed)
+  hidden = vgroup.NDVarArray(num_states=2, shape=(NH,))
+  visible = vgroup.NDVarArray(num_states=2, shape=(NV,))
+  fg = fgraph.FactorGraph(variable_groups=[hidden, visible])
+  hu = fgroup.EnumFactorGroup(variables_for_factors=[[hidden[i]] for i in range(NH)],
+                              factor_configs=np.arange(2)[:, None],
+                              log_potentials=np.stack([np.zeros_like(bh), bh], axis=1))
+  vu = fgroup.EnumFactorGroup(variables_for_factors=[[visible[j]] for j in range(NV)],
+                              factor_configs=np.arange(2)[:, None],
+                              log_potentials=np.stack([np.zeros_like(bv), bv], axis=1))
+  lpm = np.zeros((NH * NV, 2, 2), dtype=np.float32)
+  lpm[:, 1, 1] = W.ravel()
+  hv = hidden.variables
+  vv = visible.variables
+  pw = fgroup.PairwiseFactorGroup(variables_for_factors=[[hv[i], vv[j]] for i in range(NH)
+                                                         for j in range(NV)],
+                                  log_potential_matrix=lpm)
+  fg.add_factors([hu, vu, pw])
+  return fg, hidden, visible
+
+
+def gumbel_evidence(num_var_states, batch, seed):
+  rng = np.random.default_rng(seed)
+  return rng.gumbel(size=(batch, num_var_states)).astype(np.float32)
+
+
+class ClockSampler:
+  """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+  FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+            "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+            "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+  def __init__(self, device_index):
+    self.device_index = device_index
+    self.samples = []
+    self._stop = threading.Event()
+    self._thread = None
+
+  def _run(self):
+    while not self._stop.is_set():
+      try:
+        out = subprocess.run(["nvidia-smi", f"--id={self.device_index}",
+                              f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=5).stdout.strip()
+        if out:
+          self.samples.append([x.strip() for x in out.split(",")])
+      except Exception:  # pylint: disable=broad-except
+        return
+      self._stop.wait(0.2)
+
+  def __enter__(self):
+    self._thread = threading.Thread(target=self._run, daemon=True)
+    self._thread.start()
+    return self
+
+  def __exit__(self, *exc):
+    self._stop.set()
+    if self._thread:
+      self._thread.join(timeout=10)
+
+  def summary(self):
+    if not self.samples:
+      return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+    mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[i] for s in self.samples for i in range(4)
+                      if len(s) > 5 + i and s[5 + i].lower() == "active"})
+    return {"sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+            "samples": len(self.samples)}
+
+
+def read_traffic():
+  """Per-launch DRAM bytes of the pairwise kernel from the committed ncu summary, if any."""
+  try:
+    for line in open(TRAFFIC_FILE):
+      if line.startswith("traffic_bytes_per_full_launch:"):
+        return float(line.split(":")[1].split()[0])
+  except OSError:
+    pass
+  return None
+
+
+def peaks():
+  try:
+    with open(PEAKS) as f:
+      p = json.load(f)
+    return float(p["hbm_gbs"]), "measured"
+  except Exception:  # pylint: disable=broad-except
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(wiring, lp, ev, target_s=12.0):
+  """The C oracle on a bounded sample (all host cores, one thread per instance)."""
+  from oracle import oracle  # pylint: disable=g-import-not-at-top
+  w = oracle.Wiring(wiring)
+  cores = len(os.sched_getaffinity(0))
+  samples = min(cores, ev.shape[0])
+  msgs = np.zeros(w.num_edge_states, np.float32)
+  t0 = time.perf_counter()
+  oracle.run_batch(w, lp, ev[:samples], msgs, 2, DAMPING, TEMPERATURE, num_threads=cores)
+  per_iter = (time.perf_counter() - t0) / 2
+  iters = int(max(2, min(ITERS, target_s / max(per_iter, 1e-6))))
+  t0 = time.perf_counter()
+  oracle.run_batch(w, lp, ev[:samples], msgs, iters, DAMPING, TEMPERATURE, num_threads=cores)
+  dt = time.perf_counter() - t0
+  return {
+      "value": samples * NUM_EDGES * iters / dt,
+      "unit": "edge-msg updates/s",
+      "cores": cores,
+      "kind": "port",
+      "sample": f"{samples} of the {BATCH} samples x {iters} of the {ITERS} iterations "
+                f"({dt:.1f} s, C oracle, one OpenMP thread per sample)",
+  }
+
+
+def dist_setup(n_gpus):
+  world = int(os.environ.get("WORLD_SIZE", "1"))
+  rank = int(os.environ.get("RANK", "0"))
+  local = int(os.environ.get("LOCAL_RANK", "0"))
+  if world > 1:
+    import torch.distributed as dist  # pylint: disable=g-import-not-at-top
+    dist.init_process_group("nccl")
+  return world, rank, local
+
+
+def run_reference(args):
+  world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+  if rank != 0:
+    return 0
+  from pgmax_gb300 import infer  # pylint: disable=g-import-not-at-top
+  from oracle import oracle  # pylint: disable=g-import-not-at-top
+  fg, _, _ = build_rbm()
+  ctx = infer.InfererContext(fg.bp_state)
+  w = oracle.Wiring(ctx.flat_wiring())
+  lp = np.asarray(fg.fg_state.log_potentials, np.float32)
+  ev = gumbel_evidence(fg.fg_state.num_var_states, BATCH, 1)
+  cores = len(os.sched_getaffinity(0))
+  samples = min(cores, BATCH)
+  msgs = np.zeros(w.num_edge_states, np.float32)
+  iters = 4
+  times = []
+  for step in range(args.warmup + args.steps):
+    t0 = time.perf_counter()
+    oracle.run_batch(w, lp, ev[:samples], msgs, iters, DAMPING, TEMPERATURE, num_threads=cores)
+    dt = time.perf_counter() - t0
+    if step >= args.warmup:
+      times.append(dt)
+  total = sum(times)
+  value = samples * NUM_EDGES * iters * len(times) / total
+  sample = (f"each step: {samples} of the {BATCH} samples x {iters} of the {ITERS} iterations "
+            f"(C oracle, float32 restatement of PGMax run_with_diffs; PGMax itself needs jax, "
+            f"absent here)")
+  line = {
+      "impl": "reference", "metric": "edge-msg updates/s", "value": value,
+      "unit": "edge-msg updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+      "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
+      "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+      "config": {"workload": "rbm784x500_perturb_and_map", "batch": BATCH, "num_iters": ITERS,
+                 "temperature": TEMPERATURE, "damping": DAMPING, "parallelism": "cpu"},
+      "cpu_baseline": {"value": value, "unit": "edge-msg updates/s", "cores": cores,
+                       "kind": "port", "sample": sample},
+      "e2e": {"value": value, "unit": "edge-msg updates/s", "h2d_bytes_per_step": 0,
+              "d2h_bytes_per_step": 0},
+  }
+  print(json.dumps(line))
+  return 0
+
+
+def main():
+  ap = argparse.ArgumentParser()
+  ap.add_argument("--gpus", type=int, default=1)
+  ap.add_argument("--steps", type=int, default=10)
+  ap.add_argument("--warmup", type=int, default=3)
+  ap.add_argument("--impl", default="pgbp", choices=["pgbp", "reference"])
+  ap.add_argument("--no-cpu-baseline", action="store_true")
+  args = ap.parse_args()
+  if args.warmup < 3:
+    args.warmup = 3
+  if args.impl == "reference":
+    return run_reference(args)
+
+  import torch  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
+
+  world, rank, local = dist_setup(args.gpus)
+  torch.cuda.set_device(local)
+  dev = torch.device("cuda", local)
+
+  fg, hidden, visible = build_rbm(seed=0)
+  bp = infer.BP(fg.bp_state, temperature=TEMPERATURE)
+  ctx = bp.context
+  plan = ctx.plan
+  nvs = fg.fg_state.num_var_states
+  n_es = fg.fg_state.total_factor_num_states
+
+  ev_host = gumbel_evidence(nvs, BATCH, 1000 + rank)
+  lp_dev = torch.as_tensor(np.asarray(fg.fg_state.log_potentials, np.float32), device=dev)
+  ev_dev = torch.as_tensor(ev_host, device=dev)
+  msgs0 = torch.zeros(n_es, dtype=torch.float32, device=dev)
+  arrays = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_dev)
+
+  def step_device():
+    out = bp.run(arrays, num_iters=ITERS, damping=DAMPING, temperature=TEMPERATURE)
+    beliefs = bp.get_beliefs(out)
+    return infer.decode_map_states(beliefs)
+
+  stream = torch.cuda.current_stream(dev)
+
+  def barrier():
+    if world > 1:
+      import torch.distributed as dist  # pylint: disable=g-import-not-at-top
+      dist.barrier()
+    torch.cuda.synchronize(dev)
+
+  def max_over_ranks(x):
+    if world > 1:
+      import torch.distributed as dist  # pylint: disable=g-import-not-at-top
+      t = torch.tensor([x], dtype=torch.float64, device=dev)
+      dist.all_reduce(t, op=dist.ReduceOp.MAX)
+      return float(t.item())
+    return x
+
+  for _ in range(args.warmup):
+    step_device()
+  barrier()
+  native.profile_read()
+  native.profile_enable(True)
+  start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  with ClockSampler(local) as clocks:
+    barrier()
+    start.record(stream)
+    for _ in range(args.steps):
+      step_device()
+    stop.record(stream)
+    barrier()
+  native.profile_enable(False)
+  prof = native.profile_read()
+  ms = max_over_ranks(start.elapsed_time(stop))
+  ms_per_step = ms / args.steps
+  units = BATCH * NUM_EDGES * ITERS * args.steps * world
+  value = units / (ms / 1e3)
+
+  # end to end through the public API with host buffers
+  ev_pinned = torch.as_tensor(ev_host).pin_memory()
+  map_h = torch.empty((BATCH, NH), dtype=torch.int32).pin_memory()
+  map_v = torch.empty((BATCH, NV), dtype=torch.int32).pin_memory()
+
+  def step_e2e():
+    ev_d = ev_pinned.to(dev, non_blocking=True)
+    a = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_d)
+    out = bp.run(a, num_iters=ITERS, damping=DAMPING, temperature=TEMPERATURE)
+    dec = infer.decode_map_states(bp.get_beliefs(out))
+    map_h.copy_(dec[hidden], non_blocking=True)
+    map_v.copy_(dec[visible], non_blocking=True)
+
+  for _ in range(args.warmup):
+    step_e2e()
+  barrier()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  for _ in range(args.steps):
+    step_e2e()
+  e1.record(stream)
+  barrier()
+  e2e_ms = max_over_ranks(e0.elapsed_time(e1))
+  e2e_value = units / (e2e_ms / 1e3)
+
+  # roofline of the dominant kernel (dense pairwise Enum)
+  info = plan.info
+  e_pw = 4 * info["num_enum_pairwise_factors"]
+  p_pw = 4 * info["num_enum_pairwise_factors"]
+  algo_bytes = BATCH * 4 * (2 * e_pw) + BATCH * 4 * nvs + 4 * p_pw
+  n_launch, pw_ms = prof["pairwise"]
+  achieved = algo_bytes / (pw_ms / max(n_launch, 1) / 1e3) / 1e9 if n_launch else None
+  peak, peak_kind = peaks()
+  total_prof_ms = sum(v[1] for v in prof.values())
+  gpu_launches = sum(v[0] for v in prof.values())
+
+  line = {
+      "metric": "edge-msg updates/s",
+      "value": value,
+      "unit": "edge-msg updates/s",
+      "n_gpus": world,
+      "steps": args.steps,
+      "warmup": args.warmup,
+      "ms_per_step": ms_per_step,
+      "higher_is_better": True,
+      "scaling": "weak",
+      "vs_baseline": None,
+      "dtype": "f32",
+      "data": "synthetic (seeded RBM weights N(0,0.1^2), biases N(0,0.5^2), Gumbel(0,1) evidence)",
+      "config": {"workload": "rbm784x500_perturb_and_map", "batch": BATCH, "num_iters": ITERS,
+                 "temperature": TEMPERATURE, "damping": DAMPING, "num_edges": NUM_EDGES,
+                 "edge_states": n_es, "parallelism": "replicas" if world > 1 else "single",
+                 "l2": "inputs larger than L2 (804 MB of messages per buffer)"},
+      "e2e": {"value": e2e_value, "unit": "edge-msg updates/s",
+              "h2d_bytes_per_step": int(ev_pinned.numel() * 4),
+              "d2h_bytes_per_step": int((map_h.numel() + map_v.numel()) * 4)},
+      "gpu_launches": gpu_launches,
+      "roofline": {
+          "bound": "hbm",
+          "kernel": "pairwise_kernel<2,2,T0> (dense pairwise Enum, fused damping/normalise/clip)",
+          "achieved": achieved, "peak": peak, "unit": "GB/s",
+          "frac": (achieved / peak) if achieved else None,
+          "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
+          "traffic": read_traffic(),
+          "algorithmic_bytes_per_launch": algo_bytes,
+          "launch_ms": pw_ms / max(n_launch, 1),
+      },
+      "kernel_time_share": {k: (v[1] / total_prof_ms if total_prof_ms else None)
+                            for k, v in prof.items() if v[0]},
+      "iteration_roofline": {
+          "bytes_per_iter": BATCH * 4 * (2 * n_es + nvs) + 4 * int(plan.num_potentials),
+          "achieved_gbs": (BATCH * 4 * (2 * n_es + nvs) + 4 * int(plan.num_potentials)) * ITERS
+                          * args.steps / (ms / 1e3) / 1e9,
+      },
+  }
+  line["iteration_roofline"]["frac"] = line["iteration_roofline"]["achieved_gbs"] / peak
+  line["clocks"] = clocks.summary()
+  if rank == 0 and not args.no_cpu_baseline:
+    lp = np.asarray(fg.fg_state.log_potentials, np.float32)
+    line["cpu_baseline"] = cpu_baseline(ctx.flat_wiring(), lp, ev_host)
+  if rank == 0:
+    print(json.dumps(line))
+  if world > 1:
+    import torch.distributed as dist  # pylint: disable=g-import-not-at-top
+    dist.destroy_process_group()
+  return 0
+
+
+if __name__ == "__main__":
+  sys.exit(main())

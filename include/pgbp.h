@@ -1,0 +1,167 @@
+/* pgbp: GB300-native loopy belief propagation behind PGMax's BP interface.
+ *
+ * A thin C ABI over hand-written sm_103a CUDA kernels. Plain pointers and sizes only: any host
+ * binding (ctypes, jax.ffi, a torch extension) can call it. All float data is float32 and all
+ * indices int32, as PGMax computes without jax_enable_x64.
+ *
+ * Entry points and the PGMax interface each one replaces (paths relative to the PGMax tree):
+ *   pgbp_plan_create    InfererContext.__post_init__   pgmax/infer/inferer.py:65-118
+ *                       (the flat wiring it compiles becomes an immutable device plan)
+ *   pgbp_run            BP(...).run_with_diffs / run / run_bp   pgmax/infer/bp.py:63-176
+ *   pgbp_factor_update  FAC_TO_VAR_UPDATES[type](vtof, lp, T, normalize, **args)
+ *                       pgmax/factor/__init__.py:37-44 -> enum.py:398-475, logical.py:492-779,
+ *                       pool.py:276-474
+ *   pgbp_beliefs        InfererContext.get_beliefs (flat part)   pgmax/infer/inferer.py:211-222
+ *   pgbp_decode         decode_map_states                        pgmax/infer/inferer.py:251-264
+ *   pgbp_marginals      get_marginals                            pgmax/infer/bp.py:263-288
+ *
+ * Conventions
+ *   - Every call returns PGBP_OK (0) or an error code; nothing aborts or traps.
+ *     pgbp_last_error() gives a message for the calling thread's last failure.
+ *   - Device pointers are CUDA global memory on the plan's device; `stream` is a cudaStream_t
+ *     (NULL = legacy default stream). Calls only enqueue work; they do not synchronise, except
+ *     pgbp_plan_create / pgbp_plan_destroy.
+ *   - Batches follow jax.vmap over BPArrays: arrays are [batch, n] with a per-instance stride in
+ *     floats; stride 0 broadcasts one array to every instance.
+ *   - pgbp_run allocates nothing: its scratch comes from the caller (pgbp_workspace_size bytes).
+ *   - A plan is immutable after creation, so concurrent calls on different streams are safe as
+ *     long as their workspaces and outputs differ.
+ */
+#ifndef PGBP_H_
+#define PGBP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PGBP_OK = 0,
+  PGBP_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad stride */
+  PGBP_ERR_INVALID_WIRING = 2,   /* index out of range, inconsistent flat arrays */
+  PGBP_ERR_UNSUPPORTED = 3,      /* wiring layout the engine cannot schedule */
+  PGBP_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+  PGBP_ERR_WORKSPACE = 5,        /* workspace missing or too small */
+  PGBP_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up */
+};
+
+/* Factor types, in the order of PGMax's FAC_TO_VAR_UPDATES registry. */
+enum { PGBP_ENUM = 0, PGBP_OR = 1, PGBP_AND = 2, PGBP_POOL = 3 };
+
+/* The flat wiring of InfererContext (pgmax/infer/inferer.py:76-118) and of each wiring's
+ * get_inference_arguments() (enum.py:54-72, logical.py:76-104, pool.py:62-83). Host pointers.
+ * Per-type index arrays are relative to that type's message range, exactly as PGMax passes them.
+ * Arrays of an absent factor type may be NULL with length 0. */
+typedef struct {
+  int64_t num_edge_states;                     /* len(ftov_msgs) */
+  int64_t num_var_states;                      /* len(evidence) */
+  int64_t num_edges;
+  const int32_t* var_states_for_edge_states;     /* [num_edge_states] */
+  const int32_t* edge_indices_for_edge_states;   /* [num_edge_states] */
+  const int32_t* factor_indices_for_edge_states; /* [num_edge_states] */
+  int64_t msgs_range[4][2];                    /* factor_type_to_msgs_range, registry order */
+  int64_t potentials_range[4][2];              /* factor_type_to_potentials_range */
+  /* EnumFactor */
+  int64_t enum_num_rows;
+  const int32_t* enum_factor_configs_indices;     /* [enum_num_rows] */
+  const int32_t* enum_factor_configs_edge_states; /* [enum_num_rows] */
+  int64_t enum_num_val_configs;
+  /* ORFactor (index 0) and ANDFactor (index 1) */
+  int64_t logical_num_parents[2];
+  const int32_t* logical_parents_factor_indices[2];
+  const int32_t* logical_parents_msg_indices[2];
+  int64_t logical_num_factors[2];
+  const int32_t* logical_children_edge_states[2];
+  /* PoolFactor */
+  int64_t pool_num_choices;
+  const int32_t* pool_choices_factor_indices;
+  const int32_t* pool_choices_msg_indices;
+  int64_t pool_num_factors;
+  const int32_t* pool_indicators_edge_states;
+  /* Variables: evidence_to_vars (FactorGraphState.evidence_to_vars, fgraph.py:317-326), needed
+   * only by pgbp_decode / pgbp_marginals; may be NULL. */
+  int64_t num_variables;
+  const int32_t* evidence_to_vars;             /* [num_var_states] */
+} pgbp_wiring_desc;
+
+typedef struct pgbp_plan pgbp_plan;
+
+typedef struct {
+  int64_t num_edge_states, num_var_states, num_edges, num_variables;
+  int64_t num_potentials;        /* end of the last potentials range */
+  int64_t num_enum_factors, num_enum_pairwise_factors, num_or_factors, num_and_factors,
+      num_pool_factors;
+  int64_t num_pairwise_buckets;  /* (n1, n2) classes run by the dense pairwise kernel */
+  int64_t device_bytes;          /* device memory owned by the plan */
+} pgbp_plan_info;
+
+/* Compiles the wiring into device-resident schedules on `device`. Validates every index. */
+int pgbp_plan_create(const pgbp_wiring_desc* desc, int device, pgbp_plan** plan);
+int pgbp_plan_destroy(pgbp_plan* plan);
+int pgbp_plan_get_info(const pgbp_plan* plan, pgbp_plan_info* info);
+
+/* Bytes of scratch pgbp_run needs for `batch` instances and `num_iters` iterations. */
+size_t pgbp_workspace_size(const pgbp_plan* plan, int64_t batch, int64_t num_iters);
+
+/* run_with_diffs (pgmax/infer/bp.py:63-155) over `batch` instances:
+ *   log potentials clipped to +-1e6, initial messages normalised and clipped, then
+ *   max(num_iters, 1) damped iterations (num_iters <= 1 runs exactly one, as the reference does).
+ * log_potentials [batch, P] (lp_stride floats apart, 0 = shared), evidence [batch, N_vs],
+ * msgs_in / msgs_out [batch, E_s] (msgs_out rows are contiguous), deltas [batch, max(iters,1)]
+ * or NULL. damping and temperature are the Python floats of the reference call: the
+ * temperature == 0 and temperature < 0.5 branches are taken on the double values and the
+ * arithmetic uses their float32 roundings (1 - damping is rounded after the subtraction). */
+int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch,
+             const float* log_potentials, int64_t lp_stride,
+             const float* evidence, int64_t ev_stride,
+             const float* msgs_in, int64_t msgs_stride,
+             float* msgs_out, float* deltas,
+             int64_t num_iters, double damping, double temperature,
+             void* workspace, size_t workspace_bytes);
+
+/* One factor type's un-fused update: out = FAC_TO_VAR_UPDATES[type](vtof, lp, T, normalize).
+ * vtof / out are that type's message slice [batch, n_type] (stride floats apart), lp its
+ * potential slice [batch, p_type] (lp_stride, 0 = shared). No workspace is needed. */
+int pgbp_factor_update(const pgbp_plan* plan, void* stream, int type, int64_t batch,
+                       const float* vtof, int64_t vtof_stride,
+                       const float* log_potentials, int64_t lp_stride,
+                       double temperature, int normalize, float* out, int64_t out_stride);
+
+/* beliefs[b] = evidence[b].at[var_states_for_edge_states].add(msgs[b]); [batch, N_vs]. */
+int pgbp_beliefs(const pgbp_plan* plan, void* stream, int64_t batch,
+                 const float* evidence, int64_t ev_stride, const float* msgs,
+                 int64_t msgs_stride, float* beliefs);
+
+/* MAP decode: map[b, v] = argmax of variable v's states in beliefs[b] (first maximum wins).
+ * Needs evidence_to_vars in the plan. */
+int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
+                int64_t beliefs_stride, int32_t* map);
+
+/* Per-variable softmax of the flat beliefs: marginals[b] has the layout of beliefs[b]. */
+int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
+                   int64_t beliefs_stride, float* marginals);
+
+/* Kernel timing. While enabled, pgbp_run brackets every kernel launch with CUDA events on its
+ * stream (no synchronisation is added). pgbp_profile_read waits for the recorded events, returns
+ * per-class launch counts and total device milliseconds, and clears the record. Classes:
+ * 0 variable sums, 1 dense pairwise Enum, 2 generic Enum, 3 OR, 4 AND, 5 Pool,
+ * 6 layout (transposes, potential clipping, initial normalisation, residual copy-out),
+ * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals). Process-wide, not thread-safe. */
+#define PGBP_PROFILE_CLASSES 8
+typedef struct {
+  int64_t launches[PGBP_PROFILE_CLASSES];
+  double milliseconds[PGBP_PROFILE_CLASSES];
+} pgbp_profile;
+int pgbp_profile_enable(int enable);
+int pgbp_profile_read(pgbp_profile* out);
+
+const char* pgbp_last_error(void);
+int pgbp_version(void); /* major * 10000 + minor * 100 + patch */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PGBP_H_ */

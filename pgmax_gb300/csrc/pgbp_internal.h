@@ -1,0 +1,127 @@
+// Internal structures shared by the plan compiler (pgbp_plan.cpp) and the kernels (pgbp_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pgbp.h"
+
+namespace pgbp {
+
+// Dense pairwise EnumFactors with an n1 x n2 table listing every config in row-major order
+// (PairwiseFactorGroup, pgmax/fgroup/enum.py:303-310). Edge states of factor u are
+// es_begin[u] .. es_begin[u] + n1 + n2 - 1 (var0's states then var1's); its potentials are
+// cfg_begin[u] .. cfg_begin[u] + n1 * n2 - 1 (relative to the Enum potentials range).
+struct PairwiseBucket {
+  int n1 = 0, n2 = 0;
+  int64_t count = 0;
+  int32_t* es_begin = nullptr;   // device, absolute edge-state index
+  int32_t* cfg_begin = nullptr;  // device, absolute potential index
+};
+
+// Every other EnumFactor: per factor its edge-state range, edges, and config rows. Rows of config
+// k of factor f are row_begin[f] + k * n_vars[f] + i (i = variable), holding the edge state local to
+// the factor (row_les), exactly the layout of _compile_enumeration_wiring_numba (enum.py:364-394).
+struct EnumGeneric {
+  int64_t count = 0;
+  int max_es = 0;                 // largest number of edge states of one factor
+  int32_t* es_begin = nullptr;    // [count] absolute edge-state index
+  int32_t* n_es = nullptr;        // [count]
+  int32_t* edge_off = nullptr;    // [count + 1] into edge_size
+  int32_t* edge_size = nullptr;   // number of states of each edge of each factor
+  int32_t* row_begin = nullptr;   // [count] into row_les
+  int32_t* n_cfg = nullptr;       // [count]
+  int32_t* n_vars = nullptr;      // [count]
+  int32_t* cfg_begin = nullptr;   // [count] absolute potential index
+  int32_t* row_les = nullptr;     // [rows] edge state local to its factor
+};
+
+// OR (off = +1) / AND (off = -1) factors: parents par_begin[f] .. par_begin[f + 1] - 1. par_es is
+// the absolute index of each parent's "other" state (PGMax's parents_msg_indices); the relevant
+// state is par_es + off. child_es likewise (logical.py:458-488).
+struct LogicalSet {
+  int64_t count = 0, num_parents = 0;
+  int off = 1;
+  int32_t* par_begin = nullptr;  // [count + 1]
+  int32_t* par_es = nullptr;     // [num_parents]
+  int32_t* child_es = nullptr;   // [count]
+};
+
+// Pool factors: choices ch_begin[f] .. ch_begin[f + 1] - 1; ch_es / ind_es are the absolute
+// indices of state 0 of each choice / indicator (pool.py:62-83).
+struct PoolSet {
+  int64_t count = 0, num_choices = 0;
+  int32_t* ch_begin = nullptr;
+  int32_t* ch_es = nullptr;
+  int32_t* ind_es = nullptr;
+};
+
+struct Plan {
+  int device = 0;
+  int sm_count = 0;
+  int64_t num_edge_states = 0, num_var_states = 0, num_edges = 0, num_variables = 0;
+  int64_t num_potentials = 0;
+  int64_t msgs_range[4][2] = {};
+  int64_t potentials_range[4][2] = {};
+  // var-state CSR over edge states, increasing edge-state order inside each var state
+  int32_t* vs_off = nullptr;        // [num_var_states + 1]
+  int32_t* vs_edges = nullptr;      // [num_edge_states]
+  int32_t* vs_of_es = nullptr;      // [num_edge_states]
+  int32_t* edge_start = nullptr;    // [num_edges + 1]
+  int32_t* var_off = nullptr;       // [num_variables + 1] (decode / marginals), may be null
+  std::vector<PairwiseBucket> pairwise;
+  EnumGeneric enum_generic;
+  LogicalSet logical[2];
+  PoolSet pool;
+  int64_t device_bytes = 0;
+  std::vector<void*> allocations;
+  int64_t num_enum_factors = 0, num_enum_pairwise = 0;
+};
+
+// Workspace carve-up of one pgbp_run call.
+struct RunBuffers {
+  float* msgs[2];
+  float* vsum;
+  float* ev;            // transposed evidence [N_vs][B] (batched evidence only)
+  float* lp;            // clipped potentials: [P] shared or [P][B]
+  unsigned* deltas;     // [iters][B] as float bits
+};
+
+size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched, bool lp_batched);
+
+// Kernel-class timing (pgbp_profile_*): RAII bracket around one launch when profiling is on.
+enum ProfileClass { kProfVarsum = 0, kProfPairwise, kProfEnumGeneric, kProfOr, kProfAnd, kProfPool,
+                    kProfLayout, kProfReadout };
+bool profiling_enabled();
+void profile_record(int cls, cudaStream_t s, bool start);
+struct ProfileScope {
+  int cls;
+  cudaStream_t s;
+  bool on;
+  ProfileScope(int c, cudaStream_t st) : cls(c), s(st), on(profiling_enabled()) {
+    if (on) profile_record(cls, s, true);
+  }
+  ~ProfileScope() {
+    if (on) profile_record(cls, s, false);
+  }
+};
+
+// Kernel launchers (pgbp_kernels.cu). They return cudaGetLastError() of their launches.
+cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                   const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
+                   float* msgs_out, float* deltas, int64_t iters, double damping, double temperature,
+                   void* ws, size_t ws_bytes);
+cudaError_t factor_update(const Plan& p, cudaStream_t s, int type, int64_t B, const float* vtof,
+                          int64_t vtof_stride, const float* lp, int64_t lp_stride, double temperature,
+                          int normalize, float* out, int64_t out_stride);
+cudaError_t beliefs(const Plan& p, cudaStream_t s, int64_t B, const float* ev, int64_t ev_stride,
+                    const float* msgs, int64_t msgs_stride, float* out);
+cudaError_t decode(const Plan& p, cudaStream_t s, int64_t B, const float* beliefs, int64_t stride,
+                   int32_t* map);
+cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* beliefs, int64_t stride,
+                      float* out);
+
+}  // namespace pgbp

@@ -1,0 +1,650 @@
+// Plan compiler and C-ABI entry points of pgbp (see include/pgbp.h).
+//
+// pgbp_plan_create turns the flat wiring PGMax's InfererContext compiles
+// (pgmax/infer/inferer.py:76-118; per-type arguments enum.py:54-72, logical.py:76-104,
+// pool.py:62-83) into device-resident schedules:
+//   * a CSR of edge states per variable state (the scatter-add of bp.py:217, kept in increasing
+//     edge-state order so the per-variable sums are the reference's serial sums);
+//   * the edge boundaries (normalize_and_clip_msgs, bp.py:249-259);
+//   * Enum factors split into dense pairwise buckets (n1 x n2 tables in the row-major config order
+//     of PairwiseFactorGroup, fgroup/enum.py:303-310) and a generic list with per-factor config
+//     rows (enum.py:364-394);
+//   * OR / AND parents and Pool choices grouped per factor (logical.py:458-488, pool.py:151-180).
+// Every index is validated on the host first; a wiring the kernels could read out of bounds is
+// rejected with PGBP_ERR_INVALID_WIRING, one whose layout they cannot schedule with
+// PGBP_ERR_UNSUPPORTED.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "pgbp_internal.h"
+
+struct pgbp_plan {
+  pgbp::Plan p;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(PGBP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+struct Builder {
+  pgbp::Plan& p;
+  int err = PGBP_OK;
+
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    if (err) return nullptr;
+    size_t bytes = sizeof(T) * std::max<size_t>(v.size(), 1);
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, bytes);
+    if (e != cudaSuccess) {
+      err = cuda_fail(e, "cudaMalloc(plan)");
+      return nullptr;
+    }
+    p.allocations.push_back(d);
+    p.device_bytes += (int64_t)bytes;
+    if (!v.empty()) {
+      e = cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        err = cuda_fail(e, "cudaMemcpy(plan)");
+        return nullptr;
+      }
+    }
+    return static_cast<T*>(d);
+  }
+};
+
+void free_plan(pgbp::Plan& p) {
+  for (void* a : p.allocations) cudaFree(a);
+  p.allocations.clear();
+}
+
+bool in_range(int64_t x, int64_t lo, int64_t hi) { return x >= lo && x < hi; }
+
+// ----------------------------------------------------------------------------- profiling
+struct ProfEvent {
+  int cls;
+  cudaEvent_t start, stop;
+};
+bool g_prof_on = false;
+std::vector<ProfEvent> g_prof_events;  // recorded, not yet read
+std::vector<cudaEvent_t> g_prof_pool;   // created, free for reuse
+std::vector<std::pair<int, cudaEvent_t>> g_prof_open;
+
+cudaEvent_t prof_event() {
+  if (!g_prof_pool.empty()) {
+    cudaEvent_t e = g_prof_pool.back();
+    g_prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+}  // namespace
+
+namespace pgbp {
+bool profiling_enabled() { return g_prof_on; }
+void profile_record(int cls, cudaStream_t s, bool start) {
+  cudaEvent_t e = prof_event();
+  if (!e) return;
+  cudaEventRecord(e, s);
+  if (start) {
+    g_prof_open.push_back({cls, e});
+  } else if (!g_prof_open.empty()) {
+    ProfEvent pe{g_prof_open.back().first, g_prof_open.back().second, e};
+    g_prof_open.pop_back();
+    g_prof_events.push_back(pe);
+  }
+}
+}  // namespace pgbp
+
+extern "C" {
+
+int pgbp_profile_enable(int enable) {
+  g_prof_on = enable != 0;
+  return PGBP_OK;
+}
+
+int pgbp_profile_read(pgbp_profile* out) {
+  if (!out) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  memset(out, 0, sizeof(*out));
+  int rc = PGBP_OK;
+  for (const ProfEvent& pe : g_prof_events) {
+    float ms = 0.0f;
+    cudaError_t e = cudaEventSynchronize(pe.stop);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, pe.start, pe.stop);
+    if (e != cudaSuccess) rc = cuda_fail(e, "pgbp_profile_read");
+    if (pe.cls >= 0 && pe.cls < PGBP_PROFILE_CLASSES) {
+      out->launches[pe.cls] += 1;
+      out->milliseconds[pe.cls] += ms;
+    }
+    g_prof_pool.push_back(pe.start);
+    g_prof_pool.push_back(pe.stop);
+  }
+  g_prof_events.clear();
+  return rc;
+}
+
+const char* pgbp_last_error(void) { return g_last_error.c_str(); }
+
+int pgbp_version(void) { return 100; }
+
+int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
+  if (!d || !out) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  const int64_t ns = d->num_edge_states, nvs = d->num_var_states, ne = d->num_edges;
+  if (ns < 0 || nvs < 0 || ne < 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "negative size");
+  if (ns > INT32_MAX - 1 || nvs > INT32_MAX - 1)
+    return fail(PGBP_ERR_UNSUPPORTED, "more than 2^31 edge or variable states");
+  if (ns > 0 && (!d->var_states_for_edge_states || !d->edge_indices_for_edge_states ||
+                 !d->factor_indices_for_edge_states))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "missing edge-state arrays");
+
+  // --- message / potential ranges (registry order Enum, OR, AND, Pool; contiguous, fgraph.py:186-232)
+  int64_t np_total = 0;
+  {
+    int64_t prev = 0;
+    for (int t = 0; t < 4; ++t) {
+      if (d->msgs_range[t][0] != prev || d->msgs_range[t][1] < d->msgs_range[t][0])
+        return fail(PGBP_ERR_INVALID_WIRING, "message ranges must tile [0, num_edge_states)");
+      prev = d->msgs_range[t][1];
+      if (d->potentials_range[t][1] < d->potentials_range[t][0] || d->potentials_range[t][0] < 0)
+        return fail(PGBP_ERR_INVALID_WIRING, "bad potentials range for type %d", t);
+      np_total = std::max<int64_t>(np_total, d->potentials_range[t][1]);
+    }
+    if (prev != ns) return fail(PGBP_ERR_INVALID_WIRING, "message ranges end at %lld, expected %lld",
+                                (long long)prev, (long long)ns);
+  }
+
+  auto* handle = new (std::nothrow) pgbp_plan();
+  if (!handle) return fail(PGBP_ERR_INVALID_ARGUMENT, "out of host memory");
+  pgbp::Plan& p = handle->p;
+  p.device = device;
+  p.num_edge_states = ns;
+  p.num_var_states = nvs;
+  p.num_edges = ne;
+  p.num_potentials = np_total;
+  memcpy(p.msgs_range, d->msgs_range, sizeof(p.msgs_range));
+  memcpy(p.potentials_range, d->potentials_range, sizeof(p.potentials_range));
+
+  auto bail = [&](int code) {
+    free_plan(p);
+    delete handle;
+    return code;
+  };
+
+  cudaError_t ce = cudaSetDevice(device);
+  if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaSetDevice"));
+  ce = cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaDeviceGetAttribute"));
+
+  const int32_t* vs = d->var_states_for_edge_states;
+  const int32_t* ei = d->edge_indices_for_edge_states;
+  const int32_t* fi = d->factor_indices_for_edge_states;
+
+  // --- edges: states of an edge are contiguous and edges are numbered in order
+  std::vector<int32_t> edge_start(ne + 1, 0);
+  {
+    int64_t expect = 0;
+    for (int64_t i = 0; i < ns; ++i) {
+      if (!in_range(vs[i], 0, nvs))
+        return bail(fail(PGBP_ERR_INVALID_WIRING, "var state %d of edge state %lld out of range",
+                         vs[i], (long long)i));
+      if (i == 0 || ei[i] != ei[i - 1]) {
+        if (ei[i] != expect)
+          return bail(fail(PGBP_ERR_UNSUPPORTED, "edge indices must enumerate edges in order"));
+        edge_start[expect] = (int32_t)i;
+        ++expect;
+      }
+    }
+    if (expect != ne)
+      return bail(fail(PGBP_ERR_INVALID_WIRING, "found %lld edges, num_edges is %lld",
+                       (long long)expect, (long long)ne));
+    edge_start[ne] = (int32_t)ns;
+  }
+
+  // --- CSR over variable states (stable: increasing edge state inside each var state)
+  std::vector<int32_t> vs_off(nvs + 1, 0), vs_edges(ns);
+  for (int64_t i = 0; i < ns; ++i) vs_off[vs[i] + 1]++;
+  for (int64_t v = 0; v < nvs; ++v) vs_off[v + 1] += vs_off[v];
+  {
+    std::vector<int32_t> fill(vs_off.begin(), vs_off.end() - 1);
+    for (int64_t i = 0; i < ns; ++i) vs_edges[fill[vs[i]]++] = (int32_t)i;
+  }
+
+  // factor ranges from factor indices (each factor owns a contiguous run of edge states)
+  std::vector<int64_t> fac_es_begin, fac_es_end;
+  {
+    int64_t expect = 0;
+    for (int64_t i = 0; i < ns; ++i) {
+      if (i == 0 || fi[i] != fi[i - 1]) {
+        if (fi[i] != expect)
+          return bail(fail(PGBP_ERR_UNSUPPORTED, "factor indices must enumerate factors in order"));
+        fac_es_begin.push_back(i);
+        if (i > 0) fac_es_end.push_back(i);
+        ++expect;
+      }
+      // a factor's edge states lie inside one edge sequence: edges do not straddle factors
+      if (i > 0 && ei[i] == ei[i - 1] && fi[i] != fi[i - 1])
+        return bail(fail(PGBP_ERR_INVALID_WIRING, "edge %d spans two factors", ei[i]));
+    }
+    if (ns > 0) fac_es_end.push_back(ns);
+  }
+  auto factor_of = [&](int64_t es) { return (int64_t)fi[es]; };
+
+  Builder bd{p};
+  p.vs_off = bd.upload(vs_off);
+  p.vs_edges = bd.upload(vs_edges);
+  p.vs_of_es = bd.upload(std::vector<int32_t>(vs, vs + ns));
+  p.edge_start = bd.upload(edge_start);
+  if (bd.err) return bail(bd.err);
+
+  // --- Enum factors
+  {
+    const int64_t e0 = d->msgs_range[0][0], e1 = d->msgs_range[0][1];
+    const int64_t pot0 = d->potentials_range[0][0];
+    const int64_t nrows = d->enum_num_rows, ncfg = d->enum_num_val_configs;
+    const int32_t* ci = d->enum_factor_configs_indices;
+    const int32_t* cf = d->enum_factor_configs_edge_states;
+    if (nrows > 0 && (!ci || !cf)) return bail(fail(PGBP_ERR_INVALID_ARGUMENT, "missing enum rows"));
+    if (d->potentials_range[0][1] - pot0 < ncfg)
+      return bail(fail(PGBP_ERR_INVALID_WIRING, "enum potentials range shorter than num_val_configs"));
+    // Enum factors are the first factors; enumerate them by edge-state range
+    std::vector<int64_t> facs;
+    if (e1 > e0) {
+      for (int64_t f = factor_of(e0); f <= factor_of(e1 - 1); ++f) facs.push_back(f);
+    }
+    // rows grouped per factor
+    std::vector<int64_t> row_begin(facs.size() + 1, nrows);
+    {
+      int64_t r = 0;
+      for (size_t k = 0; k < facs.size(); ++k) {
+        row_begin[k] = r;
+        while (r < nrows) {
+          if (!in_range(cf[r], 0, e1 - e0) || !in_range(ci[r], 0, ncfg))
+            return bail(fail(PGBP_ERR_INVALID_WIRING, "enum row %lld out of range", (long long)r));
+          if (factor_of(e0 + cf[r]) != facs[k]) break;
+          ++r;
+        }
+      }
+      row_begin[facs.size()] = r;
+      if (r != nrows)
+        return bail(fail(PGBP_ERR_UNSUPPORTED, "enum config rows are not grouped by factor"));
+    }
+    std::map<std::pair<int, int>, std::pair<std::vector<int32_t>, std::vector<int32_t>>> buckets;
+    std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_rb, g_ncfg, g_nv, g_cfg, g_les;
+    int max_es = 0;
+    for (size_t k = 0; k < facs.size(); ++k) {
+      const int64_t f = facs[k];
+      const int64_t fb = fac_es_begin[f], fe = fac_es_end[f];
+      // edges of the factor
+      std::vector<int32_t> esz;
+      for (int64_t i = fb; i < fe; ++i)
+        if (i == fb || ei[i] != ei[i - 1]) esz.push_back(0), esz.back() = 0;
+      {
+        size_t j = 0;
+        for (int64_t i = fb; i < fe; ++i) {
+          if (i > fb && ei[i] != ei[i - 1]) ++j;
+          esz[j]++;
+        }
+      }
+      const int nv = (int)esz.size();
+      const int64_t r0 = row_begin[k], r1 = row_begin[k + 1];
+      if ((r1 - r0) % nv != 0)
+        return bail(fail(PGBP_ERR_UNSUPPORTED, "enum factor rows not a multiple of its arity"));
+      const int64_t nc = (r1 - r0) / nv;
+      const int64_t cfg0 = nc > 0 ? ci[r0] : 0;
+      // rows of config c are (var 0 .. var nv-1) with the state's edge state inside var i's edge
+      std::vector<int32_t> les((size_t)(r1 - r0));
+      std::vector<int32_t> estart(nv + 1, 0);
+      for (int j = 0; j < nv; ++j) estart[j + 1] = estart[j] + esz[j];
+      for (int64_t c = 0; c < nc; ++c) {
+        for (int i = 0; i < nv; ++i) {
+          const int64_t r = r0 + c * nv + i;
+          const int64_t le = (e0 + cf[r]) - fb;
+          if (ci[r] != cfg0 + c)
+            return bail(fail(PGBP_ERR_UNSUPPORTED, "enum config indices not contiguous per factor"));
+          if (le < estart[i] || le >= estart[i + 1])
+            return bail(fail(PGBP_ERR_UNSUPPORTED, "enum row does not follow variable order"));
+          les[(size_t)(c * nv + i)] = (int32_t)le;
+        }
+      }
+      bool dense = nv == 2 && nc == (int64_t)esz[0] * esz[1] && esz[0] <= 64 && esz[1] <= 64;
+      for (int64_t c = 0; dense && c < nc; ++c) {
+        if (les[(size_t)(2 * c)] != c / esz[1] || les[(size_t)(2 * c + 1)] != esz[0] + c % esz[1])
+          dense = false;
+      }
+      if (dense) {
+        auto& bk = buckets[{esz[0], esz[1]}];
+        bk.first.push_back((int32_t)fb);
+        bk.second.push_back((int32_t)(pot0 + cfg0));
+      } else {
+        g_es.push_back((int32_t)fb);
+        g_nes.push_back((int32_t)(fe - fb));
+        max_es = std::max<int>(max_es, (int)(fe - fb));
+        for (int j = 0; j < nv; ++j) g_esz.push_back(esz[j]);
+        g_eoff.push_back((int32_t)g_esz.size());
+        g_rb.push_back((int32_t)g_les.size());
+        g_les.insert(g_les.end(), les.begin(), les.end());
+        g_ncfg.push_back((int32_t)nc);
+        g_nv.push_back(nv);
+        g_cfg.push_back((int32_t)(pot0 + cfg0));
+      }
+    }
+    if (max_es > 512)
+      return bail(fail(PGBP_ERR_UNSUPPORTED, "an EnumFactor has %d edge states (max 512)", max_es));
+    p.num_enum_factors = (int64_t)facs.size();
+    for (auto& kv : buckets) {
+      pgbp::PairwiseBucket q;
+      q.n1 = kv.first.first;
+      q.n2 = kv.first.second;
+      q.count = (int64_t)kv.second.first.size();
+      q.es_begin = bd.upload(kv.second.first);
+      q.cfg_begin = bd.upload(kv.second.second);
+      p.num_enum_pairwise += q.count;
+      p.pairwise.push_back(q);
+    }
+    pgbp::EnumGeneric& g = p.enum_generic;
+    g.count = (int64_t)g_es.size();
+    g.max_es = max_es;
+    if (g.count > 0) {
+      g.es_begin = bd.upload(g_es);
+      g.n_es = bd.upload(g_nes);
+      g.edge_off = bd.upload(g_eoff);
+      g.edge_size = bd.upload(g_esz);
+      g.row_begin = bd.upload(g_rb);
+      g.n_cfg = bd.upload(g_ncfg);
+      g.n_vars = bd.upload(g_nv);
+      g.cfg_begin = bd.upload(g_cfg);
+      g.row_les = bd.upload(g_les);
+    }
+    if (bd.err) return bail(bd.err);
+  }
+
+  // --- OR / AND factors
+  for (int w = 0; w < 2; ++w) {
+    const int t = 1 + w;
+    const int off = w == 0 ? 1 : -1;
+    const int64_t m0 = d->msgs_range[t][0], m1 = d->msgs_range[t][1];
+    const int64_t P = d->logical_num_parents[w], F = d->logical_num_factors[w];
+    const int32_t* pfi = d->logical_parents_factor_indices[w];
+    const int32_t* pmi = d->logical_parents_msg_indices[w];
+    const int32_t* ch = d->logical_children_edge_states[w];
+    if (F == 0 && P == 0) continue;
+    if (F <= 0 || P <= 0 || !pfi || !pmi || !ch)
+      return bail(fail(PGBP_ERR_INVALID_WIRING, "logical factors without parents or children"));
+    std::vector<int32_t> pb(F + 1, 0), pes(P), ces(F);
+    int64_t cur = -1;
+    for (int64_t i = 0; i < P; ++i) {
+      if (!in_range(pfi[i], 0, F))
+        return bail(fail(PGBP_ERR_INVALID_WIRING, "parent factor index out of range"));
+      if (pfi[i] < cur || (pfi[i] > cur + 1 && i > 0) || (i == 0 && pfi[0] != 0))
+        return bail(fail(PGBP_ERR_UNSUPPORTED, "parents must be grouped by factor in order"));
+      if (pfi[i] != cur) {
+        cur = pfi[i];
+        pb[cur] = (int32_t)i;
+      }
+      const int64_t e = m0 + pmi[i];
+      if (!in_range(e, m0, m1) || !in_range(e + off, m0, m1) || ei[e] != ei[e + off] ||
+          edge_start[ei[e] + 1] - edge_start[ei[e]] != 2)
+        return bail(fail(PGBP_ERR_INVALID_WIRING, "logical parent message index out of range"));
+      pes[i] = (int32_t)e;
+    }
+    if (cur != F - 1) return bail(fail(PGBP_ERR_INVALID_WIRING, "a logical factor has no parent"));
+    pb[F] = (int32_t)P;
+    for (int64_t f = 0; f < F; ++f) {
+      const int64_t e = m0 + ch[f];
+      if (!in_range(e, m0, m1) || !in_range(e + off, m0, m1) || ei[e] != ei[e + off])
+        return bail(fail(PGBP_ERR_INVALID_WIRING, "logical child edge state out of range"));
+      ces[f] = (int32_t)e;
+    }
+    pgbp::LogicalSet& g = p.logical[w];
+    g.count = F;
+    g.num_parents = P;
+    g.off = off;
+    g.par_begin = bd.upload(pb);
+    g.par_es = bd.upload(pes);
+    g.child_es = bd.upload(ces);
+    if (bd.err) return bail(bd.err);
+  }
+
+  // --- Pool factors
+  {
+    const int64_t m0 = d->msgs_range[3][0], m1 = d->msgs_range[3][1];
+    const int64_t P = d->pool_num_choices, F = d->pool_num_factors;
+    const int32_t* cfi = d->pool_choices_factor_indices;
+    const int32_t* cmi = d->pool_choices_msg_indices;
+    const int32_t* ind = d->pool_indicators_edge_states;
+    if (F > 0 || P > 0) {
+      if (F <= 0 || P <= 0 || !cfi || !cmi || !ind)
+        return bail(fail(PGBP_ERR_INVALID_WIRING, "pool factors without choices or indicators"));
+      std::vector<int32_t> cb(F + 1, 0), ces(P), ies(F);
+      int64_t cur = -1;
+      for (int64_t i = 0; i < P; ++i) {
+        if (!in_range(cfi[i], 0, F))
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "pool factor index out of range"));
+        if (cfi[i] < cur || (cfi[i] > cur + 1 && i > 0) || (i == 0 && cfi[0] != 0))
+          return bail(fail(PGBP_ERR_UNSUPPORTED, "pool choices must be grouped by factor in order"));
+        if (cfi[i] != cur) {
+          cur = cfi[i];
+          cb[cur] = (int32_t)i;
+        }
+        const int64_t e = m0 + cmi[i];
+        if (!in_range(e, m0, m1) || !in_range(e + 1, m0, m1) || ei[e] != ei[e + 1])
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "pool choice message index out of range"));
+        ces[i] = (int32_t)e;
+      }
+      if (cur != F - 1) return bail(fail(PGBP_ERR_INVALID_WIRING, "a pool factor has no choice"));
+      cb[F] = (int32_t)P;
+      for (int64_t f = 0; f < F; ++f) {
+        const int64_t e = m0 + ind[f];
+        if (!in_range(e, m0, m1) || !in_range(e + 1, m0, m1) || ei[e] != ei[e + 1])
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "pool indicator edge state out of range"));
+        ies[f] = (int32_t)e;
+      }
+      pgbp::PoolSet& g = p.pool;
+      g.count = F;
+      g.num_choices = P;
+      g.ch_begin = bd.upload(cb);
+      g.ch_es = bd.upload(ces);
+      g.ind_es = bd.upload(ies);
+      if (bd.err) return bail(bd.err);
+    }
+  }
+
+  // --- variables (decode / marginals)
+  if (d->evidence_to_vars && d->num_variables > 0) {
+    const int64_t nv = d->num_variables;
+    std::vector<int32_t> voff(nv + 1, 0);
+    int64_t expect = 0;
+    for (int64_t i = 0; i < nvs; ++i) {
+      const int32_t v = d->evidence_to_vars[i];
+      if (i == 0 || v != d->evidence_to_vars[i - 1]) {
+        if (v != expect)
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "evidence_to_vars must enumerate variables"));
+        voff[v] = (int32_t)i;
+        ++expect;
+      }
+    }
+    if (expect != nv) return bail(fail(PGBP_ERR_INVALID_WIRING, "num_variables mismatch"));
+    voff[nv] = (int32_t)nvs;
+    p.num_variables = nv;
+    p.var_off = bd.upload(voff);
+    if (bd.err) return bail(bd.err);
+  }
+
+  ce = cudaDeviceSynchronize();
+  if (ce != cudaSuccess) return bail(cuda_fail(ce, "plan upload"));
+  *out = handle;
+  return PGBP_OK;
+}
+
+int pgbp_plan_destroy(pgbp_plan* plan) {
+  if (!plan) return PGBP_OK;
+  cudaSetDevice(plan->p.device);
+  free_plan(plan->p);
+  delete plan;
+  return PGBP_OK;
+}
+
+int pgbp_plan_get_info(const pgbp_plan* plan, pgbp_plan_info* info) {
+  if (!plan || !info) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  const pgbp::Plan& p = plan->p;
+  info->num_edge_states = p.num_edge_states;
+  info->num_var_states = p.num_var_states;
+  info->num_edges = p.num_edges;
+  info->num_variables = p.num_variables;
+  info->num_potentials = p.num_potentials;
+  info->num_enum_factors = p.num_enum_factors;
+  info->num_enum_pairwise_factors = p.num_enum_pairwise;
+  info->num_or_factors = p.logical[0].count;
+  info->num_and_factors = p.logical[1].count;
+  info->num_pool_factors = p.pool.count;
+  info->num_pairwise_buckets = (int64_t)p.pairwise.size();
+  info->device_bytes = p.device_bytes;
+  return PGBP_OK;
+}
+
+size_t pgbp_workspace_size(const pgbp_plan* plan, int64_t batch, int64_t num_iters) {
+  if (!plan) return 0;
+  // sized for batched evidence and potentials, which covers every stride choice
+  return pgbp::workspace_bytes(plan->p, batch, num_iters, true, true);
+}
+
+int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
+             int64_t lp_stride, const float* evidence, int64_t ev_stride, const float* msgs_in,
+             int64_t msgs_stride, float* msgs_out, float* deltas, int64_t num_iters, double damping,
+             double temperature, void* workspace, size_t workspace_bytes) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
+  if (lp_stride < 0 || ev_stride < 0 || msgs_stride < 0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "negative stride");
+  if (lp_stride != 0 && lp_stride < p.num_potentials)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "log_potentials stride %lld < %lld", (long long)lp_stride,
+                (long long)p.num_potentials);
+  if (ev_stride != 0 && ev_stride < p.num_var_states)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "evidence stride too small");
+  if (msgs_stride != 0 && msgs_stride < p.num_edge_states)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "messages stride too small");
+  if ((p.num_potentials > 0 && !log_potentials) || (p.num_var_states > 0 && !evidence) ||
+      (p.num_edge_states > 0 && (!msgs_in || !msgs_out)))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  if (!(damping == damping) || !(temperature == temperature) || temperature < 0.0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "damping and temperature must be numbers, temperature >= 0");
+  const size_t need = pgbp::workspace_bytes(p, batch, num_iters, ev_stride != 0, lp_stride != 0);
+  if (!workspace || workspace_bytes < need)
+    return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+    return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::run_bp(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
+                   ev_stride, msgs_in, msgs_stride, msgs_out, deltas, num_iters, damping, temperature,
+                   workspace, workspace_bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_run launch");
+  return PGBP_OK;
+}
+
+int pgbp_factor_update(const pgbp_plan* plan, void* stream, int type, int64_t batch,
+                       const float* vtof, int64_t vtof_stride, const float* log_potentials,
+                       int64_t lp_stride, double temperature, int normalize, float* out,
+                       int64_t out_stride) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (type < 0 || type > 3) return fail(PGBP_ERR_INVALID_ARGUMENT, "factor type %d", type);
+  if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
+  const int64_t n = p.msgs_range[type][1] - p.msgs_range[type][0];
+  const int64_t np = p.potentials_range[type][1] - p.potentials_range[type][0];
+  if (n == 0) return PGBP_OK;
+  if (!vtof || !out) return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  if (type == PGBP_ENUM && np > 0 && !log_potentials)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null log_potentials");
+  if ((batch > 1 && (vtof_stride < n || out_stride < n)) || (lp_stride != 0 && lp_stride < np) ||
+      lp_stride < 0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad stride");
+  if (!(temperature == temperature) || temperature < 0.0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "temperature must be >= 0");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // every output slot not written by a factor (the "other" states when normalizing) must be zero
+  for (int64_t b = 0; b < batch; ++b) {
+    e = cudaMemsetAsync(out + b * out_stride, 0, sizeof(float) * (size_t)n, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  e = pgbp::factor_update(p, s, type, batch, vtof, vtof_stride, log_potentials, lp_stride,
+                          temperature, normalize, out, out_stride);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_factor_update launch");
+  return PGBP_OK;
+}
+
+int pgbp_beliefs(const pgbp_plan* plan, void* stream, int64_t batch, const float* evidence,
+                 int64_t ev_stride, const float* msgs, int64_t msgs_stride, float* beliefs) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (batch <= 0 || ev_stride < 0 || msgs_stride < 0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad batch or stride");
+  if (p.num_var_states > 0 && (!evidence || !beliefs)) return fail(PGBP_ERR_INVALID_ARGUMENT, "null");
+  if (p.num_edge_states > 0 && !msgs) return fail(PGBP_ERR_INVALID_ARGUMENT, "null msgs");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::beliefs(p, static_cast<cudaStream_t>(stream), batch, evidence, ev_stride, msgs,
+                    msgs_stride, beliefs);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_beliefs launch");
+  return PGBP_OK;
+}
+
+int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
+                int64_t beliefs_stride, int32_t* map) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (!p.var_off) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
+  if (batch <= 0 || beliefs_stride < 0 || !beliefs || !map)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad argument");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::decode(p, static_cast<cudaStream_t>(stream), batch, beliefs, beliefs_stride, map);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_decode launch");
+  return PGBP_OK;
+}
+
+int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
+                   int64_t beliefs_stride, float* marginals) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (!p.var_off) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
+  if (batch <= 0 || beliefs_stride < 0 || !beliefs || !marginals)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad argument");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::marginals(p, static_cast<cudaStream_t>(stream), batch, beliefs, beliefs_stride, marginals);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_marginals launch");
+  return PGBP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,210 @@
+"""Host wrapper of the pgbp C ABI: one compiled plan per factor graph, device buffers from torch.
+
+PyTorch supplies device memory, the current stream and the caching allocator; every computation
+is a libpgbp kernel. There is no CPU path: without a CUDA device (or without libpgbp.so) every call
+raises.
+"""
+
+import ctypes
+from typing import Dict, Optional, Tuple
+
+import numpy as np
+
+from . import native
+
+TYPE_KEYS = ("enum", "or", "and", "pool")
+
+
+def _torch():
+  import torch  # pylint: disable=g-import-not-at-top
+  return torch
+
+
+def _require_cuda():
+  torch = _torch()
+  if not torch.cuda.is_available():
+    raise RuntimeError("pgmax_gb300 runs belief propagation on a CUDA GPU (sm_103a); no CUDA "
+                       "device is available and there is no CPU fallback")
+  return torch
+
+
+class Plan:
+  """A device plan compiled from the flat wiring (see include/pgbp.h, pgbp_plan_create).
+
+  `wiring` holds the flat arrays of the reference's InfererContext: keys
+  var_states_for_edge_states, edge_indices_for_edge_states, factor_indices_for_edge_states,
+  num_edges, num_var_states, msgs_ranges [4, 2], potentials_ranges [4, 2], the per-type inference
+  arguments (enum.factor_configs_indices, ..., pool.pool_indicators_edge_states) and optionally
+  evidence_to_vars / num_variables.
+  """
+
+  def __init__(self, wiring: Dict[str, np.ndarray], device: Optional[int] = None):
+    torch = _require_cuda()
+    self.lib = native.load()
+    self.device = torch.cuda.current_device() if device is None else int(device)
+    keep = []
+
+    def i32(key):
+      v = wiring.get(key)
+      if v is None:
+        return None, 0
+      a = np.ascontiguousarray(np.asarray(v, dtype=np.int32).reshape(-1))
+      keep.append(a)
+      return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), a.shape[0]
+
+    d = native.WiringDesc()
+    p, n = i32("var_states_for_edge_states")
+    d.var_states_for_edge_states, d.num_edge_states = p, n
+    d.edge_indices_for_edge_states, _ = i32("edge_indices_for_edge_states")
+    d.factor_indices_for_edge_states, _ = i32("factor_indices_for_edge_states")
+    d.num_var_states = int(wiring["num_var_states"])
+    d.num_edges = int(wiring["num_edges"])
+    mr = np.asarray(wiring["msgs_ranges"], dtype=np.int64).reshape(4, 2)
+    pr = np.asarray(wiring["potentials_ranges"], dtype=np.int64).reshape(4, 2)
+    for t in range(4):
+      for j in range(2):
+        d.msgs_range[t][j] = int(mr[t, j])
+        d.potentials_range[t][j] = int(pr[t, j])
+    d.enum_factor_configs_indices, d.enum_num_rows = i32("enum.factor_configs_indices")
+    d.enum_factor_configs_edge_states, _ = i32("enum.factor_configs_edge_states")
+    d.enum_num_val_configs = int(wiring.get("enum.num_val_configs", 0))
+    for w, key in enumerate(("or", "and")):
+      d.logical_parents_factor_indices[w], d.logical_num_parents[w] = i32(
+          f"{key}.parents_factor_indices")
+      d.logical_parents_msg_indices[w], _ = i32(f"{key}.parents_msg_indices")
+      d.logical_children_edge_states[w], d.logical_num_factors[w] = i32(
+          f"{key}.children_edge_states")
+    d.pool_choices_factor_indices, d.pool_num_choices = i32("pool.pool_choices_factor_indices")
+    d.pool_choices_msg_indices, _ = i32("pool.pool_choices_msg_indices")
+    d.pool_indicators_edge_states, d.pool_num_factors = i32("pool.pool_indicators_edge_states")
+    if wiring.get("evidence_to_vars") is not None:
+      d.evidence_to_vars, _ = i32("evidence_to_vars")
+      d.num_variables = int(wiring.get("num_variables",
+                                       int(np.max(wiring["evidence_to_vars"], initial=-1)) + 1))
+    handle = ctypes.c_void_p()
+    with torch.cuda.device(self.device):
+      native.check(self.lib.pgbp_plan_create(ctypes.byref(d), self.device, ctypes.byref(handle)),
+                   "pgbp_plan_create")
+    self.handle = handle
+    self.num_edge_states = int(d.num_edge_states)
+    self.num_var_states = int(d.num_var_states)
+    self.msgs_ranges = mr
+    self.potentials_ranges = pr
+    self.num_potentials = int(pr[:, 1].max()) if pr.size else 0
+    info = native.PlanInfo()
+    native.check(self.lib.pgbp_plan_get_info(handle, ctypes.byref(info)), "pgbp_plan_get_info")
+    self.info = {k: int(getattr(info, k)) for k, _ in native.PlanInfo._fields_}
+    del keep
+
+  def __del__(self):
+    h = getattr(self, "handle", None)
+    if h is not None and h.value:
+      try:
+        self.lib.pgbp_plan_destroy(h)
+      except Exception:  # pylint: disable=broad-except
+        pass
+      self.handle = None
+
+  # ------------------------------------------------------------------------- helpers
+  def _dev(self, x, dtype=None):
+    torch = _torch()
+    dtype = dtype or torch.float32
+    if isinstance(x, torch.Tensor):
+      t = x.to(device=f"cuda:{self.device}", dtype=dtype)
+    else:
+      t = torch.as_tensor(np.asarray(x), device=f"cuda:{self.device}").to(dtype)
+    return t.contiguous()
+
+  @staticmethod
+  def _rows(t, n):
+    """(pointer-able tensor, batch, stride) of a [n] or [B, n] array."""
+    if t.ndim == 1:
+      if t.shape[0] != n:
+        raise ValueError(f"expected length {n}, got {tuple(t.shape)}")
+      return t, 1, 0
+    if t.ndim == 2 and t.shape[1] == n:
+      return t, t.shape[0], t.stride(0)
+    raise ValueError(f"expected shape ({n},) or (B, {n}), got {tuple(t.shape)}")
+
+  def _stream(self):
+    return ctypes.c_void_p(_torch().cuda.current_stream(self.device).cuda_stream)
+
+  # ------------------------------------------------------------------------- entry points
+  def run(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5, temperature=0.0,
+          with_deltas=True):
+    """run_with_diffs on the GPU. Inputs [n] or [B, n]; returns (msgs [B?, E_s], deltas)."""
+    torch = _torch()
+    lp = self._dev(log_potentials) if self.num_potentials > 0 else torch.zeros(
+        1, device=f"cuda:{self.device}")
+    ev = self._dev(evidence)
+    m = self._dev(ftov_msgs)
+    lp_t, b1, lps = self._rows(lp, self.num_potentials) if self.num_potentials > 0 else (lp, 1, 0)
+    ev_t, b2, evs = self._rows(ev, self.num_var_states)
+    m_t, b3, ms = self._rows(m, self.num_edge_states)
+    bs = {b for b, nd in ((b1, lp.ndim), (b2, ev.ndim), (b3, m.ndim)) if nd == 2}
+    if len(bs) > 1:
+      raise ValueError(f"inconsistent batch sizes {sorted(bs)}")
+    B = bs.pop() if bs else 1
+    batched = any(t.ndim == 2 for t in (lp, ev, m))
+    iters = max(int(num_iters), 1)
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=m.device)
+    deltas = torch.empty((B, iters), dtype=torch.float32, device=m.device) if with_deltas else None
+    ws_bytes = int(self.lib.pgbp_workspace_size(self.handle, B, iters))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=m.device)
+    native.check(self.lib.pgbp_run(
+        self.handle, self._stream(), B, lp_t.data_ptr(), lps, ev_t.data_ptr(), evs,
+        m_t.data_ptr(), ms, out.data_ptr(), deltas.data_ptr() if deltas is not None else None,
+        int(num_iters), float(damping), float(temperature), ws.data_ptr(), ws_bytes), "pgbp_run")
+    if not batched:
+      out = out[0]
+      deltas = deltas[0] if deltas is not None else None
+    return out, deltas
+
+  def factor_update(self, ftype, vtof_msgs, log_potentials, temperature, normalize=True):
+    """FAC_TO_VAR_UPDATES[type] on one type's message slice ([n] or [B, n])."""
+    torch = _torch()
+    n = int(self.msgs_ranges[ftype, 1] - self.msgs_ranges[ftype, 0])
+    npot = int(self.potentials_ranges[ftype, 1] - self.potentials_ranges[ftype, 0])
+    v = self._dev(vtof_msgs)
+    v_t, B, vs = self._rows(v, n)
+    if log_potentials is not None and npot > 0:
+      lp = self._dev(log_potentials)
+      lp_t, _, lps = self._rows(lp, npot)
+      lp_ptr = lp_t.data_ptr()
+    else:
+      lp_ptr, lps = None, 0
+    out = torch.empty((B, n), dtype=torch.float32, device=v.device)
+    native.check(self.lib.pgbp_factor_update(
+        self.handle, self._stream(), int(ftype), B, v_t.data_ptr(), vs, lp_ptr, lps,
+        float(temperature), int(bool(normalize)), out.data_ptr(), n), "pgbp_factor_update")
+    return out if v.ndim == 2 else out[0]
+
+  def beliefs(self, evidence, ftov_msgs):
+    torch = _torch()
+    ev = self._dev(evidence)
+    m = self._dev(ftov_msgs)
+    ev_t, b1, evs = self._rows(ev, self.num_var_states)
+    m_t, b2, ms = self._rows(m, self.num_edge_states)
+    B = max(b1 if ev.ndim == 2 else 1, b2 if m.ndim == 2 else 1)
+    out = torch.empty((B, self.num_var_states), dtype=torch.float32, device=m.device)
+    native.check(self.lib.pgbp_beliefs(self.handle, self._stream(), B, ev_t.data_ptr(), evs,
+                                       m_t.data_ptr(), ms, out.data_ptr()), "pgbp_beliefs")
+    return out if (ev.ndim == 2 or m.ndim == 2) else out[0]
+
+  def decode(self, flat_beliefs, num_variables):
+    torch = _torch()
+    b = self._dev(flat_beliefs)
+    b_t, B, bs = self._rows(b, self.num_var_states)
+    out = torch.empty((B, num_variables), dtype=torch.int32, device=b.device)
+    native.check(self.lib.pgbp_decode(self.handle, self._stream(), B, b_t.data_ptr(), bs,
+                                      out.data_ptr()), "pgbp_decode")
+    return out if b.ndim == 2 else out[0]
+
+  def marginals(self, flat_beliefs):
+    torch = _torch()
+    b = self._dev(flat_beliefs)
+    b_t, B, bs = self._rows(b, self.num_var_states)
+    out = torch.empty((B, self.num_var_states), dtype=torch.float32, device=b.device)
+    native.check(self.lib.pgbp_marginals(self.handle, self._stream(), B, b_t.data_ptr(), bs,
+                                         out.data_ptr()), "pgbp_marginals")
+    return out if b.ndim == 2 else out[0]

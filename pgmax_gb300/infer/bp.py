@@ -1,0 +1,90 @@
+"""BP: the drop-in for pgmax.infer.BP (pgmax/infer/bp.py:36-288), run by the pgbp CUDA engine.
+
+`run_with_diffs(bp_arrays, num_iters, damping=0.5, temperature=T)` performs, on the GPU, exactly the
+reference's loop: clip potentials to +-1e6, normalise and clip the initial messages, then
+max(num_iters, 1) iterations of var-to-factor, factor-to-var for each type, damping,
+normalisation, clipping and the max residual. BPArrays may carry a leading batch axis (what
+`jax.vmap(bp.run)` computes); the whole batch runs in one call.
+"""
+
+import dataclasses
+import warnings
+from typing import Any, Callable, Dict, Hashable, Optional, Tuple
+
+import numpy as np
+
+from .bp_state import BPArrays, BPState
+from .inferer import Beliefs, Inferer, InfererContext, unflatten_beliefs
+
+
+def _is_torch(x):
+  return type(x).__module__.startswith("torch")
+
+
+@dataclasses.dataclass(frozen=True, eq=False)
+class BeliefPropagation(Inferer):
+  run_bp: Callable[..., BPArrays]
+  run_with_diffs: Callable[..., Tuple[BPArrays, Any]]
+  context: Any = None
+
+
+def BP(bp_state: BPState, temperature: Optional[float] = 0.0) -> BeliefPropagation:  # pylint: disable=invalid-name
+  """Returns the belief propagation functions of `bp_state`'s factor graph."""
+  ctx = InfererContext(bp_state)
+  default_t = temperature
+
+  def run_with_diffs(bp_arrays: BPArrays, num_iters: int, damping: float = 0.5,
+                     temperature: float = default_t):
+    msgs, deltas = ctx.plan.run(bp_arrays.log_potentials, bp_arrays.evidence, bp_arrays.ftov_msgs,
+                                num_iters, damping, temperature)
+    lp = bp_arrays.log_potentials
+    ev = bp_arrays.evidence
+    return BPArrays(log_potentials=lp if _is_torch(lp) else ctx.plan._dev(lp),  # pylint: disable=protected-access
+                    ftov_msgs=msgs,
+                    evidence=ev if _is_torch(ev) else ctx.plan._dev(ev)), deltas  # pylint: disable=protected-access
+
+  def run(bp_arrays: BPArrays, num_iters: int, damping: float = 0.5,
+          temperature: float = default_t) -> BPArrays:
+    return run_with_diffs(bp_arrays, num_iters, damping, temperature)[0]
+
+  def run_bp(bp_arrays: BPArrays, num_iters: int, damping: float = 0.5) -> BPArrays:
+    warnings.warn("BP.run_bp is deprecated. Please consider using BP.run instead.")
+    return run(bp_arrays, num_iters, damping, default_t)
+
+  return BeliefPropagation(init=ctx.init, update=ctx.update, to_bp_state=ctx.to_bp_state,
+                           get_beliefs=ctx.get_beliefs, run=run, run_bp=run_bp,
+                           run_with_diffs=run_with_diffs, context=ctx)
+
+
+def _softmax_last(x):
+  if _is_torch(x):
+    if x.numel() == 0:
+      return x
+    return (x - x.logsumexp(dim=-1, keepdim=True)).exp()
+  x = np.asarray(x)
+  if x.size == 0:
+    return x
+  m = np.max(x, axis=-1, keepdims=True)
+  m = np.where(np.isfinite(m), m, 0)
+  return np.exp(x - (np.log(np.sum(np.exp(x - m), axis=-1, keepdims=True)) + m))
+
+
+def get_marginals(beliefs: Dict[Hashable, Any]) -> Dict[Hashable, Any]:
+  """Per-variable softmax of the beliefs (pgmax/infer/bp.py:263-288). Beliefs from get_beliefs
+  are normalised by the pgbp_marginals kernel; padded states get probability 0."""
+  ctx = getattr(beliefs, "context", None)
+  if ctx is not None and getattr(beliefs, "flat", None) is not None and ctx.num_variables > 0:
+    flat = ctx.plan.marginals(beliefs.flat)
+    out = unflatten_beliefs(flat, ctx.bp_state.fg_state.variable_groups)
+
+    def zero_pad(x):
+      if isinstance(x, dict):
+        return {k: zero_pad(v) for k, v in x.items()}
+      return x.nan_to_num(neginf=0.0) if _is_torch(x) else np.nan_to_num(x, neginf=0.0)
+
+    return {k: zero_pad(v) for k, v in out.items()}
+
+  def tmap(t):
+    return {k: tmap(v) for k, v in t.items()} if isinstance(t, dict) else _softmax_last(t)
+
+  return tmap(beliefs)

@@ -1,0 +1,42 @@
+"""The C ABI library: it builds for sm_103a, loads, and exports every symbol include/pgbp.h
+declares. No kernel is launched here (no GPU needed)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from pgmax_gb300 import native
+
+HEADER = os.path.join(native.ROOT, "include", "pgbp.h")
+
+
+def declared_functions():
+  text = open(HEADER).read()
+  return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(pgbp_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_expected_entry_points():
+  names = declared_functions()
+  for n in ("pgbp_plan_create", "pgbp_plan_destroy", "pgbp_run", "pgbp_factor_update",
+            "pgbp_beliefs", "pgbp_decode", "pgbp_marginals", "pgbp_workspace_size",
+            "pgbp_last_error"):
+    assert n in names
+
+
+def test_library_builds_loads_and_exports_every_declared_symbol():
+  lib = native.load()
+  for n in declared_functions():
+    assert hasattr(lib, n), n
+  assert {s[0] for s in native.SIGNATURES} == set(declared_functions())
+  assert lib.pgbp_version() >= 100
+
+
+def test_null_arguments_are_rejected_with_a_status():
+  lib = native.load()
+  assert lib.pgbp_plan_create(None, 0, None) == 1
+  assert b"null" in lib.pgbp_last_error()
+  assert lib.pgbp_run(None, None, 1, None, 0, None, 0, None, 0, None, None, 1, 0.5, 0.0, None, 0) == 1
+  assert lib.pgbp_workspace_size(None, 1, 1) == 0
+  assert lib.pgbp_plan_destroy(None) == 0
