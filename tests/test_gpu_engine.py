@@ -81,6 +81,13 @@ def test_run_matches_oracle_and_reference(path):
   assert not (mism & ~_near_tie(f["flat_beliefs"], starts, ends)).any()
 
 
+# On randomly perturbed inputs at temperature > 0 the OR/AND updates subtract nearly equal
+# log-sums (logminusexp_with_temp, pgmax/factor/update_utils.py:169-190), which amplifies the ulp
+# differences between CUDA's and glibc's expf/log1pf; 1e-4 bounds the engine-oracle gap there.
+# Against the reference's own captured runs the engine stays within 1e-5 (test above).
+PERTURBED_T_POS_ATOL = 1e-4
+
+
 @pytest.mark.parametrize("name", ["case_rbm_s0", "case_mixed_T0", "case_mixed_T1", "case_deconv_T1",
                                   "case_potts_K8"])
 def test_batched_run_equals_single_instances(name):
@@ -99,13 +106,16 @@ def test_batched_run_equals_single_instances(name):
     assert out.shape == (B, f["ftov_msgs_in"].shape[0]) and deltas.shape == (B, 9)
     for b in (0, 5, B - 1):
       lpb = lp_in if lp_in.ndim == 1 else lp_in[b]
+      single, single_d = plan.run(lpb, ev[b], msgs[b], 9, 0.5, T)
+      np.testing.assert_array_equal(out[b], _np(single))
+      np.testing.assert_array_equal(deltas[b], _np(single_d))
       o, d = oracle.run(w, lpb, ev[b], msgs[b], 9, 0.5, T)
       if T == 0.0:
         np.testing.assert_array_equal(out[b], o)
         np.testing.assert_array_equal(deltas[b], d)
       else:
-        np.testing.assert_allclose(out[b], o, atol=ATOL, rtol=0)
-        np.testing.assert_allclose(deltas[b], d, atol=ATOL, rtol=0)
+        np.testing.assert_allclose(out[b], o, atol=PERTURBED_T_POS_ATOL, rtol=0)
+        np.testing.assert_allclose(deltas[b], d, atol=PERTURBED_T_POS_ATOL, rtol=0)
 
 
 def test_runs_are_bitwise_deterministic():
