@@ -121,6 +121,23 @@ int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch,
              int64_t num_iters, double damping, double temperature,
              void* workspace, size_t workspace_bytes);
 
+/* pgbp_run without any device allocation, for callers that cannot call cudaMalloc while they run
+ * inference and cannot pass a workspace either (code inside a host framework that owns all device
+ * memory and hands it only inputs and outputs; services with a fixed memory budget reserved at
+ * start-up). No counterpart in the reference, which leaves memory to XLA.
+ * Scratch is one static device array of PGBP_STATIC_SCRATCH_BYTES per GPU that loads this library,
+ * held until the process exits; a run needing more (pgbp_workspace_size) fails with
+ * PGBP_ERR_WORKSPACE. The first call on a device looks up the array's address: make it before any
+ * stream capture. All calls share the array, so calls that overlap on the GPU race; each call
+ * clears what must start at zero. Arguments and results are those of pgbp_run. */
+#define PGBP_STATIC_SCRATCH_BYTES (32u << 20)
+int pgbp_run_static_scratch(const pgbp_plan* plan, void* stream, int64_t batch,
+                            const float* log_potentials, int64_t lp_stride,
+                            const float* evidence, int64_t ev_stride,
+                            const float* msgs_in, int64_t msgs_stride,
+                            float* msgs_out, float* deltas,
+                            int64_t num_iters, double damping, double temperature);
+
 /* One factor type's un-fused update: out = FAC_TO_VAR_UPDATES[type](vtof, lp, T, normalize).
  * vtof / out are that type's message slice [batch, n_type] (stride floats apart), lp its
  * potential slice [batch, p_type] (lp_stride, 0 = shared). No workspace is needed. */

@@ -81,6 +81,9 @@ struct Plan {
   int64_t num_enum_factors = 0, num_enum_pairwise = 0;
 };
 
+// Records `message` as the calling thread's pgbp_last_error() and returns `code`.
+int set_last_error(int code, const char* message);
+
 // Workspace carve-up of one pgbp_run call.
 struct RunBuffers {
   float* msgs[2];
@@ -125,3 +128,8 @@ cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* bel
                       float* out);
 
 }  // namespace pgbp
+
+// The opaque handle of include/pgbp.h.
+struct pgbp_plan {
+  pgbp::Plan p;
+};

@@ -27,10 +27,6 @@
 
 #include "pgbp_internal.h"
 
-struct pgbp_plan {
-  pgbp::Plan p;
-};
-
 namespace {
 
 thread_local std::string g_last_error;
@@ -107,6 +103,7 @@ cudaEvent_t prof_event() {
 }  // namespace
 
 namespace pgbp {
+int set_last_error(int code, const char* message) { return fail(code, "%s", message); }
 bool profiling_enabled() { return g_prof_on; }
 void profile_record(int cls, cudaStream_t s, bool start) {
   cudaEvent_t e = prof_event();

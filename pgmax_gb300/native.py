@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libpgbp.so")
 
-SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp"]
+SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every float32 op rounds as the reference's does.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -121,6 +121,8 @@ SIGNATURES = [
     ("pgbp_workspace_size", ctypes.c_size_t, [_p, _i64, _i64]),
     ("pgbp_run", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p, _i64, _d, _d,
                                 _p, ctypes.c_size_t]),
+    ("pgbp_run_static_scratch", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p,
+                                               _p, _i64, _d, _d]),
     ("pgbp_factor_update", ctypes.c_int, [_p, _p, ctypes.c_int, _i64, _p, _i64, _p, _i64, _d,
                                           ctypes.c_int, _p, _i64]),
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
