@@ -11,27 +11,35 @@
 
 namespace pgbp {
 
+// Message storage during a run ("slots"). Every edge of the graph owns a run of slots, in edge
+// order: an edge of a binary variable owns ONE slot holding its normalised message compressed to
+// a float (after normalisation one of the two states is exactly +0, see encode/decode in
+// pgbp_kernels.cu); any other edge owns one slot per state. Slot s of instance b is at s * B + b.
+
 // Dense pairwise EnumFactors with an n1 x n2 table listing every config in row-major order
-// (PairwiseFactorGroup, pgmax/fgroup/enum.py:303-310). Edge states of factor u are
-// es_begin[u] .. es_begin[u] + n1 + n2 - 1 (var0's states then var1's); its potentials are
-// cfg_begin[u] .. cfg_begin[u] + n1 * n2 - 1 (relative to the Enum potentials range).
+// (PairwiseFactorGroup, pgmax/fgroup/enum.py:303-310). rec[u] = (first edge state, first slot,
+// first variable state of variable 0, first variable state of variable 1); cfg_begin[u] is the
+// absolute index of its first potential.
 struct PairwiseBucket {
   int n1 = 0, n2 = 0;
   int64_t count = 0;
-  int32_t* es_begin = nullptr;   // device, absolute edge-state index
-  int32_t* cfg_begin = nullptr;  // device, absolute potential index
+  int4* rec = nullptr;
+  int32_t* cfg_begin = nullptr;
 };
 
-// Every other EnumFactor: per factor its edge-state range, edges, and config rows. Rows of config
+// Every other EnumFactor: per factor its edge-state range, edges and config rows. Rows of config
 // k of factor f are row_begin[f] + k * n_vars[f] + i (i = variable), holding the edge state local to
-// the factor (row_les), exactly the layout of _compile_enumeration_wiring_numba (enum.py:364-394).
+// the factor (row_les), the layout of _compile_enumeration_wiring_numba (enum.py:364-394).
+// Per factor-edge j (edge_off[f] <= j < edge_off[f + 1]): its size, first slot, first var state.
 struct EnumGeneric {
   int64_t count = 0;
   int max_es = 0;                 // largest number of edge states of one factor
   int32_t* es_begin = nullptr;    // [count] absolute edge-state index
   int32_t* n_es = nullptr;        // [count]
-  int32_t* edge_off = nullptr;    // [count + 1] into edge_size
-  int32_t* edge_size = nullptr;   // number of states of each edge of each factor
+  int32_t* edge_off = nullptr;    // [count + 1]
+  int32_t* edge_size = nullptr;
+  int32_t* edge_slot = nullptr;
+  int32_t* edge_vs = nullptr;
   int32_t* row_begin = nullptr;   // [count] into row_les
   int32_t* n_cfg = nullptr;       // [count]
   int32_t* n_vars = nullptr;      // [count]
@@ -39,24 +47,32 @@ struct EnumGeneric {
   int32_t* row_les = nullptr;     // [rows] edge state local to its factor
 };
 
-// OR (off = +1) / AND (off = -1) factors: parents par_begin[f] .. par_begin[f + 1] - 1. par_es is
-// the absolute index of each parent's "other" state (PGMax's parents_msg_indices); the relevant
-// state is par_es + off. child_es likewise (logical.py:458-488).
+// OR (off = +1) / AND (off = -1) factors: parents par_begin[f] .. par_begin[f + 1] - 1. Every edge
+// is binary: (lower edge state, slot, first variable state) per parent and per child. The
+// relevant state is state 1 for OR and state 0 for AND (logical.py:262-279).
 struct LogicalSet {
   int64_t count = 0, num_parents = 0;
   int off = 1;
   int32_t* par_begin = nullptr;  // [count + 1]
-  int32_t* par_es = nullptr;     // [num_parents]
-  int32_t* child_es = nullptr;   // [count]
+  int4* par = nullptr;           // [num_parents] (es0, slot, vs0, 0)
+  int4* child = nullptr;         // [count]
 };
 
-// Pool factors: choices ch_begin[f] .. ch_begin[f + 1] - 1; ch_es / ind_es are the absolute
-// indices of state 0 of each choice / indicator (pool.py:62-83).
+// Pool factors: choices ch_begin[f] .. ch_begin[f + 1] - 1, binary edges as above (pool.py:62-83).
 struct PoolSet {
   int64_t count = 0, num_choices = 0;
   int32_t* ch_begin = nullptr;
-  int32_t* ch_es = nullptr;
-  int32_t* ind_es = nullptr;
+  int4* ch = nullptr;            // [num_choices]
+  int4* ind = nullptr;           // [count]
+};
+
+// Variable sums: binary variables (both states from one compressed slot per edge) and the
+// states of all other variables (one slot per edge), each with its slots in edge order.
+struct VarsumSet {
+  int64_t count = 0;
+  int32_t* vs = nullptr;         // [count] variable state (binary: state 0)
+  int32_t* off = nullptr;        // [count + 1]
+  int32_t* slots = nullptr;
 };
 
 struct Plan {
@@ -64,14 +80,16 @@ struct Plan {
   int sm_count = 0;
   int64_t num_edge_states = 0, num_var_states = 0, num_edges = 0, num_variables = 0;
   int64_t num_potentials = 0;
+  int64_t num_slots = 0;
   int64_t msgs_range[4][2] = {};
   int64_t potentials_range[4][2] = {};
-  // var-state CSR over edge states, increasing edge-state order inside each var state
+  // var-state CSR over edge states, increasing edge-state order (pgbp_beliefs)
   int32_t* vs_off = nullptr;        // [num_var_states + 1]
   int32_t* vs_edges = nullptr;      // [num_edge_states]
-  int32_t* vs_of_es = nullptr;      // [num_edge_states]
-  int32_t* edge_start = nullptr;    // [num_edges + 1]
+  int32_t* edge_start = nullptr;    // [num_edges + 1] first edge state of each edge
+  int32_t* edge_slot = nullptr;     // [num_edges + 1] first slot of each edge
   int32_t* var_off = nullptr;       // [num_variables + 1] (decode / marginals), may be null
+  VarsumSet varsum_binary, varsum_other;
   std::vector<PairwiseBucket> pairwise;
   EnumGeneric enum_generic;
   LogicalSet logical[2];
@@ -83,15 +101,6 @@ struct Plan {
 
 // Records `message` as the calling thread's pgbp_last_error() and returns `code`.
 int set_last_error(int code, const char* message);
-
-// Workspace carve-up of one pgbp_run call.
-struct RunBuffers {
-  float* msgs[2];
-  float* vsum;
-  float* ev;            // transposed evidence [N_vs][B] (batched evidence only)
-  float* lp;            // clipped potentials: [P] shared or [P][B]
-  unsigned* deltas;     // [iters][B] as float bits
-};
 
 size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched, bool lp_batched);
 

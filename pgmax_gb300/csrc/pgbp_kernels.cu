@@ -1,25 +1,28 @@
 // sm_103a kernels of the loopy-BP engine.
 //
-// Layout in HBM during a run: messages, variable sums, evidence and (batched) potentials are stored
-// "edge-major, batch innermost" - element (edge state e, instance b) at e * B + b - so the 32 lanes
-// of a warp read 32 instances of the same edge state in one 128-byte transaction and every index
-// (edge state -> variable state, factor -> first edge state, ...) is loaded once per warp and
-// broadcast. The caller's BPArrays are [B, n] (jax.vmap layout); run() transposes them in and out
-// with shared-memory tiles.
+// Layout in HBM during a run: messages live in "slots" (pgbp_internal.h), variable sums, evidence
+// and batched potentials likewise, all "slot-major, batch innermost" - element (slot s, instance
+// b) at s * B + b - so the 32 lanes of a warp read 32 instances of one slot in one 128-byte
+// transaction and every index is one broadcast load per warp. An edge of a binary variable owns
+// a single slot: after normalize_and_clip_msgs (pgmax/infer/bp.py:222-260) one of its two states
+// is exactly +0 (x - x), so the pair is stored as one float and decoded exactly (encode2/decode2
+// below); this halves the message traffic of binary graphs without changing a single bit of the
+// arithmetic. The caller's BPArrays are [B, n] (jax.vmap layout); run() transposes them in and out
+// through shared-memory tiles.
 //
 // One BP iteration (pgmax/infer/bp.py:98-137) is:
-//   varsum_kernel    var_sums[vs] = evidence[vs] + sum of msgs over vs's edge states, serially in
-//                    increasing edge-state order (the order of the reference's scatter-add,
-//                    bp.py:217);
+//   varsum kernels   var_sums[vs] = evidence[vs] + sum of msgs over vs's edge states, serially in
+//                    increasing edge-state order, the order of the reference's scatter-add
+//                    (bp.py:217);
 //   factor kernels   one per factor class (dense pairwise Enum, generic Enum, OR, AND, Pool). Each
 //                    thread owns one (factor, instance): it forms vtof = var_sums - msgs
-//                    (bp.py:218) for the factor's edge states, computes the factor-to-variable
-//                    messages, and applies damping, per-edge max-normalisation, clipping at
-//                    MSG_NEG_INF and the residual (bp.py:127-136) before writing - a factor owns all
-//                    states of its edges, so the epilogue needs nothing from other threads.
-// Everything is float32 with the reference's operation order; the build uses -fmad=false so that
-// no multiply-add is contracted. At temperature 0 the engine therefore reproduces the oracle bit
-// for bit; at temperature > 0 expf/logf/log1pf/expm1f differ from glibc's by an ulp or two.
+//                    (bp.py:218) for the factor's edges, computes the factor-to-variable messages,
+//                    and applies damping, per-edge max-normalisation, clipping at MSG_NEG_INF and
+//                    the residual (bp.py:127-136) before writing - a factor owns all states of its
+//                    edges, so the epilogue needs nothing from other threads.
+// Everything is float32 in the reference's operation order; the build uses -fmad=false so no
+// multiply-add is contracted. At temperature 0 the engine reproduces the oracle bit for bit; at
+// temperature > 0 expf/logf/log1pf/expm1f differ from glibc's by an ulp or two.
 #include <math.h>
 
 #include <algorithm>
@@ -29,13 +32,23 @@
 namespace pgbp {
 namespace {
 
-constexpr float kMsgNegInf = -1e32f;   // MSG_NEG_INF, pgmax/utils/__init__.py:26
-constexpr float kLpMaxAbs = 1e6f;      // LOG_POTENTIAL_MAX_ABS, pgmax/utils/__init__.py:32
-constexpr double kStabilityThre = 0.5; // TEMPERATURE_STABILITY_THRE, pgmax/factor/logical.py:33
+constexpr float kMsgNegInf = -1e32f;    // MSG_NEG_INF, pgmax/utils/__init__.py:26
+constexpr float kLpMaxAbs = 1e6f;       // LOG_POTENTIAL_MAX_ABS, pgmax/utils/__init__.py:32
+constexpr double kStabilityThre = 0.5;  // TEMPERATURE_STABILITY_THRE, pgmax/factor/logical.py:33
 
-// numpy / XLA maximum and minimum: NaN-propagating, first operand kept on ties.
-__device__ __forceinline__ float fmaxp(float a, float b) { return (a >= b || a != a) ? a : b; }
-__device__ __forceinline__ float fminp(float a, float b) { return (a <= b || a != a) ? a : b; }
+// NaN-propagating maximum / minimum, as jnp.maximum / jnp.minimum: one max.NaN / min.NaN
+// instruction. It equals the reference's result for every input, up to the sign of a zero when
+// +0 and -0 meet (IEEE-equal values).
+__device__ __forceinline__ float fmaxp(float a, float b) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float fminp(float a, float b) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
 
 // update_utils.py:150-166
 __device__ __forceinline__ float logaddexp_t(float a, float b, float t) {
@@ -56,6 +69,24 @@ __device__ __forceinline__ float log1mexp_f(float x) {
 __device__ __forceinline__ float logminusexp_t(float a, float b, float t, float eps) {
   const float v = t * log1mexp_f((a - b) / t) + a;
   return (a >= b + eps) ? v : -INFINITY;
+}
+
+// A normalised binary message (m0, m1) has m0 == +0 or m1 == +0 (or both NaN, since the
+// normalising max propagates NaN to both states). Stored as m1 when m0 == 0 (so <= 0), else as
+// -m0 (> 0); NaN stays NaN. Zero entries of normalised messages are always +0 (x - x is +0 in
+// round-to-nearest and the clip keeps it), so the round trip is exact.
+__device__ __forceinline__ float encode2(float m0, float m1) { return (m0 == 0.0f) ? m1 : -m0; }
+__device__ __forceinline__ void decode2(float c, float& m0, float& m1) {
+  if (c != c) {
+    m0 = c;
+    m1 = c;
+  } else if (c <= 0.0f) {
+    m0 = 0.0f;
+    m1 = c;
+  } else {
+    m0 = -c;
+    m1 = 0.0f;
+  }
 }
 
 // ----------------------------------------------------------------------------- launch mapping
@@ -92,43 +123,67 @@ __device__ __forceinline__ void block_max_to(unsigned* dst, const Lane& l, float
 }
 
 // ----------------------------------------------------------------------------- contexts
-// Fused: inside run(). vtof from var sums and the current messages; outputs go through damping,
-// normalisation, clipping and the residual, into the next messages.
+// An edge seen by a factor: its first edge state (caller layout), its first slot (run layout) and
+// its variable's first state (variable sums).
+struct EdgeRef {
+  int64_t es0, slot, vs0;
+};
+
+__device__ __forceinline__ EdgeRef edge_ref(int4 r) { return EdgeRef{r.x, r.y, r.z}; }
+
+// Fused: inside run(). vtof from variable sums and the current messages; outputs go through
+// damping, normalisation, clipping and the residual into the next messages.
 struct Fused {
   const float* __restrict__ cur;
   float* __restrict__ nxt;
   const float* __restrict__ vsum;
-  const int32_t* __restrict__ vs_of_es;
   const float* __restrict__ lp;
   int64_t lps, lpb;  // potential k of instance b at lp[k * lps + b * lpb]
   int64_t B;
   float d, omd;
 
-  __device__ __forceinline__ float vtof(int64_t e, int64_t b) const {
-    return vsum[(int64_t)__ldg(vs_of_es + e) * B + b] - cur[e * B + b];
+  __device__ __forceinline__ float pot(int64_t k, int64_t b) const {
+    return __ldg(lp + k * lps + b * lpb);
   }
-  __device__ __forceinline__ float pot(int64_t k, int64_t b) const { return __ldg(lp + k * lps + b * lpb); }
 
-  // bp.py:127-136 for one edge whose k states start at e0; outv(i) is the new factor message.
-  template <class F>
-  __device__ __forceinline__ void edge(int64_t e0, int k, F outv, int64_t b, float& dmax) const {
-    float m = -INFINITY;
-    for (int i = 0; i < k; ++i) {
-      const float o = cur[(e0 + i) * B + b];
-      const float n = d * o + omd * outv(i);
-      m = fmaxp(m, n);
+  // old[i] = current message, vt[i] = variable-to-factor message of the edge's k states.
+  __device__ __forceinline__ void load(const EdgeRef& r, int k, int64_t b, float* old,
+                                       float* vt) const {
+    if (k == 2) {
+      decode2(cur[r.slot * B + b], old[0], old[1]);
+    } else {
+      for (int i = 0; i < k; ++i) old[i] = cur[(r.slot + i) * B + b];
     }
+    for (int i = 0; i < k; ++i) vt[i] = vsum[(r.vs0 + i) * B + b] - old[i];
+  }
+
+  // bp.py:127-136 for one edge; outv(i) is the new factor-to-variable message of state i.
+  template <class F>
+  __device__ __forceinline__ void store(const EdgeRef& r, int k, const float* old, F outv,
+                                        int64_t b, float& dmax) const {
+    if (k == 2) {
+      const float n0 = d * old[0] + omd * outv(0);
+      const float n1 = d * old[1] + omd * outv(1);
+      const float m = fmaxp(fmaxp(-INFINITY, n0), n1);
+      const float v0 = fmaxp(n0 - m, kMsgNegInf);
+      const float v1 = fmaxp(n1 - m, kMsgNegInf);
+      nxt[r.slot * B + b] = encode2(v0, v1);
+      dmax = fmaxp(dmax, fabsf(v0 - old[0]));
+      dmax = fmaxp(dmax, fabsf(v1 - old[1]));
+      return;
+    }
+    float m = -INFINITY;
+    for (int i = 0; i < k; ++i) m = fmaxp(m, d * old[i] + omd * outv(i));
     for (int i = 0; i < k; ++i) {
-      const float o = cur[(e0 + i) * B + b];
-      const float n = d * o + omd * outv(i);
+      const float n = d * old[i] + omd * outv(i);
       const float v = fmaxp(n - m, kMsgNegInf);
-      nxt[(e0 + i) * B + b] = v;
-      dmax = fmaxp(dmax, fabsf(v - o));
+      nxt[(r.slot + i) * B + b] = v;
+      dmax = fmaxp(dmax, fabsf(v - old[i]));
     }
   }
 };
 
-// Update: one factor type's raw update on caller arrays [B, n_type] (FAC_TO_VAR_UPDATES call).
+// Update: one factor type's raw update on caller arrays [B, n_type] (a FAC_TO_VAR_UPDATES call).
 struct Update {
   const float* __restrict__ vt;
   int64_t vts;
@@ -139,11 +194,20 @@ struct Update {
   int64_t lpb;   // instance stride of the potentials (0 = shared)
   int64_t lpbase;
 
-  __device__ __forceinline__ float vtof(int64_t e, int64_t b) const { return vt[b * vts + (e - base)]; }
-  __device__ __forceinline__ float pot(int64_t k, int64_t b) const { return lp[b * lpb + (k - lpbase)]; }
+  __device__ __forceinline__ float pot(int64_t k, int64_t b) const {
+    return lp[b * lpb + (k - lpbase)];
+  }
+  __device__ __forceinline__ void load(const EdgeRef& r, int k, int64_t b, float* old,
+                                       float* vtof) const {
+    for (int i = 0; i < k; ++i) {
+      old[i] = 0.0f;
+      vtof[i] = vt[b * vts + (r.es0 + i - base)];
+    }
+  }
   template <class F>
-  __device__ __forceinline__ void edge(int64_t e0, int k, F outv, int64_t b, float&) const {
-    for (int i = 0; i < k; ++i) out[b * os + (e0 + i - base)] = outv(i);
+  __device__ __forceinline__ void store(const EdgeRef& r, int k, const float*, F outv, int64_t b,
+                                        float&) const {
+    for (int i = 0; i < k; ++i) out[b * os + (r.es0 + i - base)] = outv(i);
   }
 };
 
@@ -152,23 +216,20 @@ struct Update {
 // summary(i, j) = ((0 + vtof1[i]) + vtof2[j]) + lp[i * n2 + j]; the max / sum-exp over the configs
 // of an edge state run in increasing config order, the reference's scatter order.
 template <int N1, int N2, bool T0, class C>
-__device__ __forceinline__ void pairwise_body(const C& c, int64_t e0, int64_t k0, int n1d, int n2d,
-                                              int64_t b, float t, float& dmax) {
+__device__ __forceinline__ void pairwise_body(const C& c, const EdgeRef& r1, const EdgeRef& r2,
+                                              int64_t k0, int n1d, int n2d, int64_t b, float t,
+                                              float& dmax) {
   // N1, N2 > 0: sizes known at compile time, arrays live in registers (loops unroll).
-  // N1 = N2 = 0: run-time sizes up to 64, arrays in local memory, loops not unrolled.
+  // N1 = N2 = 0: run-time sizes up to 64, arrays in local memory.
   constexpr int M1 = N1 > 0 ? N1 : 64;
   constexpr int M2 = N2 > 0 ? N2 : 64;
   const int n1 = N1 > 0 ? N1 : n1d;
   const int n2 = N2 > 0 ? N2 : n2d;
-  float v1[M1], v2[M2], mx1[M1], mx2[M2];
-  for (int i = 0; i < n1; ++i) {
-    v1[i] = c.vtof(e0 + i, b);
-    mx1[i] = -INFINITY;
-  }
-  for (int j = 0; j < n2; ++j) {
-    v2[j] = c.vtof(e0 + n1 + j, b);
-    mx2[j] = -INFINITY;
-  }
+  float o1[M1], o2[M2], v1[M1], v2[M2], mx1[M1], mx2[M2];
+  c.load(r1, n1, b, o1, v1);
+  c.load(r2, n2, b, o2, v2);
+  for (int i = 0; i < n1; ++i) mx1[i] = -INFINITY;
+  for (int j = 0; j < n2; ++j) mx2[j] = -INFINITY;
   for (int i = 0; i < n1; ++i) {
     for (int j = 0; j < n2; ++j) {
       const float s = ((0.0f + v1[i]) + v2[j]) + c.pot(k0 + i * n2 + j, b);
@@ -177,8 +238,8 @@ __device__ __forceinline__ void pairwise_body(const C& c, int64_t e0, int64_t k0
     }
   }
   if (T0) {
-    c.edge(e0, n1, [&](int i) { return mx1[i] - v1[i]; }, b, dmax);
-    c.edge(e0 + n1, n2, [&](int j) { return mx2[j] - v2[j]; }, b, dmax);
+    c.store(r1, n1, o1, [&](int i) { return mx1[i] - v1[i]; }, b, dmax);
+    c.store(r2, n2, o2, [&](int j) { return mx2[j] - v2[j]; }, b, dmax);
   } else {
     float s1[M1], s2[M2];
     for (int i = 0; i < n1; ++i) s1[i] = 0.0f;
@@ -190,17 +251,23 @@ __device__ __forceinline__ void pairwise_body(const C& c, int64_t e0, int64_t k0
         s2[j] += expf((s - mx2[j]) / t);
       }
     }
-    c.edge(e0, n1, [&](int i) { return (t * logf(s1[i]) + mx1[i]) - v1[i]; }, b, dmax);
-    c.edge(e0 + n1, n2, [&](int j) { return (t * logf(s2[j]) + mx2[j]) - v2[j]; }, b, dmax);
+    c.store(r1, n1, o1, [&](int i) { return (t * logf(s1[i]) + mx1[i]) - v1[i]; }, b, dmax);
+    c.store(r2, n2, o2, [&](int j) { return (t * logf(s2[j]) + mx2[j]) - v2[j]; }, b, dmax);
   }
 }
 
 struct PairwiseDev {
-  const int32_t* __restrict__ es_begin;
+  const int4* __restrict__ rec;
   const int32_t* __restrict__ cfg_begin;
   int64_t count;
   int n1, n2;
 };
+
+__device__ __forceinline__ void pairwise_refs(const PairwiseDev& p, int4 q, EdgeRef& r1,
+                                              EdgeRef& r2) {
+  r1 = EdgeRef{q.x, q.y, q.z};
+  r2 = EdgeRef{(int64_t)q.x + p.n1, (int64_t)q.y + (p.n1 == 2 ? 1 : p.n1), q.w};
+}
 
 template <int N1, int N2, bool T0, class C>
 __global__ void __launch_bounds__(256) pairwise_kernel(C c, PairwiseDev p, int64_t B, float t,
@@ -208,9 +275,22 @@ __global__ void __launch_bounds__(256) pairwise_kernel(C c, PairwiseDev p, int64
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
-    for (int64_t u = l.u0; u < p.count; u += l.ustep) {
-      pairwise_body<N1, N2, T0>(c, (int64_t)__ldg(p.es_begin + u), (int64_t)__ldg(p.cfg_begin + u),
-                                p.n1, p.n2, l.b, t, dmax);
+    int64_t u = l.u0;
+    // two factors per step: their loads are independent, so twice as many are in flight
+    for (; u + l.ustep < p.count; u += 2 * l.ustep) {
+      const int4 qa = __ldg(p.rec + u);
+      const int4 qb = __ldg(p.rec + u + l.ustep);
+      const int64_t ka = __ldg(p.cfg_begin + u), kb = __ldg(p.cfg_begin + u + l.ustep);
+      EdgeRef a1, a2, b1, b2;
+      pairwise_refs(p, qa, a1, a2);
+      pairwise_refs(p, qb, b1, b2);
+      pairwise_body<N1, N2, T0>(c, a1, a2, ka, p.n1, p.n2, l.b, t, dmax);
+      pairwise_body<N1, N2, T0>(c, b1, b2, kb, p.n1, p.n2, l.b, t, dmax);
+    }
+    if (u < p.count) {
+      EdgeRef a1, a2;
+      pairwise_refs(p, __ldg(p.rec + u), a1, a2);
+      pairwise_body<N1, N2, T0>(c, a1, a2, __ldg(p.cfg_begin + u), p.n1, p.n2, l.b, t, dmax);
     }
   }
   block_max_to(deltas, l, dmax);
@@ -221,6 +301,8 @@ struct EnumGenericDev {
   const int32_t* __restrict__ n_es;
   const int32_t* __restrict__ edge_off;
   const int32_t* __restrict__ edge_size;
+  const int32_t* __restrict__ edge_slot;
+  const int32_t* __restrict__ edge_vs;
   const int32_t* __restrict__ row_begin;
   const int32_t* __restrict__ n_cfg;
   const int32_t* __restrict__ n_vars;
@@ -231,8 +313,8 @@ struct EnumGenericDev {
 
 // pass_enum_fac_to_var_messages (enum.py:451-475) for an arbitrary config table.
 template <int MAXES, bool T0, class C>
-__global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g, int64_t B, float t,
-                                                           unsigned* deltas) {
+__global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g, int64_t B,
+                                                           float t, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
@@ -241,9 +323,17 @@ __global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g
       const int64_t e0 = g.es_begin[f];
       const int n = g.n_es[f], nv = g.n_vars[f], ncfg = g.n_cfg[f];
       const int64_t rb = g.row_begin[f], k0 = g.cfg_begin[f];
-      float v[MAXES], mx[MAXES], se[MAXES];
+      const int j0 = g.edge_off[f], j1 = g.edge_off[f + 1];
+      float old[MAXES], v[MAXES], mx[MAXES], se[MAXES];
+      {
+        int pos = 0;
+        for (int j = j0; j < j1; ++j) {
+          const int k = g.edge_size[j];
+          c.load(EdgeRef{e0 + pos, g.edge_slot[j], g.edge_vs[j]}, k, b, old + pos, v + pos);
+          pos += k;
+        }
+      }
       for (int i = 0; i < n; ++i) {
-        v[i] = c.vtof(e0 + i, b);
         mx[i] = -INFINITY;
         se[i] = 0.0f;
       }
@@ -264,14 +354,16 @@ __global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g
         }
       }
       int pos = 0;
-      for (int j = g.edge_off[f]; j < g.edge_off[f + 1]; ++j) {
+      for (int j = j0; j < j1; ++j) {
         const int k = g.edge_size[j];
         const int p0 = pos;
+        const EdgeRef r{e0 + pos, g.edge_slot[j], g.edge_vs[j]};
         if (T0) {
-          c.edge(e0 + p0, k, [&](int i) { return mx[p0 + i] - v[p0 + i]; }, b, dmax);
+          c.store(r, k, old + p0, [&](int i) { return mx[p0 + i] - v[p0 + i]; }, b, dmax);
         } else {
-          c.edge(e0 + p0, k, [&](int i) { return (t * logf(se[p0 + i]) + mx[p0 + i]) - v[p0 + i]; },
-                 b, dmax);
+          c.store(r, k, old + p0,
+                  [&](int i) { return (t * logf(se[p0 + i]) + mx[p0 + i]) - v[p0 + i]; }, b,
+                  dmax);
         }
         pos += k;
       }
@@ -283,11 +375,22 @@ __global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g
 // ----------------------------------------------------------------------------- OR / AND factors
 struct LogicalDev {
   const int32_t* __restrict__ par_begin;
-  const int32_t* __restrict__ par_es;
-  const int32_t* __restrict__ child_es;
+  const int4* __restrict__ par;
+  const int4* __restrict__ child;
   int64_t count;
   int off;
 };
+
+// (other, relevant) variable-to-factor messages of a binary edge: relevant = state 1 for OR,
+// state 0 for AND; old[] receives the current messages in state order.
+template <class C>
+__device__ __forceinline__ void load_or(const C& c, const EdgeRef& r, int rel, int64_t b,
+                                        float* old, float& v_oth, float& v_rel) {
+  float vt[2];
+  c.load(r, 2, b, old, vt);
+  v_rel = vt[rel];
+  v_oth = vt[1 - rel];
+}
 
 // pass_logical_fac_to_var_messages, pgmax/factor/logical.py:561-779, one factor per thread.
 // Factor-level sums run over the parents in order (the reference's scatter order); the argmax is
@@ -297,16 +400,16 @@ __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t
                                                       bool low_t, int normalize, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
-  const int off = g.off;
+  const int rel = g.off > 0 ? 1 : 0;
   if (l.valid) {
     const int64_t b = l.b;
     for (int64_t f = l.u0; f < g.count; f += l.ustep) {
       const int64_t p0 = g.par_begin[f], p1 = g.par_begin[f + 1];
-      const int64_t ch = g.child_es[f];
+      float old[2];
       float fs_oth = 0.0f, max1 = -INFINITY, fs_x = 0.0f;
       for (int64_t i = p0; i < p1; ++i) {
-        const int64_t e = g.par_es[i];
-        const float vo = c.vtof(e, b), vr = c.vtof(e + off, b);
+        float vo, vr;
+        load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
         fs_oth += vo;
         max1 = fmaxp(max1, vr - vo);
         fs_x += T0 ? fmaxp(vo, vr) : logaddexp_t(vr, vo, t);
@@ -315,18 +418,21 @@ __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t
       {
         int64_t last = -1;
         for (int64_t i = p0; i < p1; ++i) {
-          const int64_t e = g.par_es[i];
-          if (c.vtof(e + off, b) - c.vtof(e, b) == max1) last = i;
+          float vo, vr;
+          load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+          if (vr - vo == max1) last = i;
         }
         if (last >= 0) arg = last;
       }
       float max2 = -INFINITY;
       for (int64_t i = p0; i < p1; ++i) {
-        const int64_t e = g.par_es[i];
-        const float dif = (i == arg) ? -INFINITY : c.vtof(e + off, b) - c.vtof(e, b);
-        max2 = fmaxp(max2, dif);
+        float vo, vr;
+        load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+        max2 = fmaxp(max2, (i == arg) ? -INFINITY : vr - vo);
       }
-      const float c_rel = c.vtof(ch + off, b), c_oth = c.vtof(ch, b);
+      const EdgeRef rc = edge_ref(g.child[f]);
+      float cold[2], c_oth, c_rel;
+      load_or(c, rc, rel, b, cold, c_oth, c_rel);
       float ch_rel;
       if (T0) {
         ch_rel = fs_x + fminp(0.0f, max1);
@@ -336,8 +442,9 @@ __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t
       }
       const bool single = (p1 - p0) == 1;
       for (int64_t i = p0; i < p1; ++i) {
-        const int64_t e = g.par_es[i];
-        const float vo = c.vtof(e, b), vr = c.vtof(e + off, b);
+        const EdgeRef r = edge_ref(g.par[i]);
+        float vo, vr;
+        load_or(c, r, rel, b, old, vo, vr);
         float p_rel, p_oth;
         if (T0) {
           const float mx = fmaxp(vo, vr);
@@ -365,20 +472,11 @@ __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t
         }
         const float rel_out = normalize ? p_rel - p_oth : p_rel;
         const float oth_out = normalize ? 0.0f : p_oth;
-        // the edge's two states in index order: (other, relevant) for OR, (relevant, other) for AND
-        if (off > 0) {
-          c.edge(e, 2, [&](int s) { return s == 0 ? oth_out : rel_out; }, b, dmax);
-        } else {
-          c.edge(e - 1, 2, [&](int s) { return s == 0 ? rel_out : oth_out; }, b, dmax);
-        }
+        c.store(r, 2, old, [&](int s) { return s == rel ? rel_out : oth_out; }, b, dmax);
       }
       const float crel_out = normalize ? ch_rel - fs_oth : ch_rel;
       const float coth_out = normalize ? 0.0f : fs_oth;
-      if (off > 0) {
-        c.edge(ch, 2, [&](int s) { return s == 0 ? coth_out : crel_out; }, b, dmax);
-      } else {
-        c.edge(ch - 1, 2, [&](int s) { return s == 0 ? crel_out : coth_out; }, b, dmax);
-      }
+      c.store(rc, 2, cold, [&](int s) { return s == rel ? crel_out : coth_out; }, b, dmax);
     }
   }
   block_max_to(deltas, l, dmax);
@@ -387,134 +485,377 @@ __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t
 // ----------------------------------------------------------------------------- Pool factors
 struct PoolDev {
   const int32_t* __restrict__ ch_begin;
-  const int32_t* __restrict__ ch_es;
-  const int32_t* __restrict__ ind_es;
+  const int4* __restrict__ ch;
+  const int4* __restrict__ ind;
   int64_t count;
 };
 
-// pass_pool_fac_to_var_messages, pgmax/factor/pool.py:328-474.
+// pass_pool_fac_to_var_messages, pgmax/factor/pool.py:328-474 (state 1 is the "on" state).
 template <bool T0, class C>
-__global__ void __launch_bounds__(256) pool_kernel(C c, PoolDev g, int64_t B, float t, int normalize,
-                                                   unsigned* deltas) {
+__global__ void __launch_bounds__(256) pool_kernel(C c, PoolDev g, int64_t B, float t,
+                                                   int normalize, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
     const int64_t b = l.b;
     for (int64_t f = l.u0; f < g.count; f += l.ustep) {
       const int64_t p0 = g.ch_begin[f], p1 = g.ch_begin[f + 1];
-      const int64_t ie = g.ind_es[f];
+      float old[2], vt[2];
       float sums0 = 0.0f, max1 = -INFINITY;
       for (int64_t i = p0; i < p1; ++i) {
-        const int64_t e = g.ch_es[i];
-        const float z = c.vtof(e, b), o = c.vtof(e + 1, b);
-        sums0 += z;
-        max1 = fmaxp(max1, o - z);
+        c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+        sums0 += vt[0];
+        max1 = fmaxp(max1, vt[1] - vt[0]);
       }
       int64_t arg = p1 - 1;
       {
         int64_t last = -1;
         for (int64_t i = p0; i < p1; ++i) {
-          const int64_t e = g.ch_es[i];
-          if (c.vtof(e + 1, b) - c.vtof(e, b) == max1) last = i;
+          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+          if (vt[1] - vt[0] == max1) last = i;
         }
         if (last >= 0) arg = last;
       }
-      const float pi_zero = c.vtof(ie, b), pi_one = c.vtof(ie + 1, b);
-      const float pi_diff = pi_one - pi_zero;
+      const EdgeRef ri = edge_ref(g.ind[f]);
+      float iold[2], ivt[2];
+      c.load(ri, 2, b, iold, ivt);
+      const float pi_one = ivt[1];
+      const float pi_diff = ivt[1] - ivt[0];
       float max2 = -INFINITY, pi_mdiff, fl = 0.0f, am = 0.0f;
       if (T0) {
         for (int64_t i = p0; i < p1; ++i) {
-          const int64_t e = g.ch_es[i];
-          const float dif = (i == arg) ? -INFINITY : c.vtof(e + 1, b) - c.vtof(e, b);
-          max2 = fmaxp(max2, dif);
+          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+          max2 = fmaxp(max2, (i == arg) ? -INFINITY : vt[1] - vt[0]);
         }
         pi_mdiff = max1;
       } else {
         float se = 0.0f;
         for (int64_t i = p0; i < p1; ++i) {
-          const int64_t e = g.ch_es[i];
-          se += expf(((c.vtof(e + 1, b) - c.vtof(e, b)) - max1) / t);
+          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+          se += expf(((vt[1] - vt[0]) - max1) / t);
         }
         pi_mdiff = t * logf(se) + max1;
         fl = logaddexp_t(pi_mdiff, -pi_diff, t);
         // -logsumexps_with_temp of the diffs with the argmax replaced by -pi_diff (pool.py:416-425)
         float mw = -INFINITY;
         for (int64_t i = p0; i < p1; ++i) {
-          const int64_t e = g.ch_es[i];
-          const float w = (i == arg) ? -pi_diff : c.vtof(e + 1, b) - c.vtof(e, b);
-          mw = fmaxp(mw, w);
+          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+          mw = fmaxp(mw, (i == arg) ? -pi_diff : vt[1] - vt[0]);
         }
         float sw = 0.0f;
         for (int64_t i = p0; i < p1; ++i) {
-          const int64_t e = g.ch_es[i];
-          const float w = (i == arg) ? -pi_diff : c.vtof(e + 1, b) - c.vtof(e, b);
+          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+          const float w = (i == arg) ? -pi_diff : vt[1] - vt[0];
           sw += expf((w - mw) / t);
         }
         am = -(t * logf(sw) + mw);
       }
       const bool single = (p1 - p0) == 1;
       for (int64_t i = p0; i < p1; ++i) {
-        const int64_t e = g.ch_es[i];
-        const float z = c.vtof(e, b), o = c.vtof(e + 1, b);
-        const float dif = o - z;
+        const EdgeRef r = edge_ref(g.ch[i]);
+        c.load(r, 2, b, old, vt);
+        const float dif = vt[1] - vt[0];
         float mdiff;
         if (T0) {
           mdiff = fminp(pi_diff, -(i == arg ? max2 : max1));
         } else {
           mdiff = (i == arg) ? am : -logminusexp_t(fl, dif, t, 1e-30f);
         }
-        float ones = (sums0 + pi_one) - z;
+        float ones = (sums0 + pi_one) - vt[0];
         if (single) {
           mdiff = pi_diff;
           ones = pi_one;
         }
         const float s1 = normalize ? mdiff : ones;
         const float s0 = normalize ? 0.0f : ones - mdiff;
-        c.edge(e, 2, [&](int s) { return s == 0 ? s0 : s1; }, b, dmax);
+        c.store(r, 2, old, [&](int s) { return s == 0 ? s0 : s1; }, b, dmax);
       }
       const float i1 = normalize ? pi_mdiff : sums0 + pi_mdiff;
       const float i0 = normalize ? 0.0f : sums0;
-      c.edge(ie, 2, [&](int s) { return s == 0 ? i0 : i1; }, b, dmax);
+      c.store(ri, 2, iold, [&](int s) { return s == 0 ? i0 : i1; }, b, dmax);
     }
   }
   block_max_to(deltas, l, dmax);
 }
 
+// ----------------------------------------------------------------------------- 4 instances per thread
+// The two kernels that carry binary pairwise graphs (RBM, Ising) also come in a form where every
+// thread owns 4 consecutive instances (B % 4 == 0): 128-bit loads and stores, index and address
+// work shared by 4 instances, 4 independent dependency chains. Per instance the arithmetic is
+// exactly the scalar kernels'.
+
+struct Lane4 {
+  int64_t b;  // first of 4 instances
+  bool valid;
+  int64_t u0, ustep;
+};
+
+__device__ __forceinline__ Lane4 lane4(int64_t B) {
+  Lane4 l;
+  l.b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  l.valid = l.b < B;
+  l.u0 = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  l.ustep = (int64_t)gridDim.y * blockDim.y;
+  return l;
+}
+
+__device__ __forceinline__ void block_max4_to(unsigned* dst, const Lane4& l, float4 v) {
+  __shared__ float4 red[256];
+  const int tx = threadIdx.x, ty = threadIdx.y, bx = blockDim.x;
+  red[ty * bx + tx] = v;
+  __syncthreads();
+  for (int s = blockDim.y / 2; s > 0; s >>= 1) {
+    if (ty < s) {
+      float4 a = red[ty * bx + tx];
+      const float4 c = red[(ty + s) * bx + tx];
+      a.x = fmaxp(a.x, c.x);
+      a.y = fmaxp(a.y, c.y);
+      a.z = fmaxp(a.z, c.z);
+      a.w = fmaxp(a.w, c.w);
+      red[ty * bx + tx] = a;
+    }
+    __syncthreads();
+  }
+  if (ty == 0 && l.valid && dst != nullptr) {
+    const float4 a = red[tx];
+    atomicMax(dst + l.b + 0, __float_as_uint(a.x));
+    atomicMax(dst + l.b + 1, __float_as_uint(a.y));
+    atomicMax(dst + l.b + 2, __float_as_uint(a.z));
+    atomicMax(dst + l.b + 3, __float_as_uint(a.w));
+  }
+}
+
+// One instance of a dense 2x2 pairwise factor with both edges binary: c1 / c2 are the compressed
+// current messages to variables 1 and 2, a0 a1 / b0 b1 their variable sums, p00..p11 the table.
+// Same operations, in the same order, as pairwise_body<2, 2> with Fused.
+template <bool T0>
+__device__ __forceinline__ void pair22(float c1, float c2, float a0, float a1, float b0, float b1,
+                                       float p00, float p01, float p10, float p11, float t,
+                                       float d, float omd, float& n1, float& n2, float& dmax) {
+  float o10, o11, o20, o21;
+  decode2(c1, o10, o11);
+  decode2(c2, o20, o21);
+  const float v10 = a0 - o10, v11 = a1 - o11, v20 = b0 - o20, v21 = b1 - o21;
+  const float s00 = ((0.0f + v10) + v20) + p00;
+  const float s01 = ((0.0f + v10) + v21) + p01;
+  const float s10 = ((0.0f + v11) + v20) + p10;
+  const float s11 = ((0.0f + v11) + v21) + p11;
+  const float m10 = fmaxp(fmaxp(-INFINITY, s00), s01);
+  const float m11 = fmaxp(fmaxp(-INFINITY, s10), s11);
+  const float m20 = fmaxp(fmaxp(-INFINITY, s00), s10);
+  const float m21 = fmaxp(fmaxp(-INFINITY, s01), s11);
+  float f10, f11, f20, f21;
+  if (T0) {
+    f10 = m10 - v10;
+    f11 = m11 - v11;
+    f20 = m20 - v20;
+    f21 = m21 - v21;
+  } else {
+    const float e10 = (0.0f + expf((s00 - m10) / t)) + expf((s01 - m10) / t);
+    const float e11 = (0.0f + expf((s10 - m11) / t)) + expf((s11 - m11) / t);
+    const float e20 = (0.0f + expf((s00 - m20) / t)) + expf((s10 - m20) / t);
+    const float e21 = (0.0f + expf((s01 - m21) / t)) + expf((s11 - m21) / t);
+    f10 = (t * logf(e10) + m10) - v10;
+    f11 = (t * logf(e11) + m11) - v11;
+    f20 = (t * logf(e20) + m20) - v20;
+    f21 = (t * logf(e21) + m21) - v21;
+  }
+  {
+    const float q0 = d * o10 + omd * f10, q1 = d * o11 + omd * f11;
+    const float m = fmaxp(fmaxp(-INFINITY, q0), q1);
+    const float w0 = fmaxp(q0 - m, kMsgNegInf), w1 = fmaxp(q1 - m, kMsgNegInf);
+    n1 = encode2(w0, w1);
+    dmax = fmaxp(dmax, fabsf(w0 - o10));
+    dmax = fmaxp(dmax, fabsf(w1 - o11));
+  }
+  {
+    const float q0 = d * o20 + omd * f20, q1 = d * o21 + omd * f21;
+    const float m = fmaxp(fmaxp(-INFINITY, q0), q1);
+    const float w0 = fmaxp(q0 - m, kMsgNegInf), w1 = fmaxp(q1 - m, kMsgNegInf);
+    n2 = encode2(w0, w1);
+    dmax = fmaxp(dmax, fabsf(w0 - o20));
+    dmax = fmaxp(dmax, fabsf(w1 - o21));
+  }
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+template <bool T0>
+__global__ void __launch_bounds__(256) pairwise22_x4_kernel(Fused c, PairwiseDev p, float t,
+                                                            unsigned* deltas) {
+  const int64_t B = c.B;
+  const Lane4 l = lane4(B);
+  float4 dm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (l.valid) {
+    const int64_t b = l.b;
+    for (int64_t u = l.u0; u < p.count; u += l.ustep) {
+      const int4 q = __ldg(p.rec + u);
+      const int64_t k0 = __ldg(p.cfg_begin + u);
+      const float4 c1 = ld4(c.cur + (int64_t)q.y * B + b);
+      const float4 c2 = ld4(c.cur + ((int64_t)q.y + 1) * B + b);
+      const float4 a0 = ld4(c.vsum + (int64_t)q.z * B + b);
+      const float4 a1 = ld4(c.vsum + ((int64_t)q.z + 1) * B + b);
+      const float4 b0 = ld4(c.vsum + (int64_t)q.w * B + b);
+      const float4 b1 = ld4(c.vsum + ((int64_t)q.w + 1) * B + b);
+      float4 p00, p01, p10, p11;
+      if (c.lpb == 0) {
+        float4 pp;
+        if ((k0 & 3) == 0) {  // 16-byte aligned table: one vector load
+          pp = __ldg(reinterpret_cast<const float4*>(c.lp + k0));
+        } else {
+          pp = make_float4(__ldg(c.lp + k0), __ldg(c.lp + k0 + 1), __ldg(c.lp + k0 + 2),
+                           __ldg(c.lp + k0 + 3));
+        }
+        p00 = make_float4(pp.x, pp.x, pp.x, pp.x);
+        p01 = make_float4(pp.y, pp.y, pp.y, pp.y);
+        p10 = make_float4(pp.z, pp.z, pp.z, pp.z);
+        p11 = make_float4(pp.w, pp.w, pp.w, pp.w);
+      } else {
+        p00 = ld4(c.lp + k0 * B + b);
+        p01 = ld4(c.lp + (k0 + 1) * B + b);
+        p10 = ld4(c.lp + (k0 + 2) * B + b);
+        p11 = ld4(c.lp + (k0 + 3) * B + b);
+      }
+      float4 n1, n2;
+      pair22<T0>(c1.x, c2.x, a0.x, a1.x, b0.x, b1.x, p00.x, p01.x, p10.x, p11.x, t, c.d, c.omd,
+                 n1.x, n2.x, dm.x);
+      pair22<T0>(c1.y, c2.y, a0.y, a1.y, b0.y, b1.y, p00.y, p01.y, p10.y, p11.y, t, c.d, c.omd,
+                 n1.y, n2.y, dm.y);
+      pair22<T0>(c1.z, c2.z, a0.z, a1.z, b0.z, b1.z, p00.z, p01.z, p10.z, p11.z, t, c.d, c.omd,
+                 n1.z, n2.z, dm.z);
+      pair22<T0>(c1.w, c2.w, a0.w, a1.w, b0.w, b1.w, p00.w, p01.w, p10.w, p11.w, t, c.d, c.omd,
+                 n1.w, n2.w, dm.w);
+      st4(c.nxt + (int64_t)q.y * B + b, n1);
+      st4(c.nxt + ((int64_t)q.y + 1) * B + b, n2);
+    }
+  }
+  block_max4_to(deltas, l, dm);
+}
+
+// Binary variable sums, 4 instances per thread, sixteen slots in flight.
+__global__ void __launch_bounds__(256) varsum_binary_x4_kernel(
+    const int32_t* __restrict__ vs, const int32_t* __restrict__ off,
+    const int32_t* __restrict__ slots, int64_t n, const float* __restrict__ msgs,
+    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum, int64_t B) {
+  const Lane4 l = lane4(B);
+  if (!l.valid) return;
+  const int64_t b = l.b;
+  const float* col = msgs + b;
+  for (int64_t u = l.u0; u < n; u += l.ustep) {
+    const int64_t v0 = vs[u];
+    float4 s0, s1;
+    if (evb == 0) {
+      const float e0 = ev[v0 * evs], e1 = ev[(v0 + 1) * evs];
+      s0 = make_float4(e0, e0, e0, e0);
+      s1 = make_float4(e1, e1, e1, e1);
+    } else {
+      s0 = ld4(ev + v0 * evs + b);
+      s1 = ld4(ev + (v0 + 1) * evs + b);
+    }
+    const int32_t k1 = off[u + 1];
+    int32_t k = off[u];
+    auto add = [&](float4 c4) {
+      float m0, m1;
+      decode2(c4.x, m0, m1);
+      s0.x += m0;
+      s1.x += m1;
+      decode2(c4.y, m0, m1);
+      s0.y += m0;
+      s1.y += m1;
+      decode2(c4.z, m0, m1);
+      s0.z += m0;
+      s1.z += m1;
+      decode2(c4.w, m0, m1);
+      s0.w += m0;
+      s1.w += m1;
+    };
+    for (; k + 16 <= k1; k += 16) {
+      float4 c4[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) c4[q] = ld4(col + (int64_t)__ldg(slots + k + q) * B);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) add(c4[q]);
+    }
+    for (; k < k1; ++k) add(ld4(col + (int64_t)__ldg(slots + k) * B));
+    st4(vsum + v0 * B + b, s0);
+    st4(vsum + (v0 + 1) * B + b, s1);
+  }
+}
+
 // ----------------------------------------------------------------------------- variable sums
-// var_sums = evidence.at[var_states_for_edge_states].add(msgs) (bp.py:217), serial per var state.
-__global__ void __launch_bounds__(256) varsum_kernel(const int32_t* __restrict__ vs_off,
-                                                     const int32_t* __restrict__ vs_edges, int64_t nvs,
-                                                     const float* __restrict__ msgs,
-                                                     const float* __restrict__ ev, int64_t evs,
-                                                     int64_t evb, float* __restrict__ vsum, int64_t B) {
+// var_sums = evidence.at[var_states_for_edge_states].add(msgs) (bp.py:217): serial per variable
+// state over its edge states in increasing order. Binary variables read one compressed slot per
+// edge and accumulate both states; eight slots are loaded before they are added.
+__global__ void __launch_bounds__(256) varsum_binary_kernel(
+    const int32_t* __restrict__ vs, const int32_t* __restrict__ off,
+    const int32_t* __restrict__ slots, int64_t n, const float* __restrict__ msgs,
+    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum, int64_t B) {
   const Lane l = lane(B);
   if (!l.valid) return;
   const int64_t b = l.b;
-  for (int64_t u = l.u0; u < nvs; u += l.ustep) {
-    float s = ev[u * evs + b * evb];
-    const int32_t k1 = vs_off[u + 1];
-    int32_t k = vs_off[u];
-    for (; k + 4 <= k1; k += 4) {
-      const float m0 = msgs[(int64_t)__ldg(vs_edges + k) * B + b];
-      const float m1 = msgs[(int64_t)__ldg(vs_edges + k + 1) * B + b];
-      const float m2 = msgs[(int64_t)__ldg(vs_edges + k + 2) * B + b];
-      const float m3 = msgs[(int64_t)__ldg(vs_edges + k + 3) * B + b];
-      s += m0;
-      s += m1;
-      s += m2;
-      s += m3;
+  const float* col = msgs + b;
+  for (int64_t u = l.u0; u < n; u += l.ustep) {
+    const int64_t v0 = vs[u];
+    float s0 = ev[v0 * evs + b * evb];
+    float s1 = ev[(v0 + 1) * evs + b * evb];
+    const int32_t k1 = off[u + 1];
+    int32_t k = off[u];
+    for (; k + 8 <= k1; k += 8) {
+      float c[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) c[q] = col[(int64_t)__ldg(slots + k + q) * B];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float m0, m1;
+        decode2(c[q], m0, m1);
+        s0 += m0;
+        s1 += m1;
+      }
     }
-    for (; k < k1; ++k) s += msgs[(int64_t)__ldg(vs_edges + k) * B + b];
-    vsum[u * B + b] = s;
+    for (; k < k1; ++k) {
+      float m0, m1;
+      decode2(col[(int64_t)__ldg(slots + k) * B], m0, m1);
+      s0 += m0;
+      s1 += m1;
+    }
+    vsum[v0 * B + b] = s0;
+    vsum[(v0 + 1) * B + b] = s1;
+  }
+}
+
+__global__ void __launch_bounds__(256) varsum_other_kernel(
+    const int32_t* __restrict__ vs, const int32_t* __restrict__ off,
+    const int32_t* __restrict__ slots, int64_t n, const float* __restrict__ msgs,
+    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum, int64_t B) {
+  const Lane l = lane(B);
+  if (!l.valid) return;
+  const int64_t b = l.b;
+  const float* col = msgs + b;
+  for (int64_t u = l.u0; u < n; u += l.ustep) {
+    const int64_t v = vs[u];
+    float s = ev[v * evs + b * evb];
+    const int32_t k1 = off[u + 1];
+    int32_t k = off[u];
+    for (; k + 8 <= k1; k += 8) {
+      float c[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) c[q] = col[(int64_t)__ldg(slots + k + q) * B];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s += c[q];
+    }
+    for (; k < k1; ++k) s += col[(int64_t)__ldg(slots + k) * B];
+    vsum[v * B + b] = s;
   }
 }
 
 // Flat beliefs from caller-layout arrays ([B, n] rows): inferer.py:218-222.
 __global__ void __launch_bounds__(256) beliefs_kernel(const int32_t* __restrict__ vs_off,
-                                                      const int32_t* __restrict__ vs_edges, int64_t nvs,
-                                                      const float* __restrict__ msgs, int64_t ms,
-                                                      const float* __restrict__ ev, int64_t evs,
-                                                      float* __restrict__ out, int64_t B) {
+                                                      const int32_t* __restrict__ vs_edges,
+                                                      int64_t nvs, const float* __restrict__ msgs,
+                                                      int64_t ms, const float* __restrict__ ev,
+                                                      int64_t evs, float* __restrict__ out,
+                                                      int64_t B) {
   const Lane l = lane(B);
   if (!l.valid) return;
   const int64_t b = l.b;
@@ -526,25 +867,57 @@ __global__ void __launch_bounds__(256) beliefs_kernel(const int32_t* __restrict_
 }
 
 // ----------------------------------------------------------------------------- layout / misc
-// normalize_and_clip_msgs (bp.py:222-260) in the run layout, one (edge, instance) per thread.
-__global__ void __launch_bounds__(256) normalize_kernel(const int32_t* __restrict__ edge_start,
-                                                        int64_t ne, float* __restrict__ msgs, int64_t B) {
+// normalize_and_clip_msgs (bp.py:222-260) of the caller's initial messages (already transposed to
+// edge-state-major, `src`), packed into slots (`dst`), one (edge, instance) per thread.
+__global__ void __launch_bounds__(256) normalize_pack_kernel(const int32_t* __restrict__ edge_start,
+                                                             const int32_t* __restrict__ edge_slot,
+                                                             int64_t ne,
+                                                             const float* __restrict__ src,
+                                                             float* __restrict__ dst, int64_t B) {
   const Lane l = lane(B);
   if (!l.valid) return;
   const int64_t b = l.b;
   for (int64_t u = l.u0; u < ne; u += l.ustep) {
-    const int64_t s0 = edge_start[u], s1 = edge_start[u + 1];
+    const int64_t s0 = edge_start[u], k = edge_start[u + 1] - s0, slot = edge_slot[u];
     float m = -INFINITY;
-    for (int64_t e = s0; e < s1; ++e) m = fmaxp(m, msgs[e * B + b]);
-    for (int64_t e = s0; e < s1; ++e) msgs[e * B + b] = fmaxp(msgs[e * B + b] - m, kMsgNegInf);
+    for (int64_t i = 0; i < k; ++i) m = fmaxp(m, src[(s0 + i) * B + b]);
+    if (k == 2) {
+      const float v0 = fmaxp(src[s0 * B + b] - m, kMsgNegInf);
+      const float v1 = fmaxp(src[(s0 + 1) * B + b] - m, kMsgNegInf);
+      dst[slot * B + b] = encode2(v0, v1);
+    } else {
+      for (int64_t i = 0; i < k; ++i)
+        dst[(slot + i) * B + b] = fmaxp(src[(s0 + i) * B + b] - m, kMsgNegInf);
+    }
+  }
+}
+
+// slots -> edge-state-major messages.
+__global__ void __launch_bounds__(256) unpack_kernel(const int32_t* __restrict__ edge_start,
+                                                     const int32_t* __restrict__ edge_slot,
+                                                     int64_t ne, const float* __restrict__ src,
+                                                     float* __restrict__ dst, int64_t B) {
+  const Lane l = lane(B);
+  if (!l.valid) return;
+  const int64_t b = l.b;
+  for (int64_t u = l.u0; u < ne; u += l.ustep) {
+    const int64_t s0 = edge_start[u], k = edge_start[u + 1] - s0, slot = edge_slot[u];
+    if (k == 2) {
+      float m0, m1;
+      decode2(src[slot * B + b], m0, m1);
+      dst[s0 * B + b] = m0;
+      dst[(s0 + 1) * B + b] = m1;
+    } else {
+      for (int64_t i = 0; i < k; ++i) dst[(s0 + i) * B + b] = src[(slot + i) * B + b];
+    }
   }
 }
 
 __device__ __forceinline__ float clip_lp(float x) { return fminp(fmaxp(x, -kLpMaxAbs), kLpMaxAbs); }
 
 // dst[i * B + b] = src[b * sstride + i] for i < n, b < B (optionally clipped), via 32x32 tiles.
-__global__ void to_inner_kernel(const float* __restrict__ src, int64_t sstride, int64_t n, int64_t B,
-                                float* __restrict__ dst, int clip) {
+__global__ void to_inner_kernel(const float* __restrict__ src, int64_t sstride, int64_t n,
+                                int64_t B, float* __restrict__ dst, int clip) {
   __shared__ float tile[32][33];
   const int64_t i0 = (int64_t)blockIdx.x * 32, b0 = (int64_t)blockIdx.y * 32;
   for (int r = threadIdx.y; r < 32; r += blockDim.y) {
@@ -686,16 +1059,19 @@ void to_outer(cudaStream_t s, const float* src, int64_t n, int64_t B, float* dst
 }
 
 PairwiseDev dev(const PairwiseBucket& q) {
-  return PairwiseDev{q.es_begin, q.cfg_begin, q.count, q.n1, q.n2};
+  return PairwiseDev{q.rec, q.cfg_begin, q.count, q.n1, q.n2};
 }
 EnumGenericDev dev(const EnumGeneric& g) {
-  return EnumGenericDev{g.es_begin, g.n_es,  g.edge_off, g.edge_size, g.row_begin,
-                        g.n_cfg,    g.n_vars, g.cfg_begin, g.row_les,   g.count};
+  return EnumGenericDev{g.es_begin,  g.n_es,  g.edge_off, g.edge_size, g.edge_slot, g.edge_vs,
+                        g.row_begin, g.n_cfg, g.n_vars,   g.cfg_begin, g.row_les,   g.count};
 }
 LogicalDev dev(const LogicalSet& g) {
-  return LogicalDev{g.par_begin, g.par_es, g.child_es, g.count, g.off};
+  return LogicalDev{g.par_begin, g.par, g.child, g.count, g.off};
 }
-PoolDev dev(const PoolSet& g) { return PoolDev{g.ch_begin, g.ch_es, g.ind_es, g.count}; }
+PoolDev dev(const PoolSet& g) { return PoolDev{g.ch_begin, g.ch, g.ind, g.count}; }
+
+// x4 launch: lanes over groups of 4 instances.
+Launch2 launch2_x4(int64_t units, int64_t B, int sm_count) { return launch2(units, B / 4, sm_count); }
 
 template <bool T0, class C>
 void launch_pairwise(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const C& c, int64_t B,
@@ -754,22 +1130,48 @@ void launch_pool(cudaStream_t s, const Plan& p, const C& c, int64_t B, float t, 
   pool_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(g), B, t, normalize, deltas);
 }
 
+void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, const float* ev,
+                   int64_t evs, int64_t evb, float* vsum) {
+  ProfileScope ps(kProfVarsum, s);
+  if (p.varsum_binary.count > 0 && B % 4 == 0) {
+    const VarsumSet& v = p.varsum_binary;
+    const Launch2 l = launch2_x4(v.count, B, p.sm_count);
+    varsum_binary_x4_kernel<<<l.grid, l.block, 0, s>>>(v.vs, v.off, v.slots, v.count, cur, ev, evs,
+                                                        evb, vsum, B);
+  } else if (p.varsum_binary.count > 0) {
+    const VarsumSet& v = p.varsum_binary;
+    const Launch2 l = launch2(v.count, B, p.sm_count);
+    varsum_binary_kernel<<<l.grid, l.block, 0, s>>>(v.vs, v.off, v.slots, v.count, cur, ev, evs,
+                                                     evb, vsum, B);
+  }
+  if (p.varsum_other.count > 0) {
+    const VarsumSet& v = p.varsum_other;
+    const Launch2 l = launch2(v.count, B, p.sm_count);
+    varsum_other_kernel<<<l.grid, l.block, 0, s>>>(v.vs, v.off, v.slots, v.count, cur, ev, evs,
+                                                    evb, vsum, B);
+  }
+}
+
 template <bool T0>
 void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool low_t, int64_t iters,
-             float* msgs0, float* msgs1, const float* ev, int64_t evs, int64_t evb, unsigned* dacc) {
-  const Launch2 lv = launch2(p.num_var_states, B, p.sm_count);
+             float* msgs0, float* msgs1, const float* ev, int64_t evs, int64_t evb,
+             unsigned* dacc) {
   for (int64_t it = 0; it < iters; ++it) {
     float* cur = (it & 1) ? msgs1 : msgs0;
     float* nxt = (it & 1) ? msgs0 : msgs1;
     c.cur = cur;
     c.nxt = nxt;
     unsigned* d = dacc + it * B;
-    if (p.num_var_states > 0) {
-      ProfileScope ps(kProfVarsum, s);
-      varsum_kernel<<<lv.grid, lv.block, 0, s>>>(p.vs_off, p.vs_edges, p.num_var_states, cur, ev,
-                                                 evs, evb, const_cast<float*>(c.vsum), B);
+    launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum));
+    for (const PairwiseBucket& q : p.pairwise) {
+      if (q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0) {
+        ProfileScope ps(kProfPairwise, s);
+        const Launch2 l = launch2_x4(q.count, B, p.sm_count);
+        pairwise22_x4_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(q), t, d);
+      } else {
+        launch_pairwise<T0>(s, p, q, c, B, t, d);
+      }
     }
-    for (const PairwiseBucket& q : p.pairwise) launch_pairwise<T0>(s, p, q, c, B, t, d);
     launch_enum_generic<T0>(s, p, c, B, t, d);
     launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d);
     launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d);
@@ -781,12 +1183,14 @@ size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
 
-size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched, bool lp_batched) {
+size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched,
+                       bool lp_batched) {
   const int64_t B = std::max<int64_t>(batch, 1);
   const int64_t it = std::max<int64_t>(iters, 1);
   size_t n = 0;
-  n += 2 * align_up(sizeof(float) * (size_t)(p.num_edge_states * B));
-  n += align_up(sizeof(float) * (size_t)(p.num_var_states * B));
+  n += 2 * align_up(sizeof(float) * (size_t)(p.num_slots * B));   // slots, ping-pong
+  n += align_up(sizeof(float) * (size_t)(p.num_edge_states * B));  // edge-state-major in / out
+  n += align_up(sizeof(float) * (size_t)(p.num_var_states * B));   // variable sums
   if (ev_batched) n += align_up(sizeof(float) * (size_t)(p.num_var_states * B));
   n += align_up(sizeof(float) * (size_t)(p.num_potentials * (lp_batched ? B : 1)));
   n += align_up(sizeof(unsigned) * (size_t)(it * B));
@@ -805,8 +1209,9 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     w += align_up(bytes);
     return r;
   };
-  float* m0 = (float*)take(sizeof(float) * (size_t)(p.num_edge_states * B));
-  float* m1 = (float*)take(sizeof(float) * (size_t)(p.num_edge_states * B));
+  float* m0 = (float*)take(sizeof(float) * (size_t)(p.num_slots * B));
+  float* m1 = (float*)take(sizeof(float) * (size_t)(p.num_slots * B));
+  float* tmp = (float*)take(sizeof(float) * (size_t)(p.num_edge_states * B));
   float* vsum = (float*)take(sizeof(float) * (size_t)(p.num_var_states * B));
   float* evt = ev_b ? (float*)take(sizeof(float) * (size_t)(p.num_var_states * B)) : nullptr;
   float* lpc = (float*)take(sizeof(float) * (size_t)(p.num_potentials * (lp_b ? B : 1)));
@@ -830,16 +1235,17 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
       lpb = 1;
     } else {
       ProfileScope ps(kProfLayout, s);
-      copy_clip_kernel<<<flat_grid(p.num_potentials, p.sm_count), 256, 0, s>>>(lp, p.num_potentials,
-                                                                               lpc, 1);
+      copy_clip_kernel<<<flat_grid(p.num_potentials, p.sm_count), 256, 0, s>>>(
+          lp, p.num_potentials, lpc, 1);
     }
   }
-  // initial messages, normalised and clipped (bp.py:92-96)
-  to_inner(s, msgs_in, msgs_stride, p.num_edge_states, B, m0, false, p.sm_count);
+  // initial messages, normalised and clipped (bp.py:92-96), packed into slots
+  to_inner(s, msgs_in, msgs_stride, p.num_edge_states, B, tmp, false, p.sm_count);
   if (p.num_edges > 0) {
     ProfileScope ps(kProfLayout, s);
     const Launch2 ln = launch2(p.num_edges, B, p.sm_count);
-    normalize_kernel<<<ln.grid, ln.block, 0, s>>>(p.edge_start, p.num_edges, m0, B);
+    normalize_pack_kernel<<<ln.grid, ln.block, 0, s>>>(p.edge_start, p.edge_slot, p.num_edges,
+                                                        tmp, m0, B);
   }
   cudaMemsetAsync(dacc, 0, sizeof(unsigned) * (size_t)(iters * B), s);
 
@@ -847,7 +1253,6 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   c.cur = m0;
   c.nxt = m1;
   c.vsum = vsum;
-  c.vs_of_es = p.vs_of_es;
   c.lp = lpc;
   c.lps = lps;
   c.lpb = lpb;
@@ -862,7 +1267,13 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     iterate<false>(s, p, B, c, t, low_t, iters, m0, m1, evp, evs, evb, dacc);
   }
   float* fin = (iters & 1) ? m1 : m0;
-  to_outer(s, fin, p.num_edge_states, B, msgs_out, p.num_edge_states, p.sm_count);
+  if (p.num_edges > 0) {
+    ProfileScope ps(kProfLayout, s);
+    const Launch2 ln = launch2(p.num_edges, B, p.sm_count);
+    unpack_kernel<<<ln.grid, ln.block, 0, s>>>(p.edge_start, p.edge_slot, p.num_edges, fin, tmp,
+                                                B);
+  }
+  to_outer(s, tmp, p.num_edge_states, B, msgs_out, p.num_edge_states, p.sm_count);
   if (deltas != nullptr) {
     ProfileScope ps(kProfLayout, s);
     deltas_out_kernel<<<flat_grid(iters * B, p.sm_count), 256, 0, s>>>(dacc, iters, B, deltas);
@@ -871,8 +1282,8 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
 }
 
 cudaError_t factor_update(const Plan& p, cudaStream_t s, int type, int64_t B, const float* vtof,
-                          int64_t vtof_stride, const float* lp, int64_t lp_stride, double temperature,
-                          int normalize, float* out, int64_t out_stride) {
+                          int64_t vtof_stride, const float* lp, int64_t lp_stride,
+                          double temperature, int normalize, float* out, int64_t out_stride) {
   Update c;
   c.vt = vtof;
   c.vts = vtof_stride;
@@ -907,8 +1318,8 @@ cudaError_t beliefs(const Plan& p, cudaStream_t s, int64_t B, const float* ev, i
   if (p.num_var_states == 0) return cudaSuccess;
   ProfileScope ps(kProfReadout, s);
   const Launch2 l = launch2(p.num_var_states, B, p.sm_count);
-  beliefs_kernel<<<l.grid, l.block, 0, s>>>(p.vs_off, p.vs_edges, p.num_var_states, msgs, msgs_stride,
-                                            ev, ev_stride, out, B);
+  beliefs_kernel<<<l.grid, l.block, 0, s>>>(p.vs_off, p.vs_edges, p.num_var_states, msgs,
+                                            msgs_stride, ev, ev_stride, out, B);
   return cudaGetLastError();
 }
 
@@ -916,8 +1327,8 @@ cudaError_t decode(const Plan& p, cudaStream_t s, int64_t B, const float* bel, i
                    int32_t* map) {
   if (p.num_variables == 0) return cudaSuccess;
   ProfileScope ps(kProfReadout, s);
-  decode_kernel<<<flat_grid(p.num_variables * B, p.sm_count), 256, 0, s>>>(p.var_off, p.num_variables,
-                                                                           bel, stride, map, B);
+  decode_kernel<<<flat_grid(p.num_variables * B, p.sm_count), 256, 0, s>>>(
+      p.var_off, p.num_variables, bel, stride, map, B);
   return cudaGetLastError();
 }
 

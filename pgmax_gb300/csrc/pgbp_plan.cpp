@@ -253,12 +253,73 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   }
   auto factor_of = [&](int64_t es) { return (int64_t)fi[es]; };
 
+  // --- slots: one per binary edge (compressed pair), one per state otherwise; edge order
+  std::vector<int32_t> edge_slot(ne + 1, 0);
+  for (int64_t e = 0; e < ne; ++e) {
+    const int32_t k = edge_start[e + 1] - edge_start[e];
+    edge_slot[e + 1] = edge_slot[e] + (k == 2 ? 1 : k);
+  }
+  p.num_slots = edge_slot[ne];
+  auto slot_of_es = [&](int64_t es) {  // slot holding edge state es (binary: the edge's slot)
+    const int32_t e = ei[es];
+    const int32_t k = edge_start[e + 1] - edge_start[e];
+    return k == 2 ? edge_slot[e] : edge_slot[e] + (int32_t)(es - edge_start[e]);
+  };
+
+  // --- variable sums: binary variables (per variable, both states) and other variable states,
+  // each listing the slots of its edges in increasing edge order (= increasing edge state)
+  std::vector<int32_t> vb_vs, vb_off{0}, vb_slots, vo_vs, vo_off{0}, vo_slots;
+  {
+    std::vector<char> binary_vs(nvs, 0);  // 1: state 0 of a binary variable, 2: its state 1
+    for (int64_t e = 0; e < ne; ++e) {
+      if (edge_start[e + 1] - edge_start[e] == 2) {
+        const int32_t v0 = vs[edge_start[e]];
+        if (vs[edge_start[e] + 1] != v0 + 1)
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "states of an edge must be consecutive"));
+        binary_vs[v0] = 1;
+        binary_vs[v0 + 1] = 2;
+      }
+    }
+    for (int64_t v = 0; v < nvs; ++v) {
+      if (vs_off[v + 1] == vs_off[v]) continue;  // no edge: its sum is never read
+      if (binary_vs[v] == 1) {
+        // both states of a binary variable see the same edges (one state each)
+        if (vs_off[v + 2] - vs_off[v + 1] != vs_off[v + 1] - vs_off[v])
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "binary variable states with different edges"));
+        vb_vs.push_back((int32_t)v);
+        for (int32_t k = vs_off[v]; k < vs_off[v + 1]; ++k) {
+          const int64_t es = vs_edges[k];
+          if (vs_edges[vs_off[v + 1] + (k - vs_off[v])] != es + 1)
+            return bail(fail(PGBP_ERR_INVALID_WIRING, "binary variable edges are not paired"));
+          vb_slots.push_back(slot_of_es(es));
+        }
+        vb_off.push_back((int32_t)vb_slots.size());
+      } else if (binary_vs[v] == 0) {
+        vo_vs.push_back((int32_t)v);
+        for (int32_t k = vs_off[v]; k < vs_off[v + 1]; ++k) vo_slots.push_back(slot_of_es(vs_edges[k]));
+        vo_off.push_back((int32_t)vo_slots.size());
+      }
+    }
+  }
+
   Builder bd{p};
   p.vs_off = bd.upload(vs_off);
   p.vs_edges = bd.upload(vs_edges);
-  p.vs_of_es = bd.upload(std::vector<int32_t>(vs, vs + ns));
   p.edge_start = bd.upload(edge_start);
+  p.edge_slot = bd.upload(edge_slot);
+  p.varsum_binary.count = (int64_t)vb_vs.size();
+  p.varsum_binary.vs = bd.upload(vb_vs);
+  p.varsum_binary.off = bd.upload(vb_off);
+  p.varsum_binary.slots = bd.upload(vb_slots);
+  p.varsum_other.count = (int64_t)vo_vs.size();
+  p.varsum_other.vs = bd.upload(vo_vs);
+  p.varsum_other.off = bd.upload(vo_off);
+  p.varsum_other.slots = bd.upload(vo_slots);
   if (bd.err) return bail(bd.err);
+  auto edge_rec = [&](int64_t es0) {  // (first edge state, first slot, first var state, 0)
+    const int32_t e = ei[es0];
+    return make_int4((int32_t)es0, edge_slot[e], vs[es0], 0);
+  };
 
   // --- Enum factors
   {
@@ -292,8 +353,9 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       if (r != nrows)
         return bail(fail(PGBP_ERR_UNSUPPORTED, "enum config rows are not grouped by factor"));
     }
-    std::map<std::pair<int, int>, std::pair<std::vector<int32_t>, std::vector<int32_t>>> buckets;
-    std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_rb, g_ncfg, g_nv, g_cfg, g_les;
+    std::map<std::pair<int, int>, std::pair<std::vector<int4>, std::vector<int32_t>>> buckets;
+    std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_eslot, g_evs, g_rb, g_ncfg, g_nv, g_cfg,
+        g_les;
     int max_es = 0;
     for (size_t k = 0; k < facs.size(); ++k) {
       const int64_t f = facs[k];
@@ -337,13 +399,19 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       }
       if (dense) {
         auto& bk = buckets[{esz[0], esz[1]}];
-        bk.first.push_back((int32_t)fb);
+        const int4 r0 = edge_rec(fb);
+        bk.first.push_back(make_int4(r0.x, r0.y, r0.z, vs[fb + esz[0]]));
         bk.second.push_back((int32_t)(pot0 + cfg0));
       } else {
         g_es.push_back((int32_t)fb);
         g_nes.push_back((int32_t)(fe - fb));
         max_es = std::max<int>(max_es, (int)(fe - fb));
-        for (int j = 0; j < nv; ++j) g_esz.push_back(esz[j]);
+        for (int j = 0; j < nv; ++j) {
+          const int4 r = edge_rec(fb + estart[j]);
+          g_esz.push_back(esz[j]);
+          g_eslot.push_back(r.y);
+          g_evs.push_back(r.z);
+        }
         g_eoff.push_back((int32_t)g_esz.size());
         g_rb.push_back((int32_t)g_les.size());
         g_les.insert(g_les.end(), les.begin(), les.end());
@@ -360,7 +428,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       q.n1 = kv.first.first;
       q.n2 = kv.first.second;
       q.count = (int64_t)kv.second.first.size();
-      q.es_begin = bd.upload(kv.second.first);
+      q.rec = bd.upload(kv.second.first);
       q.cfg_begin = bd.upload(kv.second.second);
       p.num_enum_pairwise += q.count;
       p.pairwise.push_back(q);
@@ -373,6 +441,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       g.n_es = bd.upload(g_nes);
       g.edge_off = bd.upload(g_eoff);
       g.edge_size = bd.upload(g_esz);
+      g.edge_slot = bd.upload(g_eslot);
+      g.edge_vs = bd.upload(g_evs);
       g.row_begin = bd.upload(g_rb);
       g.n_cfg = bd.upload(g_ncfg);
       g.n_vars = bd.upload(g_nv);
@@ -394,7 +464,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     if (F == 0 && P == 0) continue;
     if (F <= 0 || P <= 0 || !pfi || !pmi || !ch)
       return bail(fail(PGBP_ERR_INVALID_WIRING, "logical factors without parents or children"));
-    std::vector<int32_t> pb(F + 1, 0), pes(P), ces(F);
+    std::vector<int32_t> pb(F + 1, 0);
+    std::vector<int4> pes(P), ces(F);
     int64_t cur = -1;
     for (int64_t i = 0; i < P; ++i) {
       if (!in_range(pfi[i], 0, F))
@@ -409,23 +480,24 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       if (!in_range(e, m0, m1) || !in_range(e + off, m0, m1) || ei[e] != ei[e + off] ||
           edge_start[ei[e] + 1] - edge_start[ei[e]] != 2)
         return bail(fail(PGBP_ERR_INVALID_WIRING, "logical parent message index out of range"));
-      pes[i] = (int32_t)e;
+      pes[i] = edge_rec(std::min<int64_t>(e, e + off));
     }
     if (cur != F - 1) return bail(fail(PGBP_ERR_INVALID_WIRING, "a logical factor has no parent"));
     pb[F] = (int32_t)P;
     for (int64_t f = 0; f < F; ++f) {
       const int64_t e = m0 + ch[f];
-      if (!in_range(e, m0, m1) || !in_range(e + off, m0, m1) || ei[e] != ei[e + off])
+      if (!in_range(e, m0, m1) || !in_range(e + off, m0, m1) || ei[e] != ei[e + off] ||
+          edge_start[ei[e] + 1] - edge_start[ei[e]] != 2)
         return bail(fail(PGBP_ERR_INVALID_WIRING, "logical child edge state out of range"));
-      ces[f] = (int32_t)e;
+      ces[f] = edge_rec(std::min<int64_t>(e, e + off));
     }
     pgbp::LogicalSet& g = p.logical[w];
     g.count = F;
     g.num_parents = P;
     g.off = off;
     g.par_begin = bd.upload(pb);
-    g.par_es = bd.upload(pes);
-    g.child_es = bd.upload(ces);
+    g.par = bd.upload(pes);
+    g.child = bd.upload(ces);
     if (bd.err) return bail(bd.err);
   }
 
@@ -439,7 +511,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     if (F > 0 || P > 0) {
       if (F <= 0 || P <= 0 || !cfi || !cmi || !ind)
         return bail(fail(PGBP_ERR_INVALID_WIRING, "pool factors without choices or indicators"));
-      std::vector<int32_t> cb(F + 1, 0), ces(P), ies(F);
+      std::vector<int32_t> cb(F + 1, 0);
+      std::vector<int4> ces(P), ies(F);
       int64_t cur = -1;
       for (int64_t i = 0; i < P; ++i) {
         if (!in_range(cfi[i], 0, F))
@@ -451,24 +524,26 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
           cb[cur] = (int32_t)i;
         }
         const int64_t e = m0 + cmi[i];
-        if (!in_range(e, m0, m1) || !in_range(e + 1, m0, m1) || ei[e] != ei[e + 1])
+        if (!in_range(e, m0, m1) || !in_range(e + 1, m0, m1) || ei[e] != ei[e + 1] ||
+            edge_start[ei[e] + 1] - edge_start[ei[e]] != 2)
           return bail(fail(PGBP_ERR_INVALID_WIRING, "pool choice message index out of range"));
-        ces[i] = (int32_t)e;
+        ces[i] = edge_rec(e);
       }
       if (cur != F - 1) return bail(fail(PGBP_ERR_INVALID_WIRING, "a pool factor has no choice"));
       cb[F] = (int32_t)P;
       for (int64_t f = 0; f < F; ++f) {
         const int64_t e = m0 + ind[f];
-        if (!in_range(e, m0, m1) || !in_range(e + 1, m0, m1) || ei[e] != ei[e + 1])
+        if (!in_range(e, m0, m1) || !in_range(e + 1, m0, m1) || ei[e] != ei[e + 1] ||
+            edge_start[ei[e] + 1] - edge_start[ei[e]] != 2)
           return bail(fail(PGBP_ERR_INVALID_WIRING, "pool indicator edge state out of range"));
-        ies[f] = (int32_t)e;
+        ies[f] = edge_rec(e);
       }
       pgbp::PoolSet& g = p.pool;
       g.count = F;
       g.num_choices = P;
       g.ch_begin = bd.upload(cb);
-      g.ch_es = bd.upload(ces);
-      g.ind_es = bd.upload(ies);
+      g.ch = bd.upload(ces);
+      g.ind = bd.upload(ies);
       if (bd.err) return bail(bd.err);
     }
   }

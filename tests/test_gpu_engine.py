@@ -118,6 +118,32 @@ def test_batched_run_equals_single_instances(name):
         np.testing.assert_allclose(deltas[b], d, atol=PERTURBED_T_POS_ATOL, rtol=0)
 
 
+@pytest.mark.parametrize("name,B", [("case_rbm_s0", 8), ("case_rbm_s1", 12), ("case_ising12_T1", 4),
+                                    ("case_ising50_T0", 16)])
+def test_four_instances_per_thread_path(name, B):
+  """Batches that are a multiple of 4 run the 4-instances-per-thread kernels (binary pairwise
+  factors, binary variable sums); every instance must equal its own oracle run."""
+  f = fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
+  plan = _plan(f["wiring"])
+  w = oracle.Wiring(f["wiring"])
+  rng = np.random.default_rng(3)
+  ev = (f["evidence"][None] + rng.gumbel(size=(B,) + f["evidence"].shape)).astype(np.float32)
+  T = float(f["temperature"])
+  lp_b = (f["log_potentials"][None] + 0.05 * rng.normal(size=(B,) + f["log_potentials"].shape)
+          ).astype(np.float32)
+  for lp in (f["log_potentials"], lp_b):
+    out, deltas = plan.run(lp, ev, f["ftov_msgs_in"], 15, 0.5, T)
+    out, deltas = _np(out), _np(deltas)
+    for b in range(B):
+      o, d = oracle.run(w, lp if lp.ndim == 1 else lp[b], ev[b], f["ftov_msgs_in"], 15, 0.5, T)
+      if T == 0.0:
+        np.testing.assert_array_equal(out[b], o)
+        np.testing.assert_array_equal(deltas[b], d)
+      else:
+        np.testing.assert_allclose(out[b], o, atol=ATOL, rtol=0)
+        np.testing.assert_allclose(deltas[b], d, atol=ATOL, rtol=0)
+
+
 def test_runs_are_bitwise_deterministic():
   f = fixtures.load(f"{fixtures.FIXTURES}/case_deconv_T1.npz")
   plan = _plan(f["wiring"])
