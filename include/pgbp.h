@@ -95,6 +95,7 @@ typedef struct {
       num_pool_factors;
   int64_t num_pairwise_buckets;  /* (n1, n2) classes run by the dense pairwise kernel */
   int64_t device_bytes;          /* device memory owned by the plan */
+  int64_t num_slots;             /* message slots per instance: 1 per binary edge, else 1 per state */
 } pgbp_plan_info;
 
 /* Compiles the wiring into device-resident schedules on `device`. Validates every index. */

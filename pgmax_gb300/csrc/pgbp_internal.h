@@ -67,12 +67,18 @@ struct PoolSet {
 };
 
 // Variable sums: binary variables (both states from one compressed slot per edge) and the
-// states of all other variables (one slot per edge), each with its slots in edge order.
+// states of all other variables (one slot per edge), each with its slots in edge order. The slot
+// list of unit u is either explicit (slots[off[u] .. off[u + 1])) or, when the graph is regular
+// enough that lists compress 4:1 or better, affine runs runs[run_off[u] .. run_off[u + 1]) of
+// (first slot, stride, length): a run needs no index load in front of its message loads.
 struct VarsumSet {
   int64_t count = 0;
   int32_t* vs = nullptr;         // [count] variable state (binary: state 0)
+  bool use_runs = false;
   int32_t* off = nullptr;        // [count + 1]
   int32_t* slots = nullptr;
+  int32_t* run_off = nullptr;    // [count + 1]
+  int4* runs = nullptr;          // (first slot, stride, length, 0)
 };
 
 struct Plan {

@@ -71,22 +71,14 @@ __device__ __forceinline__ float logminusexp_t(float a, float b, float t, float 
   return (a >= b + eps) ? v : -INFINITY;
 }
 
-// A normalised binary message (m0, m1) has m0 == +0 or m1 == +0 (or both NaN, since the
-// normalising max propagates NaN to both states). Stored as m1 when m0 == 0 (so <= 0), else as
-// -m0 (> 0); NaN stays NaN. Zero entries of normalised messages are always +0 (x - x is +0 in
-// round-to-nearest and the clip keeps it), so the round trip is exact.
-__device__ __forceinline__ float encode2(float m0, float m1) { return (m0 == 0.0f) ? m1 : -m0; }
+// A normalised binary message (m0, m1) has m0 == 0 or m1 == 0 (or both NaN, since the
+// normalising max propagates NaN to both states), so it is stored as the single float
+// c = m1 - m0 (= m1 <= 0 or -m0 > 0; exact, as one operand is zero) and recovered as
+// m0 = min(-c, 0), m1 = min(c, 0), with NaN staying NaN: the same values, one instruction each.
+__device__ __forceinline__ float encode2(float m0, float m1) { return m1 - m0; }
 __device__ __forceinline__ void decode2(float c, float& m0, float& m1) {
-  if (c != c) {
-    m0 = c;
-    m1 = c;
-  } else if (c <= 0.0f) {
-    m0 = 0.0f;
-    m1 = c;
-  } else {
-    m0 = -c;
-    m1 = 0.0f;
-  }
+  m0 = fminp(-c, 0.0f);
+  m1 = fminp(c, 0.0f);
 }
 
 // ----------------------------------------------------------------------------- launch mapping
@@ -164,7 +156,7 @@ struct Fused {
     if (k == 2) {
       const float n0 = d * old[0] + omd * outv(0);
       const float n1 = d * old[1] + omd * outv(1);
-      const float m = fmaxp(fmaxp(-INFINITY, n0), n1);
+      const float m = fmaxp(n0, n1);  // = max(max(-inf, n0), n1) for every input
       const float v0 = fmaxp(n0 - m, kMsgNegInf);
       const float v1 = fmaxp(n1 - m, kMsgNegInf);
       nxt[r.slot * B + b] = encode2(v0, v1);
@@ -640,10 +632,11 @@ __device__ __forceinline__ void pair22(float c1, float c2, float a0, float a1, f
   const float s01 = ((0.0f + v10) + v21) + p01;
   const float s10 = ((0.0f + v11) + v20) + p10;
   const float s11 = ((0.0f + v11) + v21) + p11;
-  const float m10 = fmaxp(fmaxp(-INFINITY, s00), s01);
-  const float m11 = fmaxp(fmaxp(-INFINITY, s10), s11);
-  const float m20 = fmaxp(fmaxp(-INFINITY, s00), s10);
-  const float m21 = fmaxp(fmaxp(-INFINITY, s01), s11);
+  // max(max(-inf, a), b) == max(a, b) for every input, NaN included
+  const float m10 = fmaxp(s00, s01);
+  const float m11 = fmaxp(s10, s11);
+  const float m20 = fmaxp(s00, s10);
+  const float m21 = fmaxp(s01, s11);
   float f10, f11, f20, f21;
   if (T0) {
     f10 = m10 - v10;
@@ -662,7 +655,7 @@ __device__ __forceinline__ void pair22(float c1, float c2, float a0, float a1, f
   }
   {
     const float q0 = d * o10 + omd * f10, q1 = d * o11 + omd * f11;
-    const float m = fmaxp(fmaxp(-INFINITY, q0), q1);
+    const float m = fmaxp(q0, q1);
     const float w0 = fmaxp(q0 - m, kMsgNegInf), w1 = fmaxp(q1 - m, kMsgNegInf);
     n1 = encode2(w0, w1);
     dmax = fmaxp(dmax, fabsf(w0 - o10));
@@ -670,7 +663,7 @@ __device__ __forceinline__ void pair22(float c1, float c2, float a0, float a1, f
   }
   {
     const float q0 = d * o20 + omd * f20, q1 = d * o21 + omd * f21;
-    const float m = fmaxp(fmaxp(-INFINITY, q0), q1);
+    const float m = fmaxp(q0, q1);
     const float w0 = fmaxp(q0 - m, kMsgNegInf), w1 = fmaxp(q1 - m, kMsgNegInf);
     n2 = encode2(w0, w1);
     dmax = fmaxp(dmax, fabsf(w0 - o20));
@@ -681,6 +674,8 @@ __device__ __forceinline__ void pair22(float c1, float c2, float a0, float a1, f
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
+// Each unit lane walks a contiguous chunk of factors, so consecutive factors that share their
+// first variable (a PairwiseFactorGroup built row by row) reuse its variable sums from registers.
 template <bool T0>
 __global__ void __launch_bounds__(256) pairwise22_x4_kernel(Fused c, PairwiseDev p, float t,
                                                             unsigned* deltas) {
@@ -689,13 +684,21 @@ __global__ void __launch_bounds__(256) pairwise22_x4_kernel(Fused c, PairwiseDev
   float4 dm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (l.valid) {
     const int64_t b = l.b;
-    for (int64_t u = l.u0; u < p.count; u += l.ustep) {
+    const int64_t chunk = (p.count + l.ustep - 1) / l.ustep;
+    const int64_t u_begin = l.u0 * chunk;
+    const int64_t u_end = u_begin + chunk < p.count ? u_begin + chunk : p.count;
+    int32_t za = -1;
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+    for (int64_t u = u_begin; u < u_end; ++u) {
       const int4 q = __ldg(p.rec + u);
       const int64_t k0 = __ldg(p.cfg_begin + u);
       const float4 c1 = ld4(c.cur + (int64_t)q.y * B + b);
       const float4 c2 = ld4(c.cur + ((int64_t)q.y + 1) * B + b);
-      const float4 a0 = ld4(c.vsum + (int64_t)q.z * B + b);
-      const float4 a1 = ld4(c.vsum + ((int64_t)q.z + 1) * B + b);
+      if (q.z != za) {
+        za = q.z;
+        a0 = ld4(c.vsum + (int64_t)q.z * B + b);
+        a1 = ld4(c.vsum + ((int64_t)q.z + 1) * B + b);
+      }
       const float4 b0 = ld4(c.vsum + (int64_t)q.w * B + b);
       const float4 b1 = ld4(c.vsum + ((int64_t)q.w + 1) * B + b);
       float4 p00, p01, p10, p11;
@@ -733,17 +736,108 @@ __global__ void __launch_bounds__(256) pairwise22_x4_kernel(Fused c, PairwiseDev
   block_max4_to(deltas, l, dm);
 }
 
+// ----------------------------------------------------------------------------- variable sums
+// var_sums = evidence.at[var_states_for_edge_states].add(msgs) (bp.py:217): serial per variable
+// state over its edge states in increasing order. Binary variables read one compressed slot per
+// edge and accumulate both states. `for_each_slot` walks a unit's slots in order, either from
+// affine runs (no index loads) or from the explicit list, eight loads in flight.
+struct VarsumDev {
+  const int32_t* __restrict__ vs;
+  const int32_t* __restrict__ off;
+  const int32_t* __restrict__ slots;
+  const int32_t* __restrict__ run_off;
+  const int4* __restrict__ runs;
+  int64_t count;
+};
+
+template <int UNROLL, class Load, class Add>
+__device__ __forceinline__ void for_each_slot(const VarsumDev& v, bool use_runs, int64_t u,
+                                              Load load, Add add) {
+  using T = decltype(load((int64_t)0));
+  if (use_runs) {
+    for (int32_t r = v.run_off[u]; r < v.run_off[u + 1]; ++r) {
+      const int4 run = __ldg(v.runs + r);
+      const int64_t first = run.x, stride = run.y;
+      const int32_t len = run.z;
+      int32_t k = 0;
+      for (; k + UNROLL <= len; k += UNROLL) {
+        T c[UNROLL];
+#pragma unroll
+        for (int q = 0; q < UNROLL; ++q) c[q] = load(first + (int64_t)(k + q) * stride);
+#pragma unroll
+        for (int q = 0; q < UNROLL; ++q) add(c[q]);
+      }
+      for (; k < len; ++k) add(load(first + (int64_t)k * stride));
+    }
+  } else {
+    const int32_t k1 = v.off[u + 1];
+    int32_t k = v.off[u];
+    for (; k + UNROLL <= k1; k += UNROLL) {
+      T c[UNROLL];
+#pragma unroll
+      for (int q = 0; q < UNROLL; ++q) c[q] = load((int64_t)__ldg(v.slots + k + q));
+#pragma unroll
+      for (int q = 0; q < UNROLL; ++q) add(c[q]);
+    }
+    for (; k < k1; ++k) add(load((int64_t)__ldg(v.slots + k)));
+  }
+}
+
+__global__ void __launch_bounds__(256) varsum_binary_kernel(VarsumDev v, bool use_runs,
+                                                            const float* __restrict__ msgs,
+                                                            const float* __restrict__ ev,
+                                                            int64_t evs, int64_t evb,
+                                                            float* __restrict__ vsum, int64_t B) {
+  const Lane l = lane(B);
+  if (!l.valid) return;
+  const int64_t b = l.b;
+  const float* col = msgs + b;
+  for (int64_t u = l.u0; u < v.count; u += l.ustep) {
+    const int64_t v0 = v.vs[u];
+    float s0 = ev[v0 * evs + b * evb];
+    float s1 = ev[(v0 + 1) * evs + b * evb];
+    for_each_slot<16>(v, use_runs, u, [&](int64_t slot) { return col[slot * B]; },
+                     [&](float c) {
+                       float m0, m1;
+                       decode2(c, m0, m1);
+                       s0 += m0;
+                       s1 += m1;
+                     });
+    vsum[v0 * B + b] = s0;
+    vsum[(v0 + 1) * B + b] = s1;
+  }
+}
+
+__global__ void __launch_bounds__(256) varsum_other_kernel(VarsumDev v, bool use_runs,
+                                                           const float* __restrict__ msgs,
+                                                           const float* __restrict__ ev,
+                                                           int64_t evs, int64_t evb,
+                                                           float* __restrict__ vsum, int64_t B) {
+  const Lane l = lane(B);
+  if (!l.valid) return;
+  const int64_t b = l.b;
+  const float* col = msgs + b;
+  for (int64_t u = l.u0; u < v.count; u += l.ustep) {
+    const int64_t vv = v.vs[u];
+    float s = ev[vv * evs + b * evb];
+    for_each_slot<8>(v, use_runs, u, [&](int64_t slot) { return col[slot * B]; },
+                     [&](float c) { s += c; });
+    vsum[vv * B + b] = s;
+  }
+}
+
 // Binary variable sums, 4 instances per thread, sixteen slots in flight.
-__global__ void __launch_bounds__(256) varsum_binary_x4_kernel(
-    const int32_t* __restrict__ vs, const int32_t* __restrict__ off,
-    const int32_t* __restrict__ slots, int64_t n, const float* __restrict__ msgs,
-    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum, int64_t B) {
+__global__ void __launch_bounds__(256) varsum_binary_x4_kernel(VarsumDev v, bool use_runs,
+                                                               const float* __restrict__ msgs,
+                                                               const float* __restrict__ ev,
+                                                               int64_t evs, int64_t evb,
+                                                               float* __restrict__ vsum, int64_t B) {
   const Lane4 l = lane4(B);
   if (!l.valid) return;
   const int64_t b = l.b;
   const float* col = msgs + b;
-  for (int64_t u = l.u0; u < n; u += l.ustep) {
-    const int64_t v0 = vs[u];
+  for (int64_t u = l.u0; u < v.count; u += l.ustep) {
+    const int64_t v0 = v.vs[u];
     float4 s0, s1;
     if (evb == 0) {
       const float e0 = ev[v0 * evs], e1 = ev[(v0 + 1) * evs];
@@ -753,99 +847,24 @@ __global__ void __launch_bounds__(256) varsum_binary_x4_kernel(
       s0 = ld4(ev + v0 * evs + b);
       s1 = ld4(ev + (v0 + 1) * evs + b);
     }
-    const int32_t k1 = off[u + 1];
-    int32_t k = off[u];
-    auto add = [&](float4 c4) {
-      float m0, m1;
-      decode2(c4.x, m0, m1);
-      s0.x += m0;
-      s1.x += m1;
-      decode2(c4.y, m0, m1);
-      s0.y += m0;
-      s1.y += m1;
-      decode2(c4.z, m0, m1);
-      s0.z += m0;
-      s1.z += m1;
-      decode2(c4.w, m0, m1);
-      s0.w += m0;
-      s1.w += m1;
-    };
-    for (; k + 16 <= k1; k += 16) {
-      float4 c4[16];
-#pragma unroll
-      for (int q = 0; q < 16; ++q) c4[q] = ld4(col + (int64_t)__ldg(slots + k + q) * B);
-#pragma unroll
-      for (int q = 0; q < 16; ++q) add(c4[q]);
-    }
-    for (; k < k1; ++k) add(ld4(col + (int64_t)__ldg(slots + k) * B));
+    for_each_slot<16>(v, use_runs, u, [&](int64_t slot) { return ld4(col + slot * B); },
+                      [&](float4 c4) {
+                        float m0, m1;
+                        decode2(c4.x, m0, m1);
+                        s0.x += m0;
+                        s1.x += m1;
+                        decode2(c4.y, m0, m1);
+                        s0.y += m0;
+                        s1.y += m1;
+                        decode2(c4.z, m0, m1);
+                        s0.z += m0;
+                        s1.z += m1;
+                        decode2(c4.w, m0, m1);
+                        s0.w += m0;
+                        s1.w += m1;
+                      });
     st4(vsum + v0 * B + b, s0);
     st4(vsum + (v0 + 1) * B + b, s1);
-  }
-}
-
-// ----------------------------------------------------------------------------- variable sums
-// var_sums = evidence.at[var_states_for_edge_states].add(msgs) (bp.py:217): serial per variable
-// state over its edge states in increasing order. Binary variables read one compressed slot per
-// edge and accumulate both states; eight slots are loaded before they are added.
-__global__ void __launch_bounds__(256) varsum_binary_kernel(
-    const int32_t* __restrict__ vs, const int32_t* __restrict__ off,
-    const int32_t* __restrict__ slots, int64_t n, const float* __restrict__ msgs,
-    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum, int64_t B) {
-  const Lane l = lane(B);
-  if (!l.valid) return;
-  const int64_t b = l.b;
-  const float* col = msgs + b;
-  for (int64_t u = l.u0; u < n; u += l.ustep) {
-    const int64_t v0 = vs[u];
-    float s0 = ev[v0 * evs + b * evb];
-    float s1 = ev[(v0 + 1) * evs + b * evb];
-    const int32_t k1 = off[u + 1];
-    int32_t k = off[u];
-    for (; k + 8 <= k1; k += 8) {
-      float c[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) c[q] = col[(int64_t)__ldg(slots + k + q) * B];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        float m0, m1;
-        decode2(c[q], m0, m1);
-        s0 += m0;
-        s1 += m1;
-      }
-    }
-    for (; k < k1; ++k) {
-      float m0, m1;
-      decode2(col[(int64_t)__ldg(slots + k) * B], m0, m1);
-      s0 += m0;
-      s1 += m1;
-    }
-    vsum[v0 * B + b] = s0;
-    vsum[(v0 + 1) * B + b] = s1;
-  }
-}
-
-__global__ void __launch_bounds__(256) varsum_other_kernel(
-    const int32_t* __restrict__ vs, const int32_t* __restrict__ off,
-    const int32_t* __restrict__ slots, int64_t n, const float* __restrict__ msgs,
-    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum, int64_t B) {
-  const Lane l = lane(B);
-  if (!l.valid) return;
-  const int64_t b = l.b;
-  const float* col = msgs + b;
-  for (int64_t u = l.u0; u < n; u += l.ustep) {
-    const int64_t v = vs[u];
-    float s = ev[v * evs + b * evb];
-    const int32_t k1 = off[u + 1];
-    int32_t k = off[u];
-    for (; k + 8 <= k1; k += 8) {
-      float c[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) c[q] = col[(int64_t)__ldg(slots + k + q) * B];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) s += c[q];
-    }
-    for (; k < k1; ++k) s += col[(int64_t)__ldg(slots + k) * B];
-    vsum[v * B + b] = s;
   }
 }
 
@@ -1130,25 +1149,31 @@ void launch_pool(cudaStream_t s, const Plan& p, const C& c, int64_t B, float t, 
   pool_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(g), B, t, normalize, deltas);
 }
 
+VarsumDev dev(const VarsumSet& v) {
+  return VarsumDev{v.vs, v.off, v.slots, v.run_off, v.runs, v.count};
+}
+
 void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, const float* ev,
                    int64_t evs, int64_t evb, float* vsum) {
   ProfileScope ps(kProfVarsum, s);
-  if (p.varsum_binary.count > 0 && B % 4 == 0) {
-    const VarsumSet& v = p.varsum_binary;
-    const Launch2 l = launch2_x4(v.count, B, p.sm_count);
-    varsum_binary_x4_kernel<<<l.grid, l.block, 0, s>>>(v.vs, v.off, v.slots, v.count, cur, ev, evs,
-                                                        evb, vsum, B);
-  } else if (p.varsum_binary.count > 0) {
-    const VarsumSet& v = p.varsum_binary;
-    const Launch2 l = launch2(v.count, B, p.sm_count);
-    varsum_binary_kernel<<<l.grid, l.block, 0, s>>>(v.vs, v.off, v.slots, v.count, cur, ev, evs,
-                                                     evb, vsum, B);
+  const VarsumSet& vb = p.varsum_binary;
+  // 4 instances per thread only when that still leaves >= 16 warps per SM: the per-variable sums
+  // are serial chains, so latency is hidden by warps, not by the work inside one thread
+  const bool x4 = B % 4 == 0 && vb.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32;
+  if (vb.count > 0 && x4) {
+    const Launch2 l = launch2_x4(vb.count, B, p.sm_count);
+    varsum_binary_x4_kernel<<<l.grid, l.block, 0, s>>>(dev(vb), vb.use_runs, cur, ev, evs, evb,
+                                                        vsum, B);
+  } else if (vb.count > 0) {
+    const Launch2 l = launch2(vb.count, B, p.sm_count);
+    varsum_binary_kernel<<<l.grid, l.block, 0, s>>>(dev(vb), vb.use_runs, cur, ev, evs, evb, vsum,
+                                                     B);
   }
-  if (p.varsum_other.count > 0) {
-    const VarsumSet& v = p.varsum_other;
-    const Launch2 l = launch2(v.count, B, p.sm_count);
-    varsum_other_kernel<<<l.grid, l.block, 0, s>>>(v.vs, v.off, v.slots, v.count, cur, ev, evs,
-                                                    evb, vsum, B);
+  const VarsumSet& vo = p.varsum_other;
+  if (vo.count > 0) {
+    const Launch2 l = launch2(vo.count, B, p.sm_count);
+    varsum_other_kernel<<<l.grid, l.block, 0, s>>>(dev(vo), vo.use_runs, cur, ev, evs, evb, vsum,
+                                                    B);
   }
 }
 

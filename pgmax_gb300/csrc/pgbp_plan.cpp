@@ -307,14 +307,39 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   p.vs_edges = bd.upload(vs_edges);
   p.edge_start = bd.upload(edge_start);
   p.edge_slot = bd.upload(edge_slot);
-  p.varsum_binary.count = (int64_t)vb_vs.size();
-  p.varsum_binary.vs = bd.upload(vb_vs);
-  p.varsum_binary.off = bd.upload(vb_off);
-  p.varsum_binary.slots = bd.upload(vb_slots);
-  p.varsum_other.count = (int64_t)vo_vs.size();
-  p.varsum_other.vs = bd.upload(vo_vs);
-  p.varsum_other.off = bd.upload(vo_off);
-  p.varsum_other.slots = bd.upload(vo_slots);
+  // slot lists as affine runs (first, stride, length); used when they compress 4:1 or better
+  auto fill_varsum = [&](pgbp::VarsumSet& v, const std::vector<int32_t>& units,
+                         const std::vector<int32_t>& off, const std::vector<int32_t>& slots) {
+    v.count = (int64_t)units.size();
+    v.vs = bd.upload(units);
+    std::vector<int32_t> run_off{0};
+    std::vector<int4> runs;
+    for (size_t u = 0; u + 1 < off.size(); ++u) {
+      int32_t k = off[u];
+      while (k < off[u + 1]) {
+        const int32_t first = slots[k];
+        int32_t len = 1, stride = 1;
+        if (k + 1 < off[u + 1]) {
+          stride = slots[k + 1] - first;
+          len = 2;
+          while (k + len < off[u + 1] && slots[k + len] == first + len * stride) ++len;
+        }
+        runs.push_back(make_int4(first, stride, len, 0));
+        k += len;
+      }
+      run_off.push_back((int32_t)runs.size());
+    }
+    v.use_runs = !slots.empty() && runs.size() * 4 <= slots.size();
+    if (v.use_runs) {
+      v.run_off = bd.upload(run_off);
+      v.runs = bd.upload(runs);
+    } else {
+      v.off = bd.upload(off);
+      v.slots = bd.upload(slots);
+    }
+  };
+  fill_varsum(p.varsum_binary, vb_vs, vb_off, vb_slots);
+  fill_varsum(p.varsum_other, vo_vs, vo_off, vo_slots);
   if (bd.err) return bail(bd.err);
   auto edge_rec = [&](int64_t es0) {  // (first edge state, first slot, first var state, 0)
     const int32_t e = ei[es0];
@@ -598,6 +623,7 @@ int pgbp_plan_get_info(const pgbp_plan* plan, pgbp_plan_info* info) {
   info->num_pool_factors = p.pool.count;
   info->num_pairwise_buckets = (int64_t)p.pairwise.size();
   info->device_bytes = p.device_bytes;
+  info->num_slots = p.num_slots;
   return PGBP_OK;
 }
 

@@ -103,7 +103,7 @@ class PlanInfo(ctypes.Structure):
   _fields_ = [(n, _i64) for n in (
       "num_edge_states", "num_var_states", "num_edges", "num_variables", "num_potentials",
       "num_enum_factors", "num_enum_pairwise_factors", "num_or_factors", "num_and_factors",
-      "num_pool_factors", "num_pairwise_buckets", "device_bytes")]
+      "num_pool_factors", "num_pairwise_buckets", "device_bytes", "num_slots")]
 
 
 class Profile(ctypes.Structure):
