@@ -84,7 +84,12 @@ typedef struct {
    * only by pgbp_decode / pgbp_marginals; may be NULL. */
   int64_t num_variables;
   const int32_t* evidence_to_vars;             /* [num_var_states] */
+  /* Execution options (0 = automatic): PGBP_FLAG_NO_SMALL_GRAPH keeps every run on the
+   * multi-kernel path even when the graph fits the one-CTA-per-instance shared-memory path. */
+  int64_t flags;
 } pgbp_wiring_desc;
+
+#define PGBP_FLAG_NO_SMALL_GRAPH 1
 
 typedef struct pgbp_plan pgbp_plan;
 
@@ -96,6 +101,7 @@ typedef struct {
   int64_t num_pairwise_buckets;  /* (n1, n2) classes run by the dense pairwise kernel */
   int64_t device_bytes;          /* device memory owned by the plan */
   int64_t num_slots;             /* message slots per instance: 1 per binary edge, else 1 per state */
+  int64_t small_graph_smem_bytes; /* shared memory of the one-CTA-per-instance path, 0 if unused */
 } pgbp_plan_info;
 
 /* Compiles the wiring into device-resident schedules on `device`. Validates every index. */
@@ -166,8 +172,9 @@ int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const flo
  * per-class launch counts and total device milliseconds, and clears the record. Classes:
  * 0 variable sums, 1 dense pairwise Enum, 2 generic Enum, 3 OR, 4 AND, 5 Pool,
  * 6 layout (transposes, potential clipping, initial normalisation, residual copy-out),
- * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals). Process-wide, not thread-safe. */
-#define PGBP_PROFILE_CLASSES 8
+ * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals), 8 the one-CTA-per-instance
+ * small-graph kernel (all iterations in one launch). Process-wide, not thread-safe. */
+#define PGBP_PROFILE_CLASSES 9
 typedef struct {
   int64_t launches[PGBP_PROFILE_CLASSES];
   double milliseconds[PGBP_PROFILE_CLASSES];

@@ -100,6 +100,8 @@ struct Plan {
   EnumGeneric enum_generic;
   LogicalSet logical[2];
   PoolSet pool;
+  int64_t flags = 0;
+  int64_t small_graph_smem = 0;  // bytes per CTA of the small-graph path; 0 = not eligible
   int64_t device_bytes = 0;
   std::vector<void*> allocations;
   int64_t num_enum_factors = 0, num_enum_pairwise = 0;
@@ -110,9 +112,13 @@ int set_last_error(int code, const char* message);
 
 size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched, bool lp_batched);
 
+// Decides whether the plan can run on the one-CTA-per-instance shared-memory path and prepares
+// the kernels for it (pgbp_kernels.cu). Sets p.small_graph_smem.
+cudaError_t prepare_small_graph(Plan& p);
+
 // Kernel-class timing (pgbp_profile_*): RAII bracket around one launch when profiling is on.
 enum ProfileClass { kProfVarsum = 0, kProfPairwise, kProfEnumGeneric, kProfOr, kProfAnd, kProfPool,
-                    kProfLayout, kProfReadout };
+                    kProfLayout, kProfReadout, kProfSmallGraph };
 bool profiling_enabled();
 void profile_record(int cls, cudaStream_t s, bool start);
 struct ProfileScope {

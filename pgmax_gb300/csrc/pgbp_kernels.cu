@@ -303,63 +303,67 @@ struct EnumGenericDev {
   int64_t count;
 };
 
-// pass_enum_fac_to_var_messages (enum.py:451-475) for an arbitrary config table.
+// pass_enum_fac_to_var_messages (enum.py:451-475) for an arbitrary config table: factor f,
+// instance b.
+template <int MAXES, bool T0, class C>
+__device__ __forceinline__ void enum_generic_unit(const C& c, const EnumGenericDev& g, int64_t f,
+                                                  int64_t b, float t, float& dmax) {
+  const int64_t e0 = g.es_begin[f];
+  const int n = g.n_es[f], nv = g.n_vars[f], ncfg = g.n_cfg[f];
+  const int64_t rb = g.row_begin[f], k0 = g.cfg_begin[f];
+  const int j0 = g.edge_off[f], j1 = g.edge_off[f + 1];
+  float old[MAXES], v[MAXES], mx[MAXES], se[MAXES];
+  {
+    int pos = 0;
+    for (int j = j0; j < j1; ++j) {
+      const int k = g.edge_size[j];
+      c.load(EdgeRef{e0 + pos, g.edge_slot[j], g.edge_vs[j]}, k, b, old + pos, v + pos);
+      pos += k;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    mx[i] = -INFINITY;
+    se[i] = 0.0f;
+  }
+  for (int k = 0; k < ncfg; ++k) {
+    const int32_t* rows = g.row_les + rb + (int64_t)k * nv;
+    float s = 0.0f;
+    for (int i = 0; i < nv; ++i) s += v[rows[i]];
+    s = s + c.pot(k0 + k, b);
+    for (int i = 0; i < nv; ++i) mx[rows[i]] = fmaxp(mx[rows[i]], s);
+  }
+  if (!T0) {
+    for (int k = 0; k < ncfg; ++k) {
+      const int32_t* rows = g.row_les + rb + (int64_t)k * nv;
+      float s = 0.0f;
+      for (int i = 0; i < nv; ++i) s += v[rows[i]];
+      s = s + c.pot(k0 + k, b);
+      for (int i = 0; i < nv; ++i) se[rows[i]] += expf((s - mx[rows[i]]) / t);
+    }
+  }
+  int pos = 0;
+  for (int j = j0; j < j1; ++j) {
+    const int k = g.edge_size[j];
+    const int p0 = pos;
+    const EdgeRef r{e0 + pos, g.edge_slot[j], g.edge_vs[j]};
+    if (T0) {
+      c.store(r, k, old + p0, [&](int i) { return mx[p0 + i] - v[p0 + i]; }, b, dmax);
+    } else {
+      c.store(r, k, old + p0,
+              [&](int i) { return (t * logf(se[p0 + i]) + mx[p0 + i]) - v[p0 + i]; }, b, dmax);
+    }
+    pos += k;
+  }
+}
+
 template <int MAXES, bool T0, class C>
 __global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g, int64_t B,
                                                            float t, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
-    const int64_t b = l.b;
-    for (int64_t f = l.u0; f < g.count; f += l.ustep) {
-      const int64_t e0 = g.es_begin[f];
-      const int n = g.n_es[f], nv = g.n_vars[f], ncfg = g.n_cfg[f];
-      const int64_t rb = g.row_begin[f], k0 = g.cfg_begin[f];
-      const int j0 = g.edge_off[f], j1 = g.edge_off[f + 1];
-      float old[MAXES], v[MAXES], mx[MAXES], se[MAXES];
-      {
-        int pos = 0;
-        for (int j = j0; j < j1; ++j) {
-          const int k = g.edge_size[j];
-          c.load(EdgeRef{e0 + pos, g.edge_slot[j], g.edge_vs[j]}, k, b, old + pos, v + pos);
-          pos += k;
-        }
-      }
-      for (int i = 0; i < n; ++i) {
-        mx[i] = -INFINITY;
-        se[i] = 0.0f;
-      }
-      for (int k = 0; k < ncfg; ++k) {
-        const int32_t* rows = g.row_les + rb + (int64_t)k * nv;
-        float s = 0.0f;
-        for (int i = 0; i < nv; ++i) s += v[rows[i]];
-        s = s + c.pot(k0 + k, b);
-        for (int i = 0; i < nv; ++i) mx[rows[i]] = fmaxp(mx[rows[i]], s);
-      }
-      if (!T0) {
-        for (int k = 0; k < ncfg; ++k) {
-          const int32_t* rows = g.row_les + rb + (int64_t)k * nv;
-          float s = 0.0f;
-          for (int i = 0; i < nv; ++i) s += v[rows[i]];
-          s = s + c.pot(k0 + k, b);
-          for (int i = 0; i < nv; ++i) se[rows[i]] += expf((s - mx[rows[i]]) / t);
-        }
-      }
-      int pos = 0;
-      for (int j = j0; j < j1; ++j) {
-        const int k = g.edge_size[j];
-        const int p0 = pos;
-        const EdgeRef r{e0 + pos, g.edge_slot[j], g.edge_vs[j]};
-        if (T0) {
-          c.store(r, k, old + p0, [&](int i) { return mx[p0 + i] - v[p0 + i]; }, b, dmax);
-        } else {
-          c.store(r, k, old + p0,
-                  [&](int i) { return (t * logf(se[p0 + i]) + mx[p0 + i]) - v[p0 + i]; }, b,
-                  dmax);
-        }
-        pos += k;
-      }
-    }
+    for (int64_t f = l.u0; f < g.count; f += l.ustep)
+      enum_generic_unit<MAXES, T0>(c, g, f, l.b, t, dmax);
   }
   block_max_to(deltas, l, dmax);
 }
@@ -384,92 +388,96 @@ __device__ __forceinline__ void load_or(const C& c, const EdgeRef& r, int rel, i
   v_oth = vt[1 - rel];
 }
 
-// pass_logical_fac_to_var_messages, pgmax/factor/logical.py:561-779, one factor per thread.
+// pass_logical_fac_to_var_messages, pgmax/factor/logical.py:561-779: factor f, instance b.
 // Factor-level sums run over the parents in order (the reference's scatter order); the argmax is
 // the last parent attaining the maximum difference (update_utils.py:48-63).
+template <bool T0, class C>
+__device__ __forceinline__ void logical_unit(const C& c, const LogicalDev& g, int64_t f, int64_t b,
+                                             float t, bool low_t, int normalize, float& dmax) {
+  const int rel = g.off > 0 ? 1 : 0;
+  const int64_t p0 = g.par_begin[f], p1 = g.par_begin[f + 1];
+  float old[2];
+  float fs_oth = 0.0f, max1 = -INFINITY, fs_x = 0.0f;
+  for (int64_t i = p0; i < p1; ++i) {
+    float vo, vr;
+    load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+    fs_oth += vo;
+    max1 = fmaxp(max1, vr - vo);
+    fs_x += T0 ? fmaxp(vo, vr) : logaddexp_t(vr, vo, t);
+  }
+  int64_t arg = p1 - 1;
+  {
+    int64_t last = -1;
+    for (int64_t i = p0; i < p1; ++i) {
+      float vo, vr;
+      load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+      if (vr - vo == max1) last = i;
+    }
+    if (last >= 0) arg = last;
+  }
+  float max2 = -INFINITY;
+  for (int64_t i = p0; i < p1; ++i) {
+    float vo, vr;
+    load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+    max2 = fmaxp(max2, (i == arg) ? -INFINITY : vr - vo);
+  }
+  const EdgeRef rc = edge_ref(g.child[f]);
+  float cold[2], c_oth, c_rel;
+  load_or(c, rc, rel, b, cold, c_oth, c_rel);
+  float ch_rel;
+  if (T0) {
+    ch_rel = fs_x + fminp(0.0f, max1);
+  } else {
+    ch_rel = logminusexp_t(fs_x, fs_oth, t, 1e-4f);
+    if (low_t) ch_rel = fmaxp(ch_rel, logaddexp_t(fs_oth + max1, fs_oth + max2, t));
+  }
+  const bool single = (p1 - p0) == 1;
+  for (int64_t i = p0; i < p1; ++i) {
+    const EdgeRef r = edge_ref(g.par[i]);
+    float vo, vr;
+    load_or(c, r, rel, b, old, vo, vr);
+    float p_rel, p_oth;
+    if (T0) {
+      const float mx = fmaxp(vo, vr);
+      p_rel = (fs_x + c_rel) - mx;
+      const float opt1 = (c_oth + fs_oth) - vo;
+      const float opt2 = p_rel + fminp(0.0f, i == arg ? max2 : max1);
+      p_oth = fmaxp(opt1, opt2);
+    } else {
+      const float lse = logaddexp_t(vr, vo, t);
+      const float fs_lse_wo = fs_x - lse;
+      const float fs_oth_wo = fs_oth - vo;
+      p_rel = c_rel + fs_lse_wo;
+      const float opt1 = c_oth + fs_oth_wo;
+      const float opt2 = c_rel + fs_lse_wo;
+      const float opt3 = c_rel + fs_oth_wo;
+      p_oth = logminusexp_t(logaddexp_t(opt1, opt2, t), opt3, t, 1e-4f);
+      if (low_t) {
+        const float fsp = fs_oth_wo + (i == arg ? max2 : max1);
+        p_oth = fmaxp(p_oth, logaddexp_t(opt1, c_rel + fsp, t));
+      }
+    }
+    if (single) {
+      p_rel = c_rel;
+      p_oth = c_oth;
+    }
+    const float rel_out = normalize ? p_rel - p_oth : p_rel;
+    const float oth_out = normalize ? 0.0f : p_oth;
+    c.store(r, 2, old, [&](int s) { return s == rel ? rel_out : oth_out; }, b, dmax);
+  }
+  const float crel_out = normalize ? ch_rel - fs_oth : ch_rel;
+  const float coth_out = normalize ? 0.0f : fs_oth;
+  c.store(rc, 2, cold, [&](int s) { return s == rel ? crel_out : coth_out; }, b, dmax);
+}
+
 template <bool T0, class C>
 __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t B, float t,
                                                       bool low_t, int normalize, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
-  const int rel = g.off > 0 ? 1 : 0;
   if (l.valid) {
-    const int64_t b = l.b;
-    for (int64_t f = l.u0; f < g.count; f += l.ustep) {
-      const int64_t p0 = g.par_begin[f], p1 = g.par_begin[f + 1];
-      float old[2];
-      float fs_oth = 0.0f, max1 = -INFINITY, fs_x = 0.0f;
-      for (int64_t i = p0; i < p1; ++i) {
-        float vo, vr;
-        load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
-        fs_oth += vo;
-        max1 = fmaxp(max1, vr - vo);
-        fs_x += T0 ? fmaxp(vo, vr) : logaddexp_t(vr, vo, t);
-      }
-      int64_t arg = p1 - 1;
-      {
-        int64_t last = -1;
-        for (int64_t i = p0; i < p1; ++i) {
-          float vo, vr;
-          load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
-          if (vr - vo == max1) last = i;
-        }
-        if (last >= 0) arg = last;
-      }
-      float max2 = -INFINITY;
-      for (int64_t i = p0; i < p1; ++i) {
-        float vo, vr;
-        load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
-        max2 = fmaxp(max2, (i == arg) ? -INFINITY : vr - vo);
-      }
-      const EdgeRef rc = edge_ref(g.child[f]);
-      float cold[2], c_oth, c_rel;
-      load_or(c, rc, rel, b, cold, c_oth, c_rel);
-      float ch_rel;
-      if (T0) {
-        ch_rel = fs_x + fminp(0.0f, max1);
-      } else {
-        ch_rel = logminusexp_t(fs_x, fs_oth, t, 1e-4f);
-        if (low_t) ch_rel = fmaxp(ch_rel, logaddexp_t(fs_oth + max1, fs_oth + max2, t));
-      }
-      const bool single = (p1 - p0) == 1;
-      for (int64_t i = p0; i < p1; ++i) {
-        const EdgeRef r = edge_ref(g.par[i]);
-        float vo, vr;
-        load_or(c, r, rel, b, old, vo, vr);
-        float p_rel, p_oth;
-        if (T0) {
-          const float mx = fmaxp(vo, vr);
-          p_rel = (fs_x + c_rel) - mx;
-          const float opt1 = (c_oth + fs_oth) - vo;
-          const float opt2 = p_rel + fminp(0.0f, i == arg ? max2 : max1);
-          p_oth = fmaxp(opt1, opt2);
-        } else {
-          const float lse = logaddexp_t(vr, vo, t);
-          const float fs_lse_wo = fs_x - lse;
-          const float fs_oth_wo = fs_oth - vo;
-          p_rel = c_rel + fs_lse_wo;
-          const float opt1 = c_oth + fs_oth_wo;
-          const float opt2 = c_rel + fs_lse_wo;
-          const float opt3 = c_rel + fs_oth_wo;
-          p_oth = logminusexp_t(logaddexp_t(opt1, opt2, t), opt3, t, 1e-4f);
-          if (low_t) {
-            const float fsp = fs_oth_wo + (i == arg ? max2 : max1);
-            p_oth = fmaxp(p_oth, logaddexp_t(opt1, c_rel + fsp, t));
-          }
-        }
-        if (single) {
-          p_rel = c_rel;
-          p_oth = c_oth;
-        }
-        const float rel_out = normalize ? p_rel - p_oth : p_rel;
-        const float oth_out = normalize ? 0.0f : p_oth;
-        c.store(r, 2, old, [&](int s) { return s == rel ? rel_out : oth_out; }, b, dmax);
-      }
-      const float crel_out = normalize ? ch_rel - fs_oth : ch_rel;
-      const float coth_out = normalize ? 0.0f : fs_oth;
-      c.store(rc, 2, cold, [&](int s) { return s == rel ? crel_out : coth_out; }, b, dmax);
-    }
+    for (int64_t f = l.u0; f < g.count; f += l.ustep)
+      logical_unit<T0>(c, g, f, l.b, t, low_t, normalize, dmax);
   }
   block_max_to(deltas, l, dmax);
 }
@@ -482,90 +490,94 @@ struct PoolDev {
   int64_t count;
 };
 
-// pass_pool_fac_to_var_messages, pgmax/factor/pool.py:328-474 (state 1 is the "on" state).
+// pass_pool_fac_to_var_messages, pgmax/factor/pool.py:328-474 (state 1 is the "on" state):
+// factor f, instance b.
+template <bool T0, class C>
+__device__ __forceinline__ void pool_unit(const C& c, const PoolDev& g, int64_t f, int64_t b,
+                                          float t, int normalize, float& dmax) {
+  const int64_t p0 = g.ch_begin[f], p1 = g.ch_begin[f + 1];
+  float old[2], vt[2];
+  float sums0 = 0.0f, max1 = -INFINITY;
+  for (int64_t i = p0; i < p1; ++i) {
+    c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+    sums0 += vt[0];
+    max1 = fmaxp(max1, vt[1] - vt[0]);
+  }
+  int64_t arg = p1 - 1;
+  {
+    int64_t last = -1;
+    for (int64_t i = p0; i < p1; ++i) {
+      c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+      if (vt[1] - vt[0] == max1) last = i;
+    }
+    if (last >= 0) arg = last;
+  }
+  const EdgeRef ri = edge_ref(g.ind[f]);
+  float iold[2], ivt[2];
+  c.load(ri, 2, b, iold, ivt);
+  const float pi_one = ivt[1];
+  const float pi_diff = ivt[1] - ivt[0];
+  float max2 = -INFINITY, pi_mdiff, fl = 0.0f, am = 0.0f;
+  if (T0) {
+    for (int64_t i = p0; i < p1; ++i) {
+      c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+      max2 = fmaxp(max2, (i == arg) ? -INFINITY : vt[1] - vt[0]);
+    }
+    pi_mdiff = max1;
+  } else {
+    float se = 0.0f;
+    for (int64_t i = p0; i < p1; ++i) {
+      c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+      se += expf(((vt[1] - vt[0]) - max1) / t);
+    }
+    pi_mdiff = t * logf(se) + max1;
+    fl = logaddexp_t(pi_mdiff, -pi_diff, t);
+    // -logsumexps_with_temp of the diffs with the argmax replaced by -pi_diff (pool.py:416-425)
+    float mw = -INFINITY;
+    for (int64_t i = p0; i < p1; ++i) {
+      c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+      mw = fmaxp(mw, (i == arg) ? -pi_diff : vt[1] - vt[0]);
+    }
+    float sw = 0.0f;
+    for (int64_t i = p0; i < p1; ++i) {
+      c.load(edge_ref(g.ch[i]), 2, b, old, vt);
+      const float w = (i == arg) ? -pi_diff : vt[1] - vt[0];
+      sw += expf((w - mw) / t);
+    }
+    am = -(t * logf(sw) + mw);
+  }
+  const bool single = (p1 - p0) == 1;
+  for (int64_t i = p0; i < p1; ++i) {
+    const EdgeRef r = edge_ref(g.ch[i]);
+    c.load(r, 2, b, old, vt);
+    const float dif = vt[1] - vt[0];
+    float mdiff;
+    if (T0) {
+      mdiff = fminp(pi_diff, -(i == arg ? max2 : max1));
+    } else {
+      mdiff = (i == arg) ? am : -logminusexp_t(fl, dif, t, 1e-30f);
+    }
+    float ones = (sums0 + pi_one) - vt[0];
+    if (single) {
+      mdiff = pi_diff;
+      ones = pi_one;
+    }
+    const float s1 = normalize ? mdiff : ones;
+    const float s0 = normalize ? 0.0f : ones - mdiff;
+    c.store(r, 2, old, [&](int s) { return s == 0 ? s0 : s1; }, b, dmax);
+  }
+  const float i1 = normalize ? pi_mdiff : sums0 + pi_mdiff;
+  const float i0 = normalize ? 0.0f : sums0;
+  c.store(ri, 2, iold, [&](int s) { return s == 0 ? i0 : i1; }, b, dmax);
+}
+
 template <bool T0, class C>
 __global__ void __launch_bounds__(256) pool_kernel(C c, PoolDev g, int64_t B, float t,
                                                    int normalize, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
-    const int64_t b = l.b;
-    for (int64_t f = l.u0; f < g.count; f += l.ustep) {
-      const int64_t p0 = g.ch_begin[f], p1 = g.ch_begin[f + 1];
-      float old[2], vt[2];
-      float sums0 = 0.0f, max1 = -INFINITY;
-      for (int64_t i = p0; i < p1; ++i) {
-        c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-        sums0 += vt[0];
-        max1 = fmaxp(max1, vt[1] - vt[0]);
-      }
-      int64_t arg = p1 - 1;
-      {
-        int64_t last = -1;
-        for (int64_t i = p0; i < p1; ++i) {
-          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-          if (vt[1] - vt[0] == max1) last = i;
-        }
-        if (last >= 0) arg = last;
-      }
-      const EdgeRef ri = edge_ref(g.ind[f]);
-      float iold[2], ivt[2];
-      c.load(ri, 2, b, iold, ivt);
-      const float pi_one = ivt[1];
-      const float pi_diff = ivt[1] - ivt[0];
-      float max2 = -INFINITY, pi_mdiff, fl = 0.0f, am = 0.0f;
-      if (T0) {
-        for (int64_t i = p0; i < p1; ++i) {
-          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-          max2 = fmaxp(max2, (i == arg) ? -INFINITY : vt[1] - vt[0]);
-        }
-        pi_mdiff = max1;
-      } else {
-        float se = 0.0f;
-        for (int64_t i = p0; i < p1; ++i) {
-          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-          se += expf(((vt[1] - vt[0]) - max1) / t);
-        }
-        pi_mdiff = t * logf(se) + max1;
-        fl = logaddexp_t(pi_mdiff, -pi_diff, t);
-        // -logsumexps_with_temp of the diffs with the argmax replaced by -pi_diff (pool.py:416-425)
-        float mw = -INFINITY;
-        for (int64_t i = p0; i < p1; ++i) {
-          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-          mw = fmaxp(mw, (i == arg) ? -pi_diff : vt[1] - vt[0]);
-        }
-        float sw = 0.0f;
-        for (int64_t i = p0; i < p1; ++i) {
-          c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-          const float w = (i == arg) ? -pi_diff : vt[1] - vt[0];
-          sw += expf((w - mw) / t);
-        }
-        am = -(t * logf(sw) + mw);
-      }
-      const bool single = (p1 - p0) == 1;
-      for (int64_t i = p0; i < p1; ++i) {
-        const EdgeRef r = edge_ref(g.ch[i]);
-        c.load(r, 2, b, old, vt);
-        const float dif = vt[1] - vt[0];
-        float mdiff;
-        if (T0) {
-          mdiff = fminp(pi_diff, -(i == arg ? max2 : max1));
-        } else {
-          mdiff = (i == arg) ? am : -logminusexp_t(fl, dif, t, 1e-30f);
-        }
-        float ones = (sums0 + pi_one) - vt[0];
-        if (single) {
-          mdiff = pi_diff;
-          ones = pi_one;
-        }
-        const float s1 = normalize ? mdiff : ones;
-        const float s0 = normalize ? 0.0f : ones - mdiff;
-        c.store(r, 2, old, [&](int s) { return s == 0 ? s0 : s1; }, b, dmax);
-      }
-      const float i1 = normalize ? pi_mdiff : sums0 + pi_mdiff;
-      const float i0 = normalize ? 0.0f : sums0;
-      c.store(ri, 2, iold, [&](int s) { return s == 0 ? i0 : i1; }, b, dmax);
-    }
+    for (int64_t f = l.u0; f < g.count; f += l.ustep) pool_unit<T0>(c, g, f, l.b, t, normalize, dmax);
   }
   block_max_to(deltas, l, dmax);
 }
@@ -677,7 +689,7 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 // Each unit lane walks a contiguous chunk of factors, so consecutive factors that share their
 // first variable (a PairwiseFactorGroup built row by row) reuse its variable sums from registers.
 template <bool T0>
-__global__ void __launch_bounds__(256) pairwise22_x4_kernel(Fused c, PairwiseDev p, float t,
+__global__ void __launch_bounds__(256, 4) pairwise22_x4_kernel(Fused c, PairwiseDev p, float t,
                                                             unsigned* deltas) {
   const int64_t B = c.B;
   const Lane4 l = lane4(B);
@@ -760,6 +772,24 @@ __device__ __forceinline__ void for_each_slot(const VarsumDev& v, bool use_runs,
       const int64_t first = run.x, stride = run.y;
       const int32_t len = run.z;
       int32_t k = 0;
+      if (len >= 2 * UNROLL) {
+        // software pipeline: the loads of the next UNROLL slots are issued before the current
+        // UNROLL are added, so 2 * UNROLL loads are in flight per thread
+        T cur[UNROLL], nxt[UNROLL];
+#pragma unroll
+        for (int q = 0; q < UNROLL; ++q) cur[q] = load(first + (int64_t)q * stride);
+        k = UNROLL;
+        for (; k + UNROLL <= len; k += UNROLL) {
+#pragma unroll
+          for (int q = 0; q < UNROLL; ++q) nxt[q] = load(first + (int64_t)(k + q) * stride);
+#pragma unroll
+          for (int q = 0; q < UNROLL; ++q) add(cur[q]);
+#pragma unroll
+          for (int q = 0; q < UNROLL; ++q) cur[q] = nxt[q];
+        }
+#pragma unroll
+        for (int q = 0; q < UNROLL; ++q) add(cur[q]);
+      }
       for (; k + UNROLL <= len; k += UNROLL) {
         T c[UNROLL];
 #pragma unroll
@@ -783,6 +813,39 @@ __device__ __forceinline__ void for_each_slot(const VarsumDev& v, bool use_runs,
   }
 }
 
+// Variable sums of unit u (binary: both states), instance b.
+__device__ __forceinline__ void varsum_binary_unit(const VarsumDev& v, bool use_runs, int64_t u,
+                                                   int64_t b, const float* __restrict__ msgs,
+                                                   const float* __restrict__ ev, int64_t evs,
+                                                   int64_t evb, float* __restrict__ vsum,
+                                                   int64_t B) {
+  const float* col = msgs + b;
+  const int64_t v0 = v.vs[u];
+  float s0 = ev[v0 * evs + b * evb];
+  float s1 = ev[(v0 + 1) * evs + b * evb];
+  for_each_slot<16>(v, use_runs, u, [&](int64_t slot) { return col[slot * B]; },
+                    [&](float c) {
+                      float m0, m1;
+                      decode2(c, m0, m1);
+                      s0 += m0;
+                      s1 += m1;
+                    });
+  vsum[v0 * B + b] = s0;
+  vsum[(v0 + 1) * B + b] = s1;
+}
+
+__device__ __forceinline__ void varsum_other_unit(const VarsumDev& v, bool use_runs, int64_t u,
+                                                  int64_t b, const float* __restrict__ msgs,
+                                                  const float* __restrict__ ev, int64_t evs,
+                                                  int64_t evb, float* __restrict__ vsum, int64_t B) {
+  const float* col = msgs + b;
+  const int64_t vv = v.vs[u];
+  float s = ev[vv * evs + b * evb];
+  for_each_slot<8>(v, use_runs, u, [&](int64_t slot) { return col[slot * B]; },
+                   [&](float c) { s += c; });
+  vsum[vv * B + b] = s;
+}
+
 __global__ void __launch_bounds__(256) varsum_binary_kernel(VarsumDev v, bool use_runs,
                                                             const float* __restrict__ msgs,
                                                             const float* __restrict__ ev,
@@ -790,22 +853,8 @@ __global__ void __launch_bounds__(256) varsum_binary_kernel(VarsumDev v, bool us
                                                             float* __restrict__ vsum, int64_t B) {
   const Lane l = lane(B);
   if (!l.valid) return;
-  const int64_t b = l.b;
-  const float* col = msgs + b;
-  for (int64_t u = l.u0; u < v.count; u += l.ustep) {
-    const int64_t v0 = v.vs[u];
-    float s0 = ev[v0 * evs + b * evb];
-    float s1 = ev[(v0 + 1) * evs + b * evb];
-    for_each_slot<16>(v, use_runs, u, [&](int64_t slot) { return col[slot * B]; },
-                     [&](float c) {
-                       float m0, m1;
-                       decode2(c, m0, m1);
-                       s0 += m0;
-                       s1 += m1;
-                     });
-    vsum[v0 * B + b] = s0;
-    vsum[(v0 + 1) * B + b] = s1;
-  }
+  for (int64_t u = l.u0; u < v.count; u += l.ustep)
+    varsum_binary_unit(v, use_runs, u, l.b, msgs, ev, evs, evb, vsum, B);
 }
 
 __global__ void __launch_bounds__(256) varsum_other_kernel(VarsumDev v, bool use_runs,
@@ -815,15 +864,8 @@ __global__ void __launch_bounds__(256) varsum_other_kernel(VarsumDev v, bool use
                                                            float* __restrict__ vsum, int64_t B) {
   const Lane l = lane(B);
   if (!l.valid) return;
-  const int64_t b = l.b;
-  const float* col = msgs + b;
-  for (int64_t u = l.u0; u < v.count; u += l.ustep) {
-    const int64_t vv = v.vs[u];
-    float s = ev[vv * evs + b * evb];
-    for_each_slot<8>(v, use_runs, u, [&](int64_t slot) { return col[slot * B]; },
-                     [&](float c) { s += c; });
-    vsum[vv * B + b] = s;
-  }
+  for (int64_t u = l.u0; u < v.count; u += l.ustep)
+    varsum_other_unit(v, use_runs, u, l.b, msgs, ev, evs, evb, vsum, B);
 }
 
 // Binary variable sums, 4 instances per thread, sixteen slots in flight.
@@ -866,6 +908,105 @@ __global__ void __launch_bounds__(256) varsum_binary_x4_kernel(VarsumDev v, bool
     st4(vsum + v0 * B + b, s0);
     st4(vsum + (v0 + 1) * B + b, s1);
   }
+}
+
+// ----------------------------------------------------------------------------- small graphs
+// Graphs whose messages, variable sums and evidence fit in shared memory (Ising 50x50: 10,000
+// slots) run every iteration in one launch: one CTA per instance keeps its state on chip and
+// separates the variable-sum and factor phases with __syncthreads, so an iteration costs two
+// block barriers instead of two kernel launches. The per-factor work is the same device code as
+// the multi-kernel path (Fused context over shared memory, one instance per CTA).
+constexpr int kSmallMaxBuckets = 4;
+constexpr int kSmallThreads = 1024;
+
+struct SmallGraph {
+  PairwiseDev pw[kSmallMaxBuckets];
+  int n_pw;
+  EnumGenericDev eg;
+  LogicalDev lg[2];
+  PoolDev pool;
+  VarsumDev vb, vo;
+  bool vb_runs, vo_runs;
+  int64_t num_slots, num_var_states;
+  const float* ev;  // run layout: [N_vs][B] (evb = 1, evs = B) or shared [N_vs]
+  int64_t evs, evb;
+  const float* lp;
+  int64_t lps, lpb;
+  float d, omd;
+};
+
+__device__ __forceinline__ float block_max_all(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxp(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = ln < (int)(blockDim.x >> 5) ? red[ln] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxp(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;  // valid in thread 0
+}
+
+template <bool T0, int MAXES>
+__global__ void __launch_bounds__(kSmallThreads) small_graph_kernel(SmallGraph g, int64_t B,
+                                                                    int64_t iters, float t,
+                                                                    bool low_t,
+                                                                    float* __restrict__ msgs,
+                                                                    unsigned* __restrict__ dacc) {
+  extern __shared__ float sm[];
+  __shared__ float red[32];
+  const int64_t inst = blockIdx.x;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  float* cur = sm;
+  float* nxt = sm + g.num_slots;
+  float* vsum = nxt + g.num_slots;
+  float* evs = vsum + g.num_var_states;
+  for (int64_t i = tid; i < g.num_slots; i += nt) cur[i] = msgs[i * B + inst];
+  for (int64_t i = tid; i < g.num_var_states; i += nt) evs[i] = g.ev[i * g.evs + inst * g.evb];
+  __syncthreads();
+  Fused c;
+  c.vsum = vsum;
+  c.lp = g.lp + inst * g.lpb;
+  c.lps = g.lps;
+  c.lpb = 0;
+  c.B = 1;
+  c.d = g.d;
+  c.omd = g.omd;
+  for (int64_t it = 0; it < iters; ++it) {
+    for (int64_t u = tid; u < g.vb.count; u += nt)
+      varsum_binary_unit(g.vb, g.vb_runs, u, 0, cur, evs, 1, 0, vsum, 1);
+    for (int64_t u = tid; u < g.vo.count; u += nt)
+      varsum_other_unit(g.vo, g.vo_runs, u, 0, cur, evs, 1, 0, vsum, 1);
+    __syncthreads();
+    c.cur = cur;
+    c.nxt = nxt;
+    float dmax = 0.0f;
+    for (int q = 0; q < g.n_pw; ++q) {
+      const PairwiseDev& p = g.pw[q];
+      for (int64_t u = tid; u < p.count; u += nt) {
+        EdgeRef r1, r2;
+        pairwise_refs(p, __ldg(p.rec + u), r1, r2);
+        const int64_t k0 = __ldg(p.cfg_begin + u);
+        if (p.n1 == 2 && p.n2 == 2) {
+          pairwise_body<2, 2, T0>(c, r1, r2, k0, 2, 2, 0, t, dmax);
+        } else {
+          pairwise_body<0, 0, T0>(c, r1, r2, k0, p.n1, p.n2, 0, t, dmax);
+        }
+      }
+    }
+    for (int64_t f = tid; f < g.eg.count; f += nt) enum_generic_unit<MAXES, T0>(c, g.eg, f, 0, t, dmax);
+    for (int w = 0; w < 2; ++w)
+      for (int64_t f = tid; f < g.lg[w].count; f += nt)
+        logical_unit<T0>(c, g.lg[w], f, 0, t, low_t, 1, dmax);
+    for (int64_t f = tid; f < g.pool.count; f += nt) pool_unit<T0>(c, g.pool, f, 0, t, 1, dmax);
+    const float m = block_max_all(dmax, red);
+    if (tid == 0) dacc[it * B + inst] = __float_as_uint(m);
+    __syncthreads();
+    float* sw = cur;
+    cur = nxt;
+    nxt = sw;
+  }
+  for (int64_t i = tid; i < g.num_slots; i += nt) msgs[i * B + inst] = cur[i];
 }
 
 // Flat beliefs from caller-layout arrays ([B, n] rows): inferer.py:218-222.
@@ -1206,7 +1347,55 @@ void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool lo
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+constexpr int64_t kSmallMaxSmem = 200 * 1024;
+
+int small_maxes(const Plan& p) {
+  const int m = p.enum_generic.max_es;
+  return m <= 8 ? 8 : m <= 32 ? 32 : m <= 128 ? 128 : 512;
+}
+
+// The attribute is per kernel, shared by all plans: always allow the path's maximum.
+template <bool T0, int MAXES>
+cudaError_t set_small_attr(int64_t) {
+  return cudaFuncSetAttribute(small_graph_kernel<T0, MAXES>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallMaxSmem);
+}
+
+template <bool T0>
+void launch_small(cudaStream_t s, const Plan& p, const SmallGraph& g, int64_t B, int64_t iters,
+                  float t, bool low_t, float* msgs, unsigned* dacc) {
+  const dim3 grid((unsigned)B), block(kSmallThreads);
+  const size_t smem = (size_t)p.small_graph_smem;
+  switch (small_maxes(p)) {
+    case 8: small_graph_kernel<T0, 8><<<grid, block, smem, s>>>(g, B, iters, t, low_t, msgs, dacc); break;
+    case 32: small_graph_kernel<T0, 32><<<grid, block, smem, s>>>(g, B, iters, t, low_t, msgs, dacc); break;
+    case 128: small_graph_kernel<T0, 128><<<grid, block, smem, s>>>(g, B, iters, t, low_t, msgs, dacc); break;
+    default: small_graph_kernel<T0, 512><<<grid, block, smem, s>>>(g, B, iters, t, low_t, msgs, dacc); break;
+  }
+}
+
 }  // namespace
+
+cudaError_t prepare_small_graph(Plan& p) {
+  p.small_graph_smem = 0;
+  if (p.flags & PGBP_FLAG_NO_SMALL_GRAPH) return cudaSuccess;
+  if ((int64_t)p.pairwise.size() > kSmallMaxBuckets || p.num_slots == 0) return cudaSuccess;
+  const int64_t smem = (int64_t)sizeof(float) * (2 * p.num_slots + 2 * p.num_var_states);
+  if (smem > kSmallMaxSmem) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  switch (small_maxes(p)) {
+    case 8: e = set_small_attr<true, 8>(smem); if (!e) e = set_small_attr<false, 8>(smem); break;
+    case 32: e = set_small_attr<true, 32>(smem); if (!e) e = set_small_attr<false, 32>(smem); break;
+    case 128: e = set_small_attr<true, 128>(smem); if (!e) e = set_small_attr<false, 128>(smem); break;
+    default: e = set_small_attr<true, 512>(smem); if (!e) e = set_small_attr<false, 512>(smem); break;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cudaSuccess;  // path unavailable: stay on the multi-kernel path
+  }
+  p.small_graph_smem = smem;
+  return cudaSuccess;
+}
 
 size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched,
                        bool lp_batched) {
@@ -1286,12 +1475,41 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   c.omd = (float)(1.0 - damping);
   const float t = (float)temperature;
   const bool low_t = temperature < kStabilityThre;
-  if (temperature == 0.0) {
+  float* fin = (iters & 1) ? m1 : m0;
+  if (p.small_graph_smem > 0 && B <= 65535) {
+    SmallGraph g;
+    g.n_pw = (int)p.pairwise.size();
+    for (int q = 0; q < g.n_pw; ++q) g.pw[q] = dev(p.pairwise[q]);
+    g.eg = dev(p.enum_generic);
+    g.lg[0] = dev(p.logical[0]);
+    g.lg[1] = dev(p.logical[1]);
+    g.pool = dev(p.pool);
+    g.vb = dev(p.varsum_binary);
+    g.vo = dev(p.varsum_other);
+    g.vb_runs = p.varsum_binary.use_runs;
+    g.vo_runs = p.varsum_other.use_runs;
+    g.num_slots = p.num_slots;
+    g.num_var_states = p.num_var_states;
+    g.ev = evp;
+    g.evs = evs;
+    g.evb = evb;
+    g.lp = lpc;
+    g.lps = lps;
+    g.lpb = lpb;
+    g.d = c.d;
+    g.omd = c.omd;
+    ProfileScope ps(kProfSmallGraph, s);
+    if (temperature == 0.0) {
+      launch_small<true>(s, p, g, B, iters, t, low_t, m0, dacc);
+    } else {
+      launch_small<false>(s, p, g, B, iters, t, low_t, m0, dacc);
+    }
+    fin = m0;
+  } else if (temperature == 0.0) {
     iterate<true>(s, p, B, c, t, low_t, iters, m0, m1, evp, evs, evb, dacc);
   } else {
     iterate<false>(s, p, B, c, t, low_t, iters, m0, m1, evp, evs, evb, dacc);
   }
-  float* fin = (iters & 1) ? m1 : m0;
   if (p.num_edges > 0) {
     ProfileScope ps(kProfLayout, s);
     const Launch2 ln = launch2(p.num_edges, B, p.sm_count);

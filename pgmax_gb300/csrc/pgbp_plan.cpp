@@ -594,6 +594,9 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     if (bd.err) return bail(bd.err);
   }
 
+  p.flags = d->flags;
+  ce = pgbp::prepare_small_graph(p);
+  if (ce != cudaSuccess) return bail(cuda_fail(ce, "small-graph path set-up"));
   ce = cudaDeviceSynchronize();
   if (ce != cudaSuccess) return bail(cuda_fail(ce, "plan upload"));
   *out = handle;
@@ -624,6 +627,7 @@ int pgbp_plan_get_info(const pgbp_plan* plan, pgbp_plan_info* info) {
   info->num_pairwise_buckets = (int64_t)p.pairwise.size();
   info->device_bytes = p.device_bytes;
   info->num_slots = p.num_slots;
+  info->small_graph_smem_bytes = p.small_graph_smem;
   return PGBP_OK;
 }
 

@@ -38,7 +38,7 @@ class Plan:
   evidence_to_vars / num_variables.
   """
 
-  def __init__(self, wiring: Dict[str, np.ndarray], device: Optional[int] = None):
+  def __init__(self, wiring: Dict[str, np.ndarray], device: Optional[int] = None, flags: int = 0):
     torch = _require_cuda()
     self.lib = native.load()
     self.device = torch.cuda.current_device() if device is None else int(device)
@@ -81,6 +81,7 @@ class Plan:
       d.evidence_to_vars, _ = i32("evidence_to_vars")
       d.num_variables = int(wiring.get("num_variables",
                                        int(np.max(wiring["evidence_to_vars"], initial=-1)) + 1))
+    d.flags = int(flags)
     handle = ctypes.c_void_p()
     with torch.cuda.device(self.device):
       native.check(self.lib.pgbp_plan_create(ctypes.byref(d), self.device, ctypes.byref(handle)),

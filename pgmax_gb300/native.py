@@ -96,6 +96,7 @@ class WiringDesc(ctypes.Structure):
       ("pool_choices_msg_indices", _p32), ("pool_num_factors", _i64),
       ("pool_indicators_edge_states", _p32),
       ("num_variables", _i64), ("evidence_to_vars", _p32),
+      ("flags", _i64),
   ]
 
 
@@ -103,14 +104,18 @@ class PlanInfo(ctypes.Structure):
   _fields_ = [(n, _i64) for n in (
       "num_edge_states", "num_var_states", "num_edges", "num_variables", "num_potentials",
       "num_enum_factors", "num_enum_pairwise_factors", "num_or_factors", "num_and_factors",
-      "num_pool_factors", "num_pairwise_buckets", "device_bytes", "num_slots")]
+      "num_pool_factors", "num_pairwise_buckets", "device_bytes", "num_slots",
+      "small_graph_smem_bytes")]
+
+FLAG_NO_SMALL_GRAPH = 1
 
 
 class Profile(ctypes.Structure):
-  _fields_ = [("launches", _i64 * 8), ("milliseconds", ctypes.c_double * 8)]
+  _fields_ = [("launches", _i64 * 9), ("milliseconds", ctypes.c_double * 9)]
 
 
-PROFILE_CLASSES = ("varsum", "pairwise", "enum_generic", "or", "and", "pool", "layout", "readout")
+PROFILE_CLASSES = ("varsum", "pairwise", "enum_generic", "or", "and", "pool", "layout", "readout",
+                   "small_graph")
 
 # (name, restype, argtypes) of every symbol include/pgbp.h declares
 SIGNATURES = [

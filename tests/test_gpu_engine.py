@@ -26,12 +26,17 @@ def _torch():
   return torch
 
 
-def _plan(wiring):
-  from pgmax_gb300 import engine  # pylint: disable=g-import-not-at-top
+# Execution paths: "auto" lets small graphs run one CTA per instance with their state in shared
+# memory (all iterations in one launch); "multi" forces one launch per kernel class per iteration.
+PATHS = ("auto", "multi")
+
+
+def _plan(wiring, path="auto"):
+  from pgmax_gb300 import engine, native  # pylint: disable=g-import-not-at-top
   w = dict(wiring)
   if "evidence_to_vars" in w:
     w["num_variables"] = int(np.max(w["evidence_to_vars"], initial=-1)) + 1
-  return engine.Plan(w)
+  return engine.Plan(w, flags=native.FLAG_NO_SMALL_GRAPH if path == "multi" else 0)
 
 
 def _np(t):
@@ -52,10 +57,11 @@ def _near_tie(bel, starts, ends, tol=1e-4):
   return np.array(out)
 
 
+@pytest.mark.parametrize("exec_path", PATHS)
 @pytest.mark.parametrize("path", RUNS, ids=fixtures.fixture_id)
-def test_run_matches_oracle_and_reference(path):
+def test_run_matches_oracle_and_reference(path, exec_path):
   f = fixtures.load(path)
-  plan = _plan(f["wiring"])
+  plan = _plan(f["wiring"], exec_path)
   T = float(f["temperature"])
   args = (int(f["num_iters"]), float(f["damping"]), T)
   out, deltas = plan.run(f["log_potentials"], f["evidence"], f["ftov_msgs_in"], *args)
@@ -88,11 +94,12 @@ def test_run_matches_oracle_and_reference(path):
 PERTURBED_T_POS_ATOL = 1e-4
 
 
+@pytest.mark.parametrize("exec_path", PATHS)
 @pytest.mark.parametrize("name", ["case_rbm_s0", "case_mixed_T0", "case_mixed_T1", "case_deconv_T1",
                                   "case_potts_K8"])
-def test_batched_run_equals_single_instances(name):
+def test_batched_run_equals_single_instances(name, exec_path):
   f = fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
-  plan = _plan(f["wiring"])
+  plan = _plan(f["wiring"], exec_path)
   w = oracle.Wiring(f["wiring"])
   rng = np.random.default_rng(1)
   B = 37
@@ -122,9 +129,10 @@ def test_batched_run_equals_single_instances(name):
                                     ("case_ising50_T0", 16)])
 def test_four_instances_per_thread_path(name, B):
   """Batches that are a multiple of 4 run the 4-instances-per-thread kernels (binary pairwise
-  factors, binary variable sums); every instance must equal its own oracle run."""
+  factors, binary variable sums) on the multi-kernel path; every instance must equal its own
+  oracle run."""
   f = fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
-  plan = _plan(f["wiring"])
+  plan = _plan(f["wiring"], "multi")
   w = oracle.Wiring(f["wiring"])
   rng = np.random.default_rng(3)
   ev = (f["evidence"][None] + rng.gumbel(size=(B,) + f["evidence"].shape)).astype(np.float32)
@@ -144,9 +152,10 @@ def test_four_instances_per_thread_path(name, B):
         np.testing.assert_allclose(deltas[b], d, atol=ATOL, rtol=0)
 
 
-def test_runs_are_bitwise_deterministic():
+@pytest.mark.parametrize("exec_path", PATHS)
+def test_runs_are_bitwise_deterministic(exec_path):
   f = fixtures.load(f"{fixtures.FIXTURES}/case_deconv_T1.npz")
-  plan = _plan(f["wiring"])
+  plan = _plan(f["wiring"], exec_path)
   a = _np(plan.run(f["log_potentials"], f["evidence"], f["ftov_msgs_in"], 40, 0.5, 1.0)[0])
   b = _np(plan.run(f["log_potentials"], f["evidence"], f["ftov_msgs_in"], 40, 0.5, 1.0)[0])
   np.testing.assert_array_equal(a, b)
@@ -212,6 +221,12 @@ def test_drop_in_api_end_to_end():
   with pytest.warns(UserWarning, match="deprecated"):
     again = bp.run_bp(bp.init(evidence_updates=ev), num_iters=3)
   assert again.ftov_msgs.shape == bp_arrays.ftov_msgs.shape
+
+
+def test_small_graph_path_is_taken_for_small_graphs():
+  f = fixtures.load(f"{fixtures.FIXTURES}/case_ising50_T1.npz")
+  assert _plan(f["wiring"]).info["small_graph_smem_bytes"] > 0
+  assert _plan(f["wiring"], "multi").info["small_graph_smem_bytes"] == 0
 
 
 def test_full_size_rbm_batch_bit_exact_on_sampled_instances():
