@@ -96,7 +96,9 @@ def run_ising(args):
   from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
   n, iters = 50, 1000
   fg, variables = build_ising(n)
-  bp = infer.BP(fg.bp_state)
+  flags = {"auto": 0, "multi": native.FLAG_NO_SMALL_GRAPH, "small": native.FLAG_PATH_SMALL,
+           "cluster": native.FLAG_PATH_CLUSTER}[args.exec_path]
+  bp = infer.BP(fg.bp_state, exec_flags=flags)
   rng = np.random.default_rng(0)
   ev = rng.gumbel(size=(n, n, 2)).astype(np.float32)
   arrays = bp.init(evidence_updates={variables: ev})
@@ -138,7 +140,7 @@ def run_ising(args):
       "data": "synthetic (Gumbel(0,1) evidence, seed 0)",
       "config": {"workload": "ising50x50_toroidal", "batch": 1, "num_iters": iters,
                  "temperatures": [1.0, 0.0], "damping": 0.5, "num_edges": num_edges,
-                 "path": "small_graph" if info["small_graph_smem_bytes"] else "multi_kernel"},
+                 "exec_path": args.exec_path},
       "ns_per_iteration": iter_ns,
       "kernel_time_share": {k: v[1] for k, v in prof.items() if v[0]},
       "roofline": {"bound": "latency (2 block barriers per iteration)",
@@ -320,6 +322,8 @@ def main():
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="pgbp", choices=["pgbp", "reference"])
   ap.add_argument("--no-cpu-baseline", action="store_true")
+  ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
+                  help="execution path of the ising workload (auto: timed choice)")
   ap.add_argument("--workload", default="rbm", choices=["rbm", "ising"],
                   help="rbm: the headline RBM perturb-and-MAP batch (default); ising: the 50x50 "
                        "toroidal Ising configuration")

@@ -84,12 +84,21 @@ typedef struct {
    * only by pgbp_decode / pgbp_marginals; may be NULL. */
   int64_t num_variables;
   const int32_t* evidence_to_vars;             /* [num_var_states] */
-  /* Execution options (0 = automatic): PGBP_FLAG_NO_SMALL_GRAPH keeps every run on the
-   * multi-kernel path even when the graph fits the one-CTA-per-instance shared-memory path. */
+  /* Execution options, 0 = automatic. Three execution paths exist: multi-kernel (one launch per
+   * kernel class per iteration, any size), one CTA per instance with its state in shared memory,
+   * and one thread-block cluster per instance; the last two run every iteration in one launch and
+   * exist for graphs whose state fits in shared memory. Automatic mode times the eligible paths
+   * once per (batch, temperature == 0) on the first pgbp_run and keeps the fastest (the timing
+   * synchronises the stream once; under stream capture the single-CTA path is used). The flags
+   * force a path instead (a forced path the graph is not eligible for falls back to
+   * multi-kernel); results are identical on every path. */
   int64_t flags;
 } pgbp_wiring_desc;
 
-#define PGBP_FLAG_NO_SMALL_GRAPH 1
+#define PGBP_FLAG_NO_SMALL_GRAPH 1 /* multi-kernel only; the other paths are not even prepared */
+#define PGBP_FLAG_PATH_SMALL 2
+#define PGBP_FLAG_PATH_CLUSTER 4
+#define PGBP_FLAG_PATH_MULTI 8
 
 typedef struct pgbp_plan pgbp_plan;
 

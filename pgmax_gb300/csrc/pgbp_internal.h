@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -102,6 +104,10 @@ struct Plan {
   PoolSet pool;
   int64_t flags = 0;
   int64_t small_graph_smem = 0;  // bytes per CTA of the small-graph path; 0 = not eligible
+  int cluster_size = 0;          // CTAs per instance of the cluster path; 0 = not eligible
+  // execution path chosen per (batch, temperature == 0) by timing the eligible paths once
+  mutable std::mutex tune_mu;
+  mutable std::map<std::pair<int64_t, bool>, int> tuned_path;
   int64_t device_bytes = 0;
   std::vector<void*> allocations;
   int64_t num_enum_factors = 0, num_enum_pairwise = 0;

@@ -23,6 +23,7 @@
 // Everything is float32 in the reference's operation order; the build uses -fmad=false so no
 // multiply-add is contracted. At temperature 0 the engine reproduces the oracle bit for bit; at
 // temperature > 0 expf/logf/log1pf/expm1f differ from glibc's by an ulp or two.
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include <algorithm>
@@ -1009,6 +1010,72 @@ __global__ void __launch_bounds__(kSmallThreads) small_graph_kernel(SmallGraph g
   for (int64_t i = tid; i < g.num_slots; i += nt) msgs[i * B + inst] = cur[i];
 }
 
+// ----------------------------------------------------------------------------- clustered graphs
+// One thread-block cluster per instance: the cluster's CTAs split the variable-sum and factor
+// phases between them and meet at hardware cluster barriers (barrier.cluster with release /
+// acquire semantics, which order their global-memory writes), so an iteration costs two cluster
+// barriers and the work of one instance is spread over up to 16 SMs. State stays in the run
+// layout in global memory (L2-resident for the graphs this path is chosen for).
+template <bool T0, int MAXES>
+__global__ void __launch_bounds__(kSmallThreads) cluster_graph_kernel(SmallGraph g, int64_t B,
+                                                                      int64_t iters, float t,
+                                                                      bool low_t, float* m0,
+                                                                      float* m1, float* vsum,
+                                                                      unsigned* __restrict__ dacc) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ float red[32];
+  const int64_t csize = (int64_t)cluster.num_blocks();
+  const int64_t inst = blockIdx.x / csize;
+  const int64_t tid = (int64_t)cluster.block_rank() * blockDim.x + threadIdx.x;
+  const int64_t nt = csize * blockDim.x;
+  Fused c;
+  c.vsum = vsum;
+  c.lp = g.lp;
+  c.lps = g.lps;
+  c.lpb = g.lpb;
+  c.B = B;
+  c.d = g.d;
+  c.omd = g.omd;
+  float* cur = m0;
+  float* nxt = m1;
+  for (int64_t it = 0; it < iters; ++it) {
+    for (int64_t u = tid; u < g.vb.count; u += nt)
+      varsum_binary_unit(g.vb, g.vb_runs, u, inst, cur, g.ev, g.evs, g.evb, vsum, B);
+    for (int64_t u = tid; u < g.vo.count; u += nt)
+      varsum_other_unit(g.vo, g.vo_runs, u, inst, cur, g.ev, g.evs, g.evb, vsum, B);
+    cluster.sync();
+    c.cur = cur;
+    c.nxt = nxt;
+    float dmax = 0.0f;
+    for (int q = 0; q < g.n_pw; ++q) {
+      const PairwiseDev& p = g.pw[q];
+      for (int64_t u = tid; u < p.count; u += nt) {
+        EdgeRef r1, r2;
+        pairwise_refs(p, __ldg(p.rec + u), r1, r2);
+        const int64_t k0 = __ldg(p.cfg_begin + u);
+        if (p.n1 == 2 && p.n2 == 2) {
+          pairwise_body<2, 2, T0>(c, r1, r2, k0, 2, 2, inst, t, dmax);
+        } else {
+          pairwise_body<0, 0, T0>(c, r1, r2, k0, p.n1, p.n2, inst, t, dmax);
+        }
+      }
+    }
+    for (int64_t f = tid; f < g.eg.count; f += nt)
+      enum_generic_unit<MAXES, T0>(c, g.eg, f, inst, t, dmax);
+    for (int w = 0; w < 2; ++w)
+      for (int64_t f = tid; f < g.lg[w].count; f += nt)
+        logical_unit<T0>(c, g.lg[w], f, inst, t, low_t, 1, dmax);
+    for (int64_t f = tid; f < g.pool.count; f += nt) pool_unit<T0>(c, g.pool, f, inst, t, 1, dmax);
+    const float m = block_max_all(dmax, red);
+    if (threadIdx.x == 0) atomicMax(dacc + it * B + inst, __float_as_uint(m));
+    cluster.sync();
+    float* sw = cur;
+    cur = nxt;
+    nxt = sw;
+  }
+}
+
 // Flat beliefs from caller-layout arrays ([B, n] rows): inferer.py:218-222.
 __global__ void __launch_bounds__(256) beliefs_kernel(const int32_t* __restrict__ vs_off,
                                                       const int32_t* __restrict__ vs_edges,
@@ -1374,12 +1441,144 @@ void launch_small(cudaStream_t s, const Plan& p, const SmallGraph& g, int64_t B,
   }
 }
 
+template <bool T0, int MAXES>
+cudaError_t launch_cluster_t(cudaStream_t s, const SmallGraph& g, int64_t B, int64_t iters, float t,
+                             bool low_t, float* m0, float* m1, float* vsum, unsigned* dacc,
+                             int csize) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(B * csize));
+  cfg.blockDim = dim3(kSmallThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, cluster_graph_kernel<T0, MAXES>, g, B, iters, t, low_t, m0, m1,
+                            vsum, dacc);
+}
+
+template <bool T0>
+cudaError_t launch_cluster(cudaStream_t s, const Plan& p, const SmallGraph& g, int64_t B,
+                           int64_t iters, float t, bool low_t, float* m0, float* m1, float* vsum,
+                           unsigned* dacc) {
+  const int cs = p.cluster_size;
+  switch (small_maxes(p)) {
+    case 8: return launch_cluster_t<T0, 8>(s, g, B, iters, t, low_t, m0, m1, vsum, dacc, cs);
+    case 32: return launch_cluster_t<T0, 32>(s, g, B, iters, t, low_t, m0, m1, vsum, dacc, cs);
+    case 128: return launch_cluster_t<T0, 128>(s, g, B, iters, t, low_t, m0, m1, vsum, dacc, cs);
+    default: return launch_cluster_t<T0, 512>(s, g, B, iters, t, low_t, m0, m1, vsum, dacc, cs);
+  }
+}
+
+template <bool T0, int MAXES>
+cudaError_t allow_big_cluster() {
+  return cudaFuncSetAttribute(cluster_graph_kernel<T0, MAXES>,
+                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
+// Largest cluster (16, else 8) that a 1024-thread CTA of the cluster kernel can be launched with.
+int cluster_size_for(const Plan& p) {
+  cudaError_t e = cudaSuccess;
+  switch (small_maxes(p)) {
+    case 8: e = allow_big_cluster<true, 8>(); if (!e) e = allow_big_cluster<false, 8>(); break;
+    case 32: e = allow_big_cluster<true, 32>(); if (!e) e = allow_big_cluster<false, 32>(); break;
+    case 128: e = allow_big_cluster<true, 128>(); if (!e) e = allow_big_cluster<false, 128>(); break;
+    default: e = allow_big_cluster<true, 512>(); if (!e) e = allow_big_cluster<false, 512>(); break;
+  }
+  for (int cs : {16, 8, 4}) {
+    if (cs == 16 && e != cudaSuccess) continue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)cs);
+    cfg.blockDim = dim3(kSmallThreads);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    cudaError_t q = cudaOccupancyMaxActiveClusters(&n, cluster_graph_kernel<true, 8>, &cfg);
+    if (q == cudaSuccess && n > 0) return cs;
+    cudaGetLastError();
+  }
+  cudaGetLastError();
+  return 0;
+}
+
 }  // namespace
+
+enum { kPathMulti = 0, kPathSmall = 1, kPathCluster = 2 };
+
+// Execution path for (batch, temperature == 0): the cached choice, else the fastest of the
+// eligible paths timed on a short run (the trial overwrites the run's first message buffer and
+// residuals, which are then restored from the normalised inputs in `tmp`). Inside a stream
+// capture nothing is timed and the single-CTA path is used.
+template <class RunPath>
+int choose_path(const Plan& p, cudaStream_t s, int64_t B, bool t0, bool cluster_ok,
+                RunPath& run_path, const float* tmp, float* m0, unsigned* dacc, int64_t iters) {
+  const std::pair<int64_t, bool> key{B, t0};
+  {
+    std::lock_guard<std::mutex> lock(p.tune_mu);
+    auto it = p.tuned_path.find(key);
+    if (it != p.tuned_path.end()) return it->second;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return kPathSmall;
+  }
+  const int64_t trial = std::min<int64_t>(iters, 8);
+  int best = kPathSmall;
+  float best_ms = 0.0f;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    return kPathSmall;
+  }
+  const int cands[3] = {kPathSmall, kPathCluster, kPathMulti};
+  bool any = false;
+  for (int cand : cands) {
+    if (cand == kPathCluster && !cluster_ok) continue;
+    run_path(cand, 1);  // warm the path (first launches of a kernel cost extra)
+    cudaEventRecord(e0, s);
+    run_path(cand, trial);
+    cudaEventRecord(e1, s);
+    float ms = 0.0f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (!any || ms < best_ms) {
+      best = cand;
+      best_ms = ms;
+      any = true;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // restore the run's initial state
+  if (p.num_edges > 0) {
+    const Launch2 ln = launch2(p.num_edges, B, p.sm_count);
+    normalize_pack_kernel<<<ln.grid, ln.block, 0, s>>>(p.edge_start, p.edge_slot, p.num_edges, tmp,
+                                                        m0, B);
+  }
+  cudaMemsetAsync(dacc, 0, sizeof(unsigned) * (size_t)(iters * B), s);
+  std::lock_guard<std::mutex> lock(p.tune_mu);
+  p.tuned_path[key] = best;
+  return best;
+}
 
 cudaError_t prepare_small_graph(Plan& p) {
   p.small_graph_smem = 0;
+  p.cluster_size = 0;
   if (p.flags & PGBP_FLAG_NO_SMALL_GRAPH) return cudaSuccess;
   if ((int64_t)p.pairwise.size() > kSmallMaxBuckets || p.num_slots == 0) return cudaSuccess;
+  p.cluster_size = cluster_size_for(p);
   const int64_t smem = (int64_t)sizeof(float) * (2 * p.num_slots + 2 * p.num_var_states);
   if (smem > kSmallMaxSmem) return cudaSuccess;
   cudaError_t e = cudaSuccess;
@@ -1475,9 +1674,11 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   c.omd = (float)(1.0 - damping);
   const float t = (float)temperature;
   const bool low_t = temperature < kStabilityThre;
-  float* fin = (iters & 1) ? m1 : m0;
-  if (p.small_graph_smem > 0 && B <= 65535) {
-    SmallGraph g;
+  const bool t0 = temperature == 0.0;
+  SmallGraph g;
+  const bool small_ok = p.small_graph_smem > 0 && B <= 65535;
+  const bool cluster_ok = small_ok && p.cluster_size > 0;
+  if (small_ok) {
     g.n_pw = (int)p.pairwise.size();
     for (int q = 0; q < g.n_pw; ++q) g.pw[q] = dev(p.pairwise[q]);
     g.eg = dev(p.enum_generic);
@@ -1498,18 +1699,38 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     g.lpb = lpb;
     g.d = c.d;
     g.omd = c.omd;
-    ProfileScope ps(kProfSmallGraph, s);
-    if (temperature == 0.0) {
-      launch_small<true>(s, p, g, B, iters, t, low_t, m0, dacc);
-    } else {
-      launch_small<false>(s, p, g, B, iters, t, low_t, m0, dacc);
-    }
-    fin = m0;
-  } else if (temperature == 0.0) {
-    iterate<true>(s, p, B, c, t, low_t, iters, m0, m1, evp, evs, evb, dacc);
-  } else {
-    iterate<false>(s, p, B, c, t, low_t, iters, m0, m1, evp, evs, evb, dacc);
   }
+  // run `n` iterations on execution path `path`; returns the buffer holding the result
+  auto run_path = [&](int path, int64_t n) -> float* {
+    if (path == kPathSmall) {
+      ProfileScope ps(kProfSmallGraph, s);
+      if (t0) launch_small<true>(s, p, g, B, n, t, low_t, m0, dacc);
+      else launch_small<false>(s, p, g, B, n, t, low_t, m0, dacc);
+      return m0;
+    }
+    if (path == kPathCluster) {
+      ProfileScope ps(kProfSmallGraph, s);
+      if (t0) launch_cluster<true>(s, p, g, B, n, t, low_t, m0, m1, vsum, dacc);
+      else launch_cluster<false>(s, p, g, B, n, t, low_t, m0, m1, vsum, dacc);
+      return (n & 1) ? m1 : m0;
+    }
+    if (t0) iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc);
+    else iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc);
+    return (n & 1) ? m1 : m0;
+  };
+  int path = kPathMulti;
+  if (small_ok) {
+    if (p.flags & PGBP_FLAG_PATH_SMALL) {
+      path = kPathSmall;
+    } else if ((p.flags & PGBP_FLAG_PATH_CLUSTER) && cluster_ok) {
+      path = kPathCluster;
+    } else if (p.flags & PGBP_FLAG_PATH_MULTI) {
+      path = kPathMulti;
+    } else {
+      path = choose_path(p, s, B, t0, cluster_ok, run_path, tmp, m0, dacc, iters);
+    }
+  }
+  float* fin = run_path(path, iters);
   if (p.num_edges > 0) {
     ProfileScope ps(kProfLayout, s);
     const Launch2 ln = launch2(p.num_edges, B, p.sm_count);

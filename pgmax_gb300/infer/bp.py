@@ -28,9 +28,11 @@ class BeliefPropagation(Inferer):
   context: Any = None
 
 
-def BP(bp_state: BPState, temperature: Optional[float] = 0.0) -> BeliefPropagation:  # pylint: disable=invalid-name
-  """Returns the belief propagation functions of `bp_state`'s factor graph."""
-  ctx = InfererContext(bp_state)
+def BP(bp_state: BPState, temperature: Optional[float] = 0.0,  # pylint: disable=invalid-name
+       exec_flags: int = 0) -> BeliefPropagation:
+  """Returns the belief propagation functions of `bp_state`'s factor graph. `exec_flags` (not in
+  PGMax) forces an execution path of the engine (pgmax_gb300.native.FLAG_*)."""
+  ctx = InfererContext(bp_state, exec_flags)
   default_t = temperature
 
   def run_with_diffs(bp_arrays: BPArrays, num_iters: int, damping: float = 0.5,

@@ -44,6 +44,8 @@ class InfererContext:
   """Shared inference context (pgmax/infer/inferer.py:55-225)."""
 
   bp_state: BPState
+  # execution flags of the compiled plan (pgmax_gb300.native.FLAG_*; 0 = automatic path choice)
+  exec_flags: int = 0
 
   def __post_init__(self):
     fg_state = self.bp_state.fg_state
@@ -96,7 +98,7 @@ class InfererContext:
   def plan(self):
     if self._plan is None:
       from .. import engine  # pylint: disable=g-import-not-at-top
-      object.__setattr__(self, "_plan", engine.Plan(self.flat_wiring()))
+      object.__setattr__(self, "_plan", engine.Plan(self.flat_wiring(), flags=self.exec_flags))
       for t in FAC_TO_VAR_UPDATES:
         self.inference_arguments[t]["plan"] = self._plan
     return self._plan

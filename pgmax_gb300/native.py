@@ -108,6 +108,9 @@ class PlanInfo(ctypes.Structure):
       "small_graph_smem_bytes")]
 
 FLAG_NO_SMALL_GRAPH = 1
+FLAG_PATH_SMALL = 2
+FLAG_PATH_CLUSTER = 4
+FLAG_PATH_MULTI = 8
 
 
 class Profile(ctypes.Structure):

@@ -26,9 +26,11 @@ def _torch():
   return torch
 
 
-# Execution paths: "auto" lets small graphs run one CTA per instance with their state in shared
-# memory (all iterations in one launch); "multi" forces one launch per kernel class per iteration.
-PATHS = ("auto", "multi")
+# Execution paths (include/pgbp.h): "multi" = one launch per kernel class per iteration; "small" =
+# one CTA per instance with its state in shared memory; "cluster" = one thread-block cluster per
+# instance; "auto" = the fastest of the eligible ones, timed on first use. Every path must give
+# the same results.
+PATHS = ("auto", "multi", "small", "cluster")
 
 
 def _plan(wiring, path="auto"):
@@ -36,7 +38,9 @@ def _plan(wiring, path="auto"):
   w = dict(wiring)
   if "evidence_to_vars" in w:
     w["num_variables"] = int(np.max(w["evidence_to_vars"], initial=-1)) + 1
-  return engine.Plan(w, flags=native.FLAG_NO_SMALL_GRAPH if path == "multi" else 0)
+  flags = {"auto": 0, "multi": native.FLAG_NO_SMALL_GRAPH, "small": native.FLAG_PATH_SMALL,
+           "cluster": native.FLAG_PATH_CLUSTER}[path]
+  return engine.Plan(w, flags=flags)
 
 
 def _np(t):
@@ -227,6 +231,20 @@ def test_small_graph_path_is_taken_for_small_graphs():
   f = fixtures.load(f"{fixtures.FIXTURES}/case_ising50_T1.npz")
   assert _plan(f["wiring"]).info["small_graph_smem_bytes"] > 0
   assert _plan(f["wiring"], "multi").info["small_graph_smem_bytes"] == 0
+
+
+def test_all_paths_agree_bitwise_on_a_batch():
+  f = fixtures.load(f"{fixtures.FIXTURES}/case_deconv_T1.npz")
+  rng = np.random.default_rng(9)
+  ev = (f["evidence"][None] + rng.gumbel(size=(6,) + f["evidence"].shape)).astype(np.float32)
+  outs = []
+  for path in PATHS:
+    plan = _plan(f["wiring"], path)
+    o, d = plan.run(f["log_potentials"], ev, f["ftov_msgs_in"], 17, 0.5, 1.0)
+    outs.append((_np(o), _np(d)))
+  for o, d in outs[1:]:
+    np.testing.assert_array_equal(o, outs[0][0])
+    np.testing.assert_array_equal(d, outs[0][1])
 
 
 def test_full_size_rbm_batch_bit_exact_on_sampled_instances():
