@@ -263,13 +263,10 @@ def cpu_baseline(wiring, lp, ev, target_s=12.0):
 
 
 def dist_setup(n_gpus):
-  world = int(os.environ.get("WORLD_SIZE", "1"))
-  rank = int(os.environ.get("RANK", "0"))
-  local = int(os.environ.get("LOCAL_RANK", "0"))
-  if world > 1:
-    import torch.distributed as dist  # pylint: disable=g-import-not-at-top
-    dist.init_process_group("nccl")
-  return world, rank, local
+  """Replicas: one process per GPU under torchrun, each with its own batch (weak scaling)."""
+  from pgmax_gb300 import distributed  # pylint: disable=g-import-not-at-top
+  del n_gpus
+  return distributed.init("nccl")
 
 
 def run_reference(args):
@@ -362,19 +359,14 @@ def main():
 
   stream = torch.cuda.current_stream(dev)
 
+  from pgmax_gb300 import distributed  # pylint: disable=g-import-not-at-top
+
   def barrier():
-    if world > 1:
-      import torch.distributed as dist  # pylint: disable=g-import-not-at-top
-      dist.barrier()
+    distributed.barrier()
     torch.cuda.synchronize(dev)
 
   def max_over_ranks(x):
-    if world > 1:
-      import torch.distributed as dist  # pylint: disable=g-import-not-at-top
-      t = torch.tensor([x], dtype=torch.float64, device=dev)
-      dist.all_reduce(t, op=dist.ReduceOp.MAX)
-      return float(t.item())
-    return x
+    return distributed.max_over_ranks(x, device=dev)
 
   for _ in range(args.warmup):
     step_device()
