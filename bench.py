@@ -165,6 +165,186 @@ def run_ising(args):
   return 0
 
 
+ADJ_N, ADJ_B, ADJ_ITERS, ADJ_CKPT, ADJ_FLIP = 64, 32, 100, 10, 0.1
+
+
+def shape_images(n, batch, seed, flip):
+  """`batch` binary n x n images, each the union of 2-6 random axis-aligned rectangles and
+  ellipses, and their observations with every pixel flipped with probability `flip`."""
+  rng = np.random.default_rng(seed)
+  yy, xx = np.mgrid[0:n, 0:n]
+  clean = np.zeros((batch, n, n), dtype=np.int64)
+  for b in range(batch):
+    for _ in range(rng.integers(2, 7)):
+      cy, cx = rng.uniform(0, n, size=2)
+      hy, hx = rng.uniform(n / 16, n / 4, size=2)
+      if rng.random() < 0.5:
+        clean[b] |= ((np.abs(yy - cy) <= hy) & (np.abs(xx - cx) <= hx))
+      else:
+        clean[b] |= (((yy - cy) / hy) ** 2 + ((xx - cx) / hx) ** 2 <= 1.0)
+  noisy = clean ^ (rng.random(clean.shape) < flip)
+  return clean, noisy
+
+
+def build_grid(n):
+  """Open n x n binary grid with top-down and left-right PairwiseFactorGroups."""
+  from pgmax_gb300 import fgraph, fgroup, vgroup  # pylint: disable=g-import-not-at-top
+  grid = vgroup.NDVarArray(num_states=2, shape=(n, n))
+  fg = fgraph.FactorGraph(variable_groups=grid)
+  td = fgroup.PairwiseFactorGroup(
+      variables_for_factors=[[grid[i, j], grid[i + 1, j]] for i in range(n - 1) for j in range(n)],
+      log_potential_matrix=np.zeros((2, 2)))
+  lr = fgroup.PairwiseFactorGroup(
+      variables_for_factors=[[grid[i, j], grid[i, j + 1]] for i in range(n) for j in range(n - 1)],
+      log_potential_matrix=np.zeros((2, 2)))
+  fg.add_factors([td, lr])
+  return fg, grid, td, lr
+
+
+def run_adjoint(args):
+  """Differentiable loopy BP: one step = forward + hand-written backward of the mean negative
+  log-marginal of the clean labels of 32 noisy 64x64 binary images with respect to a shared
+  top-down 2x2 log potential, a shared left-right one and a unary scale (100 iterations at
+  temperature 1, damping 0.5, messages checkpointed every 10 iterations), through the drop-in
+  API: bp.init -> bp.run -> get_beliefs -> get_marginals -> loss.backward()."""
+  import torch  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
+  n, B, iters = ADJ_N, ADJ_B, ADJ_ITERS
+  fg, grid, td, lr = build_grid(n)
+  bp = infer.BP(fg.bp_state, temperature=1.0, checkpoint_every=ADJ_CKPT)
+  num_edges = 2 * 2 * n * (n - 1)
+  dev = torch.device("cuda", 0)
+  stream = torch.cuda.current_stream(dev)
+  clean, noisy = shape_images(n, B, 0, ADJ_FLIP)
+  noisy_host = torch.as_tensor(noisy.astype(np.float32)).pin_memory()
+  labels = torch.as_tensor(clean, device=dev)
+  w_td = torch.tensor([[0.5, -0.5], [-0.5, 0.5]], device=dev, requires_grad=True)
+  w_lr = torch.tensor([[0.5, -0.5], [-0.5, 0.5]], device=dev, requires_grad=True)
+  scale = torch.tensor(1.0, device=dev, requires_grad=True)
+  lo, hi = float(np.log(ADJ_FLIP)), float(np.log1p(-ADJ_FLIP))
+  loss_host = torch.empty((), dtype=torch.float32).pin_memory()
+
+  def forward(obs):
+    # log p(observed | state): rows state 0 / state 1 of every pixel
+    logp = torch.stack([torch.where(obs == 0, hi, lo), torch.where(obs == 1, hi, lo)], dim=-1)
+    arrays = bp.init(log_potentials_updates={td: w_td, lr: w_lr},
+                     evidence_updates={grid: scale * logp})
+    arrays = bp.run(arrays, num_iters=iters, damping=0.5, temperature=1.0)
+    marg = infer.get_marginals(bp.get_beliefs(arrays))[grid]
+    return -torch.log(torch.gather(marg, -1, labels[..., None])).mean()
+
+  obs_static = noisy_host.to(dev)
+
+  def step(events=None):
+    if events:
+      events[0].record(torch.cuda.current_stream(dev))
+    loss = forward(obs_static)
+    if events:
+      events[1].record(torch.cuda.current_stream(dev))
+    for p in (w_td, w_lr, scale):
+      p.grad = None
+    loss.backward()
+    if events:
+      events[2].record(torch.cuda.current_stream(dev))
+    return loss
+
+  # warm-up on a side stream (what CUDA-graph capture of an autograd step requires), eager timing
+  side = torch.cuda.Stream(dev)
+  side.wait_stream(stream)
+  with torch.cuda.stream(side):
+    for _ in range(args.warmup):
+      step()
+    ev_pairs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)]
+                for _ in range(args.steps)]
+    for k in range(args.steps):
+      step(events=ev_pairs[k])
+  stream.wait_stream(side)
+  torch.cuda.synchronize()
+  fwd_ms = sum(e[0].elapsed_time(e[1]) for e in ev_pairs) / args.steps
+  bwd_ms = sum(e[1].elapsed_time(e[2]) for e in ev_pairs) / args.steps
+  # the step captured once in a CUDA graph: every replay runs every kernel of the step again
+  graph = torch.cuda.CUDAGraph()
+  with torch.cuda.graph(graph):
+    loss_static = step()
+  graph.replay()
+  torch.cuda.synchronize()
+  s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  with ClockSampler(0) as clocks:
+    s0.record(stream)
+    for _ in range(args.steps):
+      graph.replay()
+    s1.record(stream)
+    torch.cuda.synchronize()
+  ms = s0.elapsed_time(s1)
+  # end to end: observations copied from pinned host memory and the loss read back every step
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  for _ in range(args.steps):
+    obs_static.copy_(noisy_host, non_blocking=True)
+    graph.replay()
+    loss_host.copy_(loss_static.detach(), non_blocking=True)
+  e1.record(stream)
+  torch.cuda.synchronize()
+  e2e_ms = e0.elapsed_time(e1)
+  native.profile_read()
+  native.profile_enable(True)
+  step()
+  torch.cuda.synchronize()
+  native.profile_enable(False)
+  prof = native.profile_read()
+  units = B * num_edges * iters
+  # kernels of one step: the forward engine's (profiled per launch) plus the adjoint's, counted
+  # from its structure (per chunk: normalise, k variable sums, k - 1 factor passes; per iteration
+  # backwards: factor pass + variable-sum pass; one batch reduction of the shared potentials)
+  n_buckets = bp.context.plan.info["num_pairwise_buckets"]
+  n_ck = -(-iters // ADJ_CKPT)
+  adj_kernels = (n_ck * (1 + ADJ_CKPT + (ADJ_CKPT - 1) * n_buckets) + iters * (n_buckets + 1) + 1)
+  fwd_kernels = sum(v[0] for kk, v in prof.items() if kk != "adjoint")
+  line = {
+      "metric": "edge-msg updates/s (forward + backward)", "value": units * args.steps / (ms / 1e3),
+      "unit": "edge-msg updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+      "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+      "vs_baseline": None, "dtype": "f32",
+      "data": "synthetic (rectangles/ellipses, 10% pixel flips, seed 0)",
+      "config": {"workload": "adjoint_grid64_b32", "batch": B, "num_iters": iters,
+                 "temperature": 1.0, "damping": 0.5, "checkpoint_every": ADJ_CKPT,
+                 "num_edges": num_edges, "step": "forward + backward, captured in a CUDA graph",
+                 "l2": "inputs smaller than L2 (no flush)"},
+      "eager_ms_per_step": fwd_ms + bwd_ms,
+      "forward_ms_eager": fwd_ms, "backward_ms_eager": bwd_ms,
+      "kernel_time_share": {k: v[1] for k, v in prof.items() if v[0]},
+      "gpu_launches": int((fwd_kernels + adj_kernels) * args.steps),
+      "e2e": {"value": units * args.steps / (e2e_ms / 1e3), "unit": "edge-msg updates/s",
+              "h2d_bytes_per_step": int(noisy_host.numel() * 4), "d2h_bytes_per_step": 4},
+      "clocks": clocks.summary(),
+      "loss": float(loss_static.detach()),
+  }
+  if not args.no_cpu_baseline:
+    from oracle import bp_torch  # pylint: disable=g-import-not-at-top
+    g = bp_torch.EnumGraph(bp.context.flat_wiring())
+    nb = 2
+    cores = torch.get_num_threads()
+    lp = bp.init(log_potentials_updates={td: w_td.detach().cpu(), lr: w_lr.detach().cpu()}
+                 ).log_potentials.detach().cpu().double()
+    wt = lp.clone().requires_grad_()
+    obs = torch.as_tensor(noisy[:nb])
+    logp = torch.stack([torch.where(obs == 0, hi, lo), torch.where(obs == 1, hi, lo)], -1)
+    ev = logp.reshape(nb, -1).double().requires_grad_()
+    t0 = time.perf_counter()
+    out = g.run(wt, ev, torch.zeros(g.num_edge_states, dtype=torch.float64), iters, 0.5, 1.0)
+    bel = g.beliefs(ev, out).reshape(nb, n, n, 2)
+    loss = -torch.log_softmax(bel, -1).gather(-1, torch.as_tensor(clean[:nb])[..., None]).mean()
+    loss.backward()
+    dt = time.perf_counter() - t0
+    line["cpu_baseline"] = {
+        "value": nb * num_edges * iters / dt, "unit": "edge-msg updates/s", "cores": cores,
+        "kind": "port",
+        "sample": f"{nb} of the {B} images, full {iters} iterations, forward + autograd backward "
+                  f"of the float64 torch restatement on CPU ({dt:.1f} s)"}
+  print(json.dumps(line))
+  return 0
+
+
 def gumbel_evidence(num_var_states, batch, seed):
   rng = np.random.default_rng(seed)
   return rng.gumbel(size=(batch, num_var_states)).astype(np.float32)
@@ -321,9 +501,9 @@ def main():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
                   help="execution path of the ising workload (auto: timed choice)")
-  ap.add_argument("--workload", default="rbm", choices=["rbm", "ising"],
+  ap.add_argument("--workload", default="rbm", choices=["rbm", "ising", "adjoint"],
                   help="rbm: the headline RBM perturb-and-MAP batch (default); ising: the 50x50 "
-                       "toroidal Ising configuration")
+                       "toroidal Ising configuration; adjoint: differentiable BP on 64x64 grids")
   args = ap.parse_args()
   if args.warmup < 3:
     args.warmup = 3
@@ -331,6 +511,8 @@ def main():
     return run_reference(args)
   if args.workload == "ising":
     return run_ising(args)
+  if args.workload == "adjoint":
+    return run_adjoint(args)
 
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top

@@ -154,6 +154,48 @@ int pgbp_run_static_scratch(const pgbp_plan* plan, void* stream, int64_t batch,
                             float* msgs_out, float* deltas,
                             int64_t num_iters, double damping, double temperature);
 
+/* pgbp_run that also keeps the messages every `checkpoint_every` iterations, for pgbp_run_vjp:
+ * checkpoints [ceil(iters / k)][batch][E_s] contiguous (k = min(checkpoint_every, iters), iters =
+ * max(num_iters, 1)); checkpoint 0 is msgs_in as given, checkpoint c the messages after c * k
+ * iterations. msgs_out and deltas are those of pgbp_run (bit for bit); the workspace is
+ * pgbp_workspace_size's. No reference counterpart: the reference's jax.grad stores every
+ * iteration's messages (its scan body is wrapped in jax.checkpoint, bp.py:98). */
+int pgbp_run_checkpointed(const pgbp_plan* plan, void* stream, int64_t batch,
+                          const float* log_potentials, int64_t lp_stride,
+                          const float* evidence, int64_t ev_stride,
+                          const float* msgs_in, int64_t msgs_stride,
+                          float* msgs_out, float* deltas,
+                          int64_t num_iters, int64_t checkpoint_every,
+                          double damping, double temperature, float* checkpoints,
+                          void* workspace, size_t workspace_bytes);
+
+/* Reverse mode of pgbp_run: the gradients that jax.grad gives through bp.run in the reference
+ * (its learning example, examples/grid_mrf.ipynb cells 15-16, differentiates
+ * pgmax/infer/bp.py:63-155 this way), computed by a hand-written adjoint instead of autodiff.
+ * Covers graphs whose factors are all dense pairwise EnumFactors, at temperature > 0 (else
+ * PGBP_ERR_UNSUPPORTED).
+ * checkpoints: those of pgbp_run_checkpointed with the same k = checkpoint_every (or, the same
+ *   values, msgs_in followed by the msgs_out of pgbp_run called k iterations at a time). Each
+ *   chunk is recomputed with the engine's arithmetic and walked backwards.
+ * g_msgs_out [batch, E_s]: dL/d(msgs_out). Outputs: g_log_potentials [batch, P] when lp_stride
+ *   != 0, else [P] summed over the batch; g_evidence likewise; g_msgs_in [batch, E_s] or NULL.
+ *   Potentials clipped by the forward (|lp| > 1e6) get zero gradient. */
+size_t pgbp_vjp_workspace_size(const pgbp_plan* plan, int64_t batch, int64_t num_iters,
+                               int64_t checkpoint_every);
+int pgbp_run_vjp(const pgbp_plan* plan, void* stream, int64_t batch,
+                 const float* log_potentials, int64_t lp_stride,
+                 const float* evidence, int64_t ev_stride,
+                 const float* checkpoints, int64_t num_iters, int64_t checkpoint_every,
+                 double damping, double temperature,
+                 const float* g_msgs_out, float* g_log_potentials, float* g_evidence,
+                 float* g_msgs_in, void* workspace, size_t workspace_bytes);
+
+/* Reverse mode of pgbp_beliefs with respect to the messages (jax.grad of get_beliefs,
+ * pgmax/infer/inferer.py:211-225): g_msgs[b, e] = g_beliefs[b, var_states_for_edge_states[e]];
+ * the evidence gradient is g_beliefs itself. g_msgs rows are contiguous. */
+int pgbp_beliefs_vjp(const pgbp_plan* plan, void* stream, int64_t batch, const float* g_beliefs,
+                     int64_t gb_stride, float* g_msgs);
+
 /* One factor type's un-fused update: out = FAC_TO_VAR_UPDATES[type](vtof, lp, T, normalize).
  * vtof / out are that type's message slice [batch, n_type] (stride floats apart), lp its
  * potential slice [batch, p_type] (lp_stride, 0 = shared). No workspace is needed. */
@@ -181,9 +223,11 @@ int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const flo
  * per-class launch counts and total device milliseconds, and clears the record. Classes:
  * 0 variable sums, 1 dense pairwise Enum, 2 generic Enum, 3 OR, 4 AND, 5 Pool,
  * 6 layout (transposes, potential clipping, initial normalisation, residual copy-out),
- * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals), 8 the one-CTA-per-instance
- * small-graph kernel (all iterations in one launch). Process-wide, not thread-safe. */
-#define PGBP_PROFILE_CLASSES 9
+ * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals, pgbp_beliefs_vjp), 8 the
+ * one-CTA-per-instance small-graph kernel (all iterations in one launch), 9 the adjoint kernels of
+ * pgbp_run_vjp (its forward recomputation is counted in the classes above). Process-wide, not
+ * thread-safe. */
+#define PGBP_PROFILE_CLASSES 10
 typedef struct {
   int64_t launches[PGBP_PROFILE_CLASSES];
   double milliseconds[PGBP_PROFILE_CLASSES];

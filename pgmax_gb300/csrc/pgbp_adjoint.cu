@@ -1,0 +1,617 @@
+// Reverse mode of the damped BP iterations of run_with_diffs (pgmax/infer/bp.py:63-155) for graphs
+// whose factors are all dense pairwise EnumFactors, at temperature > 0: the hand-written adjoint
+// behind differentiable BP (gradients of a loss on the final messages with respect to the log
+// potentials, the evidence and the initial messages).
+//
+// Forward iteration (per instance), with n = d * m + (1 - d) * f:
+//   vsum[v]  = ev[v] + sum_{e in v} m[e]                                       (bp.py:191-219)
+//   vtof[e]  = vsum[v(e)] - m[e]
+//   s_ij     = vtof1[i] + vtof2[j] + lp_ij                                      (enum.py:451-455)
+//   f1[i]    = T log sum_j exp((s_ij - M_i) / T) + M_i - vtof1[i], f2 likewise  (enum.py:456-474)
+//   m'[e]    = max(n[e] - max_{e' in edge} n[e'], MSG_NEG_INF)                 (bp.py:222-260)
+// Backward, given g' = dL/dm':
+//   gy  = g' where n - max(n) was not clipped, else 0
+//   gn  = gy - [e = first argmax of its edge] * sum over the edge of gy
+//   gf  = (1 - d) gn,  gdir = d gn                               (gdir: through the damping term)
+//   gs_ij = gf1[i] p1_ij + gf2[j] p2_ij,  p1_ij = softmax_j(s_ij / T), p2_ij = softmax_i(s_ij / T)
+//   gvtof1[i] = sum_j gs_ij - gf1[i],  gvtof2[j] = sum_i gs_ij - gf2[j],  glp_ij += gs_ij
+//   gvsum[v] = sum_{e in v} gvtof[e],  gev[v] += gvsum[v]
+//   g[e] (= dL/dm) = gdir[e] + gvsum[v(e)] - gvtof[e]
+// g is never stored: the next (earlier) step's factor kernel reads gdir, gvsum and gvtof of the
+// step after it and forms g for its own edges, so one backward step is two launches (factors,
+// variable sums). The potentials are clipped to +-1e6 before the loop (bp.py:85-87): a clipped
+// entry gets no gradient.
+//
+// Checkpointing: the caller keeps the messages every k iterations (pgbp_run called k iterations
+// at a time). Each chunk is recomputed here by a forward step with the engine's arithmetic (same
+// operations in the same order, so the recomputed messages are the forward's), also storing
+// every iteration's variable sums, then walked backwards. The recomputation of chunk c - 1 runs on
+// a second stream while chunk c is walked backwards (two trajectory buffers), so the two chains
+// of small launches overlap.
+// Arrays here are in the caller's [B, n] layout; one thread per (unit, instance), consecutive
+// threads on consecutive units of one instance.
+#include <math.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "pgbp_internal.h"
+
+namespace pgbp {
+namespace {
+
+constexpr float kMsgNegInf = -1e32f;  // MSG_NEG_INF (pgmax/utils/__init__.py)
+constexpr float kLpClip = 1e6f;       // potentials are clipped to +-1e6 (bp.py:85-87)
+
+// NaN-propagating maximum (jnp.maximum): one max.NaN instruction.
+__device__ __forceinline__ float maxn(float a, float b) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+// x / t; a power-of-two t multiplies by its exact reciprocal (the same correctly rounded value).
+__device__ __forceinline__ float div_t(float x, float t) {
+  const unsigned u = __float_as_uint(t);
+  const unsigned e = (u >> 23) & 0xffu;
+  if ((u & 0x807fffffu) == 0u && e >= 2u && e <= 252u) return x * __uint_as_float((254u - e) << 23);
+  return x / t;
+}
+
+__device__ __forceinline__ float clip_lp(float x) { return fminf(fmaxf(x, -kLpClip), kLpClip); }
+
+// vsum[b, v] = ev[b, v] + sum of m[b, e] over the edge states e of v, in increasing e (the
+// reference's scatter order).
+__global__ void __launch_bounds__(256) vsum_kernel(const int32_t* __restrict__ vs_off,
+                                                   const int32_t* __restrict__ vs_edges,
+                                                   int64_t nvs, const float* __restrict__ m,
+                                                   int64_t n_es, const float* __restrict__ ev,
+                                                   int64_t evs, float* __restrict__ vsum,
+                                                   int64_t B) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvs * B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / nvs, v = i % nvs;
+    float s = ev[b * evs + v];
+    for (int32_t k = vs_off[v]; k < vs_off[v + 1]; ++k) s += m[b * n_es + vs_edges[k]];
+    vsum[i] = s;
+  }
+}
+
+// The forward quantities of one (dense pairwise factor, instance) with n1, n2 <= M: old messages
+// o, variable-to-factor messages v, per-state maxima mx and sums of exponentials se, and the
+// factor messages f, in the engine's operation order (pairwise_body, pgbp_kernels.cu).
+template <int M>
+struct Pair {
+  float o1[M], o2[M], v1[M], v2[M], mx1[M], mx2[M], se1[M], se2[M], f1[M], f2[M];
+};
+
+template <int M>
+__device__ __forceinline__ void pair_forward(Pair<M>& st, const int4 q, int n1, int n2,
+                                             const float* __restrict__ m,
+                                             const float* __restrict__ vsum,
+                                             const float* __restrict__ lpb, float t) {
+  constexpr int U = M <= 8 ? M : 1;
+#pragma unroll U
+  for (int a = 0; a < M; ++a)
+    if (a < n1) {
+      st.o1[a] = m[q.x + a];
+      st.v1[a] = vsum[q.z + a] - st.o1[a];
+      st.mx1[a] = -INFINITY;
+      st.se1[a] = 0.0f;
+    }
+#pragma unroll U
+  for (int c = 0; c < M; ++c)
+    if (c < n2) {
+      st.o2[c] = m[q.x + n1 + c];
+      st.v2[c] = vsum[q.w + c] - st.o2[c];
+      st.mx2[c] = -INFINITY;
+      st.se2[c] = 0.0f;
+    }
+#pragma unroll U
+  for (int a = 0; a < M; ++a)
+#pragma unroll U
+    for (int c = 0; c < M; ++c)
+      if (a < n1 && c < n2) {
+        const float s = ((0.0f + st.v1[a]) + st.v2[c]) + clip_lp(lpb[a * n2 + c]);
+        st.mx1[a] = maxn(st.mx1[a], s);
+        st.mx2[c] = maxn(st.mx2[c], s);
+      }
+#pragma unroll U
+  for (int a = 0; a < M; ++a)
+#pragma unroll U
+    for (int c = 0; c < M; ++c)
+      if (a < n1 && c < n2) {
+        const float s = ((0.0f + st.v1[a]) + st.v2[c]) + clip_lp(lpb[a * n2 + c]);
+        st.se1[a] += expf(div_t(s - st.mx1[a], t));
+        st.se2[c] += expf(div_t(s - st.mx2[c], t));
+      }
+#pragma unroll U
+  for (int a = 0; a < M; ++a)
+    if (a < n1) st.f1[a] = (t * logf(st.se1[a]) + st.mx1[a]) - st.v1[a];
+#pragma unroll U
+  for (int c = 0; c < M; ++c)
+    if (c < n2) st.f2[c] = (t * logf(st.se2[c]) + st.mx2[c]) - st.v2[c];
+}
+
+// Damping, normalisation and clipping of one edge with k <= M states (bp.py:127-133).
+template <int M>
+__device__ __forceinline__ void edge_forward(const float* o, const float* f, int k, float d,
+                                             float omd, float* __restrict__ out) {
+  constexpr int U = M <= 8 ? M : 1;
+  float mx = -INFINITY;
+#pragma unroll U
+  for (int s = 0; s < M; ++s)
+    if (s < k) mx = maxn(mx, d * o[s] + omd * f[s]);
+#pragma unroll U
+  for (int s = 0; s < M; ++s)
+    if (s < k) out[s] = maxn((d * o[s] + omd * f[s]) - mx, kMsgNegInf);
+}
+
+// Backward of edge_forward. g: dL/d(new messages) of the edge. Writes dL/df to gf and the damping
+// path dL/do to gdir.
+template <int M>
+__device__ __forceinline__ void edge_backward(const float* o, const float* f, int k, float d,
+                                              float omd, const float* g, float* gf,
+                                              float* __restrict__ gdir) {
+  constexpr int U = M <= 8 ? M : 1;
+  int arg = 0;
+  float nmax = d * o[0] + omd * f[0];
+#pragma unroll U
+  for (int s = 1; s < M; ++s)
+    if (s < k) {
+      const float n = d * o[s] + omd * f[s];
+      if (n > nmax) {
+        nmax = n;
+        arg = s;
+      }
+    }
+  float gsum = 0.0f;
+#pragma unroll U
+  for (int s = 0; s < M; ++s)
+    if (s < k) {
+      const float gy = ((d * o[s] + omd * f[s]) - nmax >= kMsgNegInf) ? g[s] : 0.0f;
+      gf[s] = gy;
+      gsum += gy;
+    }
+#pragma unroll U
+  for (int s = 0; s < M; ++s)
+    if (s < k) {
+      const float gn = gf[s] - (s == arg ? gsum : 0.0f);
+      gf[s] = omd * gn;
+      gdir[s] = d * gn;
+    }
+}
+
+struct PairArgs {
+  const int4* __restrict__ rec;          // (first edge state, -, first var state 1, of var 2)
+  const int32_t* __restrict__ cfg_begin;
+  int64_t count;
+  int n1, n2;
+  int64_t n_es, nvs, np_, B;
+  const float* __restrict__ lp;
+  int64_t lps;
+  float d, omd, t;
+};
+
+// One forward iteration of every factor of a bucket: m (iteration input, [B, E_s]) and its
+// variable sums -> next messages.
+template <int M>
+__global__ void __launch_bounds__(256) pairwise_forward_kernel(PairArgs a, const float* m,
+                                                               const float* vsum, float* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count * a.B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / a.count, u = i % a.count;
+    const int4 q = a.rec[u];
+    Pair<M> st;
+    pair_forward<M>(st, q, a.n1, a.n2, m + b * a.n_es, vsum + b * a.nvs,
+                    a.lp + b * a.lps + a.cfg_begin[u], a.t);
+    float* o = out + b * a.n_es + q.x;
+    edge_forward<M>(st.o1, st.f1, a.n1, a.d, a.omd, o);
+    edge_forward<M>(st.o2, st.f2, a.n2, a.d, a.omd, o + a.n1);
+  }
+}
+
+// dL/d(messages of the iteration after this one): explicit (gexp, the caller's gradient, for the
+// last iteration) or formed from the step after: gdir + gvsum[v(e)] - gvtof.
+struct GradIn {
+  const float* __restrict__ gexp;
+  const float* __restrict__ gdir;
+  const float* __restrict__ gvsum;
+  const float* __restrict__ gvtof;
+};
+
+// One backward iteration of every factor of a bucket.
+template <int M>
+__global__ void __launch_bounds__(256) pairwise_backward_kernel(PairArgs a, const float* m,
+                                                                const float* vsum, GradIn gin,
+                                                                float* __restrict__ gdir,
+                                                                float* __restrict__ gvtof,
+                                                                float* __restrict__ glp) {
+  constexpr int U = M <= 8 ? M : 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count * a.B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / a.count, u = i % a.count;
+    const int4 q = a.rec[u];
+    const int64_t k0 = a.cfg_begin[u];
+    const float* lpb = a.lp + b * a.lps + k0;
+    Pair<M> st;
+    pair_forward<M>(st, q, a.n1, a.n2, m + b * a.n_es, vsum + b * a.nvs, lpb, a.t);
+    const int64_t e1 = b * a.n_es + q.x, e2 = e1 + a.n1;
+    float g1[M], g2[M];
+    if (gin.gexp) {
+#pragma unroll U
+      for (int s = 0; s < M; ++s)
+        if (s < a.n1) g1[s] = gin.gexp[e1 + s];
+#pragma unroll U
+      for (int s = 0; s < M; ++s)
+        if (s < a.n2) g2[s] = gin.gexp[e2 + s];
+    } else {
+      const float* gv = gin.gvsum + b * a.nvs;
+#pragma unroll U
+      for (int s = 0; s < M; ++s)
+        if (s < a.n1) g1[s] = (gin.gdir[e1 + s] + gv[q.z + s]) - gin.gvtof[e1 + s];
+#pragma unroll U
+      for (int s = 0; s < M; ++s)
+        if (s < a.n2) g2[s] = (gin.gdir[e2 + s] + gv[q.w + s]) - gin.gvtof[e2 + s];
+    }
+    float gf1[M], gf2[M];
+    edge_backward<M>(st.o1, st.f1, a.n1, a.d, a.omd, g1, gf1, gdir + e1);
+    edge_backward<M>(st.o2, st.f2, a.n2, a.d, a.omd, g2, gf2, gdir + e2);
+    // g1 / g2 become the accumulators of dL/dvtof
+#pragma unroll U
+    for (int s = 0; s < M; ++s)
+      if (s < a.n1) g1[s] = -gf1[s];
+#pragma unroll U
+    for (int s = 0; s < M; ++s)
+      if (s < a.n2) g2[s] = -gf2[s];
+    float* glpb = glp + b * a.np_ + k0;
+#pragma unroll U
+    for (int x = 0; x < M; ++x)
+#pragma unroll U
+      for (int y = 0; y < M; ++y)
+        if (x < a.n1 && y < a.n2) {
+          const float raw = lpb[x * a.n2 + y];
+          const float s = ((0.0f + st.v1[x]) + st.v2[y]) + clip_lp(raw);
+          const float p1 = expf(div_t(s - st.mx1[x], a.t)) / st.se1[x];
+          const float p2 = expf(div_t(s - st.mx2[y], a.t)) / st.se2[y];
+          const float gs = gf1[x] * p1 + gf2[y] * p2;
+          g1[x] += gs;
+          g2[y] += gs;
+          if (raw >= -kLpClip && raw <= kLpClip) glpb[x * a.n2 + y] += gs;
+        }
+#pragma unroll U
+    for (int s = 0; s < M; ++s)
+      if (s < a.n1) gvtof[e1 + s] = g1[s];
+#pragma unroll U
+    for (int s = 0; s < M; ++s)
+      if (s < a.n2) gvtof[e2 + s] = g2[s];
+  }
+}
+
+// gvsum[v] = sum_{e in v} gvtof[e]; gev[v] += gvsum[v].
+__global__ void __launch_bounds__(256) gvsum_kernel(const int32_t* __restrict__ vs_off,
+                                                    const int32_t* __restrict__ vs_edges,
+                                                    int64_t nvs, const float* __restrict__ gvtof,
+                                                    int64_t n_es, float* __restrict__ gvsum,
+                                                    float* __restrict__ gev, int64_t B) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvs * B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / nvs, v = i % nvs;
+    float s = 0.0f;
+    for (int32_t k = vs_off[v]; k < vs_off[v + 1]; ++k) s += gvtof[b * n_es + vs_edges[k]];
+    gvsum[i] = s;
+    gev[i] += s;
+  }
+}
+
+// The initial normalisation of run_with_diffs (bp.py:88-92), per (edge, instance):
+// out = max(x - max_edge(x), MSG_NEG_INF).
+__global__ void __launch_bounds__(256) normalize_kernel(const int32_t* __restrict__ edge_start,
+                                                        int64_t ne, const float* __restrict__ x,
+                                                        float* __restrict__ out, int64_t n_es,
+                                                        int64_t B) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ne * B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / ne, e = i % ne;
+    const int32_t lo = edge_start[e], hi = edge_start[e + 1];
+    float mx = -INFINITY;
+    for (int32_t s = lo; s < hi; ++s) mx = maxn(mx, x[b * n_es + s]);
+    for (int32_t s = lo; s < hi; ++s) out[b * n_es + s] = maxn(x[b * n_es + s] - mx, kMsgNegInf);
+  }
+}
+
+// Backward of normalize_kernel; the incoming gradient is formed from the first iteration's step
+// (gdir + gvsum[v(e)] - gvtof).
+__global__ void __launch_bounds__(256) normalize_backward_kernel(
+    const int32_t* __restrict__ edge_start, const int32_t* __restrict__ vs_of_es, int64_t ne,
+    const float* __restrict__ x, GradIn gin, float* __restrict__ gx, int64_t n_es, int64_t nvs,
+    int64_t B) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ne * B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / ne, e = i % ne;
+    const int32_t lo = edge_start[e], hi = edge_start[e + 1];
+    const float* xb = x + b * n_es;
+    auto g = [&](int32_t s) {
+      const int64_t j = b * n_es + s;
+      return gin.gexp ? gin.gexp[j]
+                      : (gin.gdir[j] + gin.gvsum[b * nvs + vs_of_es[s]]) - gin.gvtof[j];
+    };
+    float mx = xb[lo];
+    int32_t arg = lo;
+    for (int32_t s = lo + 1; s < hi; ++s)
+      if (xb[s] > mx) {
+        mx = xb[s];
+        arg = s;
+      }
+    float gsum = 0.0f;
+    for (int32_t s = lo; s < hi; ++s) gsum += (xb[s] - mx >= kMsgNegInf) ? g(s) : 0.0f;
+    for (int32_t s = lo; s < hi; ++s) {
+      const float gy = (xb[s] - mx >= kMsgNegInf) ? g(s) : 0.0f;
+      gx[b * n_es + s] = gy - (s == arg ? gsum : 0.0f);
+    }
+  }
+}
+
+// out[j] = sum over b (in increasing b) of acc[b, j]: gradients of inputs shared by the batch.
+__global__ void __launch_bounds__(256) sum_rows_kernel(const float* __restrict__ acc, int64_t n,
+                                                       int64_t B, float* __restrict__ out) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int64_t b = 0; b < B; ++b) s += acc[b * n + j];
+    out[j] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) beliefs_vjp_kernel(const int32_t* __restrict__ vs_of_es,
+                                                          int64_t n_es,
+                                                          const float* __restrict__ gb,
+                                                          int64_t gbs, float* __restrict__ gm,
+                                                          int64_t B) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_es * B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / n_es, e = i % n_es;
+    gm[i] = gb[b * gbs + vs_of_es[e]];
+  }
+}
+
+dim3 grid_for(int64_t n, int sm) {
+  const int64_t g = (n + 255) / 256;
+  return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm * 16)));
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t floats(int64_t n) { return align_up(sizeof(float) * (size_t)std::max<int64_t>(n, 1)); }
+
+int bucket_m(const PairwiseBucket& q) {
+  const int n = std::max(q.n1, q.n2);
+  return n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : 64;
+}
+
+PairArgs pair_args(const Plan& p, const PairwiseBucket& q, int64_t B, const float* lp,
+                   int64_t lps, float d, float omd, float t) {
+  return PairArgs{q.rec, q.cfg_begin, q.count, q.n1, q.n2, p.num_edge_states, p.num_var_states,
+                  p.num_potentials, B, lp, lps, d, omd, t};
+}
+
+template <int M>
+void launch_forward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m, const float* vsum,
+                      float* out) {
+  pairwise_forward_kernel<M><<<grid_for(a.count * a.B, sm), 256, 0, s>>>(a, m, vsum, out);
+}
+
+template <int M>
+void launch_backward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m,
+                       const float* vsum, const GradIn& gin, float* gdir, float* gvtof,
+                       float* glp) {
+  pairwise_backward_kernel<M><<<grid_for(a.count * a.B, sm), 256, 0, s>>>(a, m, vsum, gin, gdir,
+                                                                         gvtof, glp);
+}
+
+// One chunk's trajectory: messages [len][B][E_s] (normalised) and variable sums [len][B][N_vs].
+struct Traj {
+  float* m;
+  float* vs;
+  size_t m_step, vs_step;  // floats between iterations
+};
+
+// Recomputes the chunk that starts at checkpoint ck.
+void recompute(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lps,
+               const float* ev, int64_t evs, const float* ck, int64_t len, float d, float omd,
+               float t, const Traj& tr) {
+  ProfileScope prof(kProfAdjoint, s);
+  const int64_t n_es = p.num_edge_states, nvs = p.num_var_states;
+  normalize_kernel<<<grid_for(p.num_edges * B, p.sm_count), 256, 0, s>>>(p.edge_start, p.num_edges,
+                                                                       ck, tr.m, n_es, B);
+  for (int64_t j = 0; j < len; ++j) {
+    const float* mj = tr.m + j * tr.m_step;
+    float* vj = tr.vs + j * tr.vs_step;
+    vsum_kernel<<<grid_for(nvs * B, p.sm_count), 256, 0, s>>>(p.vs_off, p.vs_edges, nvs, mj, n_es,
+                                                              ev, evs, vj, B);
+    if (j + 1 == len) break;
+    float* next = tr.m + (j + 1) * tr.m_step;
+    for (const PairwiseBucket& q : p.pairwise) {
+      const PairArgs a = pair_args(p, q, B, lp, lps, d, omd, t);
+      switch (bucket_m(q)) {
+        case 2: launch_forward_m<2>(a, p.sm_count, s, mj, vj, next); break;
+        case 4: launch_forward_m<4>(a, p.sm_count, s, mj, vj, next); break;
+        case 8: launch_forward_m<8>(a, p.sm_count, s, mj, vj, next); break;
+        default: launch_forward_m<64>(a, p.sm_count, s, mj, vj, next); break;
+      }
+    }
+  }
+}
+
+struct GradSet {
+  float* gdir;
+  float* gvtof;
+  float* gvsum;
+};
+
+// One iteration backwards: from the gradient of its output (gin) to gdir / gvtof / gvsum of its
+// input, accumulating glp [B, P] and gev [B, N_vs].
+void backward_step(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lps,
+                   const float* m, const float* vsum, const GradIn& gin, const GradSet& out,
+                   float* glp, float* gev, float d, float omd, float t) {
+  ProfileScope prof(kProfAdjoint, s);
+  for (const PairwiseBucket& q : p.pairwise) {
+    const PairArgs a = pair_args(p, q, B, lp, lps, d, omd, t);
+    switch (bucket_m(q)) {
+      case 2: launch_backward_m<2>(a, p.sm_count, s, m, vsum, gin, out.gdir, out.gvtof, glp); break;
+      case 4: launch_backward_m<4>(a, p.sm_count, s, m, vsum, gin, out.gdir, out.gvtof, glp); break;
+      case 8: launch_backward_m<8>(a, p.sm_count, s, m, vsum, gin, out.gdir, out.gvtof, glp); break;
+      default:
+        launch_backward_m<64>(a, p.sm_count, s, m, vsum, gin, out.gdir, out.gvtof, glp);
+        break;
+    }
+  }
+  gvsum_kernel<<<grid_for(p.num_var_states * B, p.sm_count), 256, 0, s>>>(
+      p.vs_off, p.vs_edges, p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
+}
+
+// A second stream per device for the recomputation, created on first use and kept.
+constexpr int kMaxDevices = 64;
+std::mutex g_aux_mu;
+cudaStream_t g_aux[kMaxDevices] = {};
+
+cudaError_t aux_stream(int device, cudaStream_t* out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_aux_mu);
+  if (!g_aux[device]) {
+    cudaError_t e = cudaStreamCreateWithFlags(&g_aux[device], cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+  }
+  *out = g_aux[device];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+const char* adjoint_unsupported(const Plan& p) {
+  if (p.enum_generic.count > 0)
+    return "the adjoint covers dense pairwise EnumFactors only; the graph has other EnumFactors";
+  if (p.logical[0].count > 0 || p.logical[1].count > 0 || p.pool.count > 0)
+    return "the adjoint covers dense pairwise EnumFactors only; the graph has OR/AND/Pool factors";
+  return "";
+}
+
+size_t vjp_workspace_bytes(const Plan& p, int64_t B, int64_t iters, int64_t checkpoint_every,
+                           bool ev_shared, bool lp_shared) {
+  const int64_t it = std::max<int64_t>(iters, 1);
+  const int64_t k = std::max<int64_t>(1, std::min(checkpoint_every, it));
+  const int64_t n_es = p.num_edge_states, nvs = p.num_var_states;
+  size_t n = 0;
+  n += 2 * (size_t)k * (floats(n_es * B) + floats(nvs * B));  // two trajectory buffers
+  n += 2 * (2 * floats(n_es * B) + floats(nvs * B));          // two gradient sets
+  if (lp_shared) n += floats(p.num_potentials * B);
+  if (ev_shared) n += floats(nvs * B);
+  return n;
+}
+
+cudaError_t run_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                    const float* ev, int64_t ev_stride, const float* checkpoints, int64_t iters_in,
+                    int64_t checkpoint_every, double damping, double temperature,
+                    const float* g_msgs, float* g_lp, float* g_ev, float* g_msgs_in, void* ws,
+                    size_t ws_bytes) {
+  (void)ws_bytes;
+  const int64_t iters = std::max<int64_t>(iters_in, 1);
+  const int64_t k = std::max<int64_t>(1, std::min(checkpoint_every, iters));
+  const int64_t n_ck = (iters + k - 1) / k;
+  const int64_t n_es = p.num_edge_states, nvs = p.num_var_states, np_ = p.num_potentials;
+  const bool lp_shared = lp_stride == 0, ev_shared = ev_stride == 0;
+  char* w = static_cast<char*>(ws);
+  auto take = [&](size_t bytes) {
+    char* r = w;
+    w += bytes;
+    return reinterpret_cast<float*>(r);
+  };
+  Traj tr[2];
+  for (Traj& x : tr) {
+    x.m_step = floats(n_es * B) / sizeof(float);
+    x.vs_step = floats(nvs * B) / sizeof(float);
+    x.m = take((size_t)k * floats(n_es * B));
+    x.vs = take((size_t)k * floats(nvs * B));
+  }
+  GradSet gs[2];
+  for (GradSet& x : gs) {
+    x.gdir = take(floats(n_es * B));
+    x.gvtof = take(floats(n_es * B));
+    x.gvsum = take(floats(nvs * B));
+  }
+  float* glp = lp_shared ? take(floats(np_ * B)) : g_lp;
+  float* gev = ev_shared ? take(floats(nvs * B)) : g_ev;
+  const float d = (float)damping, omd = (float)(1.0 - damping), t = (float)temperature;
+  const size_t ck_step = (size_t)B * (size_t)n_es;
+  auto chunk_len = [&](int64_t c) { return std::min(k, iters - c * k); };
+
+  cudaStream_t aux = nullptr;
+  cudaError_t e = aux_stream(p.device, &aux);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t fork = nullptr, ev_r[2] = {nullptr, nullptr}, ev_b[2] = {nullptr, nullptr};
+  auto cleanup = [&]() {
+    for (cudaEvent_t x : {fork, ev_r[0], ev_r[1], ev_b[0], ev_b[1]})
+      if (x) cudaEventDestroy(x);
+  };
+  for (cudaEvent_t* x : {&fork, &ev_r[0], &ev_r[1], &ev_b[0], &ev_b[1]}) {
+    if ((e = cudaEventCreateWithFlags(x, cudaEventDisableTiming)) != cudaSuccess) {
+      cleanup();
+      return e;
+    }
+  }
+  e = cudaMemsetAsync(glp, 0, sizeof(float) * (size_t)(np_ * B), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(gev, 0, sizeof(float) * (size_t)(nvs * B), s);
+  // the recomputation reads what the caller wrote on its stream
+  if (e == cudaSuccess) e = cudaEventRecord(fork, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, fork, 0);
+  if (e != cudaSuccess) {
+    cleanup();
+    return e;
+  }
+  recompute(p, aux, B, lp, lp_stride, ev, ev_stride, checkpoints + (n_ck - 1) * ck_step,
+            chunk_len(n_ck - 1), d, omd, t, tr[(n_ck - 1) & 1]);
+  cudaEventRecord(ev_r[(n_ck - 1) & 1], aux);
+  GradIn gin{g_msgs, nullptr, nullptr, nullptr};
+  int cur = 0;
+  for (int64_t c = n_ck - 1; c >= 0; --c) {
+    if (c >= 1) {
+      // chunk c - 1 reuses the buffer of chunk c + 1: wait until that chunk has been walked
+      if (c + 1 < n_ck) cudaStreamWaitEvent(aux, ev_b[(c + 1) & 1], 0);
+      recompute(p, aux, B, lp, lp_stride, ev, ev_stride, checkpoints + (c - 1) * ck_step,
+                chunk_len(c - 1), d, omd, t, tr[(c - 1) & 1]);
+      cudaEventRecord(ev_r[(c - 1) & 1], aux);
+    }
+    cudaStreamWaitEvent(s, ev_r[c & 1], 0);
+    const Traj& x = tr[c & 1];
+    for (int64_t j = chunk_len(c) - 1; j >= 0; --j) {
+      backward_step(p, s, B, lp, lp_stride, x.m + j * x.m_step, x.vs + j * x.vs_step, gin, gs[cur],
+                    glp, gev, d, omd, t);
+      gin = GradIn{nullptr, gs[cur].gdir, gs[cur].gvsum, gs[cur].gvtof};
+      cur ^= 1;
+    }
+    cudaEventRecord(ev_b[c & 1], s);
+  }
+  {
+    ProfileScope prof(kProfAdjoint, s);
+    if (g_msgs_in)
+      normalize_backward_kernel<<<grid_for(p.num_edges * B, p.sm_count), 256, 0, s>>>(
+          p.edge_start, p.vs_of_es, p.num_edges, checkpoints, gin, g_msgs_in, n_es, nvs, B);
+    if (lp_shared && np_ > 0)
+      sum_rows_kernel<<<grid_for(np_, p.sm_count), 256, 0, s>>>(glp, np_, B, g_lp);
+    if (ev_shared && nvs > 0)
+      sum_rows_kernel<<<grid_for(nvs, p.sm_count), 256, 0, s>>>(gev, nvs, B, g_ev);
+  }
+  e = cudaGetLastError();
+  cleanup();
+  return e;
+}
+
+cudaError_t beliefs_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* g_beliefs,
+                        int64_t gb_stride, float* g_msgs) {
+  ProfileScope prof(kProfReadout, s);
+  beliefs_vjp_kernel<<<grid_for(p.num_edge_states * B, p.sm_count), 256, 0, s>>>(
+      p.vs_of_es, p.num_edge_states, g_beliefs, gb_stride, g_msgs, B);
+  return cudaGetLastError();
+}
+
+}  // namespace pgbp

@@ -94,6 +94,7 @@ struct Plan {
   // var-state CSR over edge states, increasing edge-state order (pgbp_beliefs)
   int32_t* vs_off = nullptr;        // [num_var_states + 1]
   int32_t* vs_edges = nullptr;      // [num_edge_states]
+  int32_t* vs_of_es = nullptr;      // [num_edge_states] var_states_for_edge_states (adjoint)
   int32_t* edge_start = nullptr;    // [num_edges + 1] first edge state of each edge
   int32_t* edge_slot = nullptr;     // [num_edges + 1] first slot of each edge
   int32_t* var_off = nullptr;       // [num_variables + 1] (decode / marginals), may be null
@@ -124,7 +125,7 @@ cudaError_t prepare_small_graph(Plan& p);
 
 // Kernel-class timing (pgbp_profile_*): RAII bracket around one launch when profiling is on.
 enum ProfileClass { kProfVarsum = 0, kProfPairwise, kProfEnumGeneric, kProfOr, kProfAnd, kProfPool,
-                    kProfLayout, kProfReadout, kProfSmallGraph };
+                    kProfLayout, kProfReadout, kProfSmallGraph, kProfAdjoint };
 bool profiling_enabled();
 void profile_record(int cls, cudaStream_t s, bool start);
 struct ProfileScope {
@@ -143,7 +144,8 @@ struct ProfileScope {
 cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
                    const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
                    float* msgs_out, float* deltas, int64_t iters, double damping, double temperature,
-                   void* ws, size_t ws_bytes);
+                   void* ws, size_t ws_bytes, int64_t checkpoint_every = 0,
+                   float* checkpoints = nullptr);
 cudaError_t factor_update(const Plan& p, cudaStream_t s, int type, int64_t B, const float* vtof,
                           int64_t vtof_stride, const float* lp, int64_t lp_stride, double temperature,
                           int normalize, float* out, int64_t out_stride);
@@ -153,6 +155,18 @@ cudaError_t decode(const Plan& p, cudaStream_t s, int64_t B, const float* belief
                    int32_t* map);
 cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* beliefs, int64_t stride,
                       float* out);
+
+// Adjoint (pgbp_adjoint.cu). An empty string when the plan can be differentiated, else why not.
+const char* adjoint_unsupported(const Plan& p);
+size_t vjp_workspace_bytes(const Plan& p, int64_t B, int64_t iters, int64_t checkpoint_every,
+                           bool ev_shared, bool lp_shared);
+cudaError_t run_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                    const float* ev, int64_t ev_stride, const float* checkpoints, int64_t iters,
+                    int64_t checkpoint_every, double damping, double temperature,
+                    const float* g_msgs, float* g_lp, float* g_ev, float* g_msgs_in, void* ws,
+                    size_t ws_bytes);
+cudaError_t beliefs_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* g_beliefs,
+                        int64_t gb_stride, float* g_msgs);
 
 }  // namespace pgbp
 

@@ -51,11 +51,21 @@ __device__ __forceinline__ float fminp(float a, float b) {
   return r;
 }
 
+// x / t for a temperature t > 0. When t is a power of two (1, 0.5, 2, ...) its reciprocal is
+// exact, so x * (1 / t) is the same correctly rounded value as x / t and costs one multiply
+// instead of a full division; the reciprocal's exponent field is 254 - t's.
+__device__ __forceinline__ float div_t(float x, float t) {
+  const unsigned u = __float_as_uint(t);
+  const unsigned e = (u >> 23) & 0xffu;
+  if ((u & 0x807fffffu) == 0u && e >= 2u && e <= 252u) return x * __uint_as_float((254u - e) << 23);
+  return x / t;
+}
+
 // update_utils.py:150-166
 __device__ __forceinline__ float logaddexp_t(float a, float b, float t) {
   const float mx = fmaxp(a, b);
   const float mn = fminp(a, b);
-  const float w = log1pf(expf((mn - mx) / t));
+  const float w = log1pf(expf(div_t(mn - mx, t)));
   return t * w + mx;
 }
 
@@ -68,7 +78,7 @@ __device__ __forceinline__ float log1mexp_f(float x) {
 
 // update_utils.py:169-190
 __device__ __forceinline__ float logminusexp_t(float a, float b, float t, float eps) {
-  const float v = t * log1mexp_f((a - b) / t) + a;
+  const float v = t * log1mexp_f(div_t(a - b, t)) + a;
   return (a >= b + eps) ? v : -INFINITY;
 }
 
@@ -240,8 +250,8 @@ __device__ __forceinline__ void pairwise_body(const C& c, const EdgeRef& r1, con
     for (int i = 0; i < n1; ++i) {
       for (int j = 0; j < n2; ++j) {
         const float s = ((0.0f + v1[i]) + v2[j]) + c.pot(k0 + i * n2 + j, b);
-        s1[i] += expf((s - mx1[i]) / t);
-        s2[j] += expf((s - mx2[j]) / t);
+        s1[i] += expf(div_t(s - mx1[i], t));
+        s2[j] += expf(div_t(s - mx2[j], t));
       }
     }
     c.store(r1, n1, o1, [&](int i) { return (t * logf(s1[i]) + mx1[i]) - v1[i]; }, b, dmax);
@@ -339,7 +349,7 @@ __device__ __forceinline__ void enum_generic_unit(const C& c, const EnumGenericD
       float s = 0.0f;
       for (int i = 0; i < nv; ++i) s += v[rows[i]];
       s = s + c.pot(k0 + k, b);
-      for (int i = 0; i < nv; ++i) se[rows[i]] += expf((s - mx[rows[i]]) / t);
+      for (int i = 0; i < nv; ++i) se[rows[i]] += expf(div_t(s - mx[rows[i]], t));
     }
   }
   int pos = 0;
@@ -529,7 +539,7 @@ __device__ __forceinline__ void pool_unit(const C& c, const PoolDev& g, int64_t 
     float se = 0.0f;
     for (int64_t i = p0; i < p1; ++i) {
       c.load(edge_ref(g.ch[i]), 2, b, old, vt);
-      se += expf(((vt[1] - vt[0]) - max1) / t);
+      se += expf(div_t((vt[1] - vt[0]) - max1, t));
     }
     pi_mdiff = t * logf(se) + max1;
     fl = logaddexp_t(pi_mdiff, -pi_diff, t);
@@ -543,7 +553,7 @@ __device__ __forceinline__ void pool_unit(const C& c, const PoolDev& g, int64_t 
     for (int64_t i = p0; i < p1; ++i) {
       c.load(edge_ref(g.ch[i]), 2, b, old, vt);
       const float w = (i == arg) ? -pi_diff : vt[1] - vt[0];
-      sw += expf((w - mw) / t);
+      sw += expf(div_t(w - mw, t));
     }
     am = -(t * logf(sw) + mw);
   }
@@ -657,10 +667,10 @@ __device__ __forceinline__ void pair22(float c1, float c2, float a0, float a1, f
     f20 = m20 - v20;
     f21 = m21 - v21;
   } else {
-    const float e10 = (0.0f + expf((s00 - m10) / t)) + expf((s01 - m10) / t);
-    const float e11 = (0.0f + expf((s10 - m11) / t)) + expf((s11 - m11) / t);
-    const float e20 = (0.0f + expf((s00 - m20) / t)) + expf((s10 - m20) / t);
-    const float e21 = (0.0f + expf((s01 - m21) / t)) + expf((s11 - m21) / t);
+    const float e10 = (0.0f + expf(div_t(s00 - m10, t))) + expf(div_t(s01 - m10, t));
+    const float e11 = (0.0f + expf(div_t(s10 - m11, t))) + expf(div_t(s11 - m11, t));
+    const float e20 = (0.0f + expf(div_t(s00 - m20, t))) + expf(div_t(s10 - m20, t));
+    const float e21 = (0.0f + expf(div_t(s01 - m21, t))) + expf(div_t(s11 - m21, t));
     f10 = (t * logf(e10) + m10) - v10;
     f11 = (t * logf(e11) + m11) - v11;
     f20 = (t * logf(e20) + m20) - v20;
@@ -1397,7 +1407,10 @@ void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool lo
     unsigned* d = dacc + it * B;
     launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum));
     for (const PairwiseBucket& q : p.pairwise) {
-      if (q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0) {
+      // 4 instances per thread only when that still leaves >= 16 warps per SM; below that the
+      // kernel is latency-bound and one instance per thread keeps 4x more warps in flight
+      if (q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0 &&
+          q.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32) {
         ProfileScope ps(kProfPairwise, s);
         const Launch2 l = launch2_x4(q.count, B, p.sm_count);
         pairwise22_x4_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(q), t, d);
@@ -1610,10 +1623,20 @@ size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batc
   return n;
 }
 
+// dst[b, i] = src[b * sstride + i] for a [B, n] block (sstride 0 broadcasts one row).
+__global__ void __launch_bounds__(256) copy_rows_kernel(const float* __restrict__ src,
+                                                        int64_t sstride, int64_t n, int64_t B,
+                                                        float* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * B;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[(i / n) * sstride + i % n];
+}
+
 cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
                    const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
                    float* msgs_out, float* deltas, int64_t num_iters, double damping,
-                   double temperature, void* ws, size_t ws_bytes) {
+                   double temperature, void* ws, size_t ws_bytes, int64_t checkpoint_every,
+                   float* checkpoints) {
   const int64_t iters = std::max<int64_t>(num_iters, 1);
   const bool ev_b = ev_stride != 0, lp_b = lp_stride != 0;
   char* w = static_cast<char*>(ws);
@@ -1730,14 +1753,39 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
       path = choose_path(p, s, B, t0, cluster_ok, run_path, tmp, m0, dacc, iters);
     }
   }
-  float* fin = run_path(path, iters);
-  if (p.num_edges > 0) {
+  // caller-layout messages of the run buffer `src` into dst [B, E_s]
+  auto write_out = [&](const float* src, float* dst) {
+    if (p.num_edges > 0) {
+      ProfileScope ps(kProfLayout, s);
+      const Launch2 ln = launch2(p.num_edges, B, p.sm_count);
+      unpack_kernel<<<ln.grid, ln.block, 0, s>>>(p.edge_start, p.edge_slot, p.num_edges, src, tmp,
+                                                  B);
+    }
+    to_outer(s, tmp, p.num_edge_states, B, dst, p.num_edge_states, p.sm_count);
+  };
+  // With checkpoints, the iterations run in chunks of k and the messages after every k
+  // iterations are written out (checkpoint 0 is the input as given). A chunk continues from the
+  // buffer the previous one ended in, so the messages and residuals are those of one long run.
+  const int64_t k = checkpoints ? std::max<int64_t>(1, std::min(checkpoint_every, iters)) : iters;
+  if (checkpoints) {
     ProfileScope ps(kProfLayout, s);
-    const Launch2 ln = launch2(p.num_edges, B, p.sm_count);
-    unpack_kernel<<<ln.grid, ln.block, 0, s>>>(p.edge_start, p.edge_slot, p.num_edges, fin, tmp,
-                                                B);
+    copy_rows_kernel<<<flat_grid(p.num_edge_states * B, p.sm_count), 256, 0, s>>>(
+        msgs_in, msgs_stride, p.num_edge_states, B, checkpoints);
   }
-  to_outer(s, tmp, p.num_edge_states, B, msgs_out, p.num_edge_states, p.sm_count);
+  unsigned* const dacc0 = dacc;
+  float* fin = m0;
+  for (int64_t done = 0; done < iters;) {
+    const int64_t n = std::min(k, iters - done);
+    dacc = dacc0 + done * B;
+    fin = run_path(path, n);
+    done += n;
+    if (done < iters) {
+      write_out(fin, checkpoints + (done / k) * B * p.num_edge_states);
+      if (fin != m0) std::swap(m0, m1);
+    }
+  }
+  dacc = dacc0;
+  write_out(fin, msgs_out);
   if (deltas != nullptr) {
     ProfileScope ps(kProfLayout, s);
     deltas_out_kernel<<<flat_grid(iters * B, p.sm_count), 256, 0, s>>>(dacc, iters, B, deltas);

@@ -148,7 +148,7 @@ int pgbp_profile_read(pgbp_profile* out) {
 
 const char* pgbp_last_error(void) { return g_last_error.c_str(); }
 
-int pgbp_version(void) { return 100; }
+int pgbp_version(void) { return 200; }
 
 int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   if (!d || !out) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
@@ -305,6 +305,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   Builder bd{p};
   p.vs_off = bd.upload(vs_off);
   p.vs_edges = bd.upload(vs_edges);
+  p.vs_of_es = bd.upload(std::vector<int32_t>(vs, vs + ns));
   p.edge_start = bd.upload(edge_start);
   p.edge_slot = bd.upload(edge_slot);
   // slot lists as affine runs (first, stride, length); used when they compress 4:1 or better
@@ -637,10 +638,16 @@ size_t pgbp_workspace_size(const pgbp_plan* plan, int64_t batch, int64_t num_ite
   return pgbp::workspace_bytes(plan->p, batch, num_iters, true, true);
 }
 
-int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
-             int64_t lp_stride, const float* evidence, int64_t ev_stride, const float* msgs_in,
-             int64_t msgs_stride, float* msgs_out, float* deltas, int64_t num_iters, double damping,
-             double temperature, void* workspace, size_t workspace_bytes) {
+}  // extern "C"
+
+namespace {
+
+// pgbp_run and pgbp_run_checkpointed: argument checks, then the engine.
+int run_checked(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
+                int64_t lp_stride, const float* evidence, int64_t ev_stride, const float* msgs_in,
+                int64_t msgs_stride, float* msgs_out, float* deltas, int64_t num_iters,
+                double damping, double temperature, void* workspace, size_t workspace_bytes,
+                int64_t checkpoint_every, float* checkpoints) {
   if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
   const pgbp::Plan& p = plan->p;
   if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
@@ -667,8 +674,99 @@ int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch, const float* lo
   if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
   e = pgbp::run_bp(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
                    ev_stride, msgs_in, msgs_stride, msgs_out, deltas, num_iters, damping, temperature,
-                   workspace, workspace_bytes);
+                   workspace, workspace_bytes, checkpoint_every, checkpoints);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_run launch");
+  return PGBP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
+             int64_t lp_stride, const float* evidence, int64_t ev_stride, const float* msgs_in,
+             int64_t msgs_stride, float* msgs_out, float* deltas, int64_t num_iters, double damping,
+             double temperature, void* workspace, size_t workspace_bytes) {
+  return run_checked(plan, stream, batch, log_potentials, lp_stride, evidence, ev_stride, msgs_in,
+                     msgs_stride, msgs_out, deltas, num_iters, damping, temperature, workspace,
+                     workspace_bytes, 0, nullptr);
+}
+
+int pgbp_run_checkpointed(const pgbp_plan* plan, void* stream, int64_t batch,
+                          const float* log_potentials, int64_t lp_stride, const float* evidence,
+                          int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
+                          float* msgs_out, float* deltas, int64_t num_iters,
+                          int64_t checkpoint_every, double damping, double temperature,
+                          float* checkpoints, void* workspace, size_t workspace_bytes) {
+  if (checkpoint_every <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "checkpoint_every must be >= 1");
+  if (plan && plan->p.num_edge_states > 0 && !checkpoints)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null checkpoints");
+  return run_checked(plan, stream, batch, log_potentials, lp_stride, evidence, ev_stride, msgs_in,
+                     msgs_stride, msgs_out, deltas, num_iters, damping, temperature, workspace,
+                     workspace_bytes, checkpoint_every, checkpoints);
+}
+
+size_t pgbp_vjp_workspace_size(const pgbp_plan* plan, int64_t batch, int64_t num_iters,
+                               int64_t checkpoint_every) {
+  if (!plan || batch <= 0 || checkpoint_every <= 0) return 0;
+  size_t n = 0;
+  for (int ev_shared = 0; ev_shared < 2; ++ev_shared)
+    for (int lp_shared = 0; lp_shared < 2; ++lp_shared)
+      n = std::max(n, pgbp::vjp_workspace_bytes(plan->p, batch, num_iters, checkpoint_every,
+                                                ev_shared != 0, lp_shared != 0));
+  return n;
+}
+
+int pgbp_run_vjp(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
+                 int64_t lp_stride, const float* evidence, int64_t ev_stride,
+                 const float* checkpoints, int64_t num_iters, int64_t checkpoint_every,
+                 double damping, double temperature, const float* g_msgs_out,
+                 float* g_log_potentials, float* g_evidence, float* g_msgs_in, void* workspace,
+                 size_t workspace_bytes) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  const char* why = pgbp::adjoint_unsupported(p);
+  if (why[0]) return fail(PGBP_ERR_UNSUPPORTED, "%s", why);
+  if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
+  if (checkpoint_every <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "checkpoint_every must be >= 1");
+  if (lp_stride < 0 || ev_stride < 0 || (lp_stride != 0 && lp_stride < p.num_potentials) ||
+      (ev_stride != 0 && ev_stride < p.num_var_states))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad stride");
+  if ((p.num_potentials > 0 && (!log_potentials || !g_log_potentials)) ||
+      (p.num_var_states > 0 && (!evidence || !g_evidence)) ||
+      (p.num_edge_states > 0 && (!checkpoints || !g_msgs_out)))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  if (!(damping == damping) || !(temperature > 0.0))
+    return fail(PGBP_ERR_UNSUPPORTED,
+                "the adjoint needs temperature > 0 (max-product messages are piecewise linear)");
+  const size_t need = pgbp::vjp_workspace_bytes(p, batch, num_iters, checkpoint_every,
+                                                ev_stride == 0, lp_stride == 0);
+  if (!workspace || workspace_bytes < need)
+    return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+    return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::run_vjp(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride,
+                    evidence, ev_stride, checkpoints, num_iters, checkpoint_every, damping,
+                    temperature, g_msgs_out, g_log_potentials, g_evidence, g_msgs_in, workspace,
+                    workspace_bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_run_vjp launch");
+  return PGBP_OK;
+}
+
+int pgbp_beliefs_vjp(const pgbp_plan* plan, void* stream, int64_t batch, const float* g_beliefs,
+                     int64_t gb_stride, float* g_msgs) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (batch <= 0 || gb_stride < 0 || (batch > 1 && gb_stride != 0 && gb_stride < p.num_var_states))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad batch or stride");
+  if (p.num_edge_states > 0 && (!g_beliefs || !g_msgs))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::beliefs_vjp(p, static_cast<cudaStream_t>(stream), batch, g_beliefs, gb_stride, g_msgs);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_beliefs_vjp launch");
   return PGBP_OK;
 }
 

@@ -131,9 +131,8 @@ class Plan:
     return ctypes.c_void_p(_torch().cuda.current_stream(self.device).cuda_stream)
 
   # ------------------------------------------------------------------------- entry points
-  def run(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5, temperature=0.0,
-          with_deltas=True):
-    """run_with_diffs on the GPU. Inputs [n] or [B, n]; returns (msgs [B?, E_s], deltas)."""
+  def _inputs(self, log_potentials, evidence, ftov_msgs):
+    """Device copies of the three BPArrays fields with their strides and the batch size."""
     torch = _torch()
     lp = self._dev(log_potentials) if self.num_potentials > 0 else torch.zeros(
         1, device=f"cuda:{self.device}")
@@ -147,19 +146,101 @@ class Plan:
       raise ValueError(f"inconsistent batch sizes {sorted(bs)}")
     B = bs.pop() if bs else 1
     batched = any(t.ndim == 2 for t in (lp, ev, m))
-    iters = max(int(num_iters), 1)
-    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=m.device)
-    deltas = torch.empty((B, iters), dtype=torch.float32, device=m.device) if with_deltas else None
-    ws_bytes = int(self.lib.pgbp_workspace_size(self.handle, B, iters))
-    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=m.device)
+    return (lp_t, lps), (ev_t, evs), (m_t, ms), B, batched
+
+  def _run(self, lp, ev, m, B, out, deltas, num_iters, damping, temperature):
+    ws_bytes = int(self.lib.pgbp_workspace_size(self.handle, B, max(int(num_iters), 1)))
+    ws = _torch().empty(ws_bytes, dtype=_torch().uint8, device=out.device)
     native.check(self.lib.pgbp_run(
-        self.handle, self._stream(), B, lp_t.data_ptr(), lps, ev_t.data_ptr(), evs,
-        m_t.data_ptr(), ms, out.data_ptr(), deltas.data_ptr() if deltas is not None else None,
+        self.handle, self._stream(), B, lp[0].data_ptr(), lp[1], ev[0].data_ptr(), ev[1],
+        m[0].data_ptr(), m[1], out.data_ptr(), deltas.data_ptr() if deltas is not None else None,
         int(num_iters), float(damping), float(temperature), ws.data_ptr(), ws_bytes), "pgbp_run")
+
+  def run(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5, temperature=0.0,
+          with_deltas=True):
+    """run_with_diffs on the GPU. Inputs [n] or [B, n]; returns (msgs [B?, E_s], deltas)."""
+    torch = _torch()
+    lp, ev, m, B, batched = self._inputs(log_potentials, evidence, ftov_msgs)
+    iters = max(int(num_iters), 1)
+    dev = m[0].device
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=dev)
+    deltas = torch.empty((B, iters), dtype=torch.float32, device=dev) if with_deltas else None
+    self._run(lp, ev, m, B, out, deltas, num_iters, damping, temperature)
     if not batched:
       out = out[0]
       deltas = deltas[0] if deltas is not None else None
     return out, deltas
+
+  def run_checkpointed(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5,
+                       temperature=0.0, checkpoint_every=10):
+    """run() that also keeps the messages every `checkpoint_every` iterations
+    (pgbp_run_checkpointed): returns (msgs, deltas, checkpoints [ceil(iters / k), B, E_s]) for
+    run_vjp; msgs and deltas are bit for bit those of run()."""
+    torch = _torch()
+    k = int(checkpoint_every)
+    if k < 1:
+      raise ValueError(f"checkpoint_every must be >= 1, got {k}")
+    lp, ev, m, B, batched = self._inputs(log_potentials, evidence, ftov_msgs)
+    iters = max(int(num_iters), 1)
+    k = min(k, iters)
+    n_ck = -(-iters // k)
+    dev = m[0].device
+    ck = torch.empty((n_ck, B, self.num_edge_states), dtype=torch.float32, device=dev)
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=dev)
+    deltas = torch.empty((B, iters), dtype=torch.float32, device=dev)
+    ws_bytes = int(self.lib.pgbp_workspace_size(self.handle, B, iters))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    native.check(self.lib.pgbp_run_checkpointed(
+        self.handle, self._stream(), B, lp[0].data_ptr(), lp[1], ev[0].data_ptr(), ev[1],
+        m[0].data_ptr(), m[1], out.data_ptr(), deltas.data_ptr(), int(num_iters), k,
+        float(damping), float(temperature), ck.data_ptr(), ws.data_ptr(), ws_bytes),
+                 "pgbp_run_checkpointed")
+    if not batched:
+      return out[0], deltas[0], ck
+    return out, deltas, ck
+
+  def run_vjp(self, log_potentials, evidence, checkpoints, num_iters, g_msgs, damping=0.5,
+              temperature=1.0, checkpoint_every=10, want_msgs_in=False):
+    """Gradients (g_log_potentials, g_evidence, g_msgs_in or None) of a loss with gradient g_msgs
+    on run()'s output messages, by the hand-written adjoint (pgbp_run_vjp). Shared (1-D)
+    potentials / evidence get gradients summed over the batch."""
+    torch = _torch()
+    ck = checkpoints
+    n_ck, B, n_es = ck.shape
+    lp, ev, _, b, _ = self._inputs(log_potentials, evidence, ck[0])
+    if b != B:
+      raise ValueError(f"checkpoints hold {B} instances, inputs {b}")
+    g = self._dev(g_msgs)
+    g = g.expand(B, n_es).contiguous() if g.ndim == 1 else g
+    if tuple(g.shape) != (B, n_es):
+      raise ValueError(f"g_msgs shape {tuple(g.shape)}, expected {(B, n_es)}")
+    dev = ck.device
+    P = max(self.num_potentials, 1)
+    g_lp = torch.empty((B, P) if lp[1] else (P,), dtype=torch.float32, device=dev)
+    g_ev = torch.empty((B, self.num_var_states) if ev[1] else (self.num_var_states,),
+                       dtype=torch.float32, device=dev)
+    g_m = torch.empty((B, n_es), dtype=torch.float32, device=dev) if want_msgs_in else None
+    ws_bytes = int(self.lib.pgbp_vjp_workspace_size(self.handle, B, int(num_iters),
+                                                    int(checkpoint_every)))
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+    native.check(self.lib.pgbp_run_vjp(
+        self.handle, self._stream(), B, lp[0].data_ptr(), lp[1], ev[0].data_ptr(), ev[1],
+        ck.data_ptr(), int(num_iters), int(checkpoint_every), float(damping), float(temperature),
+        g.data_ptr(), g_lp.data_ptr(), g_ev.data_ptr(), g_m.data_ptr() if g_m is not None else None,
+        ws.data_ptr(), ws_bytes), "pgbp_run_vjp")
+    if self.num_potentials == 0:
+      g_lp = g_lp[..., :0]
+    return g_lp, g_ev, g_m
+
+  def beliefs_vjp(self, g_beliefs):
+    """dL/d(messages) [B?, E_s] from dL/d(flat beliefs) (pgbp_beliefs_vjp)."""
+    torch = _torch()
+    g = self._dev(g_beliefs)
+    g_t, B, gs = self._rows(g, self.num_var_states)
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=g.device)
+    native.check(self.lib.pgbp_beliefs_vjp(self.handle, self._stream(), B, g_t.data_ptr(), gs,
+                                           out.data_ptr()), "pgbp_beliefs_vjp")
+    return out if g.ndim == 2 else out[0]
 
   def factor_update(self, ftype, vtof_msgs, log_potentials, temperature, normalize=True):
     """FAC_TO_VAR_UPDATES[type] on one type's message slice ([n] or [B, n])."""

@@ -13,6 +13,7 @@ from typing import Any, Callable, Dict, Hashable, Optional, Tuple
 
 import numpy as np
 
+from .. import autodiff
 from .bp_state import BPArrays, BPState
 from .inferer import Beliefs, Inferer, InfererContext, unflatten_beliefs
 
@@ -29,16 +30,28 @@ class BeliefPropagation(Inferer):
 
 
 def BP(bp_state: BPState, temperature: Optional[float] = 0.0,  # pylint: disable=invalid-name
-       exec_flags: int = 0) -> BeliefPropagation:
-  """Returns the belief propagation functions of `bp_state`'s factor graph. `exec_flags` (not in
-  PGMax) forces an execution path of the engine (pgmax_gb300.native.FLAG_*)."""
+       exec_flags: int = 0, checkpoint_every: int = 10) -> BeliefPropagation:
+  """Returns the belief propagation functions of `bp_state`'s factor graph.
+
+  Arguments not in PGMax: `exec_flags` forces an execution path of the engine
+  (pgmax_gb300.native.FLAG_*); `checkpoint_every` is the message checkpoint interval of
+  differentiable runs. A run whose BPArrays hold torch tensors that require grad (with grad
+  enabled) is differentiable: torch autograd reaches the log potentials, evidence and initial
+  messages through the hand-written adjoint (pgmax_gb300.autodiff), as jax.grad does through the
+  reference's bp.run.
+  """
   ctx = InfererContext(bp_state, exec_flags)
   default_t = temperature
 
   def run_with_diffs(bp_arrays: BPArrays, num_iters: int, damping: float = 0.5,
                      temperature: float = default_t):
-    msgs, deltas = ctx.plan.run(bp_arrays.log_potentials, bp_arrays.evidence, bp_arrays.ftov_msgs,
-                                num_iters, damping, temperature)
+    if autodiff.wants_grad(bp_arrays.log_potentials, bp_arrays.evidence, bp_arrays.ftov_msgs):
+      msgs, deltas = autodiff.run_with_diffs(ctx.plan, bp_arrays.log_potentials,
+                                             bp_arrays.evidence, bp_arrays.ftov_msgs, num_iters,
+                                             damping, temperature, checkpoint_every)
+    else:
+      msgs, deltas = ctx.plan.run(bp_arrays.log_potentials, bp_arrays.evidence,
+                                  bp_arrays.ftov_msgs, num_iters, damping, temperature)
     lp = bp_arrays.log_potentials
     ev = bp_arrays.evidence
     return BPArrays(log_potentials=lp if _is_torch(lp) else ctx.plan._dev(lp),  # pylint: disable=protected-access
@@ -75,7 +88,9 @@ def get_marginals(beliefs: Dict[Hashable, Any]) -> Dict[Hashable, Any]:
   """Per-variable softmax of the beliefs (pgmax/infer/bp.py:263-288). Beliefs from get_beliefs
   are normalised by the pgbp_marginals kernel; padded states get probability 0."""
   ctx = getattr(beliefs, "context", None)
-  if ctx is not None and getattr(beliefs, "flat", None) is not None and ctx.num_variables > 0:
+  flat = getattr(beliefs, "flat", None)
+  if (ctx is not None and flat is not None and ctx.num_variables > 0 and
+      not autodiff.wants_grad(flat)):
     flat = ctx.plan.marginals(beliefs.flat)
     out = unflatten_beliefs(flat, ctx.bp_state.fg_state.variable_groups)
 

@@ -107,15 +107,24 @@ class InfererContext:
   def _device(self, x):
     return self.plan._dev(x)  # pylint: disable=protected-access
 
+  def _defaults(self):
+    """Device copies of the BPState's arrays, uploaded once (the updates below never write into
+    them: they copy first). Keeps init() free of host-to-device copies, so a step that calls it
+    can be captured in a CUDA graph."""
+    cached = getattr(self, "_default_arrays", None)
+    if cached is None:
+      cached = tuple(self._device(x.value) for x in (
+          self.bp_state.log_potentials, self.bp_state.ftov_msgs, self.bp_state.evidence))
+      object.__setattr__(self, "_default_arrays", cached)
+    return cached
+
   def update(self, bp_arrays: Optional[BPArrays] = None, log_potentials_updates=None,
              ftov_msgs_updates=None, evidence_updates=None) -> BPArrays:
     fg_state = self.bp_state.fg_state
     if bp_arrays is not None:
       lp, msgs, ev = bp_arrays.log_potentials, bp_arrays.ftov_msgs, bp_arrays.evidence
     else:
-      lp = self._device(self.bp_state.log_potentials.value)
-      msgs = self._device(self.bp_state.ftov_msgs.value)
-      ev = self._device(self.bp_state.evidence.value)
+      lp, msgs, ev = self._defaults()
     if log_potentials_updates is not None:
       lp = bpstate.update_log_potentials(lp, log_potentials_updates, fg_state)
     if ftov_msgs_updates is not None:
@@ -139,7 +148,11 @@ class InfererContext:
 
   def get_beliefs(self, bp_arrays: BPArrays) -> Dict[Hashable, Any]:
     """evidence.at[var_states_for_edge_states].add(ftov_msgs), unflattened per group."""
-    flat = self.plan.beliefs(bp_arrays.evidence, bp_arrays.ftov_msgs)
+    from .. import autodiff  # pylint: disable=g-import-not-at-top
+    if autodiff.wants_grad(bp_arrays.evidence, bp_arrays.ftov_msgs):
+      flat = autodiff.beliefs(self.plan, bp_arrays.evidence, bp_arrays.ftov_msgs)
+    else:
+      flat = self.plan.beliefs(bp_arrays.evidence, bp_arrays.ftov_msgs)
     out = Beliefs(unflatten_beliefs(flat, self.bp_state.fg_state.variable_groups))
     out.flat = flat
     out.context = self

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libpgbp.so")
 
-SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu"]
+SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu", "pgbp_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every float32 op rounds as the reference's does.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -114,11 +114,11 @@ FLAG_PATH_MULTI = 8
 
 
 class Profile(ctypes.Structure):
-  _fields_ = [("launches", _i64 * 9), ("milliseconds", ctypes.c_double * 9)]
+  _fields_ = [("launches", _i64 * 10), ("milliseconds", ctypes.c_double * 10)]
 
 
 PROFILE_CLASSES = ("varsum", "pairwise", "enum_generic", "or", "and", "pool", "layout", "readout",
-                   "small_graph")
+                   "small_graph", "adjoint")
 
 # (name, restype, argtypes) of every symbol include/pgbp.h declares
 SIGNATURES = [
@@ -133,6 +133,12 @@ SIGNATURES = [
                                                _p, _i64, _d, _d]),
     ("pgbp_factor_update", ctypes.c_int, [_p, _p, ctypes.c_int, _i64, _p, _i64, _p, _i64, _d,
                                           ctypes.c_int, _p, _i64]),
+    ("pgbp_run_checkpointed", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p,
+                                             _i64, _i64, _d, _d, _p, _p, ctypes.c_size_t]),
+    ("pgbp_vjp_workspace_size", ctypes.c_size_t, [_p, _i64, _i64, _i64]),
+    ("pgbp_run_vjp", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i64, _d, _d, _p,
+                                    _p, _p, _p, _p, ctypes.c_size_t]),
+    ("pgbp_beliefs_vjp", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
     ("pgbp_decode", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_marginals", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),

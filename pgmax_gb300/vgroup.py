@@ -121,6 +121,25 @@ class NDVarArray(VarGroup):
       object.__setattr__(self, "_variable_hashes", cached)
     return cached
 
+  def _uniform_states(self) -> bool:
+    """Every variable has the maximum number of states: per-state data needs no mask."""
+    return bool(np.all(self.num_states == self.num_states.max(initial=0)))
+
+  def _state_mask(self) -> np.ndarray:
+    """[n * max_states] mask of the real states in shape + (max_states,) data."""
+    kmax = int(self.num_states.max(initial=0))
+    return (np.arange(kmax) < self.num_states[..., None]).reshape(-1)
+
+  def _torch_index(self, like):
+    """Device index tensor of the real states, built once per device: indexing with it copies no
+    host data, so flatten / unflatten can run inside a CUDA graph capture."""
+    import torch  # pylint: disable=g-import-not-at-top
+    cache = self.__dict__.setdefault("_index_cache", {})
+    key = str(like.device)
+    if key not in cache:
+      cache[key] = torch.as_tensor(np.flatnonzero(self._state_mask()), device=like.device)
+    return cache[key]
+
   def flatten(self, data):
     """shape -> per-variable flat data; shape + (max_states,) -> per-state flat data.
     A leading batch axis is kept: (B,) + shape [+ (max_states,)] -> [B, n]."""
@@ -131,12 +150,17 @@ class NDVarArray(VarGroup):
     if tshape == tuple(self.shape):
       return data.reshape(-1)
     if tshape == tuple(self.shape) + (kmax,):
-      mask = np.arange(kmax) < self.num_states[..., None]
-      return data[mask] if not _is_torch(data) else data[_torch_mask(mask, data)]
+      flat = data.reshape(-1)
+      if self._uniform_states():
+        return flat
+      mask = self._state_mask()
+      return flat[mask] if not _is_torch(data) else flat[self._torch_index(data)]
     if len(tshape) == nd + 2 and tshape[1:] == tuple(self.shape) + (kmax,):
-      mask = (np.arange(kmax) < self.num_states[..., None]).reshape(-1)
       flat = data.reshape(tshape[0], -1)
-      return flat[:, mask] if not _is_torch(data) else flat[:, _torch_mask(mask, data)]
+      if self._uniform_states():
+        return flat
+      mask = self._state_mask()
+      return flat[:, mask] if not _is_torch(data) else flat[:, self._torch_index(data)]
     if len(tshape) == nd + 1 and tshape[1:] == tuple(self.shape):
       return data.reshape(tshape[0], -1)
     raise ValueError(f"data should be of shape {tuple(self.shape)} or "
@@ -154,12 +178,14 @@ class NDVarArray(VarGroup):
         raise ValueError(f"flat_data size should be equal to {self.num_states.sum()}. "
                          f"Got size {n}.")
       kmax = int(self.num_states.max(initial=0))
-      mask = (np.arange(kmax) < self.num_states[..., None]).reshape(-1)
+      if self._uniform_states():
+        return flat_data.reshape(lead + tuple(self.shape) + (kmax,))
+      mask = self._state_mask()
       if _is_torch(flat_data):
         import torch  # pylint: disable=g-import-not-at-top
         out = torch.full(lead + (int(np.prod(self.shape)) * kmax,), -float("inf"),
                          dtype=flat_data.dtype, device=flat_data.device)
-        out[..., _torch_mask(mask, flat_data)] = flat_data
+        out[..., self._torch_index(flat_data)] = flat_data
       else:
         out = np.full(lead + (int(np.prod(self.shape)) * kmax,), -np.inf, dtype=flat_data.dtype)
         out[..., mask] = flat_data
@@ -170,9 +196,6 @@ class NDVarArray(VarGroup):
     return flat_data.reshape(lead + tuple(self.shape))
 
 
-def _torch_mask(mask, like):
-  import torch  # pylint: disable=g-import-not-at-top
-  return torch.as_tensor(np.nonzero(mask)[0], device=like.device)
 
 
 @dataclasses.dataclass(frozen=True, eq=False)

@@ -1,0 +1,71 @@
+"""The float64 torch restatement that the adjoint is checked against, pinned on CPU.
+
+Two pins: its forward messages agree with the golden fixtures recorded from the reference's own
+bp.run (Enum-only graphs at temperature > 0), and its autograd gradients agree with float64
+central finite differences (step 1e-6) of the same loss.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import fixtures
+from oracle import bp_torch
+
+ENUM_T_POS = ["case_ising12_T1", "case_potts_K4", "case_potts_K8", "case_potts_K16"]
+
+
+def _load(name):
+  return fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
+
+
+@pytest.mark.parametrize("name", ENUM_T_POS)
+def test_forward_matches_reference_fixture(name):
+  d = _load(name)
+  g = bp_torch.EnumGraph(d["wiring"])
+  f64 = lambda x: torch.as_tensor(np.asarray(x, dtype=np.float64))
+  with torch.no_grad():
+    out = g.run(f64(d["log_potentials"]), f64(d["evidence"]), f64(d["ftov_msgs_in"]),
+                int(d["num_iters"]), float(d["damping"]), float(d["temperature"]))
+    bel = g.beliefs(f64(d["evidence"]), out)
+  # float32 reference vs float64 restatement
+  np.testing.assert_allclose(out[0].numpy(), d["ftov_msgs_out"], atol=1e-5, rtol=0)
+  np.testing.assert_allclose(bel[0].numpy(), d["flat_beliefs"], atol=2e-5, rtol=0)
+
+
+def _loss(g, lp, ev, m, iters, damping, temperature, labels_w):
+  out = g.run(lp, ev, m, iters, damping, temperature)
+  bel = g.beliefs(ev, out)
+  # per-state log-softmax weighted by fixed label weights (a smooth stand-in for -log p(label))
+  return -(torch.log_softmax(bel.reshape(bel.shape[0], -1, g.k), dim=-1).reshape(bel.shape)
+           * labels_w).sum() / bel.shape[0]
+
+
+@pytest.mark.parametrize("name,batched_lp", [("case_ising12_T1", False), ("case_potts_K4", True)])
+def test_autograd_matches_central_differences(name, batched_lp):
+  d = _load(name)
+  g = bp_torch.EnumGraph(d["wiring"])
+  g.k = int(np.bincount(np.asarray(d["wiring"]["evidence_to_vars"])).max())
+  rng = np.random.default_rng(7)
+  B = 2
+  lp = np.asarray(d["log_potentials"], np.float64)
+  lp = np.stack([lp + 0.1 * rng.normal(size=lp.shape) for _ in range(B)]) if batched_lp else lp
+  ev = np.asarray(d["evidence"], np.float64)[None] + rng.normal(size=(B,) + d["evidence"].shape)
+  m = 0.3 * rng.normal(size=(B,) + d["ftov_msgs_in"].shape)
+  labels_w = torch.as_tensor(rng.random(size=(B,) + d["evidence"].shape))
+  iters, damping, temperature = 12, 0.5, float(d["temperature"])
+  args = [torch.tensor(x, dtype=torch.float64, requires_grad=True) for x in (lp, ev, m)]
+  loss = _loss(g, *args, iters, damping, temperature, labels_w)
+  grads = torch.autograd.grad(loss, args)
+  h = 1e-6
+  for which, (x, gx) in enumerate(zip(args, grads)):
+    flat = x.detach().reshape(-1)
+    for idx in rng.choice(flat.numel(), size=6, replace=False):
+      vals = []
+      for sign in (1.0, -1.0):
+        xs = [a.detach().clone() for a in args]
+        xs[which].view(-1)[idx] += sign * h
+        with torch.no_grad():
+          vals.append(float(_loss(g, *xs, iters, damping, temperature, labels_w)))
+      fd = (vals[0] - vals[1]) / (2 * h)
+      assert abs(fd - float(gx.reshape(-1)[idx])) <= 1e-6 * max(1.0, abs(fd)), (which, idx)

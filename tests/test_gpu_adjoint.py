@@ -1,0 +1,211 @@
+"""The hand-written adjoint (pgbp_run_vjp, pgbp_beliefs_vjp) on the GPU.
+
+Gradients of the CUDA path are compared with torch autograd through the float64 restatement in
+oracle/bp_torch.py (pinned to the reference fixtures and to central differences on CPU). Float32
+forward and backward against a float64 reference: |g - g_ref| <= 2e-4 * max|g_ref| + 1e-6.
+"""
+
+import numpy as np
+import pytest
+
+import fixtures
+from oracle import bp_torch
+
+pytestmark = pytest.mark.gpu
+
+ENUM_T_POS = ["case_ising12_T1", "case_potts_K4", "case_potts_K8", "case_potts_K16"]
+RTOL = 2e-4
+
+
+def _torch():
+  import torch  # pylint: disable=g-import-not-at-top
+  if not torch.cuda.is_available():
+    pytest.skip("no CUDA device")
+  return torch
+
+
+def _load(name):
+  return fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
+
+
+def _plan(d):
+  from pgmax_gb300 import engine  # pylint: disable=g-import-not-at-top
+  return engine.Plan(d["wiring"])
+
+
+def _close(got, want, what):
+  got = np.asarray(got, np.float64)
+  want = np.asarray(want, np.float64)
+  assert got.shape == want.shape, (what, got.shape, want.shape)
+  err = np.max(np.abs(got - want)) if got.size else 0.0
+  bound = RTOL * (np.max(np.abs(want)) if want.size else 0.0) + 1e-6
+  assert err <= bound, f"{what}: max error {err:.3g} > {bound:.3g}"
+
+
+def _inputs(d, B, batched_lp, batched_ev, seed=0):
+  rng = np.random.default_rng(seed)
+  lp = np.asarray(d["log_potentials"], np.float32)
+  if batched_lp:
+    lp = np.stack([lp + 0.1 * rng.normal(size=lp.shape).astype(np.float32) for _ in range(B)])
+  ev = np.asarray(d["evidence"], np.float32)
+  if batched_ev:
+    ev = ev[None] + rng.normal(size=(B,) + ev.shape).astype(np.float32)
+  m = (0.3 * rng.normal(size=(B,) + d["ftov_msgs_in"].shape)).astype(np.float32)
+  w = rng.normal(size=(B,) + d["ftov_msgs_in"].shape).astype(np.float32)
+  return lp, ev, m, w
+
+
+def _reference_grads(d, lp, ev, m, w, iters, damping, temperature):
+  torch = _torch()
+  g = bp_torch.EnumGraph(d["wiring"])
+  args = [torch.tensor(np.asarray(x, np.float64), requires_grad=True) for x in (lp, ev, m)]
+  out = g.run(*args, iters, damping, temperature)
+  loss = (out * torch.as_tensor(w, dtype=torch.float64)).sum()
+  grads = torch.autograd.grad(loss, args)
+  return out.detach().numpy(), [x.numpy() for x in grads]
+
+
+@pytest.mark.parametrize("name", ENUM_T_POS)
+@pytest.mark.parametrize("batched_lp,batched_ev", [(False, True), (True, False), (True, True)])
+def test_vjp_matches_float64_autograd(name, batched_lp, batched_ev):
+  torch = _torch()
+  d = _load(name)
+  plan = _plan(d)
+  B, iters, k = 3, 23, 5
+  damping, temperature = float(d["damping"]), float(d["temperature"])
+  lp, ev, m, w = _inputs(d, B, batched_lp, batched_ev)
+  out, _, ck = plan.run_checkpointed(lp, ev, m, iters, damping, temperature, k)
+  g_lp, g_ev, g_m = plan.run_vjp(lp, ev, ck, iters, torch.as_tensor(w).cuda(), damping,
+                                 temperature, k, want_msgs_in=True)
+  torch.cuda.synchronize()
+  ref_out, (r_lp, r_ev, r_m) = _reference_grads(d, lp, ev, m, w, iters, damping, temperature)
+  np.testing.assert_allclose(out.cpu().numpy(), ref_out, atol=2e-5, rtol=0)
+  _close(g_lp.cpu().numpy(), r_lp, "g_log_potentials")
+  _close(g_ev.cpu().numpy(), r_ev, "g_evidence")
+  _close(g_m.cpu().numpy(), r_m, "g_msgs_in")
+
+
+@pytest.mark.parametrize("iters,k", [(0, 1), (1, 1), (1, 10), (7, 1), (7, 3), (7, 7), (7, 100),
+                                     (30, 10)])
+def test_vjp_iterations_and_checkpoint_intervals(iters, k):
+  torch = _torch()
+  d = _load("case_potts_K4")
+  plan = _plan(d)
+  B = 2
+  lp, ev, m, w = _inputs(d, B, False, True, seed=iters * 100 + k)
+  out, _, ck = plan.run_checkpointed(lp, ev, m, iters, 0.5, 1.0, k)
+  g_lp, g_ev, g_m = plan.run_vjp(lp, ev, ck, iters, torch.as_tensor(w).cuda(), 0.5, 1.0, k,
+                                 want_msgs_in=True)
+  ref_out, (r_lp, r_ev, r_m) = _reference_grads(d, lp, ev, m, w, iters, 0.5, 1.0)
+  np.testing.assert_allclose(out.cpu().numpy(), ref_out, atol=2e-5, rtol=0)
+  _close(g_lp.cpu().numpy(), r_lp, "g_log_potentials")
+  _close(g_ev.cpu().numpy(), r_ev, "g_evidence")
+  _close(g_m.cpu().numpy(), r_m, "g_msgs_in")
+
+
+@pytest.mark.parametrize("k", [1, 3, 8, 1000])
+def test_checkpointed_forward_equals_one_run(k):
+  torch = _torch()
+  d = _load("case_ising12_T1")
+  plan = _plan(d)
+  lp, ev, m, _ = _inputs(d, 4, True, True, seed=k)
+  a, da = plan.run(lp, ev, m, 40, 0.5, 1.0)
+  b, db, ck = plan.run_checkpointed(lp, ev, m, 40, 0.5, 1.0, k)
+  torch.cuda.synchronize()
+  assert torch.equal(a, b) and torch.equal(da, db)
+  kk = min(k, 40)
+  assert ck.shape[0] == -(-40 // kk)
+  np.testing.assert_array_equal(ck[0].cpu().numpy(), m)
+  for c in range(1, ck.shape[0]):
+    want, _ = plan.run(lp, ev, m, c * kk, 0.5, 1.0)
+    assert torch.equal(ck[c], want), c
+
+
+def test_gradient_is_deterministic():
+  torch = _torch()
+  d = _load("case_potts_K8")
+  plan = _plan(d)
+  lp, ev, m, w = _inputs(d, 5, False, False, seed=3)
+  runs = []
+  for _ in range(2):
+    _, _, ck = plan.run_checkpointed(lp, ev, m, 15, 0.5, 1.0, 4)
+    runs.append(plan.run_vjp(lp, ev, ck, 15, torch.as_tensor(w).cuda(), 0.5, 1.0, 4))
+  for x, y in zip(runs[0][:2], runs[1][:2]):
+    assert torch.equal(x, y)
+
+
+def test_beliefs_vjp_is_the_gather():
+  torch = _torch()
+  d = _load("case_potts_K4")
+  plan = _plan(d)
+  rng = np.random.default_rng(0)
+  gb = rng.normal(size=(3, plan.num_var_states)).astype(np.float32)
+  gm = plan.beliefs_vjp(gb).cpu().numpy()
+  vs = np.asarray(d["wiring"]["var_states_for_edge_states"])
+  np.testing.assert_array_equal(gm, gb[:, vs])
+
+
+def test_unsupported_graphs_and_temperature_raise():
+  torch = _torch()
+  d = _load("case_potts_K4")
+  plan = _plan(d)
+  lp, ev, m, w = _inputs(d, 2, False, True)
+  _, _, ck = plan.run_checkpointed(lp, ev, m, 5, 0.5, 0.0, 2)
+  with pytest.raises(ValueError, match="temperature > 0"):
+    plan.run_vjp(lp, ev, ck, 5, torch.as_tensor(w).cuda(), 0.5, 0.0, 2)
+  dd = _load("case_deconv_T1")
+  p2 = _plan(dd)
+  ck2 = torch.zeros((1, 1, p2.num_edge_states), device="cuda")
+  with pytest.raises(ValueError, match="dense pairwise"):
+    p2.run_vjp(dd["log_potentials"], dd["evidence"], ck2, 1,
+               torch.zeros((1, p2.num_edge_states), device="cuda"), 0.5, 1.0, 1)
+
+
+def test_autograd_function_through_drop_in_api():
+  """bp.init(log_potentials_updates=...) -> run -> get_beliefs -> get_marginals -> loss.backward()
+  (the reference's learning example, examples/grid_mrf.ipynb cells 15-16, in torch)."""
+  torch = _torch()
+  import pgmax_gb300 as pg  # pylint: disable=g-import-not-at-top
+  from golden import cases  # pylint: disable=g-import-not-at-top
+  fg, groups, ev_updates = cases.potts(pg, L=6, K=3, seed=4)
+  grid = groups[0]
+  pair_groups = [g for g in fg.factor_groups[pg.factor.EnumFactor]]
+  bp = pg.infer.BP(fg.bp_state, temperature=1.0, checkpoint_every=4)
+  W = torch.tensor(np.eye(3, dtype=np.float32) * 0.7 + 0.1, device="cuda", requires_grad=True)
+  ev = torch.tensor(ev_updates[grid], device="cuda", requires_grad=True)
+  labels = torch.as_tensor(np.random.default_rng(1).integers(0, 3, size=(6, 6)), device="cuda")
+
+  def loss_fn(W, ev):
+    arrays = bp.init(log_potentials_updates={pair_groups[0]: W, pair_groups[1]: W},
+                     evidence_updates={grid: ev})
+    arrays = bp.run(arrays, num_iters=17, damping=0.5, temperature=1.0)
+    marg = pg.infer.get_marginals(bp.get_beliefs(arrays))[grid]
+    return -torch.log(torch.gather(marg, -1, labels[..., None])).mean()
+
+  loss = loss_fn(W, ev)
+  loss.backward()
+  # float64 autograd of the same chain through the restatement
+  ctx = bp.context
+  wiring = ctx.flat_wiring()
+  g64 = bp_torch.EnumGraph(wiring)
+  W64 = W.detach().cpu().double().requires_grad_()
+  ev64 = ev.detach().cpu().double().requires_grad_()
+  starts = ctx.bp_state.fg_state.factor_group_to_potentials_starts
+  lp64 = torch.zeros(g64.lp_range[1], dtype=torch.float64)
+  parts = []
+  pos = 0
+  for grp in sorted(pair_groups, key=lambda x: starts[x]):
+    s = starts[grp]
+    n = grp.num_factors * 9
+    assert s == pos
+    parts.append(W64.reshape(-1).repeat(grp.num_factors))
+    pos = s + n
+  lp64 = torch.cat(parts)
+  out = g64.run(lp64, ev64.reshape(-1), torch.zeros(g64.num_edge_states, dtype=torch.float64), 17,
+                0.5, 1.0)
+  bel = g64.beliefs(ev64.reshape(-1), out).reshape(6, 6, 3)
+  ref = -torch.log_softmax(bel, -1).gather(-1, labels.cpu()[..., None]).mean()
+  ref.backward()
+  assert abs(float(loss) - float(ref)) < 1e-5
+  _close(W.grad.cpu().numpy(), W64.grad.numpy(), "dL/dW")
+  _close(ev.grad.cpu().numpy(), ev64.grad.numpy(), "dL/devidence")

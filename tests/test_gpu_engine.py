@@ -130,14 +130,24 @@ def test_batched_run_equals_single_instances(name, exec_path):
 
 
 @pytest.mark.parametrize("name,B", [("case_rbm_s0", 8), ("case_rbm_s1", 12), ("case_ising12_T1", 4),
-                                    ("case_ising50_T0", 16)])
+                                    ("case_ising50_T0", 16), ("case_rbm_s0", "x4"),
+                                    ("case_ising12_T1", "x4"), ("case_ising50_T0", "x4"),
+                                    ("case_ising50_T1", "x4")])
 def test_four_instances_per_thread_path(name, B):
-  """Batches that are a multiple of 4 run the 4-instances-per-thread kernels (binary pairwise
-  factors, binary variable sums) on the multi-kernel path; every instance must equal its own
-  oracle run."""
+  """Batches that are a multiple of 4 and large enough to leave >= 16 warps per SM (B = "x4":
+  sized from the GPU's SM count) run the 4-instances-per-thread kernels (binary pairwise factors,
+  binary variable sums) on the multi-kernel path; small ones run one instance per thread. Every
+  instance must equal its own oracle run."""
+  torch = _torch()
   f = fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
   plan = _plan(f["wiring"], "multi")
   w = oracle.Wiring(f["wiring"])
+  if B == "x4":
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    n_pw = plan.info["num_enum_pairwise_factors"]
+    n_vars = int(np.max(f["wiring"]["evidence_to_vars"])) + 1
+    units = n_pw if name.startswith("case_rbm") else min(n_pw, n_vars)
+    B = 4 * (-(-sms * 16 * 32 // units))
   rng = np.random.default_rng(3)
   ev = (f["evidence"][None] + rng.gumbel(size=(B,) + f["evidence"].shape)).astype(np.float32)
   T = float(f["temperature"])
@@ -146,14 +156,13 @@ def test_four_instances_per_thread_path(name, B):
   for lp in (f["log_potentials"], lp_b):
     out, deltas = plan.run(lp, ev, f["ftov_msgs_in"], 15, 0.5, T)
     out, deltas = _np(out), _np(deltas)
-    for b in range(B):
-      o, d = oracle.run(w, lp if lp.ndim == 1 else lp[b], ev[b], f["ftov_msgs_in"], 15, 0.5, T)
-      if T == 0.0:
-        np.testing.assert_array_equal(out[b], o)
-        np.testing.assert_array_equal(deltas[b], d)
-      else:
-        np.testing.assert_allclose(out[b], o, atol=ATOL, rtol=0)
-        np.testing.assert_allclose(deltas[b], d, atol=ATOL, rtol=0)
+    o, d = oracle.run_batch(w, lp, ev, f["ftov_msgs_in"], 15, 0.5, T)
+    if T == 0.0:
+      np.testing.assert_array_equal(out, o)
+      np.testing.assert_array_equal(deltas, d)
+    else:
+      np.testing.assert_allclose(out, o, atol=ATOL, rtol=0)
+      np.testing.assert_allclose(deltas, d, atol=ATOL, rtol=0)
 
 
 @pytest.mark.parametrize("exec_path", PATHS)

@@ -188,3 +188,13 @@ def test_bp_state_errors_and_updates():
   with pytest.raises(ValueError, match="Invalid FactorGroup"):
     _ = state.log_potentials[fgroup.EnumFactorGroup(variables_for_factors=[[v[0]]],
                                                     factor_configs=np.arange(2)[:, None])]
+
+
+def test_ndvararray_flatten_torch_matches_numpy_with_ragged_states():
+  import torch  # pylint: disable=g-import-not-at-top
+  import pgmax_gb300 as pg  # pylint: disable=g-import-not-at-top
+  g = pg.vgroup.NDVarArray(num_states=np.array([[2, 3], [3, 1]]), shape=(2, 2))
+  rng = np.random.default_rng(0)
+  for shape in ((2, 2, 3), (4, 2, 2, 3)):
+    x = rng.normal(size=shape).astype(np.float32)
+    np.testing.assert_array_equal(g.flatten(torch.as_tensor(x)).numpy(), g.flatten(x))
