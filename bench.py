@@ -345,6 +345,173 @@ def run_adjoint(args):
   return 0
 
 
+MG_GRAPHS, MG_ITERS = 256, 200
+
+
+def deconv_template(n_feat=5, feat=6, im=14):
+  """The 2D binary deconvolution graph (the reference's examples/pmp_binary_deconvolution.ipynb
+  construction): features W (1, n_feat, feat, feat), activations S (1, n_feat, s, s),
+  s = im - feat + 1, auxiliaries SW = AND(S, W) and pixels X = OR of the SW covering them."""
+  from pgmax_gb300 import fgraph, fgroup, infer, vgroup  # pylint: disable=g-import-not-at-top
+  s_size = im - feat + 1
+  W = vgroup.NDVarArray(num_states=2, shape=(1, n_feat, feat, feat))
+  S = vgroup.NDVarArray(num_states=2, shape=(1, n_feat, s_size, s_size))
+  SW = vgroup.NDVarArray(num_states=2, shape=(1, 1, im, im, n_feat, feat, feat))
+  X = vgroup.NDVarArray(num_states=2, shape=(1, 1, im, im))
+  fg = fgraph.FactorGraph(variable_groups=[S, W, SW, X])
+  and_vars, or_parents = [], {}
+  for sh in range(s_size):
+    for sw in range(s_size):
+      for f in range(n_feat):
+        for fh in range(feat):
+          for fw in range(feat):
+            aux = SW[0, 0, fh + sh, fw + sw, f, fh, fw]
+            and_vars.append([S[0, f, sh, sw], W[0, f, fh, fw], aux])
+            or_parents.setdefault((fh + sh, fw + sw), []).append(aux)
+  fg.add_factors(fgroup.ANDFactorGroup(and_vars))
+  fg.add_factors(fgroup.ORFactorGroup([v + [X[0, 0, r, c]] for (r, c), v in or_parents.items()]))
+  wiring = infer.InfererContext(fg.bp_state).flat_wiring()
+  return wiring, (S.shape, W.shape, SW.shape, X.shape), (n_feat, feat, im, s_size)
+
+
+def deconv_evidence(shapes, dims, rng):
+  """Seeded evidence of one deconvolution graph: W clamped to Bernoulli(0.25) masks (+-100),
+  S prior Bernoulli(0.02) log-odds, X the OR of the true activations' features with 5% of the
+  pixels flipped, observed at +-4 log-odds."""
+  (s_shape, w_shape, sw_shape, x_shape), (n_feat, feat, im, s_size) = shapes, dims
+  w_true = rng.random(w_shape) < 0.25
+  s_true = rng.random(s_shape) < 0.02
+  x = np.zeros((im, im), bool)
+  for f in range(n_feat):
+    for r, c in zip(*np.nonzero(s_true[0, f])):
+      x[r:r + feat, c:c + feat] |= w_true[0, f]
+  x ^= rng.random((im, im)) < 0.05
+  ev_s = np.zeros(s_shape + (2,), np.float32)
+  ev_s[..., 1] = np.log(0.02) - np.log(0.98)
+  ev_w = np.zeros(w_shape + (2,), np.float32)
+  ev_w[..., 1] = np.where(w_true, 100.0, -100.0)
+  ev_sw = np.zeros(sw_shape + (2,), np.float32)
+  ev_x = np.zeros(x_shape + (2,), np.float32)
+  ev_x[0, 0, ..., 1] = np.where(x, 4.0, -4.0)
+  return np.concatenate([a.reshape(-1) for a in (ev_s, ev_w, ev_sw, ev_x)])
+
+
+def build_multigraph(seed=0, n_graphs=MG_GRAPHS):
+  """256 graphs, family g mod 3: (a) open Potts grids L ~ U{16..128}, K ~ U{2,4,8,16}, one table
+  J * I_K per graph, J ~ U(0, 1.5), unaries N(0, 1); (b) the same at K = 64 with one table
+  ~ N(0, 0.5^2) per graph; (c) binary deconvolution graphs. Returns the wirings (grids with shared
+  tables and implicit config rows), per-graph potentials and evidence, and the family sizes."""
+  from pgmax_gb300 import batch  # pylint: disable=g-import-not-at-top
+  rng = np.random.default_rng(seed)
+  dec_w, dec_shapes, dec_dims = deconv_template()
+  cache, wirings, tables, evs, fam = {}, [], [], [], {"a": 0, "b": 0, "c": 0}
+  for g in range(n_graphs):
+    kind = "abc"[g % 3]
+    fam[kind] += 1
+    if kind == "c":
+      wirings.append(dec_w)
+      tables.append(np.zeros(0, np.float32))
+      evs.append(deconv_evidence(dec_shapes, dec_dims, rng))
+      continue
+    L = int(rng.integers(16, 129))
+    if kind == "a":
+      K = int(rng.choice([2, 4, 8, 16]))
+      table = (rng.uniform(0.0, 1.5) * np.eye(K)).astype(np.float32).reshape(-1)
+    else:
+      K = 64
+      table = rng.normal(0.0, 0.5, size=K * K).astype(np.float32)
+    if (L, K) not in cache:
+      cache[(L, K)] = batch.grid_wiring(L, K, shared_table=True, implicit_rows=True)
+    wirings.append(cache[(L, K)])
+    tables.append(table)
+    evs.append(rng.normal(size=L * L * K).astype(np.float32))
+  return wirings, tables, evs, fam
+
+
+def run_multigraph(args):
+  """Config 3: the 256-graph uneven batch as one union plan, 200 iterations at T=1, damping 0.5
+  (one step = one run over every graph)."""
+  import torch  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import batch, native  # pylint: disable=g-import-not-at-top
+  t0 = time.perf_counter()
+  wirings, tables, evs, fam = build_multigraph()
+  t_gen = time.perf_counter() - t0
+  t0 = time.perf_counter()
+  gb = batch.GraphBatch(wirings)
+  torch.cuda.synchronize()
+  t_plan = time.perf_counter() - t0
+  dev = torch.device("cuda", 0)
+  stream = torch.cuda.current_stream(dev)
+  lp = torch.as_tensor(gb.concat(tables), device=dev)
+  ev = torch.as_tensor(gb.concat(evs), device=dev)
+  n_es = int(gb.layout.perm.shape[0])
+  m0 = torch.zeros(n_es, device=dev)
+  u = gb.wiring
+  num_edges, n_vs = int(u["num_edges"]), int(u["num_var_states"])
+  iters = MG_ITERS
+
+  def step():
+    out, _ = gb.run(lp, ev, m0, iters, 0.5, 1.0)
+    return out
+
+  for _ in range(args.warmup):
+    step()
+  torch.cuda.synchronize()
+  s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  with ClockSampler(0) as clocks:
+    s0.record(stream)
+    for _ in range(args.steps):
+      step()
+    s1.record(stream)
+    torch.cuda.synchronize()
+  ms = s0.elapsed_time(s1) / args.steps
+  # end to end: host evidence in, beliefs and MAP states out
+  ev_host = torch.as_tensor(gb.concat(evs)).pin_memory()
+  map_host = torch.empty(int(u["num_variables"]), dtype=torch.int32).pin_memory()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  for _ in range(args.steps):
+    evd = ev_host.to(dev, non_blocking=True)
+    out, _ = gb.run(lp, evd, m0, iters, 0.5, 1.0)
+    map_host.copy_(gb.decode(gb.beliefs(evd, out)), non_blocking=True)
+  e1.record(stream)
+  torch.cuda.synchronize()
+  e2e_ms = e0.elapsed_time(e1) / args.steps
+  native.profile_read()
+  native.profile_enable(True)
+  step()
+  torch.cuda.synchronize()
+  native.profile_enable(False)
+  prof = native.profile_read()
+  peak, src = peaks()
+  p_distinct = int(lp.numel())
+  bytes_iter = 4 * (2 * n_es + n_vs) + 4 * p_distinct
+  line = {
+      "metric": "edge-msg updates/s", "value": num_edges * iters / (ms / 1e3),
+      "unit": "edge-msg updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+      "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+      "dtype": "f32", "data": "synthetic (seed 0)",
+      "config": {"workload": "multigraph256_potts_potts64_deconv", "graphs": MG_GRAPHS,
+                 "families": fam, "num_iters": iters, "temperature": 1.0, "damping": 0.5,
+                 "num_edges": num_edges, "edge_states": n_es, "var_states": n_vs,
+                 "shared_table_floats": p_distinct,
+                 "l2": "inputs larger than L2 (%d MB of messages)" % (4 * n_es >> 20)},
+      "setup_s": {"generate": round(t_gen, 2), "plan": round(t_plan, 2)},
+      "kernel_time_share": {k: v[1] for k, v in prof.items() if v[0]},
+      "gpu_launches": int(sum(v[0] for v in prof.values()) * args.steps),
+      "iteration_roofline": {"bytes_per_iter": bytes_iter,
+                             "achieved_gbs": bytes_iter * iters / (ms / 1e3) / 1e9,
+                             "peak_gbs": peak, "frac": bytes_iter * iters / (ms / 1e3) / 1e9 / peak,
+                             "peak_source": src},
+      "e2e": {"value": num_edges * iters / (e2e_ms / 1e3), "unit": "edge-msg updates/s",
+              "h2d_bytes_per_step": int(ev_host.numel() * 4),
+              "d2h_bytes_per_step": int(map_host.numel() * 4)},
+      "clocks": clocks.summary(),
+  }
+  print(json.dumps(line))
+  return 0
+
+
 def gumbel_evidence(num_var_states, batch, seed):
   rng = np.random.default_rng(seed)
   return rng.gumbel(size=(batch, num_var_states)).astype(np.float32)
@@ -501,9 +668,10 @@ def main():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
                   help="execution path of the ising workload (auto: timed choice)")
-  ap.add_argument("--workload", default="rbm", choices=["rbm", "ising", "adjoint"],
+  ap.add_argument("--workload", default="rbm", choices=["rbm", "ising", "adjoint", "multigraph"],
                   help="rbm: the headline RBM perturb-and-MAP batch (default); ising: the 50x50 "
-                       "toroidal Ising configuration; adjoint: differentiable BP on 64x64 grids")
+                       "toroidal Ising configuration; adjoint: differentiable BP on 64x64 grids; "
+                       "multigraph: the 256-graph uneven batch")
   args = ap.parse_args()
   if args.warmup < 3:
     args.warmup = 3
@@ -513,6 +681,8 @@ def main():
     return run_ising(args)
   if args.workload == "adjoint":
     return run_adjoint(args)
+  if args.workload == "multigraph":
+    return run_multigraph(args)
 
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top

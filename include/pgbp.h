@@ -93,12 +93,26 @@ typedef struct {
    * force a path instead (a forced path the graph is not eligible for falls back to
    * multi-kernel); results are identical on every path. */
   int64_t flags;
+  /* Shared potential tables (no counterpart in PGMax, which stores one table per factor). When
+   * non-NULL, EnumFactor k (k-th Enum factor in factor order) reads the potential of its config c
+   * at log_potentials[potentials_range[PGBP_ENUM][0] + enum_factor_potential_offsets[k] + c], so
+   * factors (and graphs of a batch) may share one table and log_potentials may be compact;
+   * enum_num_val_configs then only counts configs, not potentials. NULL: PGMax's layout (factor k
+   * reads its own configs' potentials). Plans with shared tables have no adjoint. */
+  int64_t enum_num_factors;                    /* length of enum_factor_potential_offsets */
+  const int32_t* enum_factor_potential_offsets;
 } pgbp_wiring_desc;
 
 #define PGBP_FLAG_NO_SMALL_GRAPH 1 /* multi-kernel only; the other paths are not even prepared */
 #define PGBP_FLAG_PATH_SMALL 2
 #define PGBP_FLAG_PATH_CLUSTER 4
 #define PGBP_FLAG_PATH_MULTI 8
+/* The Enum config rows are implied, not passed (enum_num_rows = 0, the row arrays NULL): every
+ * Enum factor is unary (configs = its states) or pairwise (all K1 * K2 configs, row-major: the
+ * PairwiseFactorGroup layout, fgroup/enum.py:303-310), each factor's configs following the
+ * previous factor's. For large dense pairwise graphs, whose rows (2 * K1 * K2 per factor) would
+ * dwarf the messages. No counterpart in PGMax, which always materialises the rows. */
+#define PGBP_FLAG_ENUM_IMPLICIT_ROWS 16
 
 typedef struct pgbp_plan pgbp_plan;
 

@@ -489,6 +489,8 @@ cudaError_t aux_stream(int device, cudaStream_t* out) {
 }  // namespace
 
 const char* adjoint_unsupported(const Plan& p) {
+  if (p.shared_potentials)
+    return "the adjoint needs one potential table per factor; the plan shares tables";
   if (p.enum_generic.count > 0)
     return "the adjoint covers dense pairwise EnumFactors only; the graph has other EnumFactors";
   if (p.logical[0].count > 0 || p.logical[1].count > 0 || p.pool.count > 0)

@@ -104,6 +104,7 @@ struct Plan {
   LogicalSet logical[2];
   PoolSet pool;
   int64_t flags = 0;
+  bool shared_potentials = false;  // Enum factors read tables through enum_factor_potential_offsets
   int64_t small_graph_smem = 0;  // bytes per CTA of the small-graph path; 0 = not eligible
   int cluster_size = 0;          // CTAs per instance of the cluster path; 0 = not eligible
   // execution path chosen per (batch, temperature == 0) by timing the eligible paths once

@@ -354,8 +354,16 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     const int64_t nrows = d->enum_num_rows, ncfg = d->enum_num_val_configs;
     const int32_t* ci = d->enum_factor_configs_indices;
     const int32_t* cf = d->enum_factor_configs_edge_states;
+    // Implicit rows: every Enum factor is unary (configs = its states) or pairwise (all K1 x K2
+    // configs in row-major order, the PairwiseFactorGroup layout), with its configs following the
+    // previous factor's; the rows PGMax would list are not passed.
+    const bool implicit = (d->flags & PGBP_FLAG_ENUM_IMPLICIT_ROWS) != 0;
+    if (implicit && nrows != 0)
+      return bail(fail(PGBP_ERR_INVALID_ARGUMENT, "implicit enum rows: enum_num_rows must be 0"));
     if (nrows > 0 && (!ci || !cf)) return bail(fail(PGBP_ERR_INVALID_ARGUMENT, "missing enum rows"));
-    if (d->potentials_range[0][1] - pot0 < ncfg)
+    const int32_t* alias = d->enum_factor_potential_offsets;
+    const int64_t npot_enum = d->potentials_range[0][1] - pot0;
+    if (!alias && npot_enum < ncfg)
       return bail(fail(PGBP_ERR_INVALID_WIRING, "enum potentials range shorter than num_val_configs"));
     // Enum factors are the first factors; enumerate them by edge-state range
     std::vector<int64_t> facs;
@@ -364,7 +372,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     }
     // rows grouped per factor
     std::vector<int64_t> row_begin(facs.size() + 1, nrows);
-    {
+    if (!implicit) {
       int64_t r = 0;
       for (size_t k = 0; k < facs.size(); ++k) {
         row_begin[k] = r;
@@ -379,6 +387,11 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       if (r != nrows)
         return bail(fail(PGBP_ERR_UNSUPPORTED, "enum config rows are not grouped by factor"));
     }
+    if (alias && d->enum_num_factors != (int64_t)facs.size())
+      return bail(fail(PGBP_ERR_INVALID_WIRING, "enum_num_factors is %lld, the wiring has %lld",
+                       (long long)d->enum_num_factors, (long long)facs.size()));
+    p.shared_potentials = alias != nullptr;
+    int64_t implicit_cfg = 0;
     std::map<std::pair<int, int>, std::pair<std::vector<int4>, std::vector<int32_t>>> buckets;
     std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_eslot, g_evs, g_rb, g_ncfg, g_nv, g_cfg,
         g_les;
@@ -398,16 +411,36 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         }
       }
       const int nv = (int)esz.size();
-      const int64_t r0 = row_begin[k], r1 = row_begin[k + 1];
-      if ((r1 - r0) % nv != 0)
-        return bail(fail(PGBP_ERR_UNSUPPORTED, "enum factor rows not a multiple of its arity"));
-      const int64_t nc = (r1 - r0) / nv;
-      const int64_t cfg0 = nc > 0 ? ci[r0] : 0;
-      // rows of config c are (var 0 .. var nv-1) with the state's edge state inside var i's edge
-      std::vector<int32_t> les((size_t)(r1 - r0));
       std::vector<int32_t> estart(nv + 1, 0);
       for (int j = 0; j < nv; ++j) estart[j + 1] = estart[j] + esz[j];
-      for (int64_t c = 0; c < nc; ++c) {
+      int64_t nc = 0, cfg0 = 0;
+      std::vector<int32_t> les;
+      if (implicit) {
+        if (nv > 2)
+          return bail(fail(PGBP_ERR_UNSUPPORTED, "implicit enum rows need unary or pairwise factors"));
+        nc = nv == 1 ? esz[0] : (int64_t)esz[0] * esz[1];
+        cfg0 = implicit_cfg;
+        implicit_cfg += nc;
+        les.resize((size_t)(nc * nv));
+        for (int64_t c = 0; c < nc; ++c) {
+          if (nv == 1) {
+            les[(size_t)c] = (int32_t)c;
+          } else {
+            les[(size_t)(2 * c)] = (int32_t)(c / esz[1]);
+            les[(size_t)(2 * c + 1)] = (int32_t)(esz[0] + c % esz[1]);
+          }
+        }
+      }
+      const int64_t r0 = implicit ? 0 : row_begin[k], r1 = implicit ? 0 : row_begin[k + 1];
+      if (!implicit && (r1 - r0) % nv != 0)
+        return bail(fail(PGBP_ERR_UNSUPPORTED, "enum factor rows not a multiple of its arity"));
+      if (!implicit) {
+        nc = (r1 - r0) / nv;
+        cfg0 = nc > 0 ? ci[r0] : 0;
+        les.resize((size_t)(r1 - r0));
+      }
+      // rows of config c are (var 0 .. var nv-1) with the state's edge state inside var i's edge
+      for (int64_t c = 0; !implicit && c < nc; ++c) {
         for (int i = 0; i < nv; ++i) {
           const int64_t r = r0 + c * nv + i;
           const int64_t le = (e0 + cf[r]) - fb;
@@ -418,6 +451,14 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
           les[(size_t)(c * nv + i)] = (int32_t)le;
         }
       }
+      // first potential of the factor's table: its own configs', or the shared table's
+      int64_t pot_first = pot0 + cfg0;
+      if (alias) {
+        if (alias[k] < 0 || alias[k] + nc > npot_enum)
+          return bail(fail(PGBP_ERR_INVALID_WIRING, "potential offset of enum factor %lld out of range",
+                           (long long)k));
+        pot_first = pot0 + alias[k];
+      }
       bool dense = nv == 2 && nc == (int64_t)esz[0] * esz[1] && esz[0] <= 64 && esz[1] <= 64;
       for (int64_t c = 0; dense && c < nc; ++c) {
         if (les[(size_t)(2 * c)] != c / esz[1] || les[(size_t)(2 * c + 1)] != esz[0] + c % esz[1])
@@ -427,7 +468,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         auto& bk = buckets[{esz[0], esz[1]}];
         const int4 r0 = edge_rec(fb);
         bk.first.push_back(make_int4(r0.x, r0.y, r0.z, vs[fb + esz[0]]));
-        bk.second.push_back((int32_t)(pot0 + cfg0));
+        bk.second.push_back((int32_t)pot_first);
       } else {
         g_es.push_back((int32_t)fb);
         g_nes.push_back((int32_t)(fe - fb));
@@ -443,11 +484,14 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         g_les.insert(g_les.end(), les.begin(), les.end());
         g_ncfg.push_back((int32_t)nc);
         g_nv.push_back(nv);
-        g_cfg.push_back((int32_t)(pot0 + cfg0));
+        g_cfg.push_back((int32_t)pot_first);
       }
     }
     if (max_es > 512)
       return bail(fail(PGBP_ERR_UNSUPPORTED, "an EnumFactor has %d edge states (max 512)", max_es));
+    if (implicit && implicit_cfg != ncfg)
+      return bail(fail(PGBP_ERR_INVALID_WIRING, "implicit enum rows give %lld configs, num_val_configs is %lld",
+                       (long long)implicit_cfg, (long long)ncfg));
     p.num_enum_factors = (int64_t)facs.size();
     for (auto& kv : buckets) {
       pgbp::PairwiseBucket q;

@@ -81,7 +81,10 @@ class Plan:
       d.evidence_to_vars, _ = i32("evidence_to_vars")
       d.num_variables = int(wiring.get("num_variables",
                                        int(np.max(wiring["evidence_to_vars"], initial=-1)) + 1))
-    d.flags = int(flags)
+    d.flags = int(flags) | (native.FLAG_ENUM_IMPLICIT_ROWS if wiring.get("enum.implicit_rows")
+                            else 0)
+    # shared potential tables (optional): first potential of every Enum factor's table
+    d.enum_factor_potential_offsets, d.enum_num_factors = i32("enum.factor_potential_offsets")
     handle = ctypes.c_void_p()
     with torch.cuda.device(self.device):
       native.check(self.lib.pgbp_plan_create(ctypes.byref(d), self.device, ctypes.byref(handle)),

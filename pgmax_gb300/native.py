@@ -97,6 +97,8 @@ class WiringDesc(ctypes.Structure):
       ("pool_indicators_edge_states", _p32),
       ("num_variables", _i64), ("evidence_to_vars", _p32),
       ("flags", _i64),
+      ("enum_num_factors", _i64),
+      ("enum_factor_potential_offsets", ctypes.POINTER(ctypes.c_int32)),
   ]
 
 
@@ -111,6 +113,7 @@ FLAG_NO_SMALL_GRAPH = 1
 FLAG_PATH_SMALL = 2
 FLAG_PATH_CLUSTER = 4
 FLAG_PATH_MULTI = 8
+FLAG_ENUM_IMPLICIT_ROWS = 16
 
 
 class Profile(ctypes.Structure):

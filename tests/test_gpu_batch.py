@@ -1,0 +1,136 @@
+"""Multi-graph batches, shared potential tables and implicit config rows on the GPU.
+
+Every graph of a union must get the messages of its own oracle run: bit for bit at temperature 0,
+within 1e-5 above it (CUDA's expf / logf against glibc's). Shared tables are checked against the
+oracle on the same graph with the tables copied to every factor; implicit config rows against the
+same plan with explicit rows (bit for bit).
+"""
+
+import numpy as np
+import pytest
+
+import fixtures
+from oracle import oracle
+from pgmax_gb300 import batch
+
+pytestmark = pytest.mark.gpu
+
+ATOL = 1e-5
+# Graphs with OR / AND factors on perturbed evidence at T > 0: logminusexp_with_temp subtracts
+# nearly equal log-sums and amplifies the ulp differences of CUDA's and glibc's expf / log1pf
+# (the same bound as the engine tests use for them).
+ATOL_LOGICAL = 1e-4
+MIX = ["case_mixed_T1", "case_ising12_T1", "case_potts_K4", "case_deconv_T1", "case_rbm_s0"]
+PATHS = {"auto": 0, "multi": 1}   # native.FLAG_NO_SMALL_GRAPH = 1
+
+
+def _torch():
+  import torch  # pylint: disable=g-import-not-at-top
+  return torch
+
+
+def _load(name):
+  return fixtures.load(f"{fixtures.FIXTURES}/{name}.npz")
+
+
+def _wiring(d):
+  w = dict(d["wiring"])
+  w["num_variables"] = int(np.max(w["evidence_to_vars"], initial=-1)) + 1
+  return w
+
+
+def _has_logical(w):
+  mr = np.asarray(w["msgs_ranges"]).reshape(4, 2)
+  return bool(np.any(mr[1:3, 1] > mr[1:3, 0]))
+
+
+def _check(got, want, temperature, logical=False):
+  if temperature == 0.0:
+    np.testing.assert_array_equal(got, want)
+  else:
+    np.testing.assert_allclose(got, want, atol=ATOL_LOGICAL if logical else ATOL, rtol=0)
+
+
+@pytest.mark.parametrize("path", list(PATHS))
+@pytest.mark.parametrize("temperature", [0.0, 1.0])
+def test_union_of_fixture_graphs_matches_each_graph_alone(path, temperature):
+  ds = [_load(n) for n in MIX]
+  gb = batch.GraphBatch([_wiring(d) for d in ds], flags=PATHS[path])
+  lay = gb.layout
+  B = 2
+  rng = np.random.default_rng(5)
+  lp = gb.concat([d["log_potentials"].astype(np.float32) for d in ds])
+  evs = [np.asarray(d["evidence"], np.float32)[None] + rng.gumbel(size=(B,) + d["evidence"].shape)
+         .astype(np.float32) for d in ds]
+  ev = gb.concat(evs)
+  m = np.zeros(lay.perm.shape[0], np.float32)
+  out, _ = gb.run(lp, ev, m, 12, 0.5, temperature)
+  out = lay.union_to_graph_major(out.cpu().numpy())
+  for b in range(B):
+    parts = lay.split(out[b], "msgs")
+    for d, w, e, got in zip(ds, [_wiring(d) for d in ds], evs, parts):
+      want, _ = oracle.run(oracle.Wiring(w), d["log_potentials"], e[b],
+                           np.zeros(d["ftov_msgs_in"].shape, np.float32), 12, 0.5, temperature)
+      _check(got, want, temperature, _has_logical(w))
+
+
+@pytest.mark.parametrize("L,K", [(6, 2), (5, 3), (4, 8), (3, 64)])
+@pytest.mark.parametrize("temperature", [0.0, 1.0])
+def test_shared_tables_and_implicit_rows(L, K, temperature):
+  torch = _torch()
+  from pgmax_gb300 import engine  # pylint: disable=g-import-not-at-top
+  rng = np.random.default_rng(L * 100 + K)
+  table = rng.normal(0.0, 0.5, size=K * K).astype(np.float32)
+  ev = rng.normal(size=(3, L * L * K)).astype(np.float32)
+  m = np.zeros(2 * K * (2 * L * (L - 1)), np.float32)
+  w_plain = batch.grid_wiring(L, K)
+  n_fac = w_plain["num_factors"]
+  want = oracle.run_batch(oracle.Wiring(w_plain), np.tile(table, n_fac), ev, m, 10, 0.5,
+                          temperature)[0]
+  outs = []
+  for implicit in (False, True):
+    w = batch.grid_wiring(L, K, shared_table=True, implicit_rows=implicit)
+    plan = engine.Plan(w)
+    out, _ = plan.run(table, ev, m, 10, 0.5, temperature)
+    outs.append(out)
+    _check(out.cpu().numpy(), want, temperature)
+  assert torch.equal(outs[0], outs[1])
+
+
+def test_union_of_shared_grids_and_deconvolution_graphs():
+  d = _load("case_deconv_T1")
+  wd = _wiring(d)
+  specs = [(6, 2), (5, 4), (4, 8), (5, 3)]
+  ws = []
+  for i, (L, K) in enumerate(specs):
+    ws.append(batch.grid_wiring(L, K, shared_table=True, implicit_rows=True))
+    if i % 2 == 0:
+      ws.append(wd)
+  gb = batch.GraphBatch(ws)
+  rng = np.random.default_rng(9)
+  tables, evs, wants = [], [], []
+  for w in ws:
+    if w is wd:
+      tables.append(np.zeros(0, np.float32))
+      evs.append(np.asarray(d["evidence"], np.float32))
+    else:
+      K = int(np.sqrt(w["potentials_ranges"][0, 1]))
+      tables.append(rng.normal(0.0, 0.5, size=K * K).astype(np.float32))
+      evs.append(rng.normal(size=w["num_var_states"]).astype(np.float32))
+  for w, t, e in zip(ws, tables, evs):
+    if w is wd:
+      want = oracle.run(oracle.Wiring(wd), d["log_potentials"], e,
+                        np.zeros(d["ftov_msgs_in"].shape, np.float32), 15, 0.5, 1.0)[0]
+    else:
+      L = int(round(np.sqrt(w["num_variables"])))
+      K = int(np.sqrt(w["potentials_ranges"][0, 1]))
+      wp = batch.grid_wiring(L, K)
+      want = oracle.run(oracle.Wiring(wp), np.tile(t, wp["num_factors"]), e,
+                        np.zeros(wp["var_states_for_edge_states"].shape, np.float32), 15, 0.5,
+                        1.0)[0]
+    wants.append(want)
+  out, _ = gb.run(gb.concat(tables), gb.concat(evs),
+                  np.zeros(gb.layout.perm.shape[0], np.float32), 15, 0.5, 1.0)
+  parts = gb.layout.split(gb.layout.union_to_graph_major(out.cpu().numpy()), "msgs")
+  for w, got, want in zip(ws, parts, wants):
+    np.testing.assert_allclose(got, want, atol=ATOL_LOGICAL if _has_logical(w) else ATOL, rtol=0)
