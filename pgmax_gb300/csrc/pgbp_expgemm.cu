@@ -1,0 +1,471 @@
+// Shared-table exp-domain update of dense K x K pairwise EnumFactors on the tensor cores
+// (K = 16, 32, 64; temperature > 0; potentials shared by the batch).
+//
+// For a factor over variables 1 and 2 whose table psi is shared by a group of factors, the
+// reference's messages (pgmax/factor/enum.py:451-475 at temperature T > 0)
+//   f1[i] = T log sum_j exp((v1[i] + v2[j] + psi_ij - M1_i) / T) + M1_i - v1[i]
+// are, in exact arithmetic, T log sum_j exp((v2[j] + psi_ij) / T) = T log (E u)_i + m2 + r_i with
+//   r_i = max_j psi_ij,  E_ij = exp((psi_ij - r_i) / T)      per table, once per run
+//   m2 = max_j v2[j],    u_j = exp((v2[j] - m2) / T)         per factor and instance
+// and f2 likewise with E'_ji = exp((psi_ij - c_j) / T), c_j = max_i psi_ij, w_i from v1. A factor
+// then costs 2K exponentials instead of 2K^2, and the K^2 work becomes two GEMMs per tile of 64
+// (factor, instance) columns, F1 = E U and F2 = E' W (K x K by K x 64), on the tensor cores:
+// mma.sync m16n8k8 TF32 with each operand split into a tf32 high part and the tf32 rounding of the
+// remainder, three products per pair (lo*hi + hi*lo + hi*hi, fp32 accumulation), about 2^-21
+// relative; u, w and the logarithm use the fast __expf / __logf (a few ulp): float32 accuracy,
+// not bit-equal to the direct path. A sum below 1e-30 (a table row
+// spanning more than about 69 T) is recomputed directly from the messages. The epilogue (damping,
+// normalisation, clipping at MSG_NEG_INF, residual; pgmax/infer/bp.py:127-136) is the one of the
+// dense pairwise kernel.
+//
+// Work split: factors of a bucket are sorted by table (plan time); a column is (factor, instance)
+// with the instance innermost, and a tile is 64 consecutive columns of one group. CTAs are
+// persistent over a contiguous range of tiles, reloading the table only when the group changes.
+// Four threads own a column (K / 4 states of each edge each), so a thread issues all its message
+// and variable-sum loads before it uses any, and keeps the old messages in registers until the
+// epilogue. The residual is folded per CTA in shared memory and written once per instance.
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "pgbp_internal.h"
+
+namespace pgbp {
+namespace {
+
+constexpr float kMsgNegInf = -1e32f;  // MSG_NEG_INF, pgmax/utils/__init__.py
+constexpr int kCols = 64;             // (factor, instance) columns per tile
+constexpr int kThreads = 256;
+constexpr int kLdc = kCols + 8;       // row stride of the K x 64 operand / result tiles
+
+__device__ __forceinline__ float maxn(float a, float b) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+// x / t; a power-of-two t multiplies by its exact reciprocal (the same correctly rounded value).
+__device__ __forceinline__ float div_t(float x, float t) {
+  const unsigned u = __float_as_uint(t);
+  const unsigned e = (u >> 23) & 0xffu;
+  if ((u & 0x807fffffu) == 0u && e >= 2u && e <= 252u) return x * __uint_as_float((254u - e) << 23);
+  return x / t;
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - __uint_as_float(hi));
+}
+
+// D = A B + D, A 16x8 (row), B 8x8 (col), tf32 in, fp32 accumulate.
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+
+// Run-time tables of one group: E [K][K] (row i, column j), E' [K][K] (row j, column i), row
+// maxima r [K], column maxima c [K]. One CTA per group.
+template <int K>
+__global__ void __launch_bounds__(kThreads) expgemm_tables_kernel(
+    const int32_t* __restrict__ grp_table, const float* __restrict__ lpc, float t,
+    float* __restrict__ tables) {
+  const int g = blockIdx.x;
+  const float* psi = lpc + grp_table[g];
+  float* out = tables + (int64_t)g * expgemm_table_floats(K);
+  float *e = out, *f = out + K * K, *rmax = out + 2 * K * K, *cmax = rmax + K;
+  __shared__ float rs[K], cs[K];
+  for (int i = threadIdx.x; i < K; i += blockDim.x) {
+    float m = -INFINITY, n = -INFINITY;
+    for (int j = 0; j < K; ++j) {
+      m = maxn(m, psi[i * K + j]);
+      n = maxn(n, psi[j * K + i]);
+    }
+    rs[i] = m;
+    cs[i] = n;
+    rmax[i] = m;
+    cmax[i] = n;
+  }
+  __syncthreads();
+  for (int x = threadIdx.x; x < K * K; x += blockDim.x) {
+    const int i = x / K, j = x % K;
+    e[x] = expf(div_t(psi[x] - rs[i], t));
+    f[j * K + i] = expf(div_t(psi[x] - cs[j], t));
+  }
+}
+
+constexpr int kMaxB = 512;  // instances whose residual a CTA folds in shared memory
+
+struct ExpArgs {
+  const int4* __restrict__ rec;           // (first edge state, first slot, var state 1, 2)
+  const int32_t* __restrict__ grp_first;
+  const int32_t* __restrict__ grp_count;
+  const int32_t* __restrict__ grp_table;
+  int n_groups;
+  int64_t n_tiles, tiles_per_cta;
+  int64_t B;
+  const float* __restrict__ cur;
+  float* __restrict__ nxt;
+  const float* __restrict__ vsum;
+  const float* __restrict__ lpc;          // clipped shared potentials
+  const float* __restrict__ tables;
+  float d, omd, t;
+  unsigned* __restrict__ dacc;            // residual of this iteration, [B] float bits
+};
+
+template <int K>
+struct Smem {
+  static constexpr int kLde = K + 4;                  // row stride of E and E'
+  static constexpr int kFloats = 2 * K * kLde + 2 * K // E, E', r, c
+                                 + 4 * K * kLdc;      // U, W as tf32 high / low parts (U high,
+                                                      // W high then hold F1, F2)
+  static constexpr size_t kBytes = sizeof(float) * kFloats + sizeof(unsigned) * kMaxB;
+};
+
+// f for state s of one edge computed directly (the reference's formula) when the exp-domain sum
+// underflows: the other variable's vtof plus row (first edge) or column s of the table.
+template <int K>
+__device__ float direct_message(const ExpArgs& a, int4 q, int64_t b, int s, bool first_edge,
+                                int64_t table) {
+  const int64_t B = a.B;
+  float mx = -INFINITY;
+  for (int j = 0; j < K; ++j) {
+    const float v = first_edge ? a.vsum[(q.w + j) * B + b] - a.cur[(q.y + K + j) * B + b]
+                               : a.vsum[(q.z + j) * B + b] - a.cur[(q.y + j) * B + b];
+    const float p = first_edge ? a.lpc[table + s * K + j] : a.lpc[table + j * K + s];
+    mx = maxn(mx, v + p);
+  }
+  float se = 0.0f;
+  for (int j = 0; j < K; ++j) {
+    const float v = first_edge ? a.vsum[(q.w + j) * B + b] - a.cur[(q.y + K + j) * B + b]
+                               : a.vsum[(q.z + j) * B + b] - a.cur[(q.y + j) * B + b];
+    const float p = first_edge ? a.lpc[table + s * K + j] : a.lpc[table + j * K + s];
+    se += expf(div_t((v + p) - mx, a.t));
+  }
+  return a.t * logf(se) + mx;
+}
+
+// acc = T X: T (K x K, fp32 in shared memory, split per fragment) times X (K x 64, already split
+// into tf32 high and low parts).
+template <int K>
+__device__ __forceinline__ void tile_gemm(const float* T, const uint32_t* Xh, const uint32_t* Xl,
+                                          int warp, int lane, float (&acc)[K / 16][4]) {
+  constexpr int MB = K / 16;  // 16-row blocks; 8 warps x MB tiles = MB x 8 tiles of 16 x 8
+  constexpr int kLde = Smem<K>::kLde;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int r0 = ((warp * MB) / 8) * 16 + gid;
+#pragma unroll
+  for (int i = 0; i < MB; ++i)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[i][e] = 0.0f;
+#pragma unroll
+  for (int k0 = 0; k0 < K; k0 += 8) {
+    uint32_t ah[4], al[4];
+    split_tf32(T[r0 * kLde + k0 + tig], ah[0], al[0]);
+    split_tf32(T[(r0 + 8) * kLde + k0 + tig], ah[1], al[1]);
+    split_tf32(T[r0 * kLde + k0 + tig + 4], ah[2], al[2]);
+    split_tf32(T[(r0 + 8) * kLde + k0 + tig + 4], ah[3], al[3]);
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int nb = (warp * MB + i) % 8;
+      const uint32_t bh[2] = {Xh[(k0 + tig) * kLdc + nb * 8 + gid],
+                              Xh[(k0 + tig + 4) * kLdc + nb * 8 + gid]};
+      const uint32_t bl[2] = {Xl[(k0 + tig) * kLdc + nb * 8 + gid],
+                              Xl[(k0 + tig + 4) * kLdc + nb * 8 + gid]};
+      mma_tf32(acc[i], al, bh);
+      mma_tf32(acc[i], ah, bl);
+      mma_tf32(acc[i], ah, bh);
+    }
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void store_acc(float* X, int warp, int lane,
+                                          const float (&acc)[K / 16][4]) {
+  constexpr int MB = K / 16;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int r0 = ((warp * MB) / 8) * 16 + gid;
+#pragma unroll
+  for (int i = 0; i < MB; ++i) {
+    const int c0 = ((warp * MB + i) % 8) * 8 + 2 * tig;
+    X[r0 * kLdc + c0] = acc[i][0];
+    X[r0 * kLdc + c0 + 1] = acc[i][1];
+    X[(r0 + 8) * kLdc + c0] = acc[i][2];
+    X[(r0 + 8) * kLdc + c0 + 1] = acc[i][3];
+  }
+}
+
+__device__ __forceinline__ float max4(float x) {  // maximum over the 4 threads of a column
+  x = maxn(x, __shfl_xor_sync(0xffffffffu, x, 1));
+  return maxn(x, __shfl_xor_sync(0xffffffffu, x, 2));
+}
+
+// B1: one instance (slot s of the batch at s), which saves the 64-bit index arithmetic.
+template <int K, bool B1>
+__global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a) {
+  extern __shared__ float sm[];
+  constexpr int kLde = Smem<K>::kLde;
+  constexpr int SPT = K / 4;  // states of each edge per thread: s = 4 i + part
+  float* s_e = sm;                    // E  [K][kLde]
+  float* s_f = s_e + K * kLde;        // E' [K][kLde]
+  float* s_r = s_f + K * kLde;        // row maxima, then column maxima
+  float* s_c = s_r + K;
+  uint32_t* s_uh = reinterpret_cast<uint32_t*>(s_c + K);  // U high part, then F1 [K][kLdc]
+  uint32_t* s_ul = s_uh + K * kLdc;                         // U low part
+  uint32_t* s_wh = s_ul + K * kLdc;                         // W high part, then F2
+  uint32_t* s_wl = s_wh + K * kLdc;
+  float* s_f1 = reinterpret_cast<float*>(s_uh);
+  float* s_f2 = reinterpret_cast<float*>(s_wh);
+  unsigned* s_res = s_wl + K * kLdc;  // residual per instance
+  __shared__ int s_group;
+  __shared__ int64_t s_tile0;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = threadIdx.x >> 2, part = threadIdx.x & 3;  // column of the tile, quarter of it
+  const int64_t B = B1 ? 1 : a.B;
+  const bool fold = B <= kMaxB;
+  if (fold)
+    for (int64_t x = threadIdx.x; x < B; x += kThreads) s_res[x] = 0u;
+  const int64_t t_begin = (int64_t)blockIdx.x * a.tiles_per_cta;
+  const int64_t t_end = t_begin + a.tiles_per_cta < a.n_tiles ? t_begin + a.tiles_per_cta : a.n_tiles;
+  int loaded = -1;
+  if (threadIdx.x == 0) {
+    s_group = 0;
+    s_tile0 = 0;
+  }
+  __syncthreads();
+  for (int64_t tile = t_begin; tile < t_end; ++tile) {
+    // the group of this tile (the tiles of a CTA are visited in order)
+    if (threadIdx.x == 0) {
+      int g = s_group;
+      int64_t t0 = s_tile0;
+      while (g < a.n_groups) {
+        const int64_t nt = ((int64_t)a.grp_count[g] * B + kCols - 1) / kCols;
+        if (tile < t0 + nt) break;
+        t0 += nt;
+        ++g;
+      }
+      s_group = g;
+      s_tile0 = t0;
+    }
+    __syncthreads();
+    const int g = s_group;
+    const int64_t first = a.grp_first[g];
+    const int64_t cols = (int64_t)a.grp_count[g] * B;
+    const int64_t c0 = (tile - s_tile0) * kCols;
+    const int ncols = (int)(cols - c0 < kCols ? cols - c0 : kCols);
+    const int64_t table = a.grp_table[g];
+    if (g != loaded) {
+      const float* src = a.tables + (int64_t)g * expgemm_table_floats(K);
+      for (int x = threadIdx.x; x < K * K; x += kThreads) {
+        s_e[(x / K) * kLde + x % K] = src[x];
+        s_f[(x / K) * kLde + x % K] = src[K * K + x];
+      }
+      for (int x = threadIdx.x; x < 2 * K; x += kThreads) s_r[x] = src[2 * K * K + x];
+      loaded = g;
+    }
+    // ---- load: every message and variable sum of this thread's states first, then the maxima
+    const bool active = c < ncols;
+    int64_t b = 0;
+    int4 q = make_int4(0, 0, 0, 0);
+    float o1[SPT], o2[SPT], v1[SPT], v2[SPT];
+    float m1 = -INFINITY, m2 = -INFINITY;
+    if (active) {
+      const int64_t col = c0 + c;
+      b = B1 ? 0 : col % B;
+      q = a.rec[first + (B1 ? col : col / B)];
+#pragma unroll
+      for (int i = 0; i < SPT; ++i) {
+        const int s = 4 * i + part;
+        if (B1) {
+          o1[i] = a.cur[q.y + s];
+          o2[i] = a.cur[q.y + K + s];
+          v1[i] = a.vsum[q.z + s];
+          v2[i] = a.vsum[q.w + s];
+        } else {
+          o1[i] = a.cur[(q.y + s) * B + b];
+          o2[i] = a.cur[(q.y + K + s) * B + b];
+          v1[i] = a.vsum[(q.z + s) * B + b];
+          v2[i] = a.vsum[(q.w + s) * B + b];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < SPT; ++i) {
+        v1[i] -= o1[i];
+        v2[i] -= o2[i];
+        m1 = maxn(m1, v1[i]);
+        m2 = maxn(m2, v2[i]);
+      }
+    }
+    m1 = max4(m1);
+    m2 = max4(m2);
+    // u, w in [0, 1]: the fast exponential (about 2 ulp) keeps the sums at float32 accuracy
+#pragma unroll
+    for (int i = 0; i < SPT; ++i) {
+      const int s = 4 * i + part;
+      uint32_t h, l;
+      split_tf32(active ? __expf(div_t(v1[i] - m1, a.t)) : 0.0f, h, l);
+      s_wh[s * kLdc + c] = h;
+      s_wl[s * kLdc + c] = l;
+      split_tf32(active ? __expf(div_t(v2[i] - m2, a.t)) : 0.0f, h, l);
+      s_uh[s * kLdc + c] = h;
+      s_ul[s * kLdc + c] = l;
+    }
+    __syncthreads();
+    // ---- F1 = E U, F2 = E' W on the tensor cores
+    {
+      float acc[K / 16][4];
+      tile_gemm<K>(s_e, s_uh, s_ul, warp, lane, acc);
+      float acc2[K / 16][4];
+      tile_gemm<K>(s_f, s_wh, s_wl, warp, lane, acc2);
+      __syncthreads();
+      store_acc<K>(s_f1, warp, lane, acc);
+      store_acc<K>(s_f2, warp, lane, acc2);
+    }
+    __syncthreads();
+    // ---- epilogue: messages, damping, normalisation, clipping, residual
+    float x1 = -INFINITY, x2 = -INFINITY;
+    if (active) {
+#pragma unroll
+      for (int i = 0; i < SPT; ++i) {
+        const int s = 4 * i + part;
+        const float e1 = s_f1[s * kLdc + c], e2 = s_f2[s * kLdc + c];
+        // the sums are >= 1e-30 here: the fast logarithm's absolute error is about 4e-7
+        const float f1 = e1 >= 1e-30f ? (a.t * __logf(e1) + m2) + s_r[s]
+                                      : direct_message<K>(a, q, b, s, true, table);
+        const float f2 = e2 >= 1e-30f ? (a.t * __logf(e2) + m1) + s_c[s]
+                                      : direct_message<K>(a, q, b, s, false, table);
+        v1[i] = a.d * o1[i] + a.omd * f1;  // v1 / v2 now hold the damped messages
+        v2[i] = a.d * o2[i] + a.omd * f2;
+        x1 = maxn(x1, v1[i]);
+        x2 = maxn(x2, v2[i]);
+      }
+    }
+    x1 = max4(x1);
+    x2 = max4(x2);
+    float dmax = 0.0f;
+    if (active) {
+#pragma unroll
+      for (int i = 0; i < SPT; ++i) {
+        const int s = 4 * i + part;
+        const float y1 = maxn(v1[i] - x1, kMsgNegInf);
+        const float y2 = maxn(v2[i] - x2, kMsgNegInf);
+        if (B1) {
+          a.nxt[q.y + s] = y1;
+          a.nxt[q.y + K + s] = y2;
+        } else {
+          a.nxt[(q.y + s) * B + b] = y1;
+          a.nxt[(q.y + K + s) * B + b] = y2;
+        }
+        dmax = maxn(dmax, fabsf(y1 - o1[i]));
+        dmax = maxn(dmax, fabsf(y2 - o2[i]));
+      }
+    }
+    dmax = max4(dmax);
+    if (active && part == 0 && a.dacc != nullptr) {
+      if (fold) atomicMax(s_res + b, __float_as_uint(dmax));
+      else atomicMax(a.dacc + b, __float_as_uint(dmax));
+    }
+    __syncthreads();
+  }
+  if (fold && a.dacc != nullptr) {
+    for (int64_t x = threadIdx.x; x < B; x += kThreads)
+      if (s_res[x] != 0u) atomicMax(a.dacc + x, s_res[x]);
+  }
+}
+
+template <int K, bool B1>
+cudaError_t set_smem_attr() {
+  static cudaError_t once = cudaFuncSetAttribute(
+      expgemm_pairwise_kernel<K, B1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      (int)Smem<K>::kBytes);
+  return once;
+}
+
+template <int K, bool B1>
+cudaError_t launch_b(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const ExpArgs& base) {
+  cudaError_t e = set_smem_attr<K, B1>();
+  if (e != cudaSuccess) return e;
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, expgemm_pairwise_kernel<K, B1>, kThreads,
+                                                      Smem<K>::kBytes) != cudaSuccess)
+      n = 1;
+    per_sm = std::max(n, 1);
+  }
+  ExpArgs a = base;
+  int64_t tiles = 0;
+  for (int64_t c : q.grp_count_host) tiles += (c * a.B + kCols - 1) / kCols;
+  if (tiles == 0) return cudaSuccess;
+  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)p.sm_count * per_sm));
+  a.n_tiles = tiles;
+  a.tiles_per_cta = (tiles + ctas - 1) / ctas;
+  const int64_t grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
+  expgemm_pairwise_kernel<K, B1><<<(unsigned)grid, kThreads, Smem<K>::kBytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const ExpArgs& a) {
+  return a.B == 1 ? launch_b<K, true>(p, q, s, a) : launch_b<K, false>(p, q, s, a);
+}
+
+}  // namespace
+
+bool expgemm_eligible(const PairwiseBucket& q) { return q.n_groups > 0; }
+
+cudaError_t expgemm_prepare(const Plan& p, const PairwiseBucket& q, cudaStream_t s,
+                            const float* lpc, float t, float* tables) {
+  (void)p;
+  if (q.n_groups == 0) return cudaSuccess;
+  ProfileScope ps(kProfPairwise, s);
+  switch (q.n1) {
+    case 16: expgemm_tables_kernel<16><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables); break;
+    case 32: expgemm_tables_kernel<32><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables); break;
+    case 64: expgemm_tables_kernel<64><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t s, int64_t B,
+                            const float* cur, float* nxt, const float* vsum, const float* lpc,
+                            const float* tables, float d, float omd, float t, unsigned* dacc) {
+  ProfileScope ps(kProfPairwise, s);
+  ExpArgs a{};
+  a.rec = q.rec;
+  a.grp_first = q.grp_first;
+  a.grp_count = q.grp_count;
+  a.grp_table = q.grp_table;
+  a.n_groups = q.n_groups;
+  a.B = B;
+  a.cur = cur;
+  a.nxt = nxt;
+  a.vsum = vsum;
+  a.lpc = lpc;
+  a.tables = tables;
+  a.d = d;
+  a.omd = omd;
+  a.t = t;
+  a.dacc = dacc;
+  switch (q.n1) {
+    case 16: return launch<16>(p, q, s, a);
+    case 32: return launch<32>(p, q, s, a);
+    case 64: return launch<64>(p, q, s, a);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace pgbp

@@ -27,7 +27,24 @@ struct PairwiseBucket {
   int64_t count = 0;
   int4* rec = nullptr;
   int32_t* cfg_begin = nullptr;
+  // Shared-table exp-domain schedule (plans with shared tables, n1 == n2 in {16, 32, 64}): the
+  // factors are sorted by table and group g is factors grp_first[g] .. + grp_count[g] - 1, all
+  // reading the table at potential grp_table[g]. Run-time tables (exp of the potentials, split
+  // for the tensor cores) take gemm_floats floats of the run workspace.
+  int n_groups = 0;
+  int32_t* grp_first = nullptr;
+  int32_t* grp_count = nullptr;
+  int32_t* grp_table = nullptr;
+  std::vector<int64_t> grp_count_host;
+  int64_t gemm_floats = 0;
 };
+
+// Floats of run-time tables one group of a shared-table bucket with K x K tables needs:
+// E and E' (2 K^2) plus the row and column maxima (2 K).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int64_t expgemm_table_floats(int K) { return 2LL * K * K + 2LL * K; }
 
 // Every other EnumFactor: per factor its edge-state range, edges and config rows. Rows of config
 // k of factor f are row_begin[f] + k * n_vars[f] + i (i = variable), holding the edge state local to
@@ -156,6 +173,17 @@ cudaError_t decode(const Plan& p, cudaStream_t s, int64_t B, const float* belief
                    int32_t* map);
 cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* beliefs, int64_t stride,
                       float* out);
+
+// Shared-table exp-domain pairwise update (pgbp_expgemm.cu), multi-kernel path, T > 0, potentials
+// shared by the batch. expgemm_prepare fills the bucket's run-time tables from the clipped
+// potentials once per run; expgemm_iterate runs one iteration of the bucket (fused damping,
+// normalisation, clipping, residual), the counterpart of the dense pairwise kernel.
+bool expgemm_eligible(const PairwiseBucket& q);
+cudaError_t expgemm_prepare(const Plan& p, const PairwiseBucket& q, cudaStream_t s,
+                            const float* lpc, float t, float* tables);
+cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t s, int64_t B,
+                            const float* cur, float* nxt, const float* vsum, const float* lpc,
+                            const float* tables, float d, float omd, float t, unsigned* dacc);
 
 // Adjoint (pgbp_adjoint.cu). An empty string when the plan can be differentiated, else why not.
 const char* adjoint_unsupported(const Plan& p);

@@ -1398,7 +1398,7 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
 template <bool T0>
 void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool low_t, int64_t iters,
              float* msgs0, float* msgs1, const float* ev, int64_t evs, int64_t evb,
-             unsigned* dacc) {
+             unsigned* dacc, const float* gemm_tables) {
   for (int64_t it = 0; it < iters; ++it) {
     float* cur = (it & 1) ? msgs1 : msgs0;
     float* nxt = (it & 1) ? msgs0 : msgs1;
@@ -1406,7 +1406,15 @@ void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool lo
     c.nxt = nxt;
     unsigned* d = dacc + it * B;
     launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum));
+    const float* tables = gemm_tables;
     for (const PairwiseBucket& q : p.pairwise) {
+      // shared K x K tables at temperature > 0: the exp-domain tensor-core kernel
+      if (!T0 && gemm_tables != nullptr && expgemm_eligible(q)) {
+        expgemm_iterate(p, q, s, B, cur, nxt, c.vsum, c.lp, tables, c.d, c.omd, t, d);
+        tables += q.gemm_floats;
+        continue;
+      }
+      if (gemm_tables != nullptr) tables += q.gemm_floats;
       // 4 instances per thread only when that still leaves >= 16 warps per SM; below that the
       // kernel is latency-bound and one instance per thread keeps 4x more warps in flight
       if (q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0 &&
@@ -1609,6 +1617,12 @@ cudaError_t prepare_small_graph(Plan& p) {
   return cudaSuccess;
 }
 
+int64_t gemm_table_floats(const Plan& p) {
+  int64_t n = 0;
+  for (const PairwiseBucket& q : p.pairwise) n += q.gemm_floats;
+  return n;
+}
+
 size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched,
                        bool lp_batched) {
   const int64_t B = std::max<int64_t>(batch, 1);
@@ -1620,6 +1634,7 @@ size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batc
   if (ev_batched) n += align_up(sizeof(float) * (size_t)(p.num_var_states * B));
   n += align_up(sizeof(float) * (size_t)(p.num_potentials * (lp_batched ? B : 1)));
   n += align_up(sizeof(unsigned) * (size_t)(it * B));
+  n += align_up(sizeof(float) * (size_t)gemm_table_floats(p));
   return n;
 }
 
@@ -1652,6 +1667,7 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   float* evt = ev_b ? (float*)take(sizeof(float) * (size_t)(p.num_var_states * B)) : nullptr;
   float* lpc = (float*)take(sizeof(float) * (size_t)(p.num_potentials * (lp_b ? B : 1)));
   unsigned* dacc = (unsigned*)take(sizeof(unsigned) * (size_t)(iters * B));
+  float* gemm_ws = (float*)take(sizeof(float) * (size_t)gemm_table_floats(p));
   (void)ws_bytes;
 
   // evidence and potentials in the run layout; potentials clipped (bp.py:85-87)
@@ -1698,6 +1714,17 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   const float t = (float)temperature;
   const bool low_t = temperature < kStabilityThre;
   const bool t0 = temperature == 0.0;
+  // run-time tables of the shared-table exp-domain kernel (temperature > 0, potentials shared by
+  // the batch), built once per run from the clipped potentials
+  const float* gemm = nullptr;
+  if (!t0 && !lp_b && gemm_table_floats(p) > 0) {
+    float* tp = gemm_ws;
+    for (const PairwiseBucket& q : p.pairwise) {
+      if (expgemm_eligible(q)) expgemm_prepare(p, q, s, lpc, t, tp);
+      tp += q.gemm_floats;
+    }
+    gemm = gemm_ws;
+  }
   SmallGraph g;
   const bool small_ok = p.small_graph_smem > 0 && B <= 65535;
   const bool cluster_ok = small_ok && p.cluster_size > 0;
@@ -1737,8 +1764,8 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
       else launch_cluster<false>(s, p, g, B, n, t, low_t, m0, m1, vsum, dacc);
       return (n & 1) ? m1 : m0;
     }
-    if (t0) iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc);
-    else iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc);
+    if (t0) iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, nullptr);
+    else iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, gemm);
     return (n & 1) ? m1 : m0;
   };
   int path = kPathMulti;

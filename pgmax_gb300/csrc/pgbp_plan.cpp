@@ -498,6 +498,38 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       q.n1 = kv.first.first;
       q.n2 = kv.first.second;
       q.count = (int64_t)kv.second.first.size();
+      if (alias && q.n1 == q.n2 && (q.n1 == 16 || q.n1 == 32 || q.n1 == 64)) {
+        // group the factors by table (stable: factor order inside a group)
+        auto& recs = kv.second.first;
+        auto& cfg = kv.second.second;
+        std::vector<size_t> order(recs.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](size_t a, size_t b) { return cfg[a] < cfg[b]; });
+        std::vector<int4> r2(recs.size());
+        std::vector<int32_t> c2(cfg.size());
+        for (size_t i = 0; i < order.size(); ++i) {
+          r2[i] = recs[order[i]];
+          c2[i] = cfg[order[i]];
+        }
+        recs.swap(r2);
+        cfg.swap(c2);
+        std::vector<int32_t> gf, gc, gt;
+        for (size_t i = 0; i < cfg.size(); ++i) {
+          if (i == 0 || cfg[i] != cfg[i - 1]) {
+            gf.push_back((int32_t)i);
+            gc.push_back(0);
+            gt.push_back(cfg[i]);
+          }
+          gc.back()++;
+        }
+        q.n_groups = (int)gf.size();
+        q.grp_first = bd.upload(gf);
+        q.grp_count = bd.upload(gc);
+        q.grp_table = bd.upload(gt);
+        q.grp_count_host.assign(gc.begin(), gc.end());
+        q.gemm_floats = (int64_t)q.n_groups * pgbp::expgemm_table_floats(q.n1);
+      }
       q.rec = bd.upload(kv.second.first);
       q.cfg_begin = bd.upload(kv.second.second);
       p.num_enum_pairwise += q.count;

@@ -19,7 +19,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libpgbp.so")
 
-SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu", "pgbp_adjoint.cu"]
+SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu", "pgbp_adjoint.cu",
+           "pgbp_expgemm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every float32 op rounds as the reference's does.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -74,9 +74,13 @@ def test_union_of_fixture_graphs_matches_each_graph_alone(path, temperature):
       _check(got, want, temperature, _has_logical(w))
 
 
-@pytest.mark.parametrize("L,K", [(6, 2), (5, 3), (4, 8), (3, 64)])
-@pytest.mark.parametrize("temperature", [0.0, 1.0])
-def test_shared_tables_and_implicit_rows(L, K, temperature):
+@pytest.mark.parametrize("L,K", [(6, 2), (5, 3), (4, 8), (3, 16), (9, 16), (3, 32), (3, 64),
+                                 (7, 64)])
+@pytest.mark.parametrize("temperature", [0.0, 1.0, 0.7])
+@pytest.mark.parametrize("path", list(PATHS))
+def test_shared_tables_and_implicit_rows(L, K, temperature, path):
+  """On the multi-kernel path at T > 0, K = 16 / 32 / 64 run the exp-domain tensor-core kernel
+  (float32 accuracy, within 1e-5 of the oracle); everything else runs the direct kernels."""
   torch = _torch()
   from pgmax_gb300 import engine  # pylint: disable=g-import-not-at-top
   rng = np.random.default_rng(L * 100 + K)
@@ -90,7 +94,7 @@ def test_shared_tables_and_implicit_rows(L, K, temperature):
   outs = []
   for implicit in (False, True):
     w = batch.grid_wiring(L, K, shared_table=True, implicit_rows=implicit)
-    plan = engine.Plan(w)
+    plan = engine.Plan(w, flags=PATHS[path])
     out, _ = plan.run(table, ev, m, 10, 0.5, temperature)
     outs.append(out)
     _check(out.cpu().numpy(), want, temperature)
@@ -134,3 +138,45 @@ def test_union_of_shared_grids_and_deconvolution_graphs():
   parts = gb.layout.split(gb.layout.union_to_graph_major(out.cpu().numpy()), "msgs")
   for w, got, want in zip(ws, parts, wants):
     np.testing.assert_allclose(got, want, atol=ATOL_LOGICAL if _has_logical(w) else ATOL, rtol=0)
+
+
+def test_exp_domain_kernel_over_many_tables_and_instances():
+  """Groups of different tables in one bucket, columns (factor, instance) crossing factor and
+  group boundaries inside a tile, potentials shared by a batch of 3."""
+  specs = [(5, 64), (3, 64), (6, 64), (4, 32), (7, 16), (4, 64)]
+  ws = [batch.grid_wiring(L, K, shared_table=True, implicit_rows=True) for L, K in specs]
+  gb = batch.GraphBatch(ws, flags=1)
+  rng = np.random.default_rng(3)
+  tables = [rng.normal(0.0, 0.5, size=K * K).astype(np.float32) for _, K in specs]
+  evs = [rng.normal(size=(3, L * L * K)).astype(np.float32) for L, K in specs]
+  out, _ = gb.run(gb.concat(tables), gb.concat(evs), np.zeros(gb.layout.perm.shape[0], np.float32),
+                  20, 0.5, 1.0)
+  got = gb.layout.union_to_graph_major(out.cpu().numpy())
+  for b in range(3):
+    parts = gb.layout.split(got[b], "msgs")
+    for (L, K), t, e, part in zip(specs, tables, evs, parts):
+      wp = batch.grid_wiring(L, K)
+      want = oracle.run(oracle.Wiring(wp), np.tile(t, wp["num_factors"]), e[b],
+                        np.zeros(wp["var_states_for_edge_states"].shape, np.float32), 20, 0.5,
+                        1.0)[0]
+      np.testing.assert_allclose(part, want, atol=ATOL, rtol=0)
+
+
+def test_exp_domain_underflow_falls_back_to_the_direct_formula():
+  """A table whose rows span hundreds (E = exp((psi - rowmax) / T) underflows where the messages
+  concentrate) must still give the reference's messages: those sums are recomputed directly."""
+  L, K = 4, 16
+  rng = np.random.default_rng(11)
+  table = np.where(rng.random(K * K) < 0.5, -300.0, 0.0).astype(np.float32)
+  table[::K + 1] = -300.0   # the diagonal (where the evidence peaks) is far below the row max
+  ev = np.full((L * L, K), -200.0, np.float32)
+  ev[np.arange(L * L), rng.integers(0, K, L * L)] = 0.0
+  w = batch.grid_wiring(L, K, shared_table=True, implicit_rows=True)
+  from pgmax_gb300 import engine  # pylint: disable=g-import-not-at-top
+  plan = engine.Plan(w, flags=1)
+  out, _ = plan.run(table, ev.reshape(-1), np.zeros(2 * K * w["num_factors"], np.float32), 10,
+                    0.5, 1.0)
+  wp = batch.grid_wiring(L, K)
+  want = oracle.run(oracle.Wiring(wp), np.tile(table, wp["num_factors"]), ev.reshape(-1),
+                    np.zeros(2 * K * w["num_factors"], np.float32), 10, 0.5, 1.0)[0]
+  np.testing.assert_allclose(out.cpu().numpy(), want, atol=1e-4, rtol=1e-6)
