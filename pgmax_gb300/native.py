@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libpgbp.so")
 
 SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu", "pgbp_adjoint.cu",
-           "pgbp_expgemm.cu"]
+           "pgbp_expgemm.cu", "pgbp_conv.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every float32 op rounds as the reference's does.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -146,6 +146,16 @@ SIGNATURES = [
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
     ("pgbp_decode", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_marginals", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
+    # include/pgbp_learn.h
+    ("pgbp_conv3x3", ctypes.c_int, [_p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, _p, _p, _p, _p, ctypes.c_int, ctypes.c_int, _p]),
+    ("pgbp_conv3x3_wgrad_workspace", ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    ("pgbp_conv3x3_wgrad", ctypes.c_int, [_p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, _p, _p, _p, _p, _p, ctypes.c_size_t]),
+    ("pgbp_conv3x3_flip", ctypes.c_int, [_p, ctypes.c_int, ctypes.c_int, _p, _p]),
+    ("pgbp_center_mse", ctypes.c_int, [_p, _i64, ctypes.c_int, _p, _p, _p, _p, ctypes.c_float]),
+    ("pgbp_adam", ctypes.c_int, [_p, _i64, _p, _p, _p, _p, _p, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_float, ctypes.c_float, _i64]),
     ("pgbp_profile_enable", ctypes.c_int, [ctypes.c_int]),
     ("pgbp_profile_read", ctypes.c_int, [ctypes.POINTER(Profile)]),
     ("pgbp_last_error", ctypes.c_char_p, []),

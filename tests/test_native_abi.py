@@ -1,7 +1,8 @@
-"""The C ABI library: it builds for sm_103a, loads, and exports every symbol include/pgbp.h
-declares. No kernel is launched here (no GPU needed)."""
+"""The C ABI library: it builds for sm_103a, loads, and exports every symbol the headers in
+include/ declare. No kernel is launched here (no GPU needed)."""
 
 import ctypes
+import glob
 import os
 import re
 
@@ -9,11 +10,11 @@ import pytest
 
 from pgmax_gb300 import native
 
-HEADER = os.path.join(native.ROOT, "include", "pgbp.h")
+HEADERS = sorted(glob.glob(os.path.join(native.ROOT, "include", "*.h")))
 
 
 def declared_functions():
-  text = open(HEADER).read()
+  text = "".join(open(h).read() for h in HEADERS)
   return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(pgbp_\w+)\s*\(", text, re.M)))
 
 
