@@ -168,6 +168,22 @@ int pgbp_run_static_scratch(const pgbp_plan* plan, void* stream, int64_t batch,
                             float* msgs_out, float* deltas,
                             int64_t num_iters, double damping, double temperature);
 
+/* Runs BP until every instance's max message residual is below `tolerance` (the convergence loop
+ * PGMax users write around run_with_diffs, bp.py:63-155, checking its msgs_deltas), or
+ * max_iters iterations. The residual is tested every `check_every` iterations (the stream is
+ * synchronised there, so this call cannot be captured); all instances keep iterating until the
+ * last one converges. Outputs: msgs_out [batch, E_s]; first_below (device, [batch]) the first
+ * iteration (1-based) whose residual was below the tolerance, -1 if none; *iters_run (host) the
+ * iterations run. Workspace: pgbp_workspace_size(plan, batch, check_every). No counterpart in the
+ * reference's API. */
+int pgbp_run_to_tolerance(const pgbp_plan* plan, void* stream, int64_t batch,
+                          const float* log_potentials, int64_t lp_stride,
+                          const float* evidence, int64_t ev_stride,
+                          const float* msgs_in, int64_t msgs_stride, float* msgs_out,
+                          double tolerance, int64_t max_iters, int64_t check_every,
+                          double damping, double temperature, int32_t* first_below,
+                          int64_t* iters_run, void* workspace, size_t workspace_bytes);
+
 /* pgbp_run that also keeps the messages every `checkpoint_every` iterations, for pgbp_run_vjp:
  * checkpoints [ceil(iters / k)][batch][E_s] contiguous (k = min(checkpoint_every, iters), iters =
  * max(num_iters, 1)); checkpoint 0 is msgs_in as given, checkpoint c the messages after c * k

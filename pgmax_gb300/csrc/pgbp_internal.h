@@ -158,12 +158,20 @@ struct ProfileScope {
   }
 };
 
+// pgbp_run_to_tolerance: stop once every instance's residual fell below tol.
+struct ToleranceRun {
+  double tol;
+  int64_t max_iters;
+  int32_t* first_below;  // device [B]
+  int64_t* iters_run;    // host
+};
+
 // Kernel launchers (pgbp_kernels.cu). They return cudaGetLastError() of their launches.
 cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
                    const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
                    float* msgs_out, float* deltas, int64_t iters, double damping, double temperature,
                    void* ws, size_t ws_bytes, int64_t checkpoint_every = 0,
-                   float* checkpoints = nullptr);
+                   float* checkpoints = nullptr, const ToleranceRun* tol_run = nullptr);
 cudaError_t factor_update(const Plan& p, cudaStream_t s, int type, int64_t B, const float* vtof,
                           int64_t vtof_stride, const float* lp, int64_t lp_stride, double temperature,
                           int normalize, float* out, int64_t out_stride);

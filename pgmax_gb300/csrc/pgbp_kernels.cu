@@ -1635,7 +1635,24 @@ size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batc
   n += align_up(sizeof(float) * (size_t)(p.num_potentials * (lp_batched ? B : 1)));
   n += align_up(sizeof(unsigned) * (size_t)(it * B));
   n += align_up(sizeof(float) * (size_t)gemm_table_floats(p));
+  n += align_up(sizeof(int));  // convergence count of pgbp_run_to_tolerance
   return n;
+}
+
+// first[b] = the first iteration (1-based, counted from the run's start) whose residual was below
+// tol, if not already set; counts the instances still above it.
+__global__ void __launch_bounds__(256) first_below_kernel(const unsigned* __restrict__ dacc,
+                                                          int64_t n, int64_t B, float tol,
+                                                          int64_t done, int32_t* __restrict__ first,
+                                                          int* __restrict__ unconverged) {
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < B;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    int32_t f = first[b];
+    for (int64_t it = 0; f < 0 && it < n; ++it)
+      if (__uint_as_float(dacc[it * B + b]) < tol) f = (int32_t)(done + it + 1);
+    first[b] = f;
+    if (f < 0) atomicAdd(unconverged, 1);
+  }
 }
 
 // dst[b, i] = src[b * sstride + i] for a [B, n] block (sstride 0 broadcasts one row).
@@ -1651,7 +1668,7 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
                    const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
                    float* msgs_out, float* deltas, int64_t num_iters, double damping,
                    double temperature, void* ws, size_t ws_bytes, int64_t checkpoint_every,
-                   float* checkpoints) {
+                   float* checkpoints, const ToleranceRun* tol_run) {
   const int64_t iters = std::max<int64_t>(num_iters, 1);
   const bool ev_b = ev_stride != 0, lp_b = lp_stride != 0;
   char* w = static_cast<char*>(ws);
@@ -1668,7 +1685,13 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   float* lpc = (float*)take(sizeof(float) * (size_t)(p.num_potentials * (lp_b ? B : 1)));
   unsigned* dacc = (unsigned*)take(sizeof(unsigned) * (size_t)(iters * B));
   float* gemm_ws = (float*)take(sizeof(float) * (size_t)gemm_table_floats(p));
+  int* unconverged = (int*)take(sizeof(int));
   (void)ws_bytes;
+  if (tol_run != nullptr) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+      return cudaErrorStreamCaptureUnsupported;  // the stopping test reads a count on the host
+  }
 
   // evidence and potentials in the run layout; potentials clipped (bp.py:85-87)
   const float* evp = ev;
@@ -1798,6 +1821,32 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     ProfileScope ps(kProfLayout, s);
     copy_rows_kernel<<<flat_grid(p.num_edge_states * B, p.sm_count), 256, 0, s>>>(
         msgs_in, msgs_stride, p.num_edge_states, B, checkpoints);
+  }
+  if (tol_run != nullptr) {
+    // chunks of `iters` iterations until every instance's residual fell below the tolerance
+    cudaMemsetAsync(tol_run->first_below, 0xff, sizeof(int32_t) * (size_t)B, s);
+    int64_t done = 0;
+    while (done < tol_run->max_iters) {
+      const int64_t n = std::min(iters, tol_run->max_iters - done);
+      cudaMemsetAsync(dacc, 0, sizeof(unsigned) * (size_t)(n * B), s);
+      float* fin = run_path(path, n);
+      if (fin != m0) std::swap(m0, m1);
+      cudaMemsetAsync(unconverged, 0, sizeof(int), s);
+      {
+        ProfileScope ps(kProfLayout, s);
+        first_below_kernel<<<flat_grid(B, p.sm_count), 256, 0, s>>>(
+            dacc, n, B, (float)tol_run->tol, done, tol_run->first_below, unconverged);
+      }
+      done += n;
+      int left = 0;
+      cudaError_t e = cudaMemcpyAsync(&left, unconverged, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return e;
+      if (left == 0) break;
+    }
+    *tol_run->iters_run = done;
+    write_out(m0, msgs_out);
+    return cudaGetLastError();
   }
   unsigned* const dacc0 = dacc;
   float* fin = m0;

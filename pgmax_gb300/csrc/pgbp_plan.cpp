@@ -723,7 +723,8 @@ int run_checked(const pgbp_plan* plan, void* stream, int64_t batch, const float*
                 int64_t lp_stride, const float* evidence, int64_t ev_stride, const float* msgs_in,
                 int64_t msgs_stride, float* msgs_out, float* deltas, int64_t num_iters,
                 double damping, double temperature, void* workspace, size_t workspace_bytes,
-                int64_t checkpoint_every, float* checkpoints) {
+                int64_t checkpoint_every, float* checkpoints,
+                const pgbp::ToleranceRun* tol_run = nullptr) {
   if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
   const pgbp::Plan& p = plan->p;
   if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
@@ -750,7 +751,10 @@ int run_checked(const pgbp_plan* plan, void* stream, int64_t batch, const float*
   if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
   e = pgbp::run_bp(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
                    ev_stride, msgs_in, msgs_stride, msgs_out, deltas, num_iters, damping, temperature,
-                   workspace, workspace_bytes, checkpoint_every, checkpoints);
+                   workspace, workspace_bytes, checkpoint_every, checkpoints, tol_run);
+  if (e == cudaErrorStreamCaptureUnsupported && tol_run)
+    return fail(PGBP_ERR_UNSUPPORTED, "pgbp_run_to_tolerance reads a count on the host: "
+                "it cannot run inside a stream capture");
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_run launch");
   return PGBP_OK;
 }
@@ -780,6 +784,22 @@ int pgbp_run_checkpointed(const pgbp_plan* plan, void* stream, int64_t batch,
   return run_checked(plan, stream, batch, log_potentials, lp_stride, evidence, ev_stride, msgs_in,
                      msgs_stride, msgs_out, deltas, num_iters, damping, temperature, workspace,
                      workspace_bytes, checkpoint_every, checkpoints);
+}
+
+int pgbp_run_to_tolerance(const pgbp_plan* plan, void* stream, int64_t batch,
+                          const float* log_potentials, int64_t lp_stride, const float* evidence,
+                          int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
+                          float* msgs_out, double tolerance, int64_t max_iters,
+                          int64_t check_every, double damping, double temperature,
+                          int32_t* first_below, int64_t* iters_run, void* workspace,
+                          size_t workspace_bytes) {
+  if (!(tolerance > 0.0) || max_iters < 1 || check_every < 1)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "tolerance > 0, max_iters >= 1, check_every >= 1");
+  if (!first_below || !iters_run) return fail(PGBP_ERR_INVALID_ARGUMENT, "null output pointer");
+  const pgbp::ToleranceRun tr{tolerance, max_iters, first_below, iters_run};
+  return run_checked(plan, stream, batch, log_potentials, lp_stride, evidence, ev_stride, msgs_in,
+                     msgs_stride, msgs_out, nullptr, check_every, damping, temperature, workspace,
+                     workspace_bytes, 0, nullptr, &tr);
 }
 
 size_t pgbp_vjp_workspace_size(const pgbp_plan* plan, int64_t batch, int64_t num_iters,

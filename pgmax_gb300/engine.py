@@ -202,6 +202,29 @@ class Plan:
       return out[0], deltas[0], ck
     return out, deltas, ck
 
+  def run_to_tolerance(self, log_potentials, evidence, ftov_msgs, tolerance, max_iters,
+                       damping=0.5, temperature=0.0, check_every=1):
+    """BP until every instance's residual is below `tolerance` (pgbp_run_to_tolerance): returns
+    (msgs, first iteration below the tolerance per instance (-1 if none, host int32),
+    iterations run)."""
+    torch = _torch()
+    lp, ev, m, B, batched = self._inputs(log_potentials, evidence, ftov_msgs)
+    dev = m[0].device
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=dev)
+    first = torch.empty(B, dtype=torch.int32, device=dev)
+    ran = ctypes.c_int64(0)
+    ws_bytes = int(self.lib.pgbp_workspace_size(self.handle, B, int(check_every)))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    native.check(self.lib.pgbp_run_to_tolerance(
+        self.handle, self._stream(), B, lp[0].data_ptr(), lp[1], ev[0].data_ptr(), ev[1],
+        m[0].data_ptr(), m[1], out.data_ptr(), float(tolerance), int(max_iters),
+        int(check_every), float(damping), float(temperature), first.data_ptr(),
+        ctypes.byref(ran), ws.data_ptr(), ws_bytes), "pgbp_run_to_tolerance")
+    first = first.cpu()
+    if not batched:
+      return out[0], first[0], int(ran.value)
+    return out, first, int(ran.value)
+
   def run_vjp(self, log_potentials, evidence, checkpoints, num_iters, g_msgs, damping=0.5,
               temperature=1.0, checkpoint_every=10, want_msgs_in=False):
     """Gradients (g_log_potentials, g_evidence, g_msgs_in or None) of a loss with gradient g_msgs

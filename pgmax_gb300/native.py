@@ -139,6 +139,8 @@ SIGNATURES = [
                                           ctypes.c_int, _p, _i64]),
     ("pgbp_run_checkpointed", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p,
                                              _i64, _i64, _d, _d, _p, _p, ctypes.c_size_t]),
+    ("pgbp_run_to_tolerance", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _d,
+                                             _i64, _i64, _d, _d, _p, _p, _p, ctypes.c_size_t]),
     ("pgbp_vjp_workspace_size", ctypes.c_size_t, [_p, _i64, _i64, _i64]),
     ("pgbp_run_vjp", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i64, _d, _d, _p,
                                     _p, _p, _p, _p, ctypes.c_size_t]),

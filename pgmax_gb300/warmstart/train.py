@@ -67,24 +67,13 @@ class Family:
     return msgs
 
 
-def run_to_tolerance(plan, lp, ev, msgs, tol: float, max_iters: int, chunk: int = 25):
-  """BP from `msgs` until every instance's residual is below `tol` or `max_iters` iterations ran.
-  Returns (messages, iterations [B] to reach tol (-1 if never), iterations run)."""
-  torch = _torch()
-  B = msgs.shape[0]
-  first = torch.full((B,), -1, dtype=torch.int64)
-  done = 0
-  while done < max_iters:
-    n = min(chunk, max_iters - done)
-    msgs, deltas = plan.run(lp, ev, msgs, n, DAMPING, TEMPERATURE)
-    below = (deltas < tol).cpu()
-    hit = below.any(dim=1)
-    step = torch.argmax(below.to(torch.int8), dim=1) + 1 + done
-    first = torch.where((first < 0) & hit, step, first)
-    done += n
-    if bool((first >= 0).all()):
-      break
-  return msgs, first, done
+def run_to_tolerance(plan, lp, ev, msgs, tol: float, max_iters: int, chunk: int = 1):
+  """BP from `msgs` until every instance's residual is below `tol` or `max_iters` iterations ran
+  (pgbp_run_to_tolerance, residual tested every `chunk` iterations). Returns (messages,
+  iterations [B] to reach tol (-1 if never), iterations run)."""
+  out, first, ran = plan.run_to_tolerance(lp, ev, msgs, tol, max_iters, DAMPING, TEMPERATURE,
+                                          check_every=chunk)
+  return out, first.to(_torch().int64), ran
 
 
 def make_dataset(fam: Family, seed: int, n: int, batch: int = 256, tol: float = 1e-5,
@@ -98,7 +87,7 @@ def make_dataset(fam: Family, seed: int, n: int, batch: int = 256, tol: float = 
     m = min(batch, n - k)
     x, m1, lp, ev = fam.instances(seed * 1_000_003 + k, m)
     msgs0 = torch.zeros((m, fam.n_es), device="cuda")
-    msgs, first, _ = run_to_tolerance(fam.plan, lp, ev, msgs0, tol, max_iters)
+    msgs, first, _ = run_to_tolerance(fam.plan, lp, ev, msgs0, tol, max_iters, chunk=10)
     ok = (first >= 0).to("cuda")
     xs.append(x[ok])
     ys.append((fam.to_channels(msgs) - m1)[ok])
@@ -146,7 +135,7 @@ def evaluate(fam: Family, net: Optional[convnet.ConvNet], seed: int, n: int, bat
     x, m1, lp, ev = fam.instances(seed * 1_000_003 + k, m)
     zeros = torch.zeros((m, fam.n_es), device="cuda")
     # the converged plain solution (the judge of belief error)
-    ref, ref_first, _ = run_to_tolerance(fam.plan, lp, ev, zeros, 1e-5, max_iters)
+    ref, ref_first, _ = run_to_tolerance(fam.plan, lp, ev, zeros, 1e-5, max_iters, chunk=10)
     ok = ref_first >= 0
     res["skipped"] += int((~ok).sum())
     ref_m = fam.plan.marginals(fam.plan.beliefs(ev, ref))

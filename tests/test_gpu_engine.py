@@ -303,3 +303,30 @@ def test_bad_run_arguments_raise():
     plan.run(f["log_potentials"], f["evidence"][:-1], f["ftov_msgs_in"], 3)
   with pytest.raises(ValueError):
     plan.run(f["log_potentials"], f["evidence"], f["ftov_msgs_in"], 3, 0.5, -1.0)
+
+
+@pytest.mark.parametrize("check_every", [1, 3, 7])
+def test_run_to_tolerance_matches_one_run_of_the_same_length(check_every):
+  """pgbp_run_to_tolerance stops once every instance's residual fell below the tolerance; its
+  messages are those of one pgbp_run of the iterations it ran, and its first-below indices are
+  read off that run's residuals."""
+  torch = _torch()
+  f = fixtures.load(f"{fixtures.FIXTURES}/case_ising12_T1.npz")
+  plan = _plan(f["wiring"], "multi")
+  rng = np.random.default_rng(check_every)
+  B = 5
+  ev = (f["evidence"][None] + rng.gumbel(size=(B,) + f["evidence"].shape)).astype(np.float32)
+  tol = 1e-4
+  out, first, ran = plan.run_to_tolerance(f["log_potentials"], ev, f["ftov_msgs_in"], tol, 500,
+                                          0.5, 1.0, check_every=check_every)
+  want, deltas = plan.run(f["log_potentials"], ev, f["ftov_msgs_in"], ran, 0.5, 1.0)
+  torch.cuda.synchronize()
+  assert torch.equal(out, want)
+  d = deltas.cpu().numpy()
+  for b in range(B):
+    below = np.nonzero(d[b] < tol)[0]
+    assert int(first[b]) == (int(below[0]) + 1 if below.size else -1)
+  if int(first.min()) > 0:   # every instance converged: the run stopped at the first check after
+    assert ran % check_every == 0 and ran - int(first.max()) < check_every
+  else:                      # some instance oscillates: the run went to max_iters
+    assert ran == 500
