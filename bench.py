@@ -434,7 +434,7 @@ def run_multigraph(args):
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import batch, native  # pylint: disable=g-import-not-at-top
   t0 = time.perf_counter()
-  wirings, tables, evs, fam = build_multigraph()
+  wirings, tables, evs, fam = build_multigraph(n_graphs=args.graphs)
   t_gen = time.perf_counter() - t0
   t0 = time.perf_counter()
   gb = batch.GraphBatch(wirings)
@@ -491,7 +491,7 @@ def run_multigraph(args):
       "unit": "edge-msg updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
       "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
       "dtype": "f32", "data": "synthetic (seed 0)",
-      "config": {"workload": "multigraph256_potts_potts64_deconv", "graphs": MG_GRAPHS,
+      "config": {"workload": f"multigraph{args.graphs}_potts_potts64_deconv", "graphs": args.graphs,
                  "families": fam, "num_iters": iters, "temperature": 1.0, "damping": 0.5,
                  "num_edges": num_edges, "edge_states": n_es, "var_states": n_vs,
                  "shared_table_floats": p_distinct,
@@ -708,6 +708,8 @@ def main():
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="pgbp", choices=["pgbp", "reference"])
   ap.add_argument("--no-cpu-baseline", action="store_true")
+  ap.add_argument("--graphs", type=int, default=MG_GRAPHS,
+                  help="graphs of the multigraph workload (256; fewer for small profiling cases)")
   ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
                   help="execution path of the ising workload (auto: timed choice)")
   ap.add_argument("--workload", default="rbm", choices=["rbm", "ising", "adjoint", "multigraph", "warmstart"],
