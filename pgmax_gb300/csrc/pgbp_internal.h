@@ -98,6 +98,17 @@ struct VarsumSet {
   int32_t* slots = nullptr;
   int32_t* run_off = nullptr;    // [count + 1]
   int4* runs = nullptr;          // (first slot, stride, length, 0)
+  // By variable (non-binary variables, whose K states see the same edges, K slots each): the
+  // multi-kernel path reads per variable its first state and its edges' first slots, so a state
+  // costs no index load. Units are grouped by K: group g = units grp[g].y .. grp[g + 1].y - 1,
+  // state count grp[g].x, first variable grp[g].z (unit u -> variable z + (u - y) / x, state
+  // (u - y) % x); grp has a sentinel entry.
+  int byvar_groups = 0;
+  int64_t byvar_units = 0;
+  int4* byvar_grp = nullptr;
+  int32_t* byvar_vs0 = nullptr;   // [variables] first variable state
+  int32_t* byvar_eoff = nullptr;  // [variables + 1]
+  int32_t* byvar_eslot = nullptr; // first slot of each edge, edge order
 };
 
 struct Plan {

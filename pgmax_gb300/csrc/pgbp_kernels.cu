@@ -493,6 +493,144 @@ __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t
   block_max_to(deltas, l, dmax);
 }
 
+// The same update with one warp per (factor, instance), for factors with many parents: lanes
+// load parents 32 at a time and compute their terms in parallel; the factor sums are accumulated
+// in parent order by every lane from the shuffled terms (the same float additions in the same
+// order as logical_unit, so the results are identical); maxima and the last argmax are warp
+// reductions; the outputs of the parents are computed by their lanes.
+__device__ __forceinline__ float warp_max(float x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmaxp(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+template <bool T0, class C>
+__device__ __forceinline__ void logical_warp_unit(const C& c, const LogicalDev& g, int64_t f,
+                                                  int64_t b, float t, bool low_t, int normalize,
+                                                  int lane, float& dmax) {
+  const int rel = g.off > 0 ? 1 : 0;
+  const int64_t p0 = g.par_begin[f], p1 = g.par_begin[f + 1];
+  float old[2];
+  float fs_oth = 0.0f, max1 = -INFINITY, fs_x = 0.0f;
+  for (int64_t base = p0; base < p1; base += 32) {
+    const int64_t i = base + lane;
+    float vo = 0.0f, vr = 0.0f, x = 0.0f;
+    if (i < p1) {
+      load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+      x = T0 ? fmaxp(vo, vr) : logaddexp_t(vr, vo, t);
+      max1 = fmaxp(max1, vr - vo);
+    }
+    const int n = (int)(p1 - base < 32 ? p1 - base : 32);
+    for (int k = 0; k < n; ++k) {
+      fs_oth += __shfl_sync(0xffffffffu, vo, k);
+      fs_x += __shfl_sync(0xffffffffu, x, k);
+    }
+  }
+  max1 = warp_max(max1);
+  // the last parent attaining the maximum difference
+  int64_t last = -1;
+  for (int64_t i = p0 + lane; i < p1; i += 32) {
+    float vo, vr;
+    load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+    if (vr - vo == max1) last = i;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long other = __shfl_xor_sync(0xffffffffu, (long long)last, o);
+    last = other > last ? other : last;
+  }
+  const int64_t arg = last >= 0 ? last : p1 - 1;
+  float max2 = -INFINITY;
+  for (int64_t i = p0 + lane; i < p1; i += 32) {
+    float vo, vr;
+    load_or(c, edge_ref(g.par[i]), rel, b, old, vo, vr);
+    max2 = fmaxp(max2, (i == arg) ? -INFINITY : vr - vo);
+  }
+  max2 = warp_max(max2);
+  const EdgeRef rc = edge_ref(g.child[f]);
+  float cold[2], c_oth, c_rel;
+  load_or(c, rc, rel, b, cold, c_oth, c_rel);
+  float ch_rel;
+  if (T0) {
+    ch_rel = fs_x + fminp(0.0f, max1);
+  } else {
+    ch_rel = logminusexp_t(fs_x, fs_oth, t, 1e-4f);
+    if (low_t) ch_rel = fmaxp(ch_rel, logaddexp_t(fs_oth + max1, fs_oth + max2, t));
+  }
+  const bool single = (p1 - p0) == 1;
+  for (int64_t i = p0 + lane; i < p1; i += 32) {
+    const EdgeRef r = edge_ref(g.par[i]);
+    float vo, vr;
+    load_or(c, r, rel, b, old, vo, vr);
+    float p_rel, p_oth;
+    if (T0) {
+      const float mx = fmaxp(vo, vr);
+      p_rel = (fs_x + c_rel) - mx;
+      const float opt1 = (c_oth + fs_oth) - vo;
+      const float opt2 = p_rel + fminp(0.0f, i == arg ? max2 : max1);
+      p_oth = fmaxp(opt1, opt2);
+    } else {
+      const float lse = logaddexp_t(vr, vo, t);
+      const float fs_lse_wo = fs_x - lse;
+      const float fs_oth_wo = fs_oth - vo;
+      p_rel = c_rel + fs_lse_wo;
+      const float opt1 = c_oth + fs_oth_wo;
+      const float opt2 = c_rel + fs_lse_wo;
+      const float opt3 = c_rel + fs_oth_wo;
+      p_oth = logminusexp_t(logaddexp_t(opt1, opt2, t), opt3, t, 1e-4f);
+      if (low_t) {
+        const float fsp = fs_oth_wo + (i == arg ? max2 : max1);
+        p_oth = fmaxp(p_oth, logaddexp_t(opt1, c_rel + fsp, t));
+      }
+    }
+    if (single) {
+      p_rel = c_rel;
+      p_oth = c_oth;
+    }
+    const float rel_out = normalize ? p_rel - p_oth : p_rel;
+    const float oth_out = normalize ? 0.0f : p_oth;
+    c.store(r, 2, old, [&](int s) { return s == rel ? rel_out : oth_out; }, b, dmax);
+  }
+  if (lane == 0) {
+    const float crel_out = normalize ? ch_rel - fs_oth : ch_rel;
+    const float coth_out = normalize ? 0.0f : fs_oth;
+    c.store(rc, 2, cold, [&](int s) { return s == rel ? crel_out : coth_out; }, b, dmax);
+  }
+}
+
+// One warp per (factor, instance) unit, unit = factor * B + instance; the residual is folded per
+// block when the batch has one instance, else per warp.
+template <bool T0, class C>
+__global__ void __launch_bounds__(256) logical_warp_kernel(C c, LogicalDev g, int64_t B, float t,
+                                                           bool low_t, int normalize,
+                                                           unsigned* deltas) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t wstep = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  float dmax = 0.0f;
+  for (int64_t u = w0; u < g.count * B; u += wstep) {
+    const int64_t f = u / B, b = u % B;
+    float dm = 0.0f;
+    logical_warp_unit<T0>(c, g, f, b, t, low_t, normalize, lane, dm);
+    dm = warp_max(dm);
+    if (B == 1) {
+      dmax = fmaxp(dmax, dm);
+    } else if (lane == 0 && deltas != nullptr) {
+      atomicMax(deltas + b, __float_as_uint(dm));
+    }
+  }
+  if (B == 1) {
+    __shared__ float red[8];
+    if (lane == 0) red[threadIdx.x >> 5] = dmax;
+    __syncthreads();
+    if (threadIdx.x == 0 && deltas != nullptr) {
+      float m = 0.0f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxp(m, red[w]);
+      atomicMax(deltas, __float_as_uint(m));
+    }
+  }
+}
+
 // ----------------------------------------------------------------------------- Pool factors
 struct PoolDev {
   const int32_t* __restrict__ ch_begin;
@@ -877,6 +1015,32 @@ __global__ void __launch_bounds__(256) varsum_other_kernel(VarsumDev v, bool use
   if (!l.valid) return;
   for (int64_t u = l.u0; u < v.count; u += l.ustep)
     varsum_other_unit(v, use_runs, u, l.b, msgs, ev, evs, evb, vsum, B);
+}
+
+// Variable sums of non-binary variables by variable (VarsumSet::byvar_*): per (variable state,
+// instance) evidence plus the messages of the variable's edges in edge order, with the state's
+// slot at the edge's first slot + state: no per-state index. Consecutive units are consecutive
+// states of one variable, whose slots are consecutive.
+__global__ void __launch_bounds__(256) varsum_byvar_kernel(
+    const int4* __restrict__ grp, int n_groups, int64_t units, const int32_t* __restrict__ vs0,
+    const int32_t* __restrict__ eoff, const int32_t* __restrict__ eslot,
+    const float* __restrict__ msgs, const float* __restrict__ ev, int64_t evs, int64_t evb,
+    float* __restrict__ vsum, int64_t B) {
+  const Lane l = lane(B);
+  if (!l.valid) return;
+  const int64_t b = l.b;
+  int g = 0;
+  for (int64_t u = l.u0; u < units; u += l.ustep) {
+    while (g + 1 < n_groups && u >= grp[g + 1].y) ++g;
+    const int4 gr = grp[g];
+    const int32_t local = (int32_t)(u - gr.y);
+    const int32_t var = gr.z + local / gr.x, st = local % gr.x;
+    const int64_t v = (int64_t)vs0[var] + st;
+    float sum = evb == 0 ? ev[v * evs] : ev[v * evs + b];
+    const int32_t k1 = eoff[var + 1];
+    for (int32_t k = eoff[var]; k < k1; ++k) sum += msgs[((int64_t)eslot[k] + st) * B + b];
+    vsum[v * B + b] = sum;
+  }
 }
 
 // Binary variable sums, 4 instances per thread, sixteen slots in flight.
@@ -1353,6 +1517,14 @@ void launch_logical(cudaStream_t s, const Plan& p, int which, const C& c, int64_
   const LogicalSet& g = p.logical[which];
   if (g.count == 0) return;
   ProfileScope ps(which == 0 ? kProfOr : kProfAnd, s);
+  if (g.num_parents >= 8 * g.count) {  // many parents per factor: a warp per factor
+    const int64_t warps = g.count * B;
+    const int64_t blocks = std::max<int64_t>(
+        1, std::min<int64_t>((warps + 7) / 8, (int64_t)p.sm_count * 16));
+    logical_warp_kernel<T0><<<(unsigned)blocks, 256, 0, s>>>(c, dev(g), B, t, low_t, normalize,
+                                                             deltas);
+    return;
+  }
   const Launch2 l = launch2(g.count, B, p.sm_count);
   logical_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(g), B, t, low_t, normalize, deltas);
 }
@@ -1388,7 +1560,12 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
                                                      B);
   }
   const VarsumSet& vo = p.varsum_other;
-  if (vo.count > 0) {
+  if (vo.byvar_groups > 0) {
+    const Launch2 l = launch2(vo.byvar_units, B, p.sm_count);
+    varsum_byvar_kernel<<<l.grid, l.block, 0, s>>>(vo.byvar_grp, vo.byvar_groups, vo.byvar_units,
+                                                    vo.byvar_vs0, vo.byvar_eoff, vo.byvar_eslot,
+                                                    cur, ev, evs, evb, vsum, B);
+  } else if (vo.count > 0) {
     const Launch2 l = launch2(vo.count, B, p.sm_count);
     varsum_other_kernel<<<l.grid, l.block, 0, s>>>(dev(vo), vo.use_runs, cur, ev, evs, evb, vsum,
                                                     B);

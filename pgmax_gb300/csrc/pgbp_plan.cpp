@@ -342,6 +342,50 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   fill_varsum(p.varsum_binary, vb_vs, vb_off, vb_slots);
   fill_varsum(p.varsum_other, vo_vs, vo_off, vo_slots);
   if (bd.err) return bail(bd.err);
+  // the non-binary variables by variable, when every one of their edges has all K states
+  if (!vo_vs.empty()) {
+    std::map<int32_t, std::pair<int32_t, std::vector<int32_t>>> vars;  // vs0 -> (K, edge slots)
+    bool ok = true;
+    for (int64_t e = 0; e < ne && ok; ++e) {
+      const int32_t k = edge_start[e + 1] - edge_start[e];
+      if (k <= 2) continue;
+      const int32_t v0 = vs[edge_start[e]];
+      for (int32_t j = 1; j < k && ok; ++j) ok = vs[edge_start[e] + j] == v0 + j;
+      auto& var = vars[v0];
+      if (var.first == 0) var.first = k;
+      ok = ok && var.first == k;
+      var.second.push_back(edge_slot[e]);
+    }
+    int64_t units = 0;
+    for (auto& kv : vars) units += kv.second.first;
+    std::map<int32_t, std::vector<int32_t>> by_k;  // K -> variables (vs0)
+    for (auto& kv : vars) by_k[kv.second.first].push_back(kv.first);
+    ok = ok && units == (int64_t)vo_vs.size() && by_k.size() <= 16;
+    if (ok) {
+      std::vector<int4> grp;
+      std::vector<int32_t> vs0, eoff{0}, eslot;
+      int64_t first_unit = 0;
+      for (auto& kv : by_k) {
+        grp.push_back(make_int4(kv.first, (int32_t)first_unit, (int32_t)vs0.size(), 0));
+        for (int32_t v : kv.second) {
+          vs0.push_back(v);
+          const auto& slots = vars[v].second;
+          eslot.insert(eslot.end(), slots.begin(), slots.end());
+          eoff.push_back((int32_t)eslot.size());
+          first_unit += kv.first;
+        }
+      }
+      grp.push_back(make_int4(0, (int32_t)first_unit, (int32_t)vs0.size(), 0));
+      pgbp::VarsumSet& vo = p.varsum_other;
+      vo.byvar_groups = (int)by_k.size();
+      vo.byvar_units = first_unit;
+      vo.byvar_grp = bd.upload(grp);
+      vo.byvar_vs0 = bd.upload(vs0);
+      vo.byvar_eoff = bd.upload(eoff);
+      vo.byvar_eslot = bd.upload(eslot);
+      if (bd.err) return bail(bd.err);
+    }
+  }
   auto edge_rec = [&](int64_t es0) {  // (first edge state, first slot, first var state, 0)
     const int32_t e = ei[es0];
     return make_int4((int32_t)es0, edge_slot[e], vs[es0], 0);
