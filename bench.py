@@ -168,6 +168,120 @@ def run_ising(args):
 ADJ_N, ADJ_B, ADJ_ITERS, ADJ_CKPT, ADJ_FLIP = 64, 32, 100, 10, 0.1
 
 
+def run_energy(args):
+  """compute_energy of the RBM perturb-and-MAP batch: the 128 MAP decodings of one 200-iteration
+  T = 0 run (784 x 500 RBM, Gumbel evidence per sample) scored in one pgbp_energy launch against
+  their own evidence and the shared potentials. A step is one launch; L2 is flushed (a 512 MB
+  write) before each, and only the launches are timed (CUDA events around each)."""
+  import torch  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
+  dev = torch.device("cuda", 0)
+  fg, hidden, visible = build_rbm(seed=0)
+  bp = infer.BP(fg.bp_state, temperature=TEMPERATURE)
+  plan = bp.context.plan
+  nvs = fg.fg_state.num_var_states
+  ev_host = gumbel_evidence(nvs, BATCH, 1000)
+  lp_dev = torch.as_tensor(np.asarray(fg.fg_state.log_potentials, np.float32), device=dev)
+  ev_dev = torch.as_tensor(ev_host, device=dev)
+  msgs0 = torch.zeros(fg.fg_state.total_factor_num_states, dtype=torch.float32, device=dev)
+  arrays = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_dev)
+  out = bp.run(arrays, num_iters=ITERS, damping=DAMPING, temperature=TEMPERATURE)
+  dec = infer.decode_map_states(bp.get_beliefs(out))
+  maps = torch.cat([dec[hidden].reshape(BATCH, -1), dec[visible].reshape(BATCH, -1)],
+                   dim=1).to(torch.int32).contiguous()
+  stream = torch.cuda.current_stream(dev)
+  flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+  for _ in range(args.warmup):
+    energies = plan.energy(lp_dev, ev_dev, maps)
+  torch.cuda.synchronize()
+  evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+         for _ in range(args.steps)]
+  with ClockSampler(0) as clocks:
+    for e0, e1 in evs:
+      flush.zero_()
+      e0.record(stream)
+      energies = plan.energy(lp_dev, ev_dev, maps)
+      e1.record(stream)
+    torch.cuda.synchronize()
+  ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+  info = plan.info
+  nv = NH + NV
+  n_factors = info["num_enum_factors"]
+  terms = BATCH * (n_factors + nv)
+  # bytes one launch must bring from HBM (cold L2): the decodings and per-sample evidence, the
+  # shared potentials, and the plan's index arrays it walks (int4 record + first potential per
+  # pairwise factor; unary factors: 7 int32 per factor and 1 per config row; var_off, var_of_vs)
+  f_pw = info["num_enum_pairwise_factors"]
+  algo_bytes = (BATCH * 4 * (nv + nvs) + 4 * int(plan.num_potentials) + 20 * f_pw
+                + 4 * (7 * (n_factors - f_pw) + 2 * (n_factors - f_pw)) + 4 * (nv + 1 + nvs))
+  launch_s = ms / 1e3 / args.steps
+  peak, peak_kind = peaks()
+  achieved = algo_bytes / launch_s / 1e9
+  # end to end through the public API: host decodings in, host energies out
+  maps_pinned = maps.cpu().pin_memory()
+  ev_pinned = torch.as_tensor(ev_host).pin_memory()
+  en_host = torch.empty(BATCH, dtype=torch.float32).pin_memory()
+  host_arrays = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_dev)
+  map_states = {hidden: None, visible: None}
+
+  def step_e2e():
+    m = maps_pinned.to(dev, non_blocking=True)
+    e = ev_pinned.to(dev, non_blocking=True)
+    map_states[hidden] = m[:, :NH]
+    map_states[visible] = m[:, NH:]
+    a = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=e)
+    en, _, _ = infer.compute_energy(fg.bp_state, a, map_states)
+    en_host.copy_(en, non_blocking=True)
+
+  del host_arrays
+  for _ in range(args.warmup):
+    step_e2e()
+  torch.cuda.synchronize()
+  t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  t0.record(stream)
+  for _ in range(args.steps):
+    step_e2e()
+  t1.record(stream)
+  torch.cuda.synchronize()
+  e2e_ms = t0.elapsed_time(t1)
+  line = {
+      "metric": "energy terms/s", "value": terms * args.steps / (ms / 1e3),
+      "unit": "energy terms/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+      "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+      "vs_baseline": None, "dtype": "f64 sums of f32",
+      "data": "synthetic (seeded RBM, Gumbel(0,1) evidence; the decodings of a 200-iteration run)",
+      "config": {"workload": "energy_rbm784x500_b128", "batch": BATCH,
+                 "terms_per_decoding": n_factors + nv, "l2": "flushed before every launch"},
+      "decodings_per_s": BATCH * args.steps / (ms / 1e3),
+      "e2e": {"value": terms * args.steps / (e2e_ms / 1e3), "unit": "energy terms/s",
+              "h2d_bytes_per_step": int(maps_pinned.numel() * 4 + ev_pinned.numel() * 4),
+              "d2h_bytes_per_step": int(en_host.numel() * 4)},
+      "gpu_launches": 2 * args.steps,
+      "roofline": {"bound": "hbm", "kernel": "energy_partial_kernel", "achieved": achieved,
+                   "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                   "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
+                   "algorithmic_bytes_per_launch": algo_bytes, "traffic": None},
+      "clocks": clocks.summary(),
+  }
+  if not args.no_cpu_baseline:
+    from oracle import energy as oracle_energy  # pylint: disable=g-import-not-at-top
+    w = bp.context.flat_wiring()
+    lp_h = lp_dev.cpu().numpy()
+    maps_h = maps.cpu().numpy()
+    n, t_start = 0, time.perf_counter()
+    while n < BATCH and time.perf_counter() - t_start < 10.0:
+      got = oracle_energy.compute_energy(w, lp_h, ev_host[n], maps_h[n])
+      want = float(energies[n])
+      assert (np.isinf(got) and np.isinf(want)) or abs(got - want) <= 1e-4 * max(1.0, abs(got))
+      n += 1
+    dt = time.perf_counter() - t_start
+    line["cpu_baseline"] = {"value": n * (n_factors + nv) / dt, "unit": "energy terms/s",
+                            "cores": 1, "kind": "port",
+                            "sample": f"{n} of the {BATCH} decodings, NumPy oracle, {dt:.1f} s"}
+  print(json.dumps(line))
+  return 0
+
+
 def shape_images(n, batch, seed, flip):
   """`batch` binary n x n images, each the union of 2-6 random axis-aligned rectangles and
   ellipses, and their observations with every pixel flipped with probability `flip`."""
@@ -712,11 +826,12 @@ def main():
                   help="graphs of the multigraph workload (256; fewer for small profiling cases)")
   ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
                   help="execution path of the ising workload (auto: timed choice)")
-  ap.add_argument("--workload", default="rbm", choices=["rbm", "ising", "adjoint", "multigraph", "warmstart"],
+  ap.add_argument("--workload", default="rbm",
+                  choices=["rbm", "ising", "adjoint", "multigraph", "warmstart", "energy"],
                   help="rbm: the headline RBM perturb-and-MAP batch (default); ising: the 50x50 "
                        "toroidal Ising configuration; adjoint: differentiable BP on 64x64 grids; "
                        "multigraph: the 256-graph uneven batch; warmstart: learned init vs "
-                       "cold-start BP")
+                       "cold-start BP; energy: compute_energy of the RBM batch's decodings")
   args = ap.parse_args()
   if args.warmup < 3:
     args.warmup = 3
@@ -730,6 +845,8 @@ def main():
     return run_multigraph(args)
   if args.workload == "warmstart":
     return run_warmstart(args)
+  if args.workload == "energy":
+    return run_energy(args)
 
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top

@@ -14,6 +14,7 @@
  *   pgbp_beliefs        InfererContext.get_beliefs (flat part)   pgmax/infer/inferer.py:211-222
  *   pgbp_decode         decode_map_states                        pgmax/infer/inferer.py:251-264
  *   pgbp_marginals      get_marginals                            pgmax/infer/bp.py:263-288
+ *   pgbp_energy         compute_energy                           pgmax/infer/energy.py:53-148
  *
  * Conventions
  *   - Every call returns PGBP_OK (0) or an error code; nothing aborts or traps.
@@ -81,7 +82,7 @@ typedef struct {
   int64_t pool_num_factors;
   const int32_t* pool_indicators_edge_states;
   /* Variables: evidence_to_vars (FactorGraphState.evidence_to_vars, fgraph.py:317-326), needed
-   * only by pgbp_decode / pgbp_marginals; may be NULL. */
+   * only by pgbp_decode / pgbp_marginals / pgbp_energy; may be NULL. */
   int64_t num_variables;
   const int32_t* evidence_to_vars;             /* [num_var_states] */
   /* Execution options, 0 = automatic. Three execution paths exist: multi-kernel (one launch per
@@ -248,12 +249,32 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
 int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
                    int64_t beliefs_stride, float* marginals);
 
+/* Energy of decodings, lower is better: pgmax.infer.compute_energy (pgmax/infer/energy.py:53-148,
+ * debug_mode=False) for `batch` decodings at once. map [batch, num_variables] (map_stride ints
+ * apart, 0 = one decoding for all) holds each variable's state as pgbp_decode writes it; a negative
+ * state s of a K-state variable counts as s + K, a state outside [0, K) decodes no state.
+ * log_potentials and evidence as the reference's BPArrays hold them (not clipped; stride 0 =
+ * shared); energy [batch]:
+ *   -sum(onehot * evidence) - sum of the decoded Enum configs' potentials, or +inf when the number
+ *   of decoded Enum configs differs from the number of Enum factors (enum.py:276-323) or a
+ *   decoding violates an OR / AND (logical.py:295-358) or Pool (pool.py:184-239) factor.
+ * The partial sums are in double and added in a fixed order (deterministic); the reference sums in
+ * float32. With shared potential tables an Enum config's potential is its table's entry.
+ * Workspace: pgbp_energy_workspace_size(plan, batch) bytes, 256-byte aligned. Needs
+ * evidence_to_vars in the plan. */
+size_t pgbp_energy_workspace_size(const pgbp_plan* plan, int64_t batch);
+int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch,
+                const float* log_potentials, int64_t lp_stride,
+                const float* evidence, int64_t ev_stride,
+                const int32_t* map, int64_t map_stride, float* energy,
+                void* workspace, size_t workspace_bytes);
+
 /* Kernel timing. While enabled, pgbp_run brackets every kernel launch with CUDA events on its
  * stream (no synchronisation is added). pgbp_profile_read waits for the recorded events, returns
  * per-class launch counts and total device milliseconds, and clears the record. Classes:
  * 0 variable sums, 1 dense pairwise Enum, 2 generic Enum, 3 OR, 4 AND, 5 Pool,
  * 6 layout (transposes, potential clipping, initial normalisation, residual copy-out),
- * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals, pgbp_beliefs_vjp), 8 the
+ * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals, pgbp_beliefs_vjp, pgbp_energy), 8 the
  * one-CTA-per-instance small-graph kernel (all iterations in one launch), 9 the adjoint kernels of
  * pgbp_run_vjp (its forward recomputation is counted in the classes above). Process-wide, not
  * thread-safe. */

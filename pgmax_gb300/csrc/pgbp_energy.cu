@@ -1,0 +1,355 @@
+// Energy of MAP decodings on the device: compute_energy (pgmax/infer/energy.py:53-148, without
+// debug mode) with the per-type terms EnumFactor.compute_energy (pgmax/factor/enum.py:276-323),
+// LogicalFactor.compute_energy (pgmax/factor/logical.py:295-358) and PoolFactor.compute_energy
+// (pgmax/factor/pool.py:184-239). For instance b, with onehot_b(vs) = 1 when the decoded state of
+// vs's variable is vs:
+//
+//   energy[b] = -sum_vs onehot_b(vs) * evidence[b, vs]            (every state: 0 * inf is nan)
+//             + [Enum factors]  #decoded configs != #factors ? +inf : -sum lp[b, decoded configs]
+//             + [OR factors]    (all parents in state 0) != (child in state 0) for some factor ? +inf : 0
+//             + [AND factors]   the same with state 1
+//             + [Pool factors]  #choices in state 1 != (indicator in state 1) for some factor ? +inf : 0
+//
+// A term is added only when the graph has factors of its type (energy.py:140-147). A config of an
+// Enum factor is decoded when every one of its variables is in the config's state; the dense
+// pairwise factors list every config, so one config is decoded unless a state is out of range.
+// The decoded state of a variable with K states is map[b, v], a negative state taken as
+// map[b, v] + K (the reference indexes its one-hot with it, and JAX wraps a negative index once);
+// outside [0, K) no state of the variable is decoded, as JAX drops out-of-range scatters.
+//
+// Work: items are variables (the evidence term) and factors of each kind, in segments; a CTA takes
+// kEnergyChunk items of one segment for one instance and reduces them in double, in a fixed order,
+// into one partial; a second kernel (a warp per instance) adds the partials in a fixed order. The
+// result does not depend on timing. Loads per instance: the decoded states, the evidence, one
+// potential per decoded Enum config and the plan's index arrays (shared by the batch, L2-resident).
+
+#include <math.h>
+
+#include <algorithm>
+
+#include "pgbp_internal.h"
+
+namespace pgbp {
+namespace {
+
+constexpr int kEnergyThreads = 256;
+constexpr int kEnergyChunk = 4 * kEnergyThreads;
+constexpr int kMaxSegsPerLaunch = 32;
+
+enum : int { kFlagOr = 1, kFlagAnd = 2, kFlagPool = 4 };
+
+struct EnergyPartial {
+  double u;        // sum of onehot * evidence
+  double e;        // sum of the decoded configs' potentials
+  long long cnt;   // decoded Enum configs
+  int flags;       // violated OR / AND / Pool constraints
+  int pad;
+};
+static_assert(sizeof(EnergyPartial) == 32, "partial layout");
+
+// One segment as the kernel sees it: pointers of its factor kind. a = n1 (pairwise) or the
+// relevant state (logical); b = n2 (pairwise).
+struct SegDev {
+  int kind, a, b, pad;
+  int64_t items, chunk_begin;
+  const void* p0;
+  const void* p1;
+  const void* p2;
+};
+
+struct Launch {
+  int nseg;
+  SegDev seg[kMaxSegsPerLaunch];
+};
+
+struct Args {
+  const int32_t* var_off;
+  const int32_t* var_of_vs;
+  const float* lp;
+  int64_t lps;
+  const float* ev;
+  int64_t evs;
+  const int32_t* map;
+  int64_t ms;
+  int64_t B;
+  int64_t chunks;
+  EnumGeneric gen;
+};
+
+// Decoded state of variable v, or -1 when no state is decoded.
+__device__ __forceinline__ int decoded_state(const int32_t* __restrict__ map_b,
+                                             const int32_t* __restrict__ var_off, int v) {
+  const int k = __ldg(var_off + v + 1) - __ldg(var_off + v);
+  int s = map_b[v];
+  if (s < 0) s += k;
+  return (s >= 0 && s < k) ? s : -1;
+}
+
+__device__ __forceinline__ int state_of_vs(const int32_t* __restrict__ map_b, const Args& a,
+                                           int vs0) {
+  return decoded_state(map_b, a.var_off, __ldg(a.var_of_vs + vs0));
+}
+
+__device__ __forceinline__ void energy_item(const Args& a, const SegDev& sg, int64_t i,
+                                            const int32_t* __restrict__ map_b,
+                                            const float* __restrict__ ev_b,
+                                            const float* __restrict__ lp_b, double& u, double& e,
+                                            long long& cnt, int& flags) {
+  switch (sg.kind) {
+    case kEnergyVars: {
+      const int v = (int)i;
+      const int vs0 = __ldg(a.var_off + v), k = __ldg(a.var_off + v + 1) - vs0;
+      const int s = decoded_state(map_b, a.var_off, v);
+      for (int t = 0; t < k; ++t) u += (t == s ? 1.0 : 0.0) * (double)ev_b[vs0 + t];
+      break;
+    }
+    case kEnergyPairwise: {
+      const int4 r = __ldg(static_cast<const int4*>(sg.p0) + i);
+      const int sa = state_of_vs(map_b, a, r.z), sb = state_of_vs(map_b, a, r.w);
+      if (sa >= 0 && sb >= 0) {
+        ++cnt;
+        e += (double)lp_b[__ldg(static_cast<const int32_t*>(sg.p1) + i) + sa * sg.b + sb];
+      }
+      break;
+    }
+    case kEnergyGeneric: {
+      const EnumGeneric& g = a.gen;
+      const int j0 = __ldg(g.edge_off + i), nv = __ldg(g.n_vars + i), nc = __ldg(g.n_cfg + i);
+      const int rb = __ldg(g.row_begin + i), cb = __ldg(g.cfg_begin + i);
+      bool any = true;
+      for (int t = 0; t < nv && any; ++t) any = state_of_vs(map_b, a, __ldg(g.edge_vs + j0 + t)) >= 0;
+      if (!any) break;  // a variable decodes no state: no config of the factor is decoded
+      for (int c = 0; c < nc; ++c) {
+        int est = 0;
+        bool ok = true;
+        for (int t = 0; t < nv; ++t) {
+          const int j = j0 + t;
+          const int s = state_of_vs(map_b, a, __ldg(g.edge_vs + j));
+          if (__ldg(g.row_les + rb + c * nv + t) != est + s) {
+            ok = false;
+            break;
+          }
+          est += __ldg(g.edge_size + j);
+        }
+        if (ok) {
+          ++cnt;
+          e += (double)lp_b[cb + c];
+        }
+      }
+      break;
+    }
+    case kEnergyLogical: {
+      const int32_t* pb = static_cast<const int32_t*>(sg.p0);
+      const int4* par = static_cast<const int4*>(sg.p1);
+      const int4* ch = static_cast<const int4*>(sg.p2);
+      const int r = sg.a;
+      bool all = true;
+      for (int q = __ldg(pb + i), q1 = __ldg(pb + i + 1); q < q1 && all; ++q)
+        all = state_of_vs(map_b, a, __ldg(par + q).z) == r;
+      const bool child = state_of_vs(map_b, a, __ldg(ch + i).z) == r;
+      if (all != child) flags |= r == 0 ? kFlagOr : kFlagAnd;
+      break;
+    }
+    case kEnergyPool: {
+      const int32_t* cbg = static_cast<const int32_t*>(sg.p0);
+      const int4* chs = static_cast<const int4*>(sg.p1);
+      const int4* ind = static_cast<const int4*>(sg.p2);
+      int on = 0;
+      for (int q = __ldg(cbg + i), q1 = __ldg(cbg + i + 1); q < q1; ++q)
+        on += state_of_vs(map_b, a, __ldg(chs + q).z) == 1;
+      const int ind_on = state_of_vs(map_b, a, __ldg(ind + i).z) == 1;
+      if (on != ind_on) flags |= kFlagPool;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+__device__ __forceinline__ void warp_reduce(double& u, double& e, long long& cnt, int& flags) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    u += __shfl_xor_sync(0xffffffffu, u, o);
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+  }
+}
+
+// grid (chunks of this launch, min(B, 65535)); partials [B][a.chunks].
+__global__ void __launch_bounds__(kEnergyThreads) energy_partial_kernel(Args a, Launch L,
+                                                                         int64_t first_chunk,
+                                                                         EnergyPartial* part) {
+  __shared__ double s_u[kEnergyThreads / 32], s_e[kEnergyThreads / 32];
+  __shared__ long long s_c[kEnergyThreads / 32];
+  __shared__ int s_f[kEnergyThreads / 32];
+  const int64_t chunk = first_chunk + blockIdx.x;
+  int si = 0;
+  while (si + 1 < L.nseg && L.seg[si + 1].chunk_begin <= chunk) ++si;
+  const SegDev sg = L.seg[si];
+  const int64_t i0 = (chunk - sg.chunk_begin) * kEnergyChunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t b = blockIdx.y; b < a.B; b += gridDim.y) {
+    const int32_t* map_b = a.map + b * a.ms;
+    const float* ev_b = a.ev ? a.ev + b * a.evs : nullptr;
+    const float* lp_b = a.lp ? a.lp + b * a.lps : nullptr;
+    double u = 0.0, e = 0.0;
+    long long cnt = 0;
+    int flags = 0;
+    for (int k = 0; k < kEnergyChunk / kEnergyThreads; ++k) {
+      const int64_t i = i0 + (int64_t)k * kEnergyThreads + threadIdx.x;
+      if (i < sg.items) energy_item(a, sg, i, map_b, ev_b, lp_b, u, e, cnt, flags);
+    }
+    warp_reduce(u, e, cnt, flags);
+    if (lane == 0) {
+      s_u[warp] = u;
+      s_e[warp] = e;
+      s_c[warp] = cnt;
+      s_f[warp] = flags;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < kEnergyThreads / 32; ++w) {
+        u += s_u[w];
+        e += s_e[w];
+        cnt += s_c[w];
+        flags |= s_f[w];
+      }
+      EnergyPartial r;
+      r.u = u;
+      r.e = e;
+      r.cnt = cnt;
+      r.flags = flags;
+      r.pad = 0;
+      part[b * a.chunks + chunk] = r;
+    }
+    __syncthreads();
+  }
+}
+
+// One warp per instance: adds its partials (lane c, c + 32, ... then a fixed butterfly) and
+// combines the terms in the reference's order.
+__global__ void energy_final_kernel(const EnergyPartial* __restrict__ part, int64_t chunks,
+                                    int64_t B, long long num_enum, int present, float* out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (b >= B) return;
+  double u = 0.0, e = 0.0;
+  long long cnt = 0;
+  int flags = 0;
+  for (int64_t c = lane; c < chunks; c += 32) {
+    const EnergyPartial r = part[b * chunks + c];
+    u += r.u;
+    e += r.e;
+    cnt += r.cnt;
+    flags |= r.flags;
+  }
+  warp_reduce(u, e, cnt, flags);
+  if (lane != 0) return;
+  double en = -u;
+  if (present & 1) en += cnt != num_enum ? (double)INFINITY : -e;
+  if (present & 2) en += (flags & kFlagOr) ? (double)INFINITY : 0.0;
+  if (present & 4) en += (flags & kFlagAnd) ? (double)INFINITY : 0.0;
+  if (present & 8) en += (flags & kFlagPool) ? (double)INFINITY : 0.0;
+  out[b] = (float)en;
+}
+
+int64_t chunks_of(int64_t items) { return (items + kEnergyChunk - 1) / kEnergyChunk; }
+
+}  // namespace
+
+void energy_plan(Plan& p) {
+  p.energy_segs.clear();
+  int64_t c = 0;
+  auto add = [&](int kind, int param, int64_t items) {
+    if (items <= 0) return;
+    EnergySeg s;
+    s.kind = kind;
+    s.param = param;
+    s.items = items;
+    s.chunk_begin = c;
+    c += chunks_of(items);
+    p.energy_segs.push_back(s);
+  };
+  add(kEnergyVars, 0, p.num_variables);
+  for (size_t q = 0; q < p.pairwise.size(); ++q) add(kEnergyPairwise, (int)q, p.pairwise[q].count);
+  add(kEnergyGeneric, 0, p.enum_generic.count);
+  add(kEnergyLogical, 0, p.logical[0].count);
+  add(kEnergyLogical, 1, p.logical[1].count);
+  add(kEnergyPool, 0, p.pool.count);
+  p.energy_chunks = c;
+}
+
+size_t energy_workspace_bytes(const Plan& p, int64_t B) {
+  return (size_t)std::max<int64_t>(1, B * p.energy_chunks) * sizeof(EnergyPartial);
+}
+
+cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                   const float* ev, int64_t ev_stride, const int32_t* map, int64_t map_stride,
+                   float* out, void* ws, size_t ws_bytes) {
+  (void)ws_bytes;
+  ProfileScope ps(kProfReadout, s);
+  EnergyPartial* part = static_cast<EnergyPartial*>(ws);
+  Args a;
+  a.var_off = p.var_off;
+  a.var_of_vs = p.var_of_vs;
+  a.lp = lp;
+  a.lps = lp_stride;
+  a.ev = ev;
+  a.evs = ev_stride;
+  a.map = map;
+  a.ms = map_stride;
+  a.B = B;
+  a.chunks = p.energy_chunks;
+  a.gen = p.enum_generic;
+  const unsigned gy = (unsigned)std::min<int64_t>(B, 65535);
+  for (size_t s0 = 0; s0 < p.energy_segs.size(); s0 += kMaxSegsPerLaunch) {
+    Launch L;
+    L.nseg = (int)std::min<size_t>(kMaxSegsPerLaunch, p.energy_segs.size() - s0);
+    for (int k = 0; k < L.nseg; ++k) {
+      const EnergySeg& es = p.energy_segs[s0 + k];
+      SegDev& d = L.seg[k];
+      d = SegDev{};
+      d.kind = es.kind;
+      d.items = es.items;
+      d.chunk_begin = es.chunk_begin;
+      switch (es.kind) {
+        case kEnergyPairwise: {
+          const PairwiseBucket& q = p.pairwise[(size_t)es.param];
+          d.a = q.n1;
+          d.b = q.n2;
+          d.p0 = q.rec;
+          d.p1 = q.cfg_begin;
+          break;
+        }
+        case kEnergyLogical: {
+          const LogicalSet& g = p.logical[es.param];
+          d.a = g.off == 1 ? 0 : 1;  // the relevant state: 0 for OR, 1 for AND
+          d.p0 = g.par_begin;
+          d.p1 = g.par;
+          d.p2 = g.child;
+          break;
+        }
+        case kEnergyPool:
+          d.p0 = p.pool.ch_begin;
+          d.p1 = p.pool.ch;
+          d.p2 = p.pool.ind;
+          break;
+        default:
+          break;
+      }
+    }
+    const EnergySeg& last = p.energy_segs[s0 + L.nseg - 1];
+    const int64_t first = p.energy_segs[s0].chunk_begin;
+    const int64_t n = last.chunk_begin + chunks_of(last.items) - first;
+    energy_partial_kernel<<<dim3((unsigned)n, gy), kEnergyThreads, 0, s>>>(a, L, first, part);
+  }
+  const int present = (p.num_enum_factors > 0 ? 1 : 0) | (p.logical[0].count > 0 ? 2 : 0) |
+                      (p.logical[1].count > 0 ? 4 : 0) | (p.pool.count > 0 ? 8 : 0);
+  const int64_t threads = B * 32;
+  energy_final_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+      part, p.energy_chunks, B, (long long)p.num_enum_factors, present, out);
+  return cudaGetLastError();
+}
+
+}  // namespace pgbp

@@ -111,6 +111,16 @@ struct VarsumSet {
   int32_t* byvar_eslot = nullptr; // first slot of each edge, edge order
 };
 
+// Energy of a decoding (pgbp_energy): the launch walks work segments of items, each chunk of
+// kEnergyChunk items one CTA. Kinds: variables (the evidence term), one dense pairwise bucket
+// (param = bucket index), the generic Enum factors, OR (param 0) / AND (param 1) factors, Pool
+// factors.
+enum EnergyKind { kEnergyVars = 0, kEnergyPairwise, kEnergyGeneric, kEnergyLogical, kEnergyPool };
+struct EnergySeg {
+  int kind = 0, param = 0;
+  int64_t items = 0, chunk_begin = 0;
+};
+
 struct Plan {
   int device = 0;
   int sm_count = 0;
@@ -126,6 +136,9 @@ struct Plan {
   int32_t* edge_start = nullptr;    // [num_edges + 1] first edge state of each edge
   int32_t* edge_slot = nullptr;     // [num_edges + 1] first slot of each edge
   int32_t* var_off = nullptr;       // [num_variables + 1] (decode / marginals), may be null
+  int32_t* var_of_vs = nullptr;     // [num_var_states] evidence_to_vars (energy), may be null
+  std::vector<EnergySeg> energy_segs;
+  int64_t energy_chunks = 0;
   VarsumSet varsum_binary, varsum_other;
   std::vector<PairwiseBucket> pairwise;
   EnumGeneric enum_generic;
@@ -215,6 +228,13 @@ cudaError_t run_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, i
                     size_t ws_bytes);
 cudaError_t beliefs_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* g_beliefs,
                         int64_t gb_stride, float* g_msgs);
+
+// Energy of decodings (pgbp_energy.cu). energy_plan fills p.energy_segs / p.energy_chunks.
+void energy_plan(Plan& p);
+size_t energy_workspace_bytes(const Plan& p, int64_t B);
+cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                   const float* ev, int64_t ev_stride, const int32_t* map, int64_t map_stride,
+                   float* out, void* ws, size_t ws_bytes);
 
 }  // namespace pgbp
 

@@ -712,8 +712,10 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     voff[nv] = (int32_t)nvs;
     p.num_variables = nv;
     p.var_off = bd.upload(voff);
+    p.var_of_vs = bd.upload(std::vector<int32_t>(d->evidence_to_vars, d->evidence_to_vars + nvs));
     if (bd.err) return bail(bd.err);
   }
+  pgbp::energy_plan(p);
 
   p.flags = d->flags;
   ce = pgbp::prepare_small_graph(p);
@@ -970,6 +972,39 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
   if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
   e = pgbp::decode(p, static_cast<cudaStream_t>(stream), batch, beliefs, beliefs_stride, map);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_decode launch");
+  return PGBP_OK;
+}
+
+size_t pgbp_energy_workspace_size(const pgbp_plan* plan, int64_t batch) {
+  if (!plan || batch <= 0) return 0;
+  return pgbp::energy_workspace_bytes(plan->p, batch);
+}
+
+int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
+                int64_t lp_stride, const float* evidence, int64_t ev_stride, const int32_t* map,
+                int64_t map_stride, float* energy, void* workspace, size_t workspace_bytes) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (!p.var_of_vs) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
+  if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
+  if (lp_stride < 0 || ev_stride < 0 || map_stride < 0 ||
+      (lp_stride != 0 && lp_stride < p.num_potentials) ||
+      (ev_stride != 0 && ev_stride < p.num_var_states) ||
+      (map_stride != 0 && map_stride < p.num_variables))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad stride");
+  if (!map || !energy || (p.num_var_states > 0 && !evidence) ||
+      (p.num_enum_factors > 0 && !log_potentials))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  const size_t need = pgbp::energy_workspace_bytes(p, batch);
+  if (!workspace || workspace_bytes < need)
+    return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+    return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::energy(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
+                   ev_stride, map, map_stride, energy, workspace, workspace_bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_energy launch");
   return PGBP_OK;
 }
 

@@ -308,6 +308,35 @@ class Plan:
                                       out.data_ptr()), "pgbp_decode")
     return out if b.ndim == 2 else out[0]
 
+  def energy(self, log_potentials, evidence, map_states):
+    """Energies of decodings (pgbp_energy): map_states [num_variables] or [B, num_variables]
+    (int), log_potentials / evidence [n] or [B, n] as BPArrays hold them. Returns float32 [B]
+    (or a 0-d tensor when nothing is batched)."""
+    torch = _torch()
+    m = self._dev(map_states, torch.int32)
+    lp = self._dev(log_potentials) if log_potentials is not None else None
+    ev = self._dev(evidence)
+    nvars = int(self.info["num_variables"])
+    m_t, b1, mst = self._rows(m, nvars)
+    ev_t, b2, evs = self._rows(ev, self.num_var_states)
+    if lp is not None:
+      lp_t, b3, lps = self._rows(lp, self.num_potentials)
+    else:
+      lp_t, b3, lps = None, 1, 0
+    batched = [t.ndim == 2 for t in (m, ev) + ((lp,) if lp is not None else ())]
+    sizes = {b for b, bt in zip((b1, b2, b3), batched) if bt}
+    if len(sizes) > 1:
+      raise ValueError(f"batch sizes differ: {sorted(sizes)}")
+    B = sizes.pop() if sizes else 1
+    out = torch.empty(B, dtype=torch.float32, device=ev.device)
+    nb = int(self.lib.pgbp_energy_workspace_size(self.handle, B))
+    ws = torch.empty(max(nb, 1), dtype=torch.uint8, device=ev.device)
+    native.check(self.lib.pgbp_energy(
+        self.handle, self._stream(), B, lp_t.data_ptr() if lp_t is not None else None, lps,
+        ev_t.data_ptr(), evs, m_t.data_ptr(), mst, out.data_ptr(), ws.data_ptr(), nb),
+        "pgbp_energy")
+    return out if any(batched) else out[0]
+
   def marginals(self, flat_beliefs):
     torch = _torch()
     b = self._dev(flat_beliefs)

@@ -2,6 +2,7 @@
 
 from .bp import BP, BeliefPropagation, get_marginals
 from .bp_state import BPArrays, BPState, Evidence, FToVMessages, LogPotentials
+from .energy import compute_energy
 from .inferer import Inferer, InfererContext, decode_map_states
 
 

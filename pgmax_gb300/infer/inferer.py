@@ -19,6 +19,18 @@ from .bp_state import BPArrays, BPState, Evidence, FToVMessages, LogPotentials
 TYPE_KEYS = ("enum", "or", "and", "pool")
 
 
+
+def registered_context(fg_state):
+  """The first context of `fg_state` that compiled a plan (kept on the FactorGraphState), or
+  None: functions that take only a BPState (compute_energy) reuse its plan."""
+  return getattr(fg_state, "_pgbp_context", None)
+
+
+def register_context(ctx):
+  if registered_context(ctx.bp_state.fg_state) is None:
+    object.__setattr__(ctx.bp_state.fg_state, "_pgbp_context", ctx)
+
+
 def _is_torch(x):
   return type(x).__module__.startswith("torch")
 
@@ -101,6 +113,7 @@ class InfererContext:
       object.__setattr__(self, "_plan", engine.Plan(self.flat_wiring(), flags=self.exec_flags))
       for t in FAC_TO_VAR_UPDATES:
         self.inference_arguments[t]["plan"] = self._plan
+      register_context(self)
     return self._plan
 
   # ------------------------------------------------------------------------- state

@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libpgbp.so")
 
 SOURCES = ["pgbp_kernels.cu", "pgbp_plan.cpp", "pgbp_static_scratch.cu", "pgbp_adjoint.cu",
-           "pgbp_expgemm.cu", "pgbp_conv.cu"]
+           "pgbp_expgemm.cu", "pgbp_conv.cu", "pgbp_energy.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every float32 op rounds as the reference's does.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -148,6 +148,9 @@ SIGNATURES = [
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
     ("pgbp_decode", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_marginals", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
+    ("pgbp_energy_workspace_size", ctypes.c_size_t, [_p, _i64]),
+    ("pgbp_energy", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p,
+                                   ctypes.c_size_t]),
     # include/pgbp_learn.h
     ("pgbp_conv3x3", ctypes.c_int, [_p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, _p, _p, _p, _p, ctypes.c_int, ctypes.c_int, _p]),

@@ -11,7 +11,12 @@ FIXTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "f
 
 def run_fixture_paths():
   return sorted(p for p in glob.glob(os.path.join(FIXTURES, "*.npz"))
-                if not os.path.basename(p).startswith("factor_updates"))
+                if not os.path.basename(p).startswith(("factor_updates", "energy_")))
+
+
+def energy_fixture_paths():
+  """compute_energy calls of the reference: wiring, log_potentials, evidence, map_flat, energy."""
+  return sorted(glob.glob(os.path.join(FIXTURES, "energy_*.npz")))
 
 
 def load(path):

@@ -143,15 +143,22 @@ def deconv(api, n_feat=2, feat=3, im=6, seed=0, flip=0.05):
   return fg, [S, W, SW, X], ev
 
 
-def mixed(api, seed=0):
-  """Enum (pairwise + ternary tables), OR, AND and Pool factors sharing variables."""
+def mixed(api, seed=0, vardict=True):
+  """Enum (pairwise + ternary tables), OR, AND and Pool factors sharing variables. With
+  vardict=False the five 3-state variables are an NDVarArray instead of a VarDict (the reference's
+  compute_energy takes NDVarArrays only); the graph and the random draws are otherwise the same."""
   rng = np.random.RandomState(seed)
   nb = 24
   binary = api.vgroup.NDVarArray(num_states=2, shape=(nb,))
   ns = np.array([3, 4, 2, 3, 4, 3], dtype=np.int64)
   multi = api.vgroup.NDVarArray(num_states=ns, shape=(len(ns),))
   names = tuple(f"d{i}" for i in range(5))
-  vdict = api.vgroup.VarDict(variable_names=names, num_states=3)
+  if vardict:
+    vdict = api.vgroup.VarDict(variable_names=names, num_states=3)
+    third = lambda i: vdict[names[i]]
+  else:
+    vdict = api.vgroup.NDVarArray(num_states=3, shape=(len(names),))
+    third = lambda i: vdict[i]
   fg = api.fgraph.FactorGraph(variable_groups=[binary, multi, vdict])
 
   # Pairwise EnumFactors with per-factor tables between multi-state variables.
@@ -164,8 +171,7 @@ def mixed(api, seed=0):
   configs = np.array([c for c in itertools.product(range(3), repeat=3) if sum(c) % 2 == 0])
   fg.add_factors(
       api.fgroup.EnumFactorGroup(
-          variables_for_factors=[[vdict[names[i]], vdict[names[i + 1]], vdict[names[i + 2]]]
-                                 for i in range(3)],
+          variables_for_factors=[[third(i), third(i + 1), third(i + 2)] for i in range(3)],
           factor_configs=configs,
           log_potentials=rng.normal(size=(3, configs.shape[0])),
       )
@@ -173,7 +179,7 @@ def mixed(api, seed=0):
   # Single EnumFactor linking a binary variable and a VarDict variable.
   fg.add_factors(
       api.factor.EnumFactor(
-          variables=[binary[0], vdict[names[4]]],
+          variables=[binary[0], third(4)],
           factor_configs=np.array([[0, 0], [1, 1], [1, 2]]),
           log_potentials=rng.normal(size=(3,)),
       )
@@ -192,8 +198,8 @@ def mixed(api, seed=0):
       binary: rng.gumbel(size=(nb, 2)),
       multi: np.where(np.arange(4)[None] < ns[:, None], rng.gumbel(size=(len(ns), 4)), 0.0),
   }
-  for name in names:
-    ev[vdict[name]] = rng.gumbel(size=(3,))
+  for i in range(len(names)):
+    ev[third(i)] = rng.gumbel(size=(3,))
   return fg, [binary, multi, vdict], ev
 
 
@@ -205,6 +211,47 @@ def mixed_ftov_updates(api, variable_groups, seed=0):
     for var in vg.variables:
       updates[var] = rng.normal(size=(int(var[1]),))
   return updates
+
+
+def repair_decoding(w, m):
+  """Sets OR / AND children and Pool indicators (and surplus Pool choices) so that a decoding
+  satisfies every logical and Pool factor of the flat wiring `w`."""
+  m = np.array(m, dtype=np.int64)
+  e2v = np.asarray(w["evidence_to_vars"], np.int64)
+  vs_of_es = np.asarray(w["var_states_for_edge_states"], np.int64)
+  mr = np.asarray(w["msgs_ranges"], np.int64)
+  var = lambda es: int(e2v[vs_of_es[es]])
+  for _ in range(32):
+    changed = False
+    for t, name, r in ((1, "or", 0), (2, "and", 1)):
+      m0 = mr[t][0]
+      if mr[t][1] <= m0:
+        continue
+      pfi = np.asarray(w[f"{name}.parents_factor_indices"])
+      pmi = np.asarray(w[f"{name}.parents_msg_indices"])
+      ch = np.asarray(w[f"{name}.children_edge_states"])
+      for f in range(ch.shape[0]):
+        all_r = all(m[var(m0 + e)] == r for e in pmi[pfi == f])
+        c = var(m0 + ch[f])
+        want = r if all_r else 1 - r
+        if m[c] != want:
+          m[c], changed = want, True
+    m0 = mr[3][0]
+    if mr[3][1] > m0:
+      cfi = np.asarray(w["pool.pool_choices_factor_indices"])
+      cmi = np.asarray(w["pool.pool_choices_msg_indices"])
+      ind = np.asarray(w["pool.pool_indicators_edge_states"])
+      for f in range(ind.shape[0]):
+        on = [var(m0 + e) for e in cmi[cfi == f] if m[var(m0 + e)] == 1]
+        for v in on[1:]:
+          m[v], changed = 0, True
+        i = var(m0 + ind[f])
+        want = 1 if on else 0
+        if m[i] != want:
+          m[i], changed = want, True
+    if not changed:
+      break
+  return m.astype(np.int32)
 
 
 BUILDERS = {

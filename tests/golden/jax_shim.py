@@ -10,7 +10,8 @@ Semantics reproduced (JAX with `jax_enable_x64` off, the PGMax default):
     `jnp.*` call, at `jax.device_put` and at `jax.jit` boundaries;
   * `x.at[idx].add/max/min/multiply/set` are functional scatters. `add`, `max`, `min` and
     `multiply` apply updates serially in index order (`np.ufunc.at`), which is the order XLA:CPU's
-    scatter loop uses; out-of-range indices are dropped (JAX's default scatter mode);
+    scatter loop uses; out-of-range indices (on any axis of a tuple of integer index arrays,
+    after one negative wrap) are dropped (JAX's default scatter mode);
   * `jax.jit`, `jax.checkpoint` and `numba.jit` are identity decorators; `jax.lax.scan` is a loop;
   * `jax.tree_util` handles dicts, lists, tuples, None and classes registered with
     `register_pytree_node_class`.
@@ -90,7 +91,23 @@ class _AtRef:
         n = out.shape[0]
         keep = (idx < n) & (idx >= -n)
         return out, idx, keep
+    if isinstance(idx, tuple) and idx and all(
+        isinstance(i, (np.ndarray, int, np.integer)) and np.issubdtype(np.asarray(i).dtype, np.integer)
+        for i in idx):
+      # advanced indexing with integer arrays on the leading axes: an update whose index is out of
+      # range on any axis (after one negative wrap) is dropped
+      parts = np.broadcast_arrays(*[np.asarray(i).view(np.ndarray) for i in idx])
+      keep = np.ones(parts[0].shape, dtype=bool)
+      for a, n in zip(parts, out.shape):
+        keep &= (a < n) & (a >= -n)
+      return out, tuple(parts), keep
     return out, idx, None
+
+  @staticmethod
+  def _select(idx, keep):
+    if isinstance(idx, tuple):
+      return tuple(a[keep] for a in idx)
+    return idx[keep]
 
   def _apply(self, ufunc, values):
     out, idx, keep = self._prep()
@@ -98,9 +115,9 @@ class _AtRef:
     if isinstance(vals, np.ndarray):
       vals = vals.astype(out.dtype, copy=False)
     if keep is not None and not keep.all():
-      idx = idx[keep]
       if isinstance(vals, np.ndarray) and vals.ndim > 0:
-        vals = vals[keep]
+        vals = np.broadcast_to(vals, keep.shape)[keep]
+      idx = self._select(idx, keep)
     ufunc.at(out, idx, vals)
     return out.view(Arr)
 
@@ -120,9 +137,9 @@ class _AtRef:
     out, idx, keep = self._prep()
     vals = _canon_in(values)
     if keep is not None and not keep.all():
-      idx = idx[keep]
       if isinstance(vals, np.ndarray) and vals.ndim > 0:
-        vals = vals[keep]
+        vals = np.broadcast_to(vals, keep.shape)[keep]
+      idx = self._select(idx, keep)
     out[idx] = vals
     return out.view(Arr)
 

@@ -15,7 +15,14 @@ the MAP decode). Two sources of runs are captured:
      deconvolution, a mixed Enum/OR/AND/Pool graph), which the tests rebuild with pgmax_gb300 to
      check that the host-side wiring is identical.
 It also records single factor-update calls (`FAC_TO_VAR_UPDATES[type](...)`, normalize True and
-False, several temperatures) on the mixed graph.
+False, several temperatures) on the mixed graph, and every `infer.compute_energy` call
+(pgmax/infer/energy.py:53-148, debug_mode=False) made by the reference's energy, OR, AND and Pool
+tests and by `energy_cases` (BP decodings, random decodings, random decodings repaired to satisfy
+the OR / AND / Pool factors, out-of-range and negative states, infinite evidence) as
+`energy_*.npz`: the flat wiring, the BPArrays' log potentials and evidence, the decoding (a state
+per variable, evidence_to_vars order) and the reference's energy.
+
+`--energy-only` regenerates the energy fixtures alone and leaves the others untouched.
 """
 
 import argparse
@@ -69,6 +76,7 @@ class Recorder:
 
   def __init__(self):
     self.runs = []
+    self.energies = []
     self.allclose_args = []
     self.current = "unnamed"
     self.meta = {}
@@ -144,6 +152,115 @@ def install_capture(pgmax):
   jnp.allclose = allclose
 
 
+def flat_map(groups, map_states):
+  """A decoding dict {VarGroup: states} as one state per variable, variable-group order."""
+  out = []
+  for vg in groups:
+    m = map_states[vg]
+    if isinstance(m, dict):
+      out += [int(np.asarray(m[n]).reshape(-1)[0]) for n in vg.variable_names]
+    else:
+      out += list(np.asarray(m).reshape(-1).astype(np.int64))
+  return np.array(out, dtype=np.int32)
+
+
+def unflat_map(groups, flat):
+  """Inverse of flat_map for NDVarArray groups."""
+  out, k = {}, 0
+  for vg in groups:
+    n = int(np.prod(vg.shape))
+    out[vg] = np.asarray(flat[k:k + n], dtype=np.int32).reshape(vg.shape)
+    k += n
+  return out
+
+
+def install_energy_capture():
+  """Wraps pgmax.infer.compute_energy so that every non-debug call is recorded."""
+  energy_mod = importlib.import_module("pgmax.infer.energy")
+  inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  orig = energy_mod.compute_energy
+
+  def compute_energy(bp_state, bp_arrays, map_states, debug_mode=False):
+    res = orig(bp_state, bp_arrays, map_states, debug_mode)
+    if not debug_mode:
+      ctx = inferer_mod.InfererContext(bp_state)
+      REC.energies.append({
+          "source": REC.current,
+          "meta": dict(REC.meta),
+          "wiring": wiring_arrays(ctx, bp_state.fg_state),
+          "log_potentials": _np(bp_arrays.log_potentials, np.float32),
+          "evidence": _np(bp_arrays.evidence, np.float32),
+          "map_flat": flat_map(bp_state.fg_state.variable_groups, map_states),
+          "energy": np.float32(np.asarray(res[0])),
+      })
+    return res
+
+  energy_mod.compute_energy = compute_energy
+  importlib.import_module("pgmax.infer").compute_energy = compute_energy
+
+
+def energy_cases(api):
+  """compute_energy on the seeded graphs of cases.py for several kinds of decodings."""
+  sys.path.insert(0, HERE)
+  import cases  # pylint: disable=g-import-not-at-top
+  inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  plans = [
+      ("ising12", "ising", dict(n=12, seed=3), dict(num_iters=50, temperature=0.0)),
+      ("rbm", "rbm", dict(nh=20, nv=30, seed=0, sample=0), dict(num_iters=30, temperature=0.0)),
+      ("potts_K4", "potts", dict(L=6, K=4, seed=1), dict(num_iters=20, temperature=0.0)),
+      ("deconv", "deconv", dict(seed=0), dict(num_iters=40, temperature=0.0)),
+      ("mixed0", "mixed", dict(seed=0, vardict=False), dict(num_iters=7, temperature=0.0)),
+      ("mixed1", "mixed", dict(seed=1, vardict=False), dict(num_iters=7, temperature=1.0)),
+  ]
+  for name, builder, bkw, rkw in plans:
+    fg, groups, ev = cases.BUILDERS[builder](api, **bkw)
+    bp = api.infer.BP(fg.bp_state, temperature=rkw["temperature"])
+    bp_arrays = bp.run(bp.init(evidence_updates=ev), num_iters=rkw["num_iters"])
+    decoded = api.infer.decode_map_states(bp.get_beliefs(bp_arrays))
+    flat = flat_map(groups, decoded)
+    w = wiring_arrays(inferer_mod.InfererContext(fg.bp_state), fg.bp_state.fg_state)
+    nstates = np.bincount(np.asarray(w["evidence_to_vars"], np.int64))
+    rng = np.random.default_rng(len(name) * 1000 + bkw.get("seed", 0))
+    decodings = [("decode", flat)]
+    for k in range(3):
+      rand = (rng.random(flat.shape[0]) * nstates).astype(np.int32)
+      decodings.append((f"random{k}", rand))
+      decodings.append((f"repaired{k}", cases.repair_decoding(w, rand)))
+    bad = flat.copy()
+    bad[flat.shape[0] // 2] = nstates[flat.shape[0] // 2]
+    decodings.append(("out_of_range", bad))
+    neg = cases.repair_decoding(w, flat)
+    neg[::7] -= nstates[::7]
+    decodings.append(("negative", neg))
+    for kind, m in decodings:
+      REC.current = f"energy_case::{name}::{kind}"
+      REC.meta = {"case": name, "builder": builder, "builder_kwargs": bkw, "kind": kind}
+      api.infer.compute_energy(fg.bp_state, bp_arrays, unflat_map(groups, m))
+    # infinite evidence on a state that the decoding does not pick: 0 * inf is nan
+    g0 = groups[0]
+    ev_inf = np.zeros(tuple(g0.shape) + (int(np.max(g0.num_states)),), np.float32)
+    ev_inf[(0,) * len(g0.shape) + (1,)] = -np.inf
+    arrays_inf = bp.update(bp_arrays=bp_arrays, evidence_updates={g0: ev_inf})
+    m = flat.copy()
+    m[0] = 0
+    REC.current = f"energy_case::{name}::evidence_inf"
+    REC.meta = {"case": name, "builder": builder, "builder_kwargs": bkw, "kind": "evidence_inf"}
+    api.infer.compute_energy(fg.bp_state, arrays_inf, unflat_map(groups, m))
+
+
+def save_energies():
+  counts = {}
+  for rec in REC.energies:
+    src = rec["source"].replace("::", "__").replace(".", "_")
+    counts[src] = counts.get(src, 0) + 1
+    arrays = {"w." + k: v for k, v in rec["wiring"].items()}
+    for k in ("log_potentials", "evidence", "map_flat", "energy"):
+      arrays[k] = rec[k]
+    arrays["meta"] = np.array(json.dumps({"source": rec["source"], **rec["meta"]}))
+    np.savez_compressed(os.path.join(OUT, f"energy_{src}_{counts[src]:02d}.npz"), **arrays)
+  return len(REC.energies)
+
+
 def save_run(path, run, extra=None):
   arrays = {}
   for k, v in run["wiring"].items():
@@ -158,10 +275,10 @@ def save_run(path, run, extra=None):
   np.savez_compressed(path, **arrays)
 
 
-def run_reference_tests(ref):
+def run_reference_tests(ref, modules=None):
   """Runs selected reference test functions unmodified; returns {name: error or None}."""
   status = {}
-  modules = {
+  modules = modules or {
       "test_pgmax": ["test_e2e_sanity_check", "test_e2e_heretic"],
       "test_clipping": None,
       "factor.test_or": None,
@@ -264,6 +381,7 @@ def factor_update_fixtures(api):
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument("--reference", default=os.environ.get("PGMAX_REFERENCE", "/root/reference"))
+  ap.add_argument("--energy-only", action="store_true")
   args = ap.parse_args()
   sys.path.insert(0, HERE)
   import jax_shim  # pylint: disable=g-import-not-at-top
@@ -272,9 +390,21 @@ def main():
   import pgmax  # pylint: disable=g-import-not-at-top
   from pgmax import factor, fgraph, fgroup, infer, vgroup  # pylint: disable=g-import-not-at-top
   install_capture(pgmax)
+  install_energy_capture()
   api = types.SimpleNamespace(factor=factor, fgraph=fgraph, fgroup=fgroup, infer=infer,
                               vgroup=vgroup)
   os.makedirs(OUT, exist_ok=True)
+  energy_tests = {"test_energy": None, "factor.test_or": None, "factor.test_and": None,
+                  "factor.test_pool": None}
+  if args.energy_only:
+    for f in os.listdir(OUT):
+      if f.startswith("energy_") and f.endswith(".npz"):
+        os.remove(os.path.join(OUT, f))
+    status = run_reference_tests(args.reference, energy_tests)
+    energy_cases(api)
+    n = save_energies()
+    print(json.dumps({"energy_reference_tests": status, "energy_fixtures": n}, indent=1))
+    return
   for f in os.listdir(OUT):
     if f.endswith(".npz"):
       os.remove(os.path.join(OUT, f))
@@ -283,6 +413,10 @@ def main():
   n_ref = len(REC.runs)
   run_cases(api)
   factor_update_fixtures(api)
+  REC.energies = [r for r in REC.energies if r["source"].startswith("factor.")]
+  status.update(run_reference_tests(args.reference, {"test_energy": None}))
+  energy_cases(api)
+  save_energies()
 
   # Golden vector of tests/test_pgmax.py: the (messages, expected) pair of its allclose call.
   golden = [a for a in REC.allclose_args if a[0] == "test_pgmax::test_e2e_sanity_check"]
