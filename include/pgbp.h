@@ -15,6 +15,8 @@
  *   pgbp_decode         decode_map_states                        pgmax/infer/inferer.py:251-264
  *   pgbp_marginals      get_marginals                            pgmax/infer/bp.py:263-288
  *   pgbp_energy         compute_energy                           pgmax/infer/energy.py:53-148
+ *   pgbp_sdlp_run       SDLP(...).run_with_objvals               pgmax/infer/dual_lp.py:238-313
+ *   pgbp_sdlp_objective smooth_dual_objval_and_grad / get_bp_updates  dual_lp.py:65-236, 419-448
  *
  * Conventions
  *   - Every call returns PGBP_OK (0) or an error code; nothing aborts or traps.
@@ -82,7 +84,7 @@ typedef struct {
   int64_t pool_num_factors;
   const int32_t* pool_indicators_edge_states;
   /* Variables: evidence_to_vars (FactorGraphState.evidence_to_vars, fgraph.py:317-326), needed
-   * only by pgbp_decode / pgbp_marginals / pgbp_energy; may be NULL. */
+   * only by pgbp_decode / pgbp_marginals / pgbp_energy / pgbp_sdlp_*; may be NULL. */
   int64_t num_variables;
   const int32_t* evidence_to_vars;             /* [num_var_states] */
   /* Execution options, 0 = automatic. Three execution paths exist: multi-kernel (one launch per
@@ -249,6 +251,36 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
 int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
                    int64_t beliefs_stride, float* marginals);
 
+/* Smooth dual LP-MAP solver (SDLP): pgmax.infer.SDLP (pgmax/infer/dual_lp.py:60-463), the dual of
+ * the LP relaxation of MAP smoothed by a log-sum-exp at temperature logsumexp_temp in [0, 1]
+ * (0: the non-smooth dual and its subgradient). Messages are the dual variables, [batch, E_s]
+ * rows msgs_stride floats apart (msgs_out contiguous); evidence and potentials as in pgbp_run.
+ * pgbp_sdlp_objective: smooth_dual_objval_and_grad (dual_lp.py:65-236) at msgs: objval [batch];
+ *   optionally the gradient grad [batch, E_s], the un-normalised factor updates at -msgs
+ *   bp_updates [batch, E_s] and the per-edge log-sum-exp (max at temperature 0) of
+ *   bp_updates - msgs, edge_lse [batch, num_edges] (get_bp_updates, dual_lp.py:419-448;
+ *   get_primal_upper_bound is objval at temperature 0).
+ * pgbp_sdlp_run: run_with_objvals (dual_lp.py:238-313): num_iters steps of accelerated gradient
+ *   descent (temperature > 0, learning rate lr <= temperature) or of subgradient descent with
+ *   step lr / sqrt(it + 1) (temperature 0); lr <= 0 takes the reference's default (the
+ *   temperature, or 0.01 at 0). objvals [batch, num_iters] (may be NULL): the objective before
+ *   each step. Objective sums are double, added in a fixed order.
+ * Workspace: pgbp_sdlp_workspace_size(plan, batch) bytes, 256-byte aligned, for both. Needs
+ * evidence_to_vars in the plan. */
+size_t pgbp_sdlp_workspace_size(const pgbp_plan* plan, int64_t batch);
+int pgbp_sdlp_objective(const pgbp_plan* plan, void* stream, int64_t batch,
+                        const float* log_potentials, int64_t lp_stride,
+                        const float* evidence, int64_t ev_stride,
+                        const float* msgs, int64_t msgs_stride, double logsumexp_temp,
+                        float* objval, float* grad, float* bp_updates, float* edge_lse,
+                        void* workspace, size_t workspace_bytes);
+int pgbp_sdlp_run(const pgbp_plan* plan, void* stream, int64_t batch,
+                  const float* log_potentials, int64_t lp_stride,
+                  const float* evidence, int64_t ev_stride,
+                  const float* msgs_in, int64_t msgs_stride, float* msgs_out, float* objvals,
+                  int64_t num_iters, double logsumexp_temp, double lr,
+                  void* workspace, size_t workspace_bytes);
+
 /* Energy of decodings, lower is better: pgmax.infer.compute_energy (pgmax/infer/energy.py:53-148,
  * debug_mode=False) for `batch` decodings at once. map [batch, num_variables] (map_stride ints
  * apart, 0 = one decoding for all) holds each variable's state as pgbp_decode writes it; a negative
@@ -274,7 +306,8 @@ int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch,
  * per-class launch counts and total device milliseconds, and clears the record. Classes:
  * 0 variable sums, 1 dense pairwise Enum, 2 generic Enum, 3 OR, 4 AND, 5 Pool,
  * 6 layout (transposes, potential clipping, initial normalisation, residual copy-out),
- * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals, pgbp_beliefs_vjp, pgbp_energy), 8 the
+ * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals, pgbp_beliefs_vjp, pgbp_energy, the
+ * SDLP per-variable and per-factor kernels; the SDLP factor passes count in classes 1-5), 8 the
  * one-CTA-per-instance small-graph kernel (all iterations in one launch), 9 the adjoint kernels of
  * pgbp_run_vjp (its forward recomputation is counted in the classes above). Process-wide, not
  * thread-safe. */

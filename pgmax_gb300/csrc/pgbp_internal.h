@@ -135,6 +135,8 @@ struct Plan {
   int32_t* vs_of_es = nullptr;      // [num_edge_states] var_states_for_edge_states (adjoint)
   int32_t* edge_start = nullptr;    // [num_edges + 1] first edge state of each edge
   int32_t* edge_slot = nullptr;     // [num_edges + 1] first slot of each edge
+  int64_t num_factors = 0;
+  int32_t* fac_edge_off = nullptr;  // [num_factors + 1] first edge of each factor (SDLP)
   int32_t* var_off = nullptr;       // [num_variables + 1] (decode / marginals), may be null
   int32_t* var_of_vs = nullptr;     // [num_var_states] evidence_to_vars (energy), may be null
   std::vector<EnergySeg> energy_segs;
@@ -228,6 +230,19 @@ cudaError_t run_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, i
                     size_t ws_bytes);
 cudaError_t beliefs_vjp(const Plan& p, cudaStream_t s, int64_t B, const float* g_beliefs,
                         int64_t gb_stride, float* g_msgs);
+
+// Smooth dual LP-MAP (SDLP, pgbp_kernels.cu). One objective evaluation (objval [B]; optional
+// gradient, raw factor updates [B][E_s] and per-edge logsumexp [B][num_edges]) or num_iters
+// accelerated (sub)gradient steps. Messages are [B][E_s] rows, ms floats apart.
+size_t sdlp_workspace_bytes(const Plan& p, int64_t B);
+cudaError_t sdlp_objective(const Plan& p, cudaStream_t s, int64_t B, const float* lp,
+                           int64_t lp_stride, const float* ev, int64_t ev_stride,
+                           const float* msgs, int64_t ms, double temperature, float* objval,
+                           float* grad, float* updates, float* edge_lse, void* ws);
+cudaError_t sdlp_run(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                     const float* ev, int64_t ev_stride, const float* msgs_in, int64_t ms,
+                     float* msgs_out, float* objvals, int64_t iters, double temperature, double lr,
+                     void* ws);
 
 // Energy of decodings (pgbp_energy.cu). energy_plan fills p.energy_segs / p.energy_chunks.
 void energy_plan(Plan& p);

@@ -2106,4 +2106,387 @@ cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* bel
   return cudaGetLastError();
 }
 
+// ============================================================================= SDLP
+// The smooth dual of the LP relaxation of MAP (pgmax/infer/dual_lp.py:60-463). One objective
+// evaluation (smooth_dual_objval_and_grad, dual_lp.py:65-236):
+//   var_sums = evidence.at[var_states_for_edge_states].add(ftov)
+//   per variable: softmax and T-logsumexp of var_sums (T = 0: last argmax indicator and max)
+//   bp = FAC_TO_VAR_UPDATES[type](-ftov, lp, T, normalize=False)            (the factor kernels)
+//   per edge: softmax and T-logsumexp of bp - ftov over its states (T = 0: -1 at the last argmax
+//   and the max); grad = softmax_var[var_states_for_edge_states] - softmax_edge
+//   objval = sum_variables lse + sum_factors max over the factor's edges of the edge lse
+// and one step of run_with_objvals (dual_lp.py:285-307):
+//   eta' = ftov - step * grad (step = lr, or lr / sqrt(it + 1) at T = 0)
+//   ftov' = eta' + (it + 1) / (it + 4) * (eta' - eta)
+// Layout during a run: every per-state array is [n][B] (the instance index fastest), so the
+// lanes of a warp, which run one unit for consecutive instances, read consecutive words; caller
+// arrays [B][n] are transposed once on entry and exit. The per-edge part runs in the store
+// epilogue of the factor kernels (the Sdlp access class): a step reads each message, eta and the
+// edge's variable softmax once and writes the message, eta and the edge's logsumexp once.
+// float32 throughout, operations in the reference's order (label scatters in index order); the
+// objective sums are double, reduced in a fixed order (per block over its unit lanes, then per
+// instance over the blocks).
+namespace {
+
+struct Sdlp {
+  const float* __restrict__ cur;   // dual messages [E_s][B]
+  const float* __restrict__ lp;
+  int64_t lps, lpb;                // potential k of instance b at lp[k * lps + b * lpb]
+  const float* __restrict__ svar;  // variable softmax (T > 0) / argmax indicator (T = 0) [N_vs][B]
+  float* __restrict__ lse;         // edge logsumexp (max at T = 0) at the edge's first slot [S][B]
+  float* __restrict__ nxt;         // step: next messages [E_s][B]; null = no step
+  float* __restrict__ eta;         // step: the sequence eta [E_s][B], in place
+  float* __restrict__ upd;         // optional: factor updates, caller layout [B][E_s]
+  float* __restrict__ grad;        // optional: gradient, caller layout [B][E_s]
+  int64_t B, n_es;
+  float t, step, coef;
+  bool t0;
+
+  __device__ __forceinline__ float pot(int64_t k, int64_t b) const {
+    return __ldg(lp + k * lps + b * lpb);
+  }
+
+  __device__ __forceinline__ void load(const EdgeRef& r, int k, int64_t b, float* old,
+                                       float* vt) const {
+    for (int i = 0; i < k; ++i) {
+      old[i] = cur[(r.es0 + i) * B + b];
+      vt[i] = -old[i];
+    }
+  }
+
+  template <class F>
+  __device__ __forceinline__ void store(const EdgeRef& r, int k, const float* old, F outv,
+                                        int64_t b, float&) const {
+    // softmax_and_logsumexps_with_temp / get_maxes_and_argmaxes (update_utils.py:26-131) over
+    // the edge's states of data = bp - ftov
+    float m = -INFINITY;
+    for (int i = 0; i < k; ++i) m = fmaxp(m, outv(i) - old[i]);
+    int arg = k - 1;  // the last state attaining the max (the last state when none does)
+    float sum = 0.0f;
+    if (t0) {
+      for (int i = 0; i < k; ++i) arg = (outv(i) - old[i] == m) ? i : arg;
+    } else {
+      for (int i = 0; i < k; ++i) sum = sum + t * expf((outv(i) - old[i] - m) / t);
+    }
+    lse[r.slot * B + b] = t0 ? m : m + t * logf(sum / t);
+    for (int i = 0; i < k; ++i) {
+      const int64_t at = (r.es0 + i) * B + b;
+      const float sv = svar[(r.vs0 + i) * B + b];
+      const float g = t0 ? sv + (i == arg ? -1.0f : 0.0f)
+                         : sv - (t * expf((outv(i) - old[i] - m) / t)) / sum;
+      if (upd != nullptr) upd[b * n_es + r.es0 + i] = outv(i);
+      if (grad != nullptr) grad[b * n_es + r.es0 + i] = g;
+      if (nxt != nullptr) {
+        const float e = old[i] - step * g;
+        nxt[at] = e + coef * (e - eta[at]);
+        eta[at] = e;
+      }
+    }
+  }
+};
+
+// Sums v (double) over the block's unit lanes in a fixed order; thread (tx, 0) gets the block's
+// total for instance lane tx.
+__device__ __forceinline__ double block_sum_units(double v) {
+  __shared__ double red[256];
+  const int tx = threadIdx.x, ty = threadIdx.y, bx = blockDim.x;
+  red[ty * bx + tx] = v;
+  __syncthreads();
+  for (int s = blockDim.y / 2; s > 0; s >>= 1) {
+    if (ty < s) red[ty * bx + tx] += red[(ty + s) * bx + tx];
+    __syncthreads();
+  }
+  const double r = red[tx];
+  __syncthreads();
+  return r;
+}
+
+// Per (variable, instance): the variable sums (evidence plus the messages of the state's edges in
+// edge order), their softmax and T-logsumexp (T = 0: indicator of the last argmax and the max).
+// The block's sum of the logsumexp goes to part[blockIdx.y][b].
+__global__ void __launch_bounds__(256) sdlp_var_kernel(
+    const int32_t* __restrict__ var_off, int64_t nv, const int32_t* __restrict__ vs_off,
+    const int32_t* __restrict__ vs_edges, const float* __restrict__ cur,
+    const float* __restrict__ ev, int64_t evs, int64_t evb, float* __restrict__ vsum,
+    float* __restrict__ svar, double* __restrict__ part, int64_t B, float t, bool t0) {
+  const Lane l = lane(B);
+  const int64_t b = l.b;
+  double acc = 0.0;
+  for (int64_t v = l.u0; l.valid && v < nv; v += l.ustep) {
+    const int64_t s0 = var_off[v], s1 = var_off[v + 1];
+    float m = -INFINITY;
+    for (int64_t s = s0; s < s1; ++s) {
+      float x = ev[s * evs + b * evb];
+      for (int32_t k = vs_off[s]; k < vs_off[s + 1]; ++k) x = x + cur[(int64_t)vs_edges[k] * B + b];
+      vsum[s * B + b] = x;
+      m = fmaxp(m, x);
+    }
+    float obj;
+    if (t0) {
+      int64_t arg = s1 - 1;
+      for (int64_t s = s0; s < s1; ++s) arg = vsum[s * B + b] == m ? s : arg;
+      for (int64_t s = s0; s < s1; ++s) svar[s * B + b] = s == arg ? 1.0f : 0.0f;
+      obj = m;
+    } else {
+      float sum = 0.0f;
+      for (int64_t s = s0; s < s1; ++s) sum = sum + t * expf((vsum[s * B + b] - m) / t);
+      for (int64_t s = s0; s < s1; ++s) svar[s * B + b] = (t * expf((vsum[s * B + b] - m) / t)) / sum;
+      obj = m + t * logf(sum / t);
+    }
+    acc += (double)obj;
+  }
+  const double tot = block_sum_units(acc);
+  if (threadIdx.y == 0 && l.valid) part[blockIdx.y * B + b] = tot;
+}
+
+// Per (factor, instance): the max over the factor's edges of the edge logsumexp (dual_lp.py:
+// 221-229, a scatter-max from -inf); the block's sum goes to part[blockIdx.y][b].
+__global__ void __launch_bounds__(256) sdlp_factor_kernel(
+    const int32_t* __restrict__ fac_edge_off, const int32_t* __restrict__ edge_slot, int64_t nf,
+    const float* __restrict__ lse, double* __restrict__ part, int64_t B) {
+  const Lane l = lane(B);
+  const int64_t b = l.b;
+  double acc = 0.0;
+  for (int64_t f = l.u0; l.valid && f < nf; f += l.ustep) {
+    float m = -INFINITY;
+    for (int32_t e = fac_edge_off[f]; e < fac_edge_off[f + 1]; ++e)
+      m = fmaxp(m, lse[(int64_t)edge_slot[e] * B + b]);
+    acc += (double)m;
+  }
+  const double tot = block_sum_units(acc);
+  if (threadIdx.y == 0 && l.valid) part[blockIdx.y * B + b] = tot;
+}
+
+// objval[b] = (sum of the variable partials) + (sum of the factor partials), in block order.
+__global__ void sdlp_objval_kernel(const double* __restrict__ pv, int64_t nv_blocks,
+                                   const double* __restrict__ pf, int64_t nf_blocks, int64_t B,
+                                   float* __restrict__ out, int64_t out_stride) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  double sv = 0.0, sf = 0.0;
+  for (int64_t i = 0; i < nv_blocks; ++i) sv += pv[i * B + b];
+  for (int64_t i = 0; i < nf_blocks; ++i) sf += pf[i * B + b];
+  out[b * out_stride] = (float)(sv + sf);
+}
+
+// dst[c][r] = src[r * src_stride + c] for r < rows, c < cols (32 x 32 tiles through shared memory).
+__global__ void transpose_kernel(const float* __restrict__ src, int64_t rows, int64_t cols,
+                                 int64_t src_stride, float* __restrict__ dst) {
+  __shared__ float tile[32][33];
+  const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int64_t r = r0 + j, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[j][threadIdx.x] = src[r * src_stride + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int64_t c = c0 + j, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[c * rows + r] = tile[threadIdx.x][j];
+  }
+}
+
+void transpose(cudaStream_t s, const float* src, int64_t rows, int64_t cols, int64_t src_stride,
+               float* dst) {
+  if (rows <= 0 || cols <= 0) return;
+  const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  transpose_kernel<<<grid, dim3(32, 8), 0, s>>>(src, rows, cols, src_stride, dst);
+}
+
+// edge_lse[b][e] = lse at edge e's first slot.
+__global__ void sdlp_edge_lse_kernel(const int32_t* __restrict__ edge_slot, int64_t ne,
+                                     const float* __restrict__ lse, float* __restrict__ out,
+                                     int64_t B) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < ne * B;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = u / ne, e = u % ne;
+    out[b * ne + e] = lse[(int64_t)edge_slot[e] * B + b];
+  }
+}
+
+// Workspace: 256-byte aligned pieces.
+struct SdlpWs {
+  float *cur, *buf, *eta, *vsum, *svar, *lse, *ev;
+  double *pv, *pf;
+  int64_t nv_blocks, nf_blocks;
+};
+
+size_t align256(size_t n) { return (n + 255) / 256 * 256; }
+
+size_t sdlp_layout(const Plan& p, int64_t B, char* base, SdlpWs* w) {
+  const Launch2 lv = launch2(p.num_variables, B, p.sm_count);
+  const Launch2 lf = launch2(p.num_factors, B, p.sm_count);
+  const int64_t n_es = p.num_edge_states, nvs = p.num_var_states;
+  const size_t fsz[7] = {(size_t)(n_es * B), (size_t)(n_es * B), (size_t)(n_es * B),
+                         (size_t)(nvs * B),  (size_t)(nvs * B),  (size_t)(p.num_slots * B),
+                         (size_t)(nvs * B)};
+  SdlpWs tmp;
+  float** dst[7] = {&tmp.cur, &tmp.buf, &tmp.eta, &tmp.vsum, &tmp.svar, &tmp.lse, &tmp.ev};
+  size_t off = 0;
+  for (int i = 0; i < 7; ++i) {
+    *dst[i] = base ? reinterpret_cast<float*>(base + off) : nullptr;
+    off += align256(std::max<size_t>(fsz[i], 1) * sizeof(float));
+  }
+  tmp.nv_blocks = lv.grid.y;
+  tmp.nf_blocks = lf.grid.y;
+  tmp.pv = base ? reinterpret_cast<double*>(base + off) : nullptr;
+  off += align256((size_t)(tmp.nv_blocks * B) * sizeof(double));
+  tmp.pf = base ? reinterpret_cast<double*>(base + off) : nullptr;
+  off += align256((size_t)(tmp.nf_blocks * B) * sizeof(double));
+  if (w) *w = tmp;
+  return off;
+}
+
+// Inputs of a pass: evidence in the run layout [N_vs][B] (or shared), potentials as given.
+struct SdlpIn {
+  const float* ev;
+  int64_t evs, evb;
+  const float* lp;
+  int64_t lps, lpb;
+};
+
+SdlpIn sdlp_inputs(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                   const float* ev, int64_t ev_stride, const SdlpWs& w) {
+  SdlpIn in;
+  if (ev_stride == 0 || B == 1) {
+    in.ev = ev;
+    in.evs = 1;
+    in.evb = 0;
+  } else {
+    transpose(s, ev, B, p.num_var_states, ev_stride, w.ev);
+    in.ev = w.ev;
+    in.evs = B;
+    in.evb = 1;
+  }
+  // potentials stay in the caller's layout: shared by the batch in the common case (the factor
+  // kernels then read one table for every lane); per-instance potentials are read row-wise
+  in.lp = lp;
+  in.lps = 1;
+  in.lpb = B == 1 ? 0 : lp_stride;
+  return in;
+}
+
+// One objective evaluation at c.cur; with c.nxt set, also the step. objval (may be null) gets
+// [B] values out_stride apart.
+void sdlp_pass(const Plan& p, cudaStream_t s, int64_t B, const SdlpIn& in, const SdlpWs& w,
+               const Sdlp& c, float* objval, int64_t out_stride) {
+  const float t = c.t;
+  const bool t0 = c.t0;
+  {
+    ProfileScope ps(kProfVarsum, s);
+    const Launch2 l = launch2(p.num_variables, B, p.sm_count);
+    sdlp_var_kernel<<<l.grid, l.block, 0, s>>>(p.var_off, p.num_variables, p.vs_off, p.vs_edges,
+                                               c.cur, in.ev, in.evs, in.evb, w.vsum, w.svar, w.pv,
+                                               B, t, t0);
+  }
+  const bool low_t = (double)t < kStabilityThre;
+  for (const PairwiseBucket& q : p.pairwise) {
+    if (t0) launch_pairwise<true>(s, p, q, c, B, t, nullptr);
+    else launch_pairwise<false>(s, p, q, c, B, t, nullptr);
+  }
+  if (t0) launch_enum_generic<true>(s, p, c, B, t, nullptr);
+  else launch_enum_generic<false>(s, p, c, B, t, nullptr);
+  for (int which = 0; which < 2; ++which) {
+    if (t0) launch_logical<true>(s, p, which, c, B, t, low_t, 0, nullptr);
+    else launch_logical<false>(s, p, which, c, B, t, low_t, 0, nullptr);
+  }
+  if (t0) launch_pool<true>(s, p, c, B, t, 0, nullptr);
+  else launch_pool<false>(s, p, c, B, t, 0, nullptr);
+  ProfileScope ps(kProfReadout, s);
+  if (p.num_factors > 0) {
+    const Launch2 l = launch2(p.num_factors, B, p.sm_count);
+    sdlp_factor_kernel<<<l.grid, l.block, 0, s>>>(p.fac_edge_off, p.edge_slot, p.num_factors,
+                                                  w.lse, w.pf, B);
+  }
+  if (objval != nullptr)
+    sdlp_objval_kernel<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(
+        w.pv, p.num_variables > 0 ? w.nv_blocks : 0, w.pf, p.num_factors > 0 ? w.nf_blocks : 0, B,
+        objval, out_stride);
+}
+
+Sdlp sdlp_access(const Plan& p, int64_t B, const float* cur, const SdlpIn& in, const SdlpWs& w,
+                 float t) {
+  Sdlp c;
+  c.cur = cur;
+  c.lp = in.lp;
+  c.lps = in.lps;
+  c.lpb = in.lpb;
+  c.svar = w.svar;
+  c.lse = w.lse;
+  c.nxt = nullptr;
+  c.eta = nullptr;
+  c.upd = nullptr;
+  c.grad = nullptr;
+  c.B = B;
+  c.n_es = p.num_edge_states;
+  c.t = t;
+  c.step = 0.0f;
+  c.coef = 0.0f;
+  c.t0 = t == 0.0f;
+  return c;
+}
+
+}  // namespace
+
+size_t sdlp_workspace_bytes(const Plan& p, int64_t B) { return sdlp_layout(p, B, nullptr, nullptr); }
+
+cudaError_t sdlp_objective(const Plan& p, cudaStream_t s, int64_t B, const float* lp,
+                           int64_t lp_stride, const float* ev, int64_t ev_stride,
+                           const float* msgs, int64_t ms, double temperature, float* objval,
+                           float* grad, float* updates, float* edge_lse, void* ws) {
+  SdlpWs w;
+  sdlp_layout(p, B, static_cast<char*>(ws), &w);
+  const SdlpIn in = sdlp_inputs(p, s, B, lp, lp_stride, ev, ev_stride, w);
+  transpose(s, msgs, B, p.num_edge_states, ms, w.cur);
+  Sdlp c = sdlp_access(p, B, w.cur, in, w, (float)temperature);
+  c.grad = grad;
+  c.upd = updates;
+  sdlp_pass(p, s, B, in, w, c, objval, 1);
+  if (edge_lse != nullptr && p.num_edges > 0)
+    sdlp_edge_lse_kernel<<<flat_grid(p.num_edges * B, p.sm_count), 256, 0, s>>>(
+        p.edge_slot, p.num_edges, w.lse, edge_lse, B);
+  return cudaGetLastError();
+}
+
+cudaError_t sdlp_run(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
+                     const float* ev, int64_t ev_stride, const float* msgs_in, int64_t ms,
+                     float* msgs_out, float* objvals, int64_t iters, double temperature, double lr,
+                     void* ws) {
+  SdlpWs w;
+  sdlp_layout(p, B, static_cast<char*>(ws), &w);
+  const int64_t n = p.num_edge_states;
+  if (iters <= 0) {
+    if (n > 0) {
+      const size_t row = (size_t)n * sizeof(float);
+      cudaError_t e = cudaMemcpy2DAsync(msgs_out, row, msgs_in, (size_t)ms * sizeof(float), row,
+                                        (size_t)B, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+  }
+  const SdlpIn in = sdlp_inputs(p, s, B, lp, lp_stride, ev, ev_stride, w);
+  transpose(s, msgs_in, B, n, ms, w.cur);
+  if (n > 0) {
+    cudaError_t e = cudaMemcpyAsync(w.eta, w.cur, (size_t)(n * B) * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  const float t = (float)temperature;
+  const float lrf = (float)lr;
+  float* cur = w.cur;
+  float* nxt = w.buf;
+  for (int64_t it = 0; it < iters; ++it) {
+    Sdlp c = sdlp_access(p, B, cur, in, w, t);
+    const float itf = (float)it;
+    // dual_lp.py:295-305 in float32: lr * grad, or lr / sqrt(it + 1.0) * grad at T = 0
+    c.step = t > 0.0f ? lrf : lrf / sqrtf(itf + 1.0f);
+    c.coef = (itf + 1.0f) / (itf + 4.0f);
+    c.nxt = nxt;
+    c.eta = w.eta;
+    sdlp_pass(p, s, B, in, w, c, objvals != nullptr ? objvals + it : nullptr, iters);
+    std::swap(cur, nxt);
+  }
+  transpose(s, cur, n, B, B, msgs_out);
+  return cudaGetLastError();
+}
+
 }  // namespace pgbp

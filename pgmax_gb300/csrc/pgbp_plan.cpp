@@ -308,6 +308,13 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   p.vs_of_es = bd.upload(std::vector<int32_t>(vs, vs + ns));
   p.edge_start = bd.upload(edge_start);
   p.edge_slot = bd.upload(edge_slot);
+  {
+    // edges of factor f: fac_edge_off[f] .. fac_edge_off[f + 1] - 1 (edges follow factor order)
+    std::vector<int32_t> feo(fac_es_begin.size() + 1, (int32_t)ne);
+    for (size_t f = 0; f < fac_es_begin.size(); ++f) feo[f] = ei[fac_es_begin[f]];
+    p.num_factors = (int64_t)fac_es_begin.size();
+    p.fac_edge_off = bd.upload(feo);
+  }
   // slot lists as affine runs (first, stride, length); used when they compress 4:1 or better
   auto fill_varsum = [&](pgbp::VarsumSet& v, const std::vector<int32_t>& units,
                          const std::vector<int32_t>& off, const std::vector<int32_t>& slots) {
@@ -972,6 +979,83 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
   if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
   e = pgbp::decode(p, static_cast<cudaStream_t>(stream), batch, beliefs, beliefs_stride, map);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_decode launch");
+  return PGBP_OK;
+}
+
+size_t pgbp_sdlp_workspace_size(const pgbp_plan* plan, int64_t batch) {
+  if (!plan || batch <= 0) return 0;
+  return pgbp::sdlp_workspace_bytes(plan->p, batch);
+}
+
+// Argument checks shared by the SDLP entry points; the temperature message is the reference's
+// (dual_lp.py:270-274).
+static int sdlp_check(const pgbp::Plan& p, int64_t batch, const float* lp, int64_t lp_stride,
+               const float* ev, int64_t ev_stride, const float* msgs, int64_t ms,
+               double temperature, void* workspace, size_t workspace_bytes) {
+  if (!p.var_off) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
+  if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
+  if (!(temperature >= 0.0 && temperature <= 1.0))
+    return fail(PGBP_ERR_INVALID_ARGUMENT,
+                "The log sum-exp temperature of the Dual LP-MAP solver has to be between 0.0 "
+                "and 1.0");
+  if (lp_stride < 0 || ev_stride < 0 || (lp_stride != 0 && lp_stride < p.num_potentials) ||
+      (ev_stride != 0 && ev_stride < p.num_var_states) ||
+      ms < (batch > 1 ? p.num_edge_states : 0))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad stride");
+  if ((p.num_potentials > 0 && !lp) || (p.num_var_states > 0 && !ev) ||
+      (p.num_edge_states > 0 && !msgs))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  const size_t need = pgbp::sdlp_workspace_bytes(p, batch);
+  if (!workspace || workspace_bytes < need)
+    return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+    return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  return PGBP_OK;
+}
+
+int pgbp_sdlp_objective(const pgbp_plan* plan, void* stream, int64_t batch,
+                        const float* log_potentials, int64_t lp_stride, const float* evidence,
+                        int64_t ev_stride, const float* msgs, int64_t msgs_stride,
+                        double logsumexp_temp, float* objval, float* grad, float* bp_updates,
+                        float* edge_lse, void* workspace, size_t workspace_bytes) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  int rc = sdlp_check(p, batch, log_potentials, lp_stride, evidence, ev_stride, msgs, msgs_stride,
+                      logsumexp_temp, workspace, workspace_bytes);
+  if (rc) return rc;
+  if (!objval) return fail(PGBP_ERR_INVALID_ARGUMENT, "null objval");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::sdlp_objective(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride,
+                           evidence, ev_stride, msgs, msgs_stride, logsumexp_temp, objval, grad,
+                           bp_updates, edge_lse, workspace);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_sdlp_objective launch");
+  return PGBP_OK;
+}
+
+int pgbp_sdlp_run(const pgbp_plan* plan, void* stream, int64_t batch, const float* log_potentials,
+                  int64_t lp_stride, const float* evidence, int64_t ev_stride,
+                  const float* msgs_in, int64_t msgs_stride, float* msgs_out, float* objvals,
+                  int64_t num_iters, double logsumexp_temp, double lr, void* workspace,
+                  size_t workspace_bytes) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  int rc = sdlp_check(p, batch, log_potentials, lp_stride, evidence, ev_stride, msgs_in,
+                      msgs_stride, logsumexp_temp, workspace, workspace_bytes);
+  if (rc) return rc;
+  if (num_iters < 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "num_iters must be >= 0");
+  if (p.num_edge_states > 0 && !msgs_out) return fail(PGBP_ERR_INVALID_ARGUMENT, "null msgs_out");
+  if (!(lr > 0.0)) lr = logsumexp_temp != 0.0 ? logsumexp_temp : 0.01;  // dual_lp.py:282-286
+  else if (logsumexp_temp != 0.0 && lr > logsumexp_temp)
+    return fail(PGBP_ERR_INVALID_ARGUMENT,
+                "For gradient descent, the learning rate must be smaller than the log sum-exp "
+                "temperature.");
+  cudaError_t e = cudaSetDevice(p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = pgbp::sdlp_run(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride,
+                     evidence, ev_stride, msgs_in, msgs_stride, msgs_out, objvals, num_iters,
+                     logsumexp_temp, lr, workspace);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_sdlp_run launch");
   return PGBP_OK;
 }
 

@@ -308,6 +308,51 @@ class Plan:
                                       out.data_ptr()), "pgbp_decode")
     return out if b.ndim == 2 else out[0]
 
+  # ------------------------------------------------------------------------- SDLP
+  def _sdlp_ws(self, B, dev):
+    nb = int(self.lib.pgbp_sdlp_workspace_size(self.handle, B))
+    return _torch().empty(max(nb, 1), dtype=_torch().uint8, device=dev), nb
+
+  def sdlp_run(self, log_potentials, evidence, ftov_msgs, num_iters, temperature, lr=None):
+    """run_with_objvals of the smooth dual LP-MAP solver (pgbp_sdlp_run): returns
+    (messages [B?, E_s], objective values [B?, num_iters])."""
+    torch = _torch()
+    lp, ev, m, B, batched = self._inputs(log_potentials, evidence, ftov_msgs)
+    dev = m[0].device
+    iters = int(num_iters)
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=dev)
+    objvals = torch.empty((B, max(iters, 0)), dtype=torch.float32, device=dev)
+    ws, nb = self._sdlp_ws(B, dev)
+    native.check(self.lib.pgbp_sdlp_run(
+        self.handle, self._stream(), B, lp[0].data_ptr(), lp[1], ev[0].data_ptr(), ev[1],
+        m[0].data_ptr(), m[1], out.data_ptr(), objvals.data_ptr() if iters > 0 else None, iters,
+        float(temperature), -1.0 if lr is None else float(lr), ws.data_ptr(), nb),
+                 "pgbp_sdlp_run")
+    return (out, objvals) if batched else (out[0], objvals[0])
+
+  def sdlp_objective(self, log_potentials, evidence, ftov_msgs, temperature, grad=False,
+                     updates=False, edge_lse=False):
+    """smooth_dual_objval_and_grad (pgbp_sdlp_objective): a dict with "objval" [B?] and, when
+    asked for, "grad" and "updates" [B?, E_s] and "edge_lse" [B?, num_edges]."""
+    torch = _torch()
+    lp, ev, m, B, batched = self._inputs(log_potentials, evidence, ftov_msgs)
+    dev = m[0].device
+    n_es, ne = self.num_edge_states, int(self.info["num_edges"])
+    out = {"objval": torch.empty(B, dtype=torch.float32, device=dev)}
+    if grad:
+      out["grad"] = torch.empty((B, n_es), dtype=torch.float32, device=dev)
+    if updates:
+      out["updates"] = torch.empty((B, n_es), dtype=torch.float32, device=dev)
+    if edge_lse:
+      out["edge_lse"] = torch.empty((B, ne), dtype=torch.float32, device=dev)
+    ptr = lambda k: out[k].data_ptr() if k in out else None
+    ws, nb = self._sdlp_ws(B, dev)
+    native.check(self.lib.pgbp_sdlp_objective(
+        self.handle, self._stream(), B, lp[0].data_ptr(), lp[1], ev[0].data_ptr(), ev[1],
+        m[0].data_ptr(), m[1], float(temperature), ptr("objval"), ptr("grad"), ptr("updates"),
+        ptr("edge_lse"), ws.data_ptr(), nb), "pgbp_sdlp_objective")
+    return out if batched else {k: v[0] for k, v in out.items()}
+
   def energy(self, log_potentials, evidence, map_states):
     """Energies of decodings (pgbp_energy): map_states [num_variables] or [B, num_variables]
     (int), log_potentials / evidence [n] or [B, n] as BPArrays hold them. Returns float32 [B]

@@ -148,6 +148,11 @@ SIGNATURES = [
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
     ("pgbp_decode", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_marginals", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
+    ("pgbp_sdlp_workspace_size", ctypes.c_size_t, [_p, _i64]),
+    ("pgbp_sdlp_objective", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _d, _p, _p,
+                                           _p, _p, _p, ctypes.c_size_t]),
+    ("pgbp_sdlp_run", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p, _i64, _d,
+                                     _d, _p, ctypes.c_size_t]),
     ("pgbp_energy_workspace_size", ctypes.c_size_t, [_p, _i64]),
     ("pgbp_energy", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p,
                                    ctypes.c_size_t]),

@@ -11,7 +11,7 @@ FIXTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "f
 
 def run_fixture_paths():
   return sorted(p for p in glob.glob(os.path.join(FIXTURES, "*.npz"))
-                if not os.path.basename(p).startswith(("factor_updates", "energy_")))
+                if not os.path.basename(p).startswith(("factor_updates", "energy_", "sdlp_")))
 
 
 def energy_fixture_paths():
@@ -30,3 +30,8 @@ def load(path):
 
 def fixture_id(path):
   return os.path.basename(path)[:-4]
+
+
+def sdlp_fixture_paths():
+  """SDLP calls of the reference: wiring, BPArrays, call kind and its outputs."""
+  return sorted(glob.glob(os.path.join(FIXTURES, "sdlp_*.npz")))

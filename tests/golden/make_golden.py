@@ -22,7 +22,13 @@ the OR / AND / Pool factors, out-of-range and negative states, infinite evidence
 `energy_*.npz`: the flat wiring, the BPArrays' log potentials and evidence, the decoding (a state
 per variable, evidence_to_vars order) and the reference's energy.
 
-`--energy-only` regenerates the energy fixtures alone and leaves the others untouched.
+The smooth dual LP-MAP solver (`infer.SDLP`, pgmax/infer/dual_lp.py) is recorded the same way as
+`sdlp_*.npz`: every `run_with_objvals` / `run` (inputs, output messages, objective values),
+`get_bp_updates` (factor updates and per-edge log-sum-exp) and `get_primal_upper_bound` call of the
+reference's tests/lp/test_bp_for_lp.py and of `sdlp_cases` (the seeded graphs of cases.py with
+cold and random initial messages, temperatures 0 to 1, default and explicit learning rates).
+
+`--energy-only` / `--sdlp-only` regenerate those fixtures alone and leave the others untouched.
 """
 
 import argparse
@@ -77,6 +83,7 @@ class Recorder:
   def __init__(self):
     self.runs = []
     self.energies = []
+    self.sdlp = []
     self.allclose_args = []
     self.current = "unnamed"
     self.meta = {}
@@ -261,6 +268,111 @@ def save_energies():
   return len(REC.energies)
 
 
+def install_sdlp_capture():
+  """Wraps pgmax.infer.SDLP so that the solver calls of every SDLP object are recorded."""
+  dual_mod = importlib.import_module("pgmax.infer.dual_lp")
+  inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  infer_pkg = importlib.import_module("pgmax.infer")
+  orig = dual_mod.SDLP
+
+  def SDLP(bp_state):  # pylint: disable=invalid-name
+    sd = orig(bp_state)
+    wiring = wiring_arrays(inferer_mod.InfererContext(bp_state), bp_state.fg_state)
+
+    def arrays_of(a):
+      return {"log_potentials": _np(a.log_potentials, np.float32),
+              "evidence": _np(a.evidence, np.float32),
+              "ftov_msgs_in": _np(a.ftov_msgs, np.float32)}
+
+    def record(kind, a, extra):
+      REC.sdlp.append({"source": REC.current, "meta": dict(REC.meta, call=kind),
+                       "wiring": wiring, **arrays_of(a), **extra})
+
+    def run_with_objvals(sdlp_arrays, logsumexp_temp, num_iters, lr=None):
+      out, objvals = sd.run_with_objvals(sdlp_arrays, logsumexp_temp, num_iters, lr)
+      record("run_with_objvals", sdlp_arrays, {
+          "logsumexp_temp": np.float64(logsumexp_temp), "num_iters": np.int64(num_iters),
+          "lr": np.float64(-1.0 if lr is None else lr),
+          "ftov_msgs_out": _np(out.ftov_msgs, np.float32),
+          "objvals": _np(objvals, np.float32).reshape(-1)})
+      return out, objvals
+
+    def run(sdlp_arrays, logsumexp_temp, num_iters, lr=None):
+      return run_with_objvals(sdlp_arrays, logsumexp_temp, num_iters, lr)[0]
+
+    def get_bp_updates(sdlp_arrays, logsumexp_temp):
+      upd, lse = sd.get_bp_updates(sdlp_arrays, logsumexp_temp)
+      record("get_bp_updates", sdlp_arrays, {
+          "logsumexp_temp": np.float64(logsumexp_temp), "bp_updates": _np(upd, np.float32),
+          "edge_lse": _np(lse, np.float32)})
+      return upd, lse
+
+    def get_primal_upper_bound(sdlp_arrays):
+      ub = sd.get_primal_upper_bound(sdlp_arrays)
+      record("get_primal_upper_bound", sdlp_arrays, {
+          "logsumexp_temp": np.float64(0.0), "objval": np.float32(np.asarray(ub))})
+      return ub
+
+    return dual_mod.SmoothDualLP(
+        init=sd.init, update=sd.update, to_bp_state=sd.to_bp_state, get_beliefs=sd.get_beliefs,
+        run=run, run_with_objvals=run_with_objvals, decode_primal_unaries=sd.decode_primal_unaries,
+        get_primal_upper_bound=get_primal_upper_bound, get_map_lower_bound=sd.get_map_lower_bound,
+        get_bp_updates=get_bp_updates)
+
+  dual_mod.SDLP = SDLP
+  infer_pkg.SDLP = SDLP
+
+
+def sdlp_cases(api):
+  """SDLP on the seeded graphs of cases.py."""
+  sys.path.insert(0, HERE)
+  import cases  # pylint: disable=g-import-not-at-top
+  bp_state_mod = importlib.import_module("pgmax.infer.bp_state")
+  jnp = importlib.import_module("jax.numpy")
+  plans = [
+      ("ising6", "ising", dict(n=6, seed=2)),
+      ("potts_K3", "potts", dict(L=5, K=3, seed=4)),
+      ("rbm", "rbm", dict(nh=8, nv=12, seed=1, sample=0)),
+      ("deconv", "deconv", dict(seed=0)),
+      ("mixed", "mixed", dict(seed=0)),
+  ]
+  runs = [(0.0, 1, None), (0.0, 60, None), (0.0, 40, 0.05), (1e-3, 60, None), (0.05, 40, None),
+          (0.05, 40, 0.01), (0.3, 25, 0.1), (1.0, 30, None)]
+  for name, builder, bkw in plans:
+    fg, _, ev = cases.BUILDERS[builder](api, **bkw)
+    sdlp = api.infer.build_inferer(fg.bp_state, backend="sdlp")
+    cold = sdlp.init(evidence_updates=ev)
+    rng = np.random.default_rng(len(name))
+    warm = bp_state_mod.BPArrays(
+        log_potentials=cold.log_potentials,
+        ftov_msgs=jnp.asarray(rng.normal(size=cold.ftov_msgs.shape).astype(np.float32)),
+        evidence=cold.evidence)
+    for init_name, arrays in (("cold", cold), ("random", warm)):
+      REC.meta = {"case": name, "builder": builder, "builder_kwargs": bkw, "init": init_name}
+      for temp, iters, lr in runs:
+        REC.current = f"sdlp_case::{name}::{init_name}::T{temp}_n{iters}"
+        out = sdlp.run(arrays, logsumexp_temp=temp, num_iters=iters, lr=lr)
+      REC.current = f"sdlp_case::{name}::{init_name}::bounds"
+      sdlp.get_primal_upper_bound(out)
+      for temp in (0.0, 1e-3, 0.2, 1.0):
+        REC.current = f"sdlp_case::{name}::{init_name}::updates_T{temp}"
+        sdlp.get_bp_updates(out, logsumexp_temp=temp)
+
+
+def save_sdlp():
+  counts = {}
+  for rec in REC.sdlp:
+    src = rec["source"].replace("::", "__").replace(".", "_")
+    counts[src] = counts.get(src, 0) + 1
+    arrays = {"w." + k: v for k, v in rec["wiring"].items()}
+    for k, v in rec.items():
+      if k not in ("source", "meta", "wiring"):
+        arrays[k] = v
+    arrays["meta"] = np.array(json.dumps({"source": rec["source"], **rec["meta"]}))
+    np.savez_compressed(os.path.join(OUT, f"sdlp_{src}_{counts[src]:02d}.npz"), **arrays)
+  return len(REC.sdlp)
+
+
 def save_run(path, run, extra=None):
   arrays = {}
   for k, v in run["wiring"].items():
@@ -382,6 +494,7 @@ def main():
   ap = argparse.ArgumentParser()
   ap.add_argument("--reference", default=os.environ.get("PGMAX_REFERENCE", "/root/reference"))
   ap.add_argument("--energy-only", action="store_true")
+  ap.add_argument("--sdlp-only", action="store_true")
   args = ap.parse_args()
   sys.path.insert(0, HERE)
   import jax_shim  # pylint: disable=g-import-not-at-top
@@ -391,11 +504,22 @@ def main():
   from pgmax import factor, fgraph, fgroup, infer, vgroup  # pylint: disable=g-import-not-at-top
   install_capture(pgmax)
   install_energy_capture()
+  install_sdlp_capture()
   api = types.SimpleNamespace(factor=factor, fgraph=fgraph, fgroup=fgroup, infer=infer,
                               vgroup=vgroup)
   os.makedirs(OUT, exist_ok=True)
   energy_tests = {"test_energy": None, "factor.test_or": None, "factor.test_and": None,
                   "factor.test_pool": None}
+  sdlp_tests = {"lp.test_bp_for_lp": None}
+  if args.sdlp_only:
+    for f in os.listdir(OUT):
+      if f.startswith("sdlp_") and f.endswith(".npz"):
+        os.remove(os.path.join(OUT, f))
+    status = run_reference_tests(args.reference, sdlp_tests)
+    sdlp_cases(api)
+    n = save_sdlp()
+    print(json.dumps({"sdlp_reference_tests": status, "sdlp_fixtures": n}, indent=1))
+    return
   if args.energy_only:
     for f in os.listdir(OUT):
       if f.startswith("energy_") and f.endswith(".npz"):
@@ -417,6 +541,10 @@ def main():
   status.update(run_reference_tests(args.reference, {"test_energy": None}))
   energy_cases(api)
   save_energies()
+  REC.sdlp = []
+  status.update(run_reference_tests(args.reference, sdlp_tests))
+  sdlp_cases(api)
+  save_sdlp()
 
   # Golden vector of tests/test_pgmax.py: the (messages, expected) pair of its allclose call.
   golden = [a for a in REC.allclose_args if a[0] == "test_pgmax::test_e2e_sanity_check"]
