@@ -177,14 +177,15 @@ def run_sdlp(args):
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
   dev = torch.device("cuda", 0)
+  nb = args.batch
   fg, _, _ = build_rbm(seed=0)
   sdlp = infer.build_inferer(fg.bp_state, backend="sdlp")
   nvs = fg.fg_state.num_var_states
   n_es = fg.fg_state.total_factor_num_states
-  ev_host = gumbel_evidence(nvs, BATCH, 1000)
+  ev_host = gumbel_evidence(nvs, nb, 1000)
   lp_dev = torch.as_tensor(np.asarray(fg.fg_state.log_potentials, np.float32), device=dev)
   ev_dev = torch.as_tensor(ev_host, device=dev)
-  msgs0 = torch.zeros((BATCH, n_es), dtype=torch.float32, device=dev)
+  msgs0 = torch.zeros((nb, n_es), dtype=torch.float32, device=dev)
   arrays = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_dev)
   stream = torch.cuda.current_stream(dev)
 
@@ -208,11 +209,20 @@ def run_sdlp(args):
   torch.cuda.synchronize()
   native.profile_enable(False)
   prof = native.profile_read()
-  units = BATCH * n_es * SDLP_ITERS * args.steps
+  # the same steps as subgradient descent (logsumexp_temp 0: max-product updates, no exp / log)
+  sdlp.run_with_objvals(arrays, logsumexp_temp=0.0, num_iters=SDLP_ITERS)
+  torch.cuda.synchronize()
+  e0.record(stream)
+  for _ in range(args.steps):
+    sdlp.run_with_objvals(arrays, logsumexp_temp=0.0, num_iters=SDLP_ITERS)
+  e1.record(stream)
+  torch.cuda.synchronize()
+  ms_t0 = e0.elapsed_time(e1)
+  units = nb * n_es * SDLP_ITERS * args.steps
   # per step and instance: messages read by the variable sums and the factor pass, eta read and
   # written, the next messages written; variable sums written and read, the variable softmax
   # written and gathered once per edge state; the evidence; potentials shared by the batch
-  iter_bytes = BATCH * 4 * (5 * n_es + 4 * nvs) + 4 * int(lp_dev.numel())
+  iter_bytes = nb * 4 * (5 * n_es + 4 * nvs) + 4 * int(lp_dev.numel())
   achieved = iter_bytes * SDLP_ITERS * args.steps / (ms / 1e3) / 1e9
   peak, peak_kind = peaks()
   line = {
@@ -221,10 +231,12 @@ def run_sdlp(args):
       "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
       "vs_baseline": None, "dtype": "f32",
       "data": "synthetic (seeded RBM, Gumbel(0,1) evidence per sample)",
-      "config": {"workload": "sdlp_rbm784x500_b128", "batch": BATCH, "num_iters": SDLP_ITERS,
+      "config": {"workload": f"sdlp_rbm784x500_b{nb}", "batch": nb, "num_iters": SDLP_ITERS,
                  "logsumexp_temp": SDLP_TEMP, "edge_states": n_es,
                  "l2": "inputs larger than L2 (804 MB of messages per buffer)"},
       "final_objval_mean": float(objvals[:, -1].mean()),
+      "temp0": {"ms_per_step": ms_t0 / args.steps, "value": units / (ms_t0 / 1e3),
+                "frac_of_hbm": iter_bytes * SDLP_ITERS * args.steps / (ms_t0 / 1e3) / 1e9 / peak},
       "kernel_time_share": {k: v[1] for k, v in prof.items() if v[0]},
       "gpu_launches": sum(v[0] for v in prof.values()) * args.steps,
       "roofline": {"bound": "hbm", "kernel": "one SDLP step (all launches)", "achieved": achieved,
@@ -911,6 +923,8 @@ def main():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--graphs", type=int, default=MG_GRAPHS,
                   help="graphs of the multigraph workload (256; fewer for small profiling cases)")
+  ap.add_argument("--batch", type=int, default=BATCH,
+                  help="samples of the sdlp and energy workloads (128; fewer for profiling cases)")
   ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
                   help="execution path of the ising workload (auto: timed choice)")
   ap.add_argument("--workload", default="rbm",

@@ -186,6 +186,13 @@ struct Fused {
   }
 };
 
+// Minimum resident blocks of 256 threads per SM the dense 2 x 2 pairwise kernel is compiled for,
+// per access class (the register budget follows: 65536 / (256 * blocks)).
+template <class C>
+struct PairwiseMinBlocks {
+  static constexpr int value = 1;
+};
+
 // Update: one factor type's raw update on caller arrays [B, n_type] (a FAC_TO_VAR_UPDATES call).
 struct Update {
   const float* __restrict__ vt;
@@ -273,8 +280,8 @@ __device__ __forceinline__ void pairwise_refs(const PairwiseDev& p, int4 q, Edge
 }
 
 template <int N1, int N2, bool T0, class C>
-__global__ void __launch_bounds__(256) pairwise_kernel(C c, PairwiseDev p, int64_t B, float t,
-                                                       unsigned* deltas) {
+__global__ void __launch_bounds__(256, (N1 == 2 && N2 == 2) ? PairwiseMinBlocks<C>::value : 1)
+    pairwise_kernel(C c, PairwiseDev p, int64_t B, float t, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
@@ -2154,11 +2161,53 @@ struct Sdlp {
     }
   }
 
+  // The epilogue of one edge with data d[i] = bp - ftov and e[i] = t exp((d[i] - m) / t)
+  // materialised once (edges of up to kMaxK states; registers once the factor kernel's state count
+  // is a compile-time constant).
+  static constexpr int kMaxK = 64;
+
   template <class F>
   __device__ __forceinline__ void store(const EdgeRef& r, int k, const float* old, F outv,
-                                        int64_t b, float&) const {
-    // softmax_and_logsumexps_with_temp / get_maxes_and_argmaxes (update_utils.py:26-131) over
-    // the edge's states of data = bp - ftov
+                                        int64_t b, float& dmax) const {
+    if (k > kMaxK) {
+      store_long(r, k, old, outv, b, dmax);
+      return;
+    }
+    float d[kMaxK], e[kMaxK];
+    float m = -INFINITY;
+    for (int i = 0; i < k; ++i) {
+      d[i] = outv(i) - old[i];
+      m = fmaxp(m, d[i]);
+    }
+    int arg = k - 1;
+    float sum = 0.0f;
+    if (t0) {
+      for (int i = 0; i < k; ++i) arg = d[i] == m ? i : arg;
+    } else {
+      for (int i = 0; i < k; ++i) {
+        e[i] = t * expf((d[i] - m) / t);
+        sum = sum + e[i];
+      }
+    }
+    lse[r.slot * B + b] = t0 ? m : m + t * logf(sum / t);
+    for (int i = 0; i < k; ++i) {
+      const int64_t at = (r.es0 + i) * B + b;
+      const float sv = svar[(r.vs0 + i) * B + b];
+      const float g = t0 ? sv + (i == arg ? -1.0f : 0.0f) : sv - e[i] / sum;
+      if (upd != nullptr) upd[b * n_es + r.es0 + i] = outv(i);
+      if (grad != nullptr) grad[b * n_es + r.es0 + i] = g;
+      if (nxt != nullptr) {
+        const float en = old[i] - step * g;
+        nxt[at] = en + coef * (en - eta[at]);
+        eta[at] = en;
+      }
+    }
+  }
+
+  // Edges of more than kMaxK states: the same arithmetic, recomputed instead of kept.
+  template <class F>
+  __device__ __noinline__ void store_long(const EdgeRef& r, int k, const float* old, F outv,
+                                          int64_t b, float&) const {
     float m = -INFINITY;
     for (int i = 0; i < k; ++i) m = fmaxp(m, outv(i) - old[i]);
     int arg = k - 1;  // the last state attaining the max (the last state when none does)
@@ -2183,6 +2232,14 @@ struct Sdlp {
       }
     }
   }
+};
+
+// The SDLP pass over 2 x 2 factors is issue- and latency-bound (divisions, exp and log per state
+// at T > 0): four blocks per SM (64 registers) keep more warps in flight than the three that 80
+// registers allow.
+template <>
+struct PairwiseMinBlocks<Sdlp> {
+  static constexpr int value = 4;
 };
 
 // Sums v (double) over the block's unit lanes in a fixed order; thread (tx, 0) gets the block's
