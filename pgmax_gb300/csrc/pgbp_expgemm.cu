@@ -124,20 +124,36 @@ struct ExpArgs {
   unsigned* __restrict__ dacc;            // residual of this iteration, [B] float bits
 };
 
+// Shared-memory layout of one CTA.
+//   E, E' [K][kLde] fp32 with the columns of every 8-block in the order 0 4 1 5 2 6 3 7, so the
+//     (k, k + 4) pair of an A fragment row is one 64-bit load; kLde = K + 8 puts the rows of a
+//     half-warp's loads in distinct 32-byte bank groups.
+//   row maxima r [K], column maxima c [K].
+//   U, W as tf32 high / low parts, [K / 8][4][kLdx] uint4 = (hi(k), hi(k + 4), lo(k), lo(k + 4))
+//     for k = 8 kb + tig, column n: one 128-bit load per B fragment; kLdx = 66 puts the 4 rows of
+//     a quarter-warp's loads in distinct bank groups. F1 / F2 ([K][kLdc] fp32) overwrite U / W.
 template <int K>
 struct Smem {
-  static constexpr int kLde = K + 4;                  // row stride of E and E'
-  static constexpr int kFloats = 2 * K * kLde + 2 * K // E, E', r, c
-                                 + 4 * K * kLdc;      // U, W as tf32 high / low parts (U high,
-                                                      // W high then hold F1, F2)
+  static constexpr int kLde = K + 8;
+  static constexpr int kLdx = kCols + 2;
+  static constexpr int kXWords = (K / 8) * 4 * kLdx * 4;  // 32-bit words of one of U, W
+  static_assert(K * kLdc <= kXWords, "F1 / F2 must fit in the space of U / W");
+  static constexpr int kFloats = 2 * K * kLde + 2 * K + 2 * kXWords;
   static constexpr size_t kBytes = sizeof(float) * kFloats + sizeof(unsigned) * kMaxB;
 };
+
+// Position of table column j in the permuted order of its 8-block.
+__device__ __forceinline__ int perm8(int j) { return (j & ~7) + ((j & 3) << 1) + ((j >> 2) & 1); }
+
+// State of slot i (0 .. K / 4 - 1) of the thread that owns quarter `part` of a column: the pair
+// (8 kb + part, 8 kb + part + 4) for kb = i / 2, the pair the B fragment layout stores together.
+__device__ __forceinline__ int state_of(int i, int part) { return (i >> 1) * 8 + part + 4 * (i & 1); }
 
 // f for state s of one edge computed directly (the reference's formula) when the exp-domain sum
 // underflows: the other variable's vtof plus row (first edge) or column s of the table.
 template <int K>
-__device__ float direct_message(const ExpArgs& a, int4 q, int64_t b, int s, bool first_edge,
-                                int64_t table) {
+__device__ float direct_message(const ExpArgs& a, int4 q, int64_t b, int s,
+                               bool first_edge, int64_t table) {
   const int64_t B = a.B;
   float mx = -INFINITY;
   for (int j = 0; j < K; ++j) {
@@ -156,38 +172,46 @@ __device__ float direct_message(const ExpArgs& a, int4 q, int64_t b, int s, bool
   return a.t * logf(se) + mx;
 }
 
-// acc = T X: T (K x K, fp32 in shared memory, split per fragment) times X (K x 64, already split
-// into tf32 high and low parts).
+// acc = T X: T (K x K fp32, permuted columns, split per fragment) times X (K x 64, split, in the
+// uint4 layout). The A_lo x B_hi product accumulates apart from the other two (two chains of
+// mma.sync per output tile instead of one twice as long) and is added at the end.
 template <int K>
-__device__ __forceinline__ void tile_gemm(const float* T, const uint32_t* Xh, const uint32_t* Xl,
-                                          int warp, int lane, float (&acc)[K / 16][4]) {
+__device__ __forceinline__ void tile_gemm(const float* T, const uint4* X, int warp, int lane,
+                                          float (&acc)[K / 16][4]) {
   constexpr int MB = K / 16;  // 16-row blocks; 8 warps x MB tiles = MB x 8 tiles of 16 x 8
   constexpr int kLde = Smem<K>::kLde;
+  constexpr int kLdx = Smem<K>::kLdx;
   const int gid = lane >> 2, tig = lane & 3;
   const int r0 = ((warp * MB) / 8) * 16 + gid;
+  float x1[MB][4];
 #pragma unroll
   for (int i = 0; i < MB; ++i)
 #pragma unroll
-    for (int e = 0; e < 4; ++e) acc[i][e] = 0.0f;
+    for (int e = 0; e < 4; ++e) acc[i][e] = x1[i][e] = 0.0f;
 #pragma unroll
   for (int k0 = 0; k0 < K; k0 += 8) {
+    const float2 t0 = *reinterpret_cast<const float2*>(T + r0 * kLde + k0 + 2 * tig);
+    const float2 t1 = *reinterpret_cast<const float2*>(T + (r0 + 8) * kLde + k0 + 2 * tig);
     uint32_t ah[4], al[4];
-    split_tf32(T[r0 * kLde + k0 + tig], ah[0], al[0]);
-    split_tf32(T[(r0 + 8) * kLde + k0 + tig], ah[1], al[1]);
-    split_tf32(T[r0 * kLde + k0 + tig + 4], ah[2], al[2]);
-    split_tf32(T[(r0 + 8) * kLde + k0 + tig + 4], ah[3], al[3]);
+    split_tf32(t0.x, ah[0], al[0]);  // (r0, k0 + tig)
+    split_tf32(t1.x, ah[1], al[1]);  // (r0 + 8, k0 + tig)
+    split_tf32(t0.y, ah[2], al[2]);  // (r0, k0 + tig + 4)
+    split_tf32(t1.y, ah[3], al[3]);  // (r0 + 8, k0 + tig + 4)
 #pragma unroll
     for (int i = 0; i < MB; ++i) {
       const int nb = (warp * MB + i) % 8;
-      const uint32_t bh[2] = {Xh[(k0 + tig) * kLdc + nb * 8 + gid],
-                              Xh[(k0 + tig + 4) * kLdc + nb * 8 + gid]};
-      const uint32_t bl[2] = {Xl[(k0 + tig) * kLdc + nb * 8 + gid],
-                              Xl[(k0 + tig + 4) * kLdc + nb * 8 + gid]};
-      mma_tf32(acc[i], al, bh);
+      const uint4 v = X[((k0 / 8) * 4 + tig) * kLdx + nb * 8 + gid];
+      const uint32_t bh[2] = {v.x, v.y};
+      const uint32_t bl[2] = {v.z, v.w};
+      mma_tf32(x1[i], al, bh);
       mma_tf32(acc[i], ah, bl);
       mma_tf32(acc[i], ah, bh);
     }
   }
+#pragma unroll
+  for (int i = 0; i < MB; ++i)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[i][e] += x1[i][e];
 }
 
 template <int K>
@@ -214,20 +238,19 @@ __device__ __forceinline__ float max4(float x) {  // maximum over the 4 threads 
 // B1: one instance (slot s of the batch at s), which saves the 64-bit index arithmetic.
 template <int K, bool B1>
 __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a) {
-  extern __shared__ float sm[];
+  extern __shared__ __align__(16) float sm[];
   constexpr int kLde = Smem<K>::kLde;
-  constexpr int SPT = K / 4;  // states of each edge per thread: s = 4 i + part
-  float* s_e = sm;                    // E  [K][kLde]
+  constexpr int kLdx = Smem<K>::kLdx;
+  constexpr int SPT = K / 4;  // states of each edge per thread (state_of)
+  float* s_e = sm;                    // E  [K][kLde], permuted columns
   float* s_f = s_e + K * kLde;        // E' [K][kLde]
   float* s_r = s_f + K * kLde;        // row maxima, then column maxima
   float* s_c = s_r + K;
-  uint32_t* s_uh = reinterpret_cast<uint32_t*>(s_c + K);  // U high part, then F1 [K][kLdc]
-  uint32_t* s_ul = s_uh + K * kLdc;                         // U low part
-  uint32_t* s_wh = s_ul + K * kLdc;                         // W high part, then F2
-  uint32_t* s_wl = s_wh + K * kLdc;
-  float* s_f1 = reinterpret_cast<float*>(s_uh);
-  float* s_f2 = reinterpret_cast<float*>(s_wh);
-  unsigned* s_res = s_wl + K * kLdc;  // residual per instance
+  uint4* s_u = reinterpret_cast<uint4*>(s_c + K);           // U (split), then F1
+  uint4* s_w = s_u + Smem<K>::kXWords / 4;                  // W (split), then F2
+  float* s_f1 = reinterpret_cast<float*>(s_u);
+  float* s_f2 = reinterpret_cast<float*>(s_w);
+  unsigned* s_res = reinterpret_cast<unsigned*>(s_w + Smem<K>::kXWords / 4);
   __shared__ int s_group;
   __shared__ int64_t s_tile0;
 
@@ -269,8 +292,9 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
     if (g != loaded) {
       const float* src = a.tables + (int64_t)g * expgemm_table_floats(K);
       for (int x = threadIdx.x; x < K * K; x += kThreads) {
-        s_e[(x / K) * kLde + x % K] = src[x];
-        s_f[(x / K) * kLde + x % K] = src[K * K + x];
+        const int at = (x / K) * kLde + perm8(x % K);
+        s_e[at] = src[x];
+        s_f[at] = src[K * K + x];
       }
       for (int x = threadIdx.x; x < 2 * K; x += kThreads) s_r[x] = src[2 * K * K + x];
       loaded = g;
@@ -287,7 +311,7 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
       q = a.rec[first + (B1 ? col : col / B)];
 #pragma unroll
       for (int i = 0; i < SPT; ++i) {
-        const int s = 4 * i + part;
+        const int s = state_of(i, part);
         if (B1) {
           o1[i] = a.cur[q.y + s];
           o2[i] = a.cur[q.y + K + s];
@@ -310,28 +334,29 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
     }
     m1 = max4(m1);
     m2 = max4(m2);
-    // u, w in [0, 1]: the fast exponential (about 2 ulp) keeps the sums at float32 accuracy
+    // u, w in [0, 1]: the fast exponential (about 2 ulp) keeps the sums at float32 accuracy.
+    // Slots 2 kb and 2 kb + 1 are the states (8 kb + part, 8 kb + part + 4): one 128-bit store each
 #pragma unroll
-    for (int i = 0; i < SPT; ++i) {
-      const int s = 4 * i + part;
-      uint32_t h, l;
-      split_tf32(active ? __expf(div_t(v1[i] - m1, a.t)) : 0.0f, h, l);
-      s_wh[s * kLdc + c] = h;
-      s_wl[s * kLdc + c] = l;
-      split_tf32(active ? __expf(div_t(v2[i] - m2, a.t)) : 0.0f, h, l);
-      s_uh[s * kLdc + c] = h;
-      s_ul[s * kLdc + c] = l;
+    for (int kb = 0; kb < K / 8; ++kb) {
+      uint32_t h0, l0, h1, l1;
+      split_tf32(active ? __expf(div_t(v1[2 * kb] - m1, a.t)) : 0.0f, h0, l0);
+      split_tf32(active ? __expf(div_t(v1[2 * kb + 1] - m1, a.t)) : 0.0f, h1, l1);
+      s_w[(kb * 4 + part) * kLdx + c] = make_uint4(h0, h1, l0, l1);
+      split_tf32(active ? __expf(div_t(v2[2 * kb] - m2, a.t)) : 0.0f, h0, l0);
+      split_tf32(active ? __expf(div_t(v2[2 * kb + 1] - m2, a.t)) : 0.0f, h1, l1);
+      s_u[(kb * 4 + part) * kLdx + c] = make_uint4(h0, h1, l0, l1);
     }
     __syncthreads();
-    // ---- F1 = E U, F2 = E' W on the tensor cores
+    // ---- F1 = E U, F2 = E' W on the tensor cores, one accumulator set live at a time (each
+    // result overwrites its own operand once every warp is done reading it)
     {
       float acc[K / 16][4];
-      tile_gemm<K>(s_e, s_uh, s_ul, warp, lane, acc);
-      float acc2[K / 16][4];
-      tile_gemm<K>(s_f, s_wh, s_wl, warp, lane, acc2);
+      tile_gemm<K>(s_e, s_u, warp, lane, acc);
       __syncthreads();
       store_acc<K>(s_f1, warp, lane, acc);
-      store_acc<K>(s_f2, warp, lane, acc2);
+      tile_gemm<K>(s_f, s_w, warp, lane, acc);
+      __syncthreads();
+      store_acc<K>(s_f2, warp, lane, acc);
     }
     __syncthreads();
     // ---- epilogue: messages, damping, normalisation, clipping, residual
@@ -339,7 +364,7 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
     if (active) {
 #pragma unroll
       for (int i = 0; i < SPT; ++i) {
-        const int s = 4 * i + part;
+        const int s = state_of(i, part);
         const float e1 = s_f1[s * kLdc + c], e2 = s_f2[s * kLdc + c];
         // the sums are >= 1e-30 here: the fast logarithm's absolute error is about 4e-7
         const float f1 = e1 >= 1e-30f ? (a.t * __logf(e1) + m2) + s_r[s]
@@ -358,7 +383,7 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
     if (active) {
 #pragma unroll
       for (int i = 0; i < SPT; ++i) {
-        const int s = 4 * i + part;
+        const int s = state_of(i, part);
         const float y1 = maxn(v1[i] - x1, kMsgNegInf);
         const float y2 = maxn(v2[i] - x2, kMsgNegInf);
         if (B1) {
