@@ -9,8 +9,9 @@ Follows, over the flat wiring dict of oracle.py:
   run_with_diffs           pgmax/infer/bp.py:84-146 (potential clip, initial normalisation, loop)
   pass_var_to_fac_messages pgmax/infer/bp.py:191-219
   normalize_and_clip_msgs  pgmax/infer/bp.py:222-260
-  pass_enum_fac_to_var_messages  pgmax/factor/enum.py:398-475 (temperature > 0 branch; the
-    shift M is detached, which leaves T log sum exp((s - M) / T) + M and its gradient unchanged)
+  pass_enum_fac_to_var_messages  pgmax/factor/enum.py:398-475 (temperature > 0: the shift M is
+    detached, which leaves T log sum exp((s - M) / T) + M and its gradient unchanged; temperature
+    0: the max-product branch, forward values only)
   get_beliefs              pgmax/infer/inferer.py:211-225
 """
 
@@ -51,12 +52,15 @@ class EnumGraph:
     return evidence.index_add(1, self.vs, msgs)
 
   def enum_update(self, vtof, lp, temperature):
-    """Factor-to-variable messages of every EnumFactor at temperature > 0 (enum.py:398-475)."""
+    """Factor-to-variable messages of every EnumFactor (enum.py:398-475); temperature 0 is the
+    max-product branch (forward only)."""
     B = vtof.shape[0]
     summary = torch.zeros((B, self.num_cfg), dtype=vtof.dtype, device=vtof.device)
     summary = summary.index_add(1, self.cfg, vtof[:, self.cfg_es]) + lp
     rows = summary[:, self.cfg]
     mx = torch.full((B, self.num_edge_states), -float("inf"), dtype=vtof.dtype, device=vtof.device)
+    if temperature == 0:
+      return mx.scatter_reduce(1, self.cfg_es.expand(B, -1), rows, "amax", include_self=True) - vtof
     mx = mx.scatter_reduce(1, self.cfg_es.expand(B, -1), rows.detach(), "amax", include_self=True)
     ex = torch.exp((rows - mx[:, self.cfg_es]) / temperature)
     se = torch.zeros_like(vtof).index_add(1, self.cfg_es, ex)
@@ -68,10 +72,12 @@ class EnumGraph:
     f = self.enum_update(vtof, lp, temperature)
     return self.normalize(damping * msgs + (1.0 - damping) * f)
 
-  def run(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5, temperature=1.0):
-    """Final messages [B, E_s] of run_with_diffs; inputs [n] (shared) or [B, n]."""
-    if temperature <= 0:
-      raise ValueError("bp_torch differentiates the temperature > 0 updates")
+  def run(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5, temperature=1.0,
+          with_last_delta=False):
+    """Final messages [B, E_s] of run_with_diffs; inputs [n] (shared) or [B, n]. With
+    with_last_delta, also the last iteration's max |change| per instance (msgs_deltas[-1])."""
+    if temperature < 0:
+      raise ValueError("temperature must be >= 0")
     shapes = [x.shape[0] for x in (log_potentials, evidence, ftov_msgs) if x.ndim == 2]
     B = shapes[0] if shapes else 1
     lp = log_potentials if log_potentials.ndim == 2 else log_potentials.expand(B, -1)
@@ -81,7 +87,10 @@ class EnumGraph:
     lp = lp[:, self.lp_range[0]:self.lp_range[1]]
     m = self.normalize(m)
     for _ in range(max(int(num_iters), 1)):
+      prev = m
       m = self.iterate(m, lp, ev, damping, temperature)
+    if with_last_delta:
+      return m, (m - prev).abs().amax(dim=1)
     return m
 
   def beliefs(self, evidence, msgs):

@@ -13,6 +13,7 @@ import fixtures
 from oracle import bp_torch
 
 ENUM_T_POS = ["case_ising12_T1", "case_potts_K4", "case_potts_K8", "case_potts_K16"]
+ENUM_T0 = ["case_ising50_T0", "case_rbm_s0", "case_rbm_s1"]
 
 
 def _load(name):
@@ -31,6 +32,18 @@ def test_forward_matches_reference_fixture(name):
   # float32 reference vs float64 restatement
   np.testing.assert_allclose(out[0].numpy(), d["ftov_msgs_out"], atol=1e-5, rtol=0)
   np.testing.assert_allclose(bel[0].numpy(), d["flat_beliefs"], atol=2e-5, rtol=0)
+
+
+@pytest.mark.parametrize("name", ENUM_T0)
+def test_max_product_forward_matches_reference_fixture(name):
+  """The float64 restatement's temperature-0 branch against the reference's float32 run (the
+  float64 side of the per-configuration FP64 error)."""
+  d = _load(name)
+  g = bp_torch.EnumGraph(d["wiring"])
+  f64 = lambda x: torch.as_tensor(np.asarray(x, dtype=np.float64))
+  out = g.run(f64(d["log_potentials"]), f64(d["evidence"]), f64(d["ftov_msgs_in"]),
+              int(d["num_iters"]), float(d["damping"]), 0.0)
+  np.testing.assert_allclose(out[0].numpy(), d["ftov_msgs_out"], atol=1e-4, rtol=0)
 
 
 def _loss(g, lp, ev, m, iters, damping, temperature, labels_w):
