@@ -251,6 +251,31 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
 int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
                    int64_t beliefs_stride, float* marginals);
 
+/* Autotuner decisions. pgbp_run times, once per (batch, temperature == 0), the eligible execution
+ * paths and then, on the multi-kernel path, the kernel variants of each launch site (the binary
+ * variable sums: 1 or 4 instances per thread; each dense 2 x 2 pairwise bucket: 1 or 4 instances
+ * per thread; OR and AND: a thread or a warp per factor). Those variants give bit-identical
+ * results. A site of shared K x K tables at temperature > 0 is not timed (the exp-domain
+ * tensor-core kernel, variant 1, agrees with the direct kernel, variant 0, within float32
+ * accuracy only) but may be set here. These calls export and import the decision table so that a
+ * host can cache it across processes: sites are site[0] the binary variable sums, site[1 .. B] the pairwise buckets
+ * in plan order, then OR, AND (num_sites = 3 + number of pairwise buckets); -1 = the built-in
+ * rule; path -1 = not tuned. pgbp_plan_signature writes a string identifying the plan's structure
+ * and the device's SM count: the key under which a table may be reused. */
+#define PGBP_TUNE_MAX_SITES 64
+typedef struct {
+  int64_t batch;
+  int32_t temperature0;
+  int32_t path;        /* 0 multi-kernel, 1 one CTA per instance, 2 one cluster per instance */
+  int32_t num_sites;   /* 0 when the sites are not tuned */
+  int32_t site[PGBP_TUNE_MAX_SITES];
+} pgbp_tuning_entry;
+int64_t pgbp_plan_tuning_count(const pgbp_plan* plan);
+int pgbp_plan_tuning_get(const pgbp_plan* plan, pgbp_tuning_entry* entries, int64_t max_entries);
+int pgbp_plan_tuning_set(const pgbp_plan* plan, const pgbp_tuning_entry* entries,
+                         int64_t num_entries);
+int pgbp_plan_signature(const pgbp_plan* plan, char* buf, size_t len);
+
 /* Smooth dual LP-MAP solver (SDLP): pgmax.infer.SDLP (pgmax/infer/dual_lp.py:60-463), the dual of
  * the LP relaxation of MAP smoothed by a log-sum-exp at temperature logsumexp_temp in [0, 1]
  * (0: the non-smooth dual and its subgradient). Messages are the dual variables, [batch, E_s]

@@ -1518,13 +1518,16 @@ void launch_enum_generic(cudaStream_t s, const Plan& p, const C& c, int64_t B, f
   }
 }
 
+// variant: 0 a thread per (factor, instance), 1 a warp per (factor, instance), -1 the built-in
+// rule (a warp when factors have 8 parents or more on average)
 template <bool T0, class C>
 void launch_logical(cudaStream_t s, const Plan& p, int which, const C& c, int64_t B, float t,
-                    bool low_t, int normalize, unsigned* deltas) {
+                    bool low_t, int normalize, unsigned* deltas, int variant = -1) {
   const LogicalSet& g = p.logical[which];
   if (g.count == 0) return;
   ProfileScope ps(which == 0 ? kProfOr : kProfAnd, s);
-  if (g.num_parents >= 8 * g.count) {  // many parents per factor: a warp per factor
+  const bool warp = variant >= 0 ? variant == 1 : g.num_parents >= 8 * g.count;
+  if (warp) {  // many parents per factor: a warp per factor
     const int64_t warps = g.count * B;
     const int64_t blocks = std::max<int64_t>(
         1, std::min<int64_t>((warps + 7) / 8, (int64_t)p.sm_count * 16));
@@ -1550,13 +1553,16 @@ VarsumDev dev(const VarsumSet& v) {
   return VarsumDev{v.vs, v.off, v.slots, v.run_off, v.runs, v.count};
 }
 
+// vb_variant: 0 one instance per thread for the binary variables, 1 four (B % 4 == 0), -1 the
+// built-in rule
 void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, const float* ev,
-                   int64_t evs, int64_t evb, float* vsum) {
+                   int64_t evs, int64_t evb, float* vsum, int vb_variant = -1) {
   ProfileScope ps(kProfVarsum, s);
   const VarsumSet& vb = p.varsum_binary;
   // 4 instances per thread only when that still leaves >= 16 warps per SM: the per-variable sums
   // are serial chains, so latency is hidden by warps, not by the work inside one thread
-  const bool x4 = B % 4 == 0 && vb.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32;
+  const bool x4 = B % 4 == 0 && (vb_variant >= 0 ? vb_variant == 1
+                                                 : vb.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32);
   if (vb.count > 0 && x4) {
     const Launch2 l = launch2_x4(vb.count, B, p.sm_count);
     varsum_binary_x4_kernel<<<l.grid, l.block, 0, s>>>(dev(vb), vb.use_runs, cur, ev, evs, evb,
@@ -1579,42 +1585,138 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
   }
 }
 
+// One dense pairwise bucket of one iteration. variant: for 2 x 2 tables 0 one instance per
+// thread, 1 four (B % 4 == 0); for shared K x K tables at temperature > 0 (tables != null) 0 the
+// direct kernel, 1 the exp-domain tensor-core kernel; -1 the built-in rule.
+template <bool T0>
+void launch_bucket(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const Fused& c,
+                   int64_t B, float t, unsigned* d, const float* tables, int variant) {
+  if (!T0 && tables != nullptr && expgemm_eligible(q) && variant != 0) {
+    expgemm_iterate(p, q, s, B, c.cur, c.nxt, c.vsum, c.lp, tables, c.d, c.omd, t, d);
+    return;
+  }
+  // 4 instances per thread only when that still leaves >= 16 warps per SM; below that the
+  // kernel is latency-bound and one instance per thread keeps 4x more warps in flight
+  const bool x4 = q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0 &&
+                  (variant >= 0 ? variant == 1 : q.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32);
+  if (x4) {
+    ProfileScope ps(kProfPairwise, s);
+    const Launch2 l = launch2_x4(q.count, B, p.sm_count);
+    pairwise22_x4_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(q), t, d);
+  } else {
+    launch_pairwise<T0>(s, p, q, c, B, t, d);
+  }
+}
+
+int num_sites(const Plan& p) { return 3 + (int)p.pairwise.size(); }
+
+// sites: the tuned variant per launch site (tuned_sites' layout) or null for the built-in rules
 template <bool T0>
 void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool low_t, int64_t iters,
              float* msgs0, float* msgs1, const float* ev, int64_t evs, int64_t evb,
-             unsigned* dacc, const float* gemm_tables) {
+             unsigned* dacc, const float* gemm_tables, const int* sites) {
+  const int nq = (int)p.pairwise.size();
+  auto site = [&](int i) { return sites != nullptr ? sites[i] : -1; };
   for (int64_t it = 0; it < iters; ++it) {
     float* cur = (it & 1) ? msgs1 : msgs0;
     float* nxt = (it & 1) ? msgs0 : msgs1;
     c.cur = cur;
     c.nxt = nxt;
     unsigned* d = dacc + it * B;
-    launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum));
+    launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum), site(0));
     const float* tables = gemm_tables;
-    for (const PairwiseBucket& q : p.pairwise) {
-      // shared K x K tables at temperature > 0: the exp-domain tensor-core kernel
-      if (!T0 && gemm_tables != nullptr && expgemm_eligible(q)) {
-        expgemm_iterate(p, q, s, B, cur, nxt, c.vsum, c.lp, tables, c.d, c.omd, t, d);
-        tables += q.gemm_floats;
-        continue;
-      }
-      if (gemm_tables != nullptr) tables += q.gemm_floats;
-      // 4 instances per thread only when that still leaves >= 16 warps per SM; below that the
-      // kernel is latency-bound and one instance per thread keeps 4x more warps in flight
-      if (q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0 &&
-          q.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32) {
-        ProfileScope ps(kProfPairwise, s);
-        const Launch2 l = launch2_x4(q.count, B, p.sm_count);
-        pairwise22_x4_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(q), t, d);
-      } else {
-        launch_pairwise<T0>(s, p, q, c, B, t, d);
-      }
+    for (int qi = 0; qi < nq; ++qi) {
+      const PairwiseBucket& q = p.pairwise[qi];
+      launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(1 + qi));
+      if (tables != nullptr) tables += q.gemm_floats;
     }
     launch_enum_generic<T0>(s, p, c, B, t, d);
-    launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d);
-    launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d);
+    launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d, site(1 + nq));
+    launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d, site(2 + nq));
     launch_pool<T0>(s, p, c, B, t, 1, d);
   }
+}
+
+// Variant per launch site of the multi-kernel path for (batch, temperature == 0): the cached
+// choice, else each site with more than one bit-identical variant timed on the run's own buffers
+// (three launches per variant after one warm-up), so the choice never changes a result. The trials write the next-message buffer, the variable sums and the first
+// row of residuals, which the caller resets. Inside a stream capture nothing is timed and the
+// built-in rules apply (null).
+template <bool T0>
+const int* tune_sites(const Plan& p, cudaStream_t s, int64_t B, Fused c, float t, bool low_t,
+                      const float* ev, int64_t evs, int64_t evb, unsigned* dacc,
+                      const float* gemm_tables, bool* tuned_now) {
+  *tuned_now = false;
+  const std::pair<int64_t, bool> key{B, T0};
+  {
+    std::lock_guard<std::mutex> lock(p.tune_mu);
+    auto it = p.tuned_sites.find(key);
+    if (it != p.tuned_sites.end()) return it->second.data();
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const int nq = (int)p.pairwise.size();
+  std::vector<int> choice(num_sites(p), -1);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  float* vsum = const_cast<float*>(c.vsum);
+  // fastest of `n` variants of one site; launch(v) enqueues variant v
+  auto pick = [&](int n, auto&& launch) {
+    int best = -1;
+    float best_ms = 0.0f;
+    for (int v = 0; v < n; ++v) {
+      launch(v);
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 3; ++r) launch(v);
+      cudaEventRecord(e1, s);
+      float ms = 0.0f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if (best < 0 || ms < best_ms) {
+        best = v;
+        best_ms = ms;
+      }
+    }
+    return best;
+  };
+  if (p.varsum_binary.count > 0 && B % 4 == 0)
+    choice[0] = pick(2, [&](int v) { launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, v); });
+  else
+    launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum);  // variable sums for the factor trials
+  const float* tables = gemm_tables;
+  for (int qi = 0; qi < nq; ++qi) {
+    const PairwiseBucket& q = p.pairwise[qi];
+    // only variants that give bit-identical results are timed: the exp-domain kernel (shared
+    // tables at T > 0) agrees with the direct one within float32 accuracy, not bit for bit, so
+    // it stays the rule there (a host can still choose it through pgbp_plan_tuning_set)
+    const bool two = q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0;
+    if (two)
+      choice[1 + qi] = pick(2, [&](int v) {
+        launch_bucket<T0>(s, p, q, c, B, t, dacc, tables, v);
+      });
+    if (tables != nullptr) tables += q.gemm_floats;
+  }
+  for (int w = 0; w < 2; ++w) {
+    if (p.logical[w].count > 0)
+      choice[1 + nq + w] = pick(2, [&](int v) {
+        launch_logical<T0>(s, p, w, c, B, t, low_t, 1, dacc, v);
+      });
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *tuned_now = true;
+  std::lock_guard<std::mutex> lock(p.tune_mu);
+  auto& slot = p.tuned_sites[key];
+  slot = choice;
+  return slot.data();
 }
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -1957,6 +2059,8 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     g.d = c.d;
     g.omd = c.omd;
   }
+  // kernel variants of the multi-kernel path (null: built-in rules until tuned)
+  const int* sites = nullptr;
   // run `n` iterations on execution path `path`; returns the buffer holding the result
   auto run_path = [&](int path, int64_t n) -> float* {
     if (path == kPathSmall) {
@@ -1971,8 +2075,8 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
       else launch_cluster<false>(s, p, g, B, n, t, low_t, m0, m1, vsum, dacc);
       return (n & 1) ? m1 : m0;
     }
-    if (t0) iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, nullptr);
-    else iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, gemm);
+    if (t0) iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, nullptr, sites);
+    else iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, gemm, sites);
     return (n & 1) ? m1 : m0;
   };
   int path = kPathMulti;
@@ -1986,6 +2090,12 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     } else {
       path = choose_path(p, s, B, t0, cluster_ok, run_path, tmp, m0, dacc, iters);
     }
+  }
+  if (path == kPathMulti) {
+    bool tuned_now = false;
+    sites = t0 ? tune_sites<true>(p, s, B, c, t, low_t, evp, evs, evb, dacc, nullptr, &tuned_now)
+               : tune_sites<false>(p, s, B, c, t, low_t, evp, evs, evb, dacc, gemm, &tuned_now);
+    if (tuned_now) cudaMemsetAsync(dacc, 0, sizeof(unsigned) * (size_t)(iters * B), s);
   }
   // caller-layout messages of the run buffer `src` into dst [B, E_s]
   auto write_out = [&](const float* src, float* dst) {

@@ -982,6 +982,94 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
   return PGBP_OK;
 }
 
+namespace {
+
+// Every (batch, temperature == 0) key the plan has a path or site decision for.
+std::vector<std::pair<int64_t, bool>> tuning_keys(const pgbp::Plan& p) {
+  std::vector<std::pair<int64_t, bool>> keys;
+  for (const auto& kv : p.tuned_path) keys.push_back(kv.first);
+  for (const auto& kv : p.tuned_sites)
+    if (!p.tuned_path.count(kv.first)) keys.push_back(kv.first);
+  std::sort(keys.begin(), keys.end());
+  return keys;
+}
+
+}  // namespace
+
+int64_t pgbp_plan_tuning_count(const pgbp_plan* plan) {
+  if (!plan) return 0;
+  std::lock_guard<std::mutex> lock(plan->p.tune_mu);
+  return (int64_t)tuning_keys(plan->p).size();
+}
+
+int pgbp_plan_tuning_get(const pgbp_plan* plan, pgbp_tuning_entry* entries, int64_t max_entries) {
+  if (!plan || (max_entries > 0 && !entries)) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  const pgbp::Plan& p = plan->p;
+  std::lock_guard<std::mutex> lock(p.tune_mu);
+  const auto keys = tuning_keys(p);
+  for (int64_t i = 0; i < (int64_t)keys.size() && i < max_entries; ++i) {
+    pgbp_tuning_entry& e = entries[i];
+    memset(&e, 0, sizeof(e));
+    e.batch = keys[(size_t)i].first;
+    e.temperature0 = keys[(size_t)i].second ? 1 : 0;
+    auto pt = p.tuned_path.find(keys[(size_t)i]);
+    e.path = pt != p.tuned_path.end() ? pt->second : -1;
+    auto st = p.tuned_sites.find(keys[(size_t)i]);
+    if (st != p.tuned_sites.end() && st->second.size() <= PGBP_TUNE_MAX_SITES) {
+      e.num_sites = (int32_t)st->second.size();
+      for (size_t k = 0; k < st->second.size(); ++k) e.site[k] = st->second[k];
+    }
+  }
+  return PGBP_OK;
+}
+
+int pgbp_plan_tuning_set(const pgbp_plan* plan, const pgbp_tuning_entry* entries,
+                         int64_t num_entries) {
+  if (!plan || (num_entries > 0 && !entries)) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  const pgbp::Plan& p = plan->p;
+  const int sites = 3 + (int)p.pairwise.size();
+  for (int64_t i = 0; i < num_entries; ++i) {
+    const pgbp_tuning_entry& e = entries[i];
+    if (e.batch <= 0 || e.path < -1 || e.path > 2 || (e.num_sites != 0 && e.num_sites != sites))
+      return fail(PGBP_ERR_INVALID_ARGUMENT, "tuning entry %lld does not fit this plan", (long long)i);
+    for (int k = 0; k < e.num_sites; ++k)
+      if (e.site[k] < -1 || e.site[k] > 1)
+        return fail(PGBP_ERR_INVALID_ARGUMENT, "tuning entry %lld: variant out of range", (long long)i);
+    if ((e.path == 1 && p.small_graph_smem == 0) || (e.path == 2 && p.cluster_size == 0))
+      return fail(PGBP_ERR_INVALID_ARGUMENT, "tuning entry %lld: path not available", (long long)i);
+  }
+  std::lock_guard<std::mutex> lock(p.tune_mu);
+  for (int64_t i = 0; i < num_entries; ++i) {
+    const pgbp_tuning_entry& e = entries[i];
+    const std::pair<int64_t, bool> key{e.batch, e.temperature0 != 0};
+    if (e.path >= 0) p.tuned_path[key] = e.path;
+    if (e.num_sites > 0) p.tuned_sites[key] = std::vector<int>(e.site, e.site + e.num_sites);
+  }
+  return PGBP_OK;
+}
+
+int pgbp_plan_signature(const pgbp_plan* plan, char* buf, size_t len) {
+  if (!plan || !buf || len == 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  const pgbp::Plan& p = plan->p;
+  std::string sig = "pgbp200|sm=" + std::to_string(p.sm_count) + "|es=" +
+                    std::to_string(p.num_edge_states) + "|vs=" + std::to_string(p.num_var_states) +
+                    "|slots=" + std::to_string(p.num_slots) + "|vb=" +
+                    std::to_string(p.varsum_binary.count) + "|vo=" +
+                    std::to_string(p.varsum_other.count) + "|pw=";
+  for (const pgbp::PairwiseBucket& q : p.pairwise)
+    sig += std::to_string(q.n1) + "x" + std::to_string(q.n2) + ":" + std::to_string(q.count) + ":" +
+           std::to_string(q.n_groups) + ",";
+  sig += "|gen=" + std::to_string(p.enum_generic.count) + "|or=" +
+         std::to_string(p.logical[0].count) + ":" + std::to_string(p.logical[0].num_parents) +
+         "|and=" + std::to_string(p.logical[1].count) + ":" +
+         std::to_string(p.logical[1].num_parents) + "|pool=" + std::to_string(p.pool.count) +
+         "|flags=" + std::to_string(p.flags);
+  if (sig.size() + 1 > len) return fail(PGBP_ERR_INVALID_ARGUMENT, "buffer of %zu bytes, need %zu", len,
+                                        sig.size() + 1);
+  memcpy(buf, sig.c_str(), sig.size() + 1);
+  return PGBP_OK;
+}
+
 size_t pgbp_sdlp_workspace_size(const pgbp_plan* plan, int64_t batch) {
   if (!plan || batch <= 0) return 0;
   return pgbp::sdlp_workspace_bytes(plan->p, batch);

@@ -5,14 +5,23 @@ is a libpgbp kernel. There is no CPU path: without a CUDA device (or without lib
 raises.
 """
 
+import atexit
 import ctypes
-from typing import Dict, Optional, Tuple
+import json
+import os
+import weakref
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
 from . import native
 
 TYPE_KEYS = ("enum", "or", "and", "pool")
+
+# A JSON file caching the autotuner's decision tables across processes, keyed by plan signature
+# ({signature: [entries]}): read when a plan is created, merged and written back at exit.
+TUNE_CACHE_ENV = "PGBP_TUNE_CACHE"
+_LIVE_PLANS = weakref.WeakSet()
 
 
 def _torch():
@@ -99,6 +108,12 @@ class Plan:
     native.check(self.lib.pgbp_plan_get_info(handle, ctypes.byref(info)), "pgbp_plan_get_info")
     self.info = {k: int(getattr(info, k)) for k, _ in native.PlanInfo._fields_}
     del keep
+    cache = os.environ.get(TUNE_CACHE_ENV)
+    if cache:
+      table = _read_cache(cache)
+      if self.signature() in table:
+        self.load_tuning(table[self.signature()])
+    _LIVE_PLANS.add(self)
 
   def __del__(self):
     h = getattr(self, "handle", None)
@@ -108,6 +123,49 @@ class Plan:
       except Exception:  # pylint: disable=broad-except
         pass
       self.handle = None
+
+  # ------------------------------------------------------------------------- autotuner
+  def signature(self) -> str:
+    buf = ctypes.create_string_buffer(1024)
+    native.check(self.lib.pgbp_plan_signature(self.handle, buf, len(buf)), "pgbp_plan_signature")
+    return buf.value.decode()
+
+  def tuning(self) -> List[Dict]:
+    """The autotuner's decisions so far: one dict per (batch, temperature == 0) with the
+    execution path (-1: not tuned) and the kernel variant of every multi-kernel launch site."""
+    n = int(self.lib.pgbp_plan_tuning_count(self.handle))
+    arr = (native.TuningEntry * max(n, 1))()
+    native.check(self.lib.pgbp_plan_tuning_get(self.handle, arr, n), "pgbp_plan_tuning_get")
+    return [{"batch": int(e.batch), "temperature0": bool(e.temperature0), "path": int(e.path),
+             "sites": [int(e.site[k]) for k in range(e.num_sites)]} for e in arr[:n]]
+
+  def load_tuning(self, entries: List[Dict]):
+    """Installs decisions (as tuning() returns them); later runs with those keys skip timing."""
+    arr = (native.TuningEntry * max(len(entries), 1))()
+    for i, d in enumerate(entries):
+      sites = list(d.get("sites", []))
+      if len(sites) > native.TUNE_MAX_SITES:
+        raise ValueError("too many launch sites in a tuning entry")
+      arr[i].batch = int(d["batch"])
+      arr[i].temperature0 = int(bool(d["temperature0"]))
+      arr[i].path = int(d.get("path", -1))
+      arr[i].num_sites = len(sites)
+      for k, v in enumerate(sites):
+        arr[i].site[k] = int(v)
+    native.check(self.lib.pgbp_plan_tuning_set(self.handle, arr, len(entries)),
+                 "pgbp_plan_tuning_set")
+
+  def save_tuning(self, path: str):
+    """Merges this plan's decisions into the JSON decision table at `path`."""
+    table = _read_cache(path)
+    mine = {(e["batch"], e["temperature0"]): e for e in table.get(self.signature(), [])}
+    for e in self.tuning():
+      mine[(e["batch"], e["temperature0"])] = e
+    table[self.signature()] = list(mine.values())
+    tmp = f"{path}.tmp{os.getpid()}"
+    with open(tmp, "w") as f:
+      json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
 
   # ------------------------------------------------------------------------- helpers
   def _dev(self, x, dtype=None):
@@ -390,3 +448,25 @@ class Plan:
     native.check(self.lib.pgbp_marginals(self.handle, self._stream(), B, b_t.data_ptr(), bs,
                                          out.data_ptr()), "pgbp_marginals")
     return out if b.ndim == 2 else out[0]
+
+
+def _read_cache(path: str) -> Dict:
+  try:
+    with open(path) as f:
+      table = json.load(f)
+    return table if isinstance(table, dict) else {}
+  except (OSError, ValueError):
+    return {}
+
+
+@atexit.register
+def _save_live_tunings():
+  path = os.environ.get(TUNE_CACHE_ENV)
+  if not path:
+    return
+  for plan in list(_LIVE_PLANS):
+    try:
+      if plan.handle is not None and plan.tuning():
+        plan.save_tuning(path)
+    except Exception:  # pylint: disable=broad-except
+      pass

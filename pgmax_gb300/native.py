@@ -148,6 +148,10 @@ SIGNATURES = [
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
     ("pgbp_decode", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_marginals", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
+    ("pgbp_plan_tuning_count", _i64, [_p]),
+    ("pgbp_plan_tuning_get", ctypes.c_int, [_p, _p, _i64]),
+    ("pgbp_plan_tuning_set", ctypes.c_int, [_p, _p, _i64]),
+    ("pgbp_plan_signature", ctypes.c_int, [_p, ctypes.c_char_p, ctypes.c_size_t]),
     ("pgbp_sdlp_workspace_size", ctypes.c_size_t, [_p, _i64]),
     ("pgbp_sdlp_objective", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _d, _p, _p,
                                            _p, _p, _p, ctypes.c_size_t]),
@@ -205,6 +209,14 @@ def check(code, what=""):
 
 def profile_enable(on=True):
   load().pgbp_profile_enable(1 if on else 0)
+
+
+TUNE_MAX_SITES = 64
+
+
+class TuningEntry(ctypes.Structure):
+  _fields_ = [("batch", _i64), ("temperature0", ctypes.c_int32), ("path", ctypes.c_int32),
+              ("num_sites", ctypes.c_int32), ("site", ctypes.c_int32 * TUNE_MAX_SITES)]
 
 
 def profile_read():

@@ -15,7 +15,8 @@ HEADERS = sorted(glob.glob(os.path.join(native.ROOT, "include", "*.h")))
 
 def declared_functions():
   text = "".join(open(h).read() for h in HEADERS)
-  return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(pgbp_\w+)\s*\(", text, re.M)))
+  return sorted(set(re.findall(r"^\s*(?:int|int64_t|size_t|const char\*)\s+(pgbp_\w+)\s*\(",
+                              text, re.M)))
 
 
 def test_header_declares_expected_entry_points():
