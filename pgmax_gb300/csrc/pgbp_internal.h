@@ -137,6 +137,10 @@ struct Plan {
   int32_t* edge_slot = nullptr;     // [num_edges + 1] first slot of each edge
   int64_t num_factors = 0;
   int32_t* fac_edge_off = nullptr;  // [num_factors + 1] first edge of each factor (SDLP)
+  // every edge binary and no variable with more than kInlineMaxDegree edges: the cluster path may
+  // compute a factor's variable sums inline (vb_unit_of_vs[first state] = its binary varsum unit)
+  bool inline_vsum = false;
+  int32_t* vb_unit_of_vs = nullptr;  // [num_var_states], -1 where no unit starts
   int32_t* var_off = nullptr;       // [num_variables + 1] (decode / marginals), may be null
   int32_t* var_of_vs = nullptr;     // [num_var_states] evidence_to_vars (energy), may be null
   std::vector<EnergySeg> energy_segs;

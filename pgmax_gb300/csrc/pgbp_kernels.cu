@@ -27,6 +27,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "pgbp_internal.h"
 
@@ -1101,7 +1102,39 @@ __global__ void __launch_bounds__(256) varsum_binary_x4_kernel(VarsumDev v, bool
 constexpr int kSmallMaxBuckets = 4;
 constexpr int kSmallThreads = 1024;
 
+// Fused with each variable's two sums formed inline, for graphs whose edges are all binary: the
+// evidence plus the variable's compressed slots in the order of varsum_binary_unit (the same
+// float additions, so the same values as a variable-sum pass), so an iteration needs no phase
+// (and no barrier) between the variable sums and the factor updates.
+struct FusedInline : Fused {
+  VarsumDev vb;
+  bool runs;
+  const int32_t* __restrict__ unit_of_vs;
+  const float* __restrict__ ev;
+  int64_t evs, evb;
+
+  __device__ __forceinline__ void load(const EdgeRef& r, int k, int64_t b, float* old,
+                                       float* vt) const {
+    (void)k;  // every edge of an eligible graph is binary
+    decode2(cur[r.slot * B + b], old[0], old[1]);
+    const int64_t u = __ldg(unit_of_vs + r.vs0);
+    float s0 = ev[r.vs0 * evs + b * evb];
+    float s1 = ev[(r.vs0 + 1) * evs + b * evb];
+    const float* col = cur + b;
+    for_each_slot<16>(vb, runs, u, [&](int64_t slot) { return col[slot * B]; },
+                      [&](float c) {
+                        float m0, m1;
+                        decode2(c, m0, m1);
+                        s0 += m0;
+                        s1 += m1;
+                      });
+    vt[0] = s0 - old[0];
+    vt[1] = s1 - old[1];
+  }
+};
+
 struct SmallGraph {
+  const int32_t* unit_of_vs;  // inline variable sums (Plan::vb_unit_of_vs), or null
   PairwiseDev pw[kSmallMaxBuckets];
   int n_pw;
   EnumGenericDev eg;
@@ -1197,7 +1230,9 @@ __global__ void __launch_bounds__(kSmallThreads) small_graph_kernel(SmallGraph g
 // acquire semantics, which order their global-memory writes), so an iteration costs two cluster
 // barriers and the work of one instance is spread over up to 16 SMs. State stays in the run
 // layout in global memory (L2-resident for the graphs this path is chosen for).
-template <bool T0, int MAXES>
+// INL: the variable sums are formed inline by the factor units (FusedInline; all-binary Enum
+// graphs of low degree), which leaves one cluster barrier per iteration.
+template <bool T0, int MAXES, bool INL>
 __global__ void __launch_bounds__(kSmallThreads) cluster_graph_kernel(SmallGraph g, int64_t B,
                                                                       int64_t iters, float t,
                                                                       bool low_t, float* m0,
@@ -1210,7 +1245,7 @@ __global__ void __launch_bounds__(kSmallThreads) cluster_graph_kernel(SmallGraph
   const int64_t inst = blockIdx.x / csize;
   const int64_t tid = (int64_t)cluster.block_rank() * blockDim.x + threadIdx.x;
   const int64_t nt = csize * blockDim.x;
-  Fused c;
+  typename std::conditional<INL, FusedInline, Fused>::type c;
   c.vsum = vsum;
   c.lp = g.lp;
   c.lps = g.lps;
@@ -1218,14 +1253,24 @@ __global__ void __launch_bounds__(kSmallThreads) cluster_graph_kernel(SmallGraph
   c.B = B;
   c.d = g.d;
   c.omd = g.omd;
+  if constexpr (INL) {
+    c.vb = g.vb;
+    c.runs = g.vb_runs;
+    c.unit_of_vs = g.unit_of_vs;
+    c.ev = g.ev;
+    c.evs = g.evs;
+    c.evb = g.evb;
+  }
   float* cur = m0;
   float* nxt = m1;
   for (int64_t it = 0; it < iters; ++it) {
-    for (int64_t u = tid; u < g.vb.count; u += nt)
-      varsum_binary_unit(g.vb, g.vb_runs, u, inst, cur, g.ev, g.evs, g.evb, vsum, B);
-    for (int64_t u = tid; u < g.vo.count; u += nt)
-      varsum_other_unit(g.vo, g.vo_runs, u, inst, cur, g.ev, g.evs, g.evb, vsum, B);
-    cluster.sync();
+    if constexpr (!INL) {
+      for (int64_t u = tid; u < g.vb.count; u += nt)
+        varsum_binary_unit(g.vb, g.vb_runs, u, inst, cur, g.ev, g.evs, g.evb, vsum, B);
+      for (int64_t u = tid; u < g.vo.count; u += nt)
+        varsum_other_unit(g.vo, g.vo_runs, u, inst, cur, g.ev, g.evs, g.evb, vsum, B);
+      cluster.sync();
+    }
     c.cur = cur;
     c.nxt = nxt;
     float dmax = 0.0f;
@@ -1764,8 +1809,11 @@ cudaError_t launch_cluster_t(cudaStream_t s, const SmallGraph& g, int64_t B, int
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, cluster_graph_kernel<T0, MAXES>, g, B, iters, t, low_t, m0, m1,
-                            vsum, dacc);
+  if (g.unit_of_vs != nullptr)
+    return cudaLaunchKernelEx(&cfg, cluster_graph_kernel<T0, MAXES, true>, g, B, iters, t, low_t,
+                              m0, m1, vsum, dacc);
+  return cudaLaunchKernelEx(&cfg, cluster_graph_kernel<T0, MAXES, false>, g, B, iters, t, low_t, m0,
+                            m1, vsum, dacc);
 }
 
 template <bool T0>
@@ -1783,8 +1831,12 @@ cudaError_t launch_cluster(cudaStream_t s, const Plan& p, const SmallGraph& g, i
 
 template <bool T0, int MAXES>
 cudaError_t allow_big_cluster() {
-  return cudaFuncSetAttribute(cluster_graph_kernel<T0, MAXES>,
-                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaError_t e = cudaFuncSetAttribute(cluster_graph_kernel<T0, MAXES, false>,
+                                       cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(cluster_graph_kernel<T0, MAXES, true>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
 }
 
 // Largest cluster (16, else 8) that a 1024-thread CTA of the cluster kernel can be launched with.
@@ -1809,8 +1861,11 @@ int cluster_size_for(const Plan& p) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    cudaError_t q = cudaOccupancyMaxActiveClusters(&n, cluster_graph_kernel<true, 8>, &cfg);
-    if (q == cudaSuccess && n > 0) return cs;
+    cudaError_t q = cudaOccupancyMaxActiveClusters(&n, cluster_graph_kernel<true, 8, false>, &cfg);
+    int n2 = 0;
+    if (q == cudaSuccess)
+      q = cudaOccupancyMaxActiveClusters(&n2, cluster_graph_kernel<false, 8, true>, &cfg);
+    if (q == cudaSuccess && n > 0 && n2 > 0) return cs;
     cudaGetLastError();
   }
   cudaGetLastError();
@@ -2048,6 +2103,7 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     g.vo = dev(p.varsum_other);
     g.vb_runs = p.varsum_binary.use_runs;
     g.vo_runs = p.varsum_other.use_runs;
+    g.unit_of_vs = p.inline_vsum ? p.vb_unit_of_vs : nullptr;
     g.num_slots = p.num_slots;
     g.num_var_states = p.num_var_states;
     g.ev = evp;

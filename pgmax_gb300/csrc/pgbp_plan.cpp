@@ -348,6 +348,17 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   };
   fill_varsum(p.varsum_binary, vb_vs, vb_off, vb_slots);
   fill_varsum(p.varsum_other, vo_vs, vo_off, vo_slots);
+  {
+    // inline variable sums (cluster path): all-binary graphs of low degree
+    bool ok = vo_vs.empty() && 2 * p.num_slots == ns && !vb_vs.empty();
+    for (size_t u = 0; ok && u < vb_vs.size(); ++u) ok = vb_off[u + 1] - vb_off[u] <= 16;
+    if (ok) {
+      std::vector<int32_t> unit_of(nvs, -1);
+      for (size_t u = 0; u < vb_vs.size(); ++u) unit_of[vb_vs[u]] = (int32_t)u;
+      p.vb_unit_of_vs = bd.upload(unit_of);
+      p.inline_vsum = true;
+    }
+  }
   if (bd.err) return bail(bd.err);
   // the non-binary variables by variable, when every one of their edges has all K states
   if (!vo_vs.empty()) {
@@ -722,6 +733,10 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     p.var_of_vs = bd.upload(std::vector<int32_t>(d->evidence_to_vars, d->evidence_to_vars + nvs));
     if (bd.err) return bail(bd.err);
   }
+  // inline variable sums only for graphs of Enum factors: the OR / AND / Pool units load each
+  // parent's messages several times, which would repeat the sums
+  p.inline_vsum = p.inline_vsum && p.logical[0].count == 0 && p.logical[1].count == 0 &&
+                  p.pool.count == 0;
   pgbp::energy_plan(p);
 
   p.flags = d->flags;
