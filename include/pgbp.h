@@ -253,14 +253,15 @@ int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const flo
 
 /* Autotuner decisions. pgbp_run times, once per (batch, temperature == 0), the eligible execution
  * paths and then, on the multi-kernel path, the kernel variants of each launch site (the binary
- * variable sums: 1 or 4 instances per thread; each dense 2 x 2 pairwise bucket: 1 or 4 instances
- * per thread; OR and AND: a thread or a warp per factor). Those variants give bit-identical
- * results. A site of shared K x K tables at temperature > 0 is not timed (the exp-domain
- * tensor-core kernel, variant 1, agrees with the direct kernel, variant 0, within float32
- * accuracy only) but may be set here. These calls export and import the decision table so that a
- * host can cache it across processes: sites are site[0] the binary variable sums, site[1 .. B] the pairwise buckets
- * in plan order, then OR, AND (num_sites = 3 + number of pairwise buckets); -1 = the built-in
- * rule; path -1 = not tuned. pgbp_plan_signature writes a string identifying the plan's structure
+ * variable sums: 1 or 4 instances per thread; the other variable sums: per state or by
+ * variable; each dense 2 x 2 pairwise bucket: 1 or 4 instances per thread; OR and AND: a thread
+ * or a warp per factor). Those variants give bit-identical results. A site of shared K x K tables
+ * at temperature > 0 is not timed (the exp-domain tensor-core kernel, variant 1, agrees with the
+ * direct kernel, variant 0, within float32 accuracy only) but may be set here. These calls export
+ * and import the decision table so that a host can cache it across processes: sites are site[0]
+ * the binary variable sums, site[1] the other variable sums, site[2 .. P + 1] the P pairwise
+ * buckets in plan order, then OR, AND (num_sites = 4 + P); -1 = the built-in rule; path -1 = not
+ * tuned. pgbp_plan_signature writes a string identifying the plan's structure
  * and the device's SM count: the key under which a table may be reused. */
 #define PGBP_TUNE_MAX_SITES 64
 typedef struct {

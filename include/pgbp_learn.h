@@ -3,9 +3,9 @@
  * No counterpart in PGMax: the reference has no learned initialisation. A small convolutional
  * network (pgmax_gb300/warmstart) maps each variable's unaries and couplings to initial
  * log-messages of its edges; plain BP (pgbp_run) then runs from them. These entry points are the
- * network's training and inference kernels: 3x3 convolutions with circular padding (toroidal
- * grids) over NHWC BF16 images with FP32 accumulation on the tensor cores, their gradients, a
- * mean-centred squared-error loss and Adam. Conventions as in pgbp.h (status codes, caller's
+ * network's training and inference kernels: its input features, 3x3 convolutions with circular
+ * padding (toroidal grids) over NHWC BF16 images with FP32 accumulation on the tensor cores, their
+ * gradients, a mean-centred squared-error loss and Adam. Conventions as in pgbp.h (status codes, caller's
  * stream, caller-owned device buffers, pgbp_last_error).
  *
  * Layouts: images [n][h][w][c] BF16, c contiguous; weights [9][co][ci] BF16, tap
@@ -51,6 +51,16 @@ int pgbp_center_mse(void* stream, int64_t groups, int group, const float* pred,
  * the BF16 copy w_bf16 when it is not NULL. */
 int pgbp_adam(void* stream, int64_t n, float* w, const float* g, float* m, float* v, void* w_bf16,
               float lr, float beta1, float beta2, float eps, int64_t step);
+
+/* The network's inputs for toroidal L x L Potts grids with K-state variables and per-edge tables
+ * J_e I_K (the warm-start family): J [n][2 L^2] FP32 (down factors (i, j)-(i+1, j), then right
+ * factors (i, j)-(i, j+1)), u [n][L^2][K] FP32 unaries. Per variable and each of its factors in
+ * the order down, right, up, left (coupling J_k, other variable's unaries a_k): the closed-form
+ * one-step message m_k(s) = log(exp(logsumexp(a_k)) + expm1(J_k) exp(a_k(s))) minus its maximum.
+ * x [n][L][L][64] BF16 = (unaries minus their mean, the four couplings, the four messages, zeros);
+ * m1 [n][L][L][4 K] FP32 = the four messages. Supported: K = 8, L >= 3. */
+int pgbp_potts_features(void* stream, int64_t n, int L, int K, const float* J, const float* u,
+                        void* x, float* m1);
 
 #ifdef __cplusplus
 }

@@ -31,48 +31,60 @@ __device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) {
 }
 
 // ------------------------------------------------------------------------------- forward
-// One CTA step = one output row (w pixels, w % 16 == 0, w <= 128) of one image; warp m owns
-// pixels 16 m .. 16 m + 15 and all co output channels. Weights stay in shared memory for the
-// CTA's whole range of rows; the three input rows are staged per output row.
+// One CTA step = kRows consecutive output rows of one image (fewer at the image's last rows);
+// w % 16 == 0, w <= 128. Warp m owns row m / (w / 16) of the step and pixels 16 (m % (w / 16)) ..
+// + 15, all co output channels. Weights stay in shared memory for the CTA's whole range of steps;
+// the kRows + 2 input rows a step reads are staged once per step (each serves three output rows),
+// with 16-byte copies.
 template <int CI, int CO>
 struct ConvSmem {
   static constexpr int kLd = CI + 8;  // BF16 row stride (conflict-free 32-bit fragment loads)
-  static size_t bytes(int w) { return sizeof(__nv_bfloat16) * (size_t)(9 * CO + 3 * w) * kLd; }
+  static constexpr int kRows = 4;     // output rows per CTA step
+  static size_t bytes(int w) {
+    return sizeof(__nv_bfloat16) * (size_t)(9 * CO + (kRows + 2) * w) * kLd;
+  }
 };
 
 template <int CI, int CO>
-__global__ void conv3x3_kernel(int64_t n, int h, int w, const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(1024) conv3x3_kernel(int64_t n, int h, int w,
+                                                       const __nv_bfloat16* __restrict__ in,
                                const __nv_bfloat16* __restrict__ wts,
                                const float* __restrict__ bias, void* __restrict__ out,
                                int out_f32, int relu, const __nv_bfloat16* __restrict__ mask,
-                               int64_t rows_per_cta) {
+                               int64_t steps_per_cta) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int kLd = ConvSmem<CI, CO>::kLd;
+  constexpr int kRows = ConvSmem<CI, CO>::kRows;
   __nv_bfloat16* s_w = reinterpret_cast<__nv_bfloat16*>(smem_raw);  // [9][CO][kLd]
-  __nv_bfloat16* s_in = s_w + 9 * CO * kLd;                          // [3][w][kLd]
+  __nv_bfloat16* s_in = s_w + 9 * CO * kLd;                          // [kRows + 2][w][kLd]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
+  const int wpr = w / 16;             // warps per output row
+  const int j = warp / wpr;           // this warp's row within a step
+  const int x0 = (warp % wpr) * 16;   // and its first pixel
   for (int x = threadIdx.x; x < 9 * CO * CI; x += blockDim.x) {
     const int t = x / (CO * CI), o = (x / CI) % CO, i = x % CI;
     s_w[(t * CO + o) * kLd + i] = wts[x];
   }
-  const int64_t total = n * h;
-  const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
-  const int64_t r1 = r0 + rows_per_cta < total ? r0 + rows_per_cta : total;
-  for (int64_t r = r0; r < r1; ++r) {
-    const int64_t b = r / h;
-    const int y = (int)(r % h);
-    __syncthreads();  // previous row's fragments read (and the weights stored)
-    for (int x = threadIdx.x; x < 3 * w * (CI / 2); x += blockDim.x) {
-      const int dy = x / (w * (CI / 2)), px = (x / (CI / 2)) % w, i2 = x % (CI / 2);
-      const int yy = (y + dy - 1 + h) % h;
-      const uint32_t v =
-          *reinterpret_cast<const uint32_t*>(in + ((b * h + yy) * w + px) * CI + 2 * i2);
-      *reinterpret_cast<uint32_t*>(s_in + (dy * w + px) * kLd + 2 * i2) = v;
+  const int64_t per_image = (h + kRows - 1) / kRows;
+  const int64_t total = n * per_image;
+  const int64_t g0 = (int64_t)blockIdx.x * steps_per_cta;
+  const int64_t g1 = g0 + steps_per_cta < total ? g0 + steps_per_cta : total;
+  for (int64_t g = g0; g < g1; ++g) {
+    const int64_t b = g / per_image;
+    const int y0 = (int)(g % per_image) * kRows;
+    const int nrows = h - y0 < kRows ? h - y0 : kRows;
+    __syncthreads();  // previous step's fragments read (and the weights stored)
+    // input rows y0 - 1 .. y0 + nrows (circular), 8 channels per copy
+    for (int x = threadIdx.x; x < (nrows + 2) * w * (CI / 8); x += blockDim.x) {
+      const int dy = x / (w * (CI / 8)), px = (x / (CI / 8)) % w, i8 = x % (CI / 8);
+      const int yy = (y0 + dy - 1 + h) % h;
+      *reinterpret_cast<uint4*>(s_in + (dy * w + px) * kLd + 8 * i8) =
+          *reinterpret_cast<const uint4*>(in + ((b * h + yy) * w + px) * CI + 8 * i8);
     }
     __syncthreads();
-    const int x0 = warp * 16;
-    if (x0 < w) {
+    if (j < nrows) {
+      const int y = y0 + j;
       float acc[CO / 8][4];
 #pragma unroll
       for (int nb = 0; nb < CO / 8; ++nb)
@@ -82,8 +94,8 @@ __global__ void conv3x3_kernel(int64_t n, int h, int w, const __nv_bfloat16* __r
       for (int t = 0; t < 9; ++t) {
         const int dy = t / 3, dx = t % 3 - 1;
         const int xa = (x0 + gid + dx + w) % w, xb = (x0 + gid + 8 + dx + w) % w;
-        const __nv_bfloat16* ra = s_in + (dy * w + xa) * kLd;
-        const __nv_bfloat16* rb = s_in + (dy * w + xb) * kLd;
+        const __nv_bfloat16* ra = s_in + ((j + dy) * w + xa) * kLd;
+        const __nv_bfloat16* rb = s_in + ((j + dy) * w + xb) * kLd;
 #pragma unroll
         for (int k0 = 0; k0 < CI; k0 += 16) {
           const uint32_t a[4] = {ld32(ra + k0 + 2 * tig), ld32(rb + k0 + 2 * tig),
@@ -266,6 +278,77 @@ __global__ void adam_kernel(int64_t n, float* __restrict__ w, const float* __res
   }
 }
 
+// ------------------------------------------------------------------------------- Potts features
+// Network inputs and closed-form one-step messages of toroidal L x L Potts grids with K-state
+// variables and per-edge tables J_e I_K (pgmax_gb300/warmstart/potts.py): J [n][2 L^2] (down
+// factors (i, j)-(i+1, j) first, then right factors (i, j)-(i, j+1)), u [n][L^2][K]. Per variable,
+// its four factors in the order down, right, up, left, with coupling J_k and the other variable's
+// unaries a_k: one-step message m_k(s) = log(exp(lse(a_k)) + expm1(J_k) exp(a_k(s))), minus its
+// maximum over s. x[n][i][j][64] (BF16) = (u - mean u, the four couplings, the four messages,
+// zeros); m1[n][i][j][4 K] (FP32) = the four messages. One thread per (instance, variable).
+template <int K>
+__global__ void potts_features_kernel(int64_t n, int L, const float* __restrict__ J,
+                                      const float* __restrict__ u,
+                                      __nv_bfloat16* __restrict__ x, float* __restrict__ m1) {
+  constexpr int kCh = 64;
+  const int64_t total = n * (int64_t)L * L;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = q / ((int64_t)L * L);
+    const int p = (int)(q % ((int64_t)L * L));
+    const int i = p / L, j = p % L;
+    const int up = ((i - 1 + L) % L) * L + j, down = ((i + 1) % L) * L + j;
+    const int left = i * L + (j - 1 + L) % L, right = i * L + (j + 1) % L;
+    const float* Jb = J + b * 2LL * L * L;
+    const float* ub = u + b * (int64_t)L * L * K;
+    const float cpl[4] = {Jb[p], Jb[L * L + p], Jb[up], Jb[L * L + left]};
+    const int nb[4] = {down, right, up, left};
+    float out[kCh];
+    float mean = 0.0f;
+#pragma unroll
+    for (int s = 0; s < K; ++s) mean += ub[(int64_t)p * K + s];
+    mean = mean / (float)K;
+#pragma unroll
+    for (int s = 0; s < K; ++s) out[s] = ub[(int64_t)p * K + s] - mean;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[K + k] = cpl[k];
+    float* mo = m1 + q * 4 * K;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float a[K];
+      float mx = -INFINITY;
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        a[s] = ub[(int64_t)nb[k] * K + s];
+        mx = fmaxf(mx, a[s]);
+      }
+      float se = 0.0f;
+#pragma unroll
+      for (int s = 0; s < K; ++s) se += expf(a[s] - mx);
+      const float tot = expf(mx + logf(se));  // exp(logsumexp(a)), as the torch form computes it
+      const float em = expm1f(cpl[k]);
+      float mk[K];
+      float top = -INFINITY;
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        mk[s] = logf(tot + em * expf(a[s]));
+        top = fmaxf(top, mk[s]);
+      }
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        const float v = mk[s] - top;
+        out[K + 4 + k * K + s] = v;
+        mo[k * K + s] = v;
+      }
+    }
+#pragma unroll
+    for (int c = K + 4 + 4 * K; c < kCh; ++c) out[c] = 0.0f;
+    __nv_bfloat162* xo = reinterpret_cast<__nv_bfloat162*>(x + q * kCh);
+#pragma unroll
+    for (int c = 0; c < kCh / 2; ++c) xo[c] = __floats2bfloat162_rn(out[2 * c], out[2 * c + 1]);
+  }
+}
+
 int sm_count() {
   static int n = [] {
     int d = 0, c = 0;
@@ -292,11 +375,18 @@ cudaError_t launch_conv(cudaStream_t s, int64_t n, int h, int w, const void* in,
     if (e != cudaSuccess) return e;
     attr = smem;
   }
-  const int64_t rows = n * h;
-  const int64_t ctas = std::min<int64_t>(rows, (int64_t)sm_count() * 2);
-  const int64_t per = (rows + ctas - 1) / ctas;
-  const int threads = 32 * ((w + 15) / 16);
-  conv3x3_kernel<CI, CO><<<(unsigned)((rows + per - 1) / per), threads, smem, s>>>(
+  constexpr int kRows = ConvSmem<CI, CO>::kRows;
+  const int64_t steps = n * ((h + kRows - 1) / kRows);
+  int per_sm = 1;
+  const int threads = 32 * kRows * (w / 16);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3x3_kernel<CI, CO>, threads,
+                                                    smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  const int64_t ctas = std::min<int64_t>(steps, (int64_t)sm_count() * per_sm);
+  const int64_t per = (steps + ctas - 1) / ctas;
+  conv3x3_kernel<CI, CO><<<(unsigned)((steps + per - 1) / per), threads, smem, s>>>(
       n, h, w, static_cast<const __nv_bfloat16*>(in), static_cast<const __nv_bfloat16*>(wts), bias,
       out, out_f32, relu, static_cast<const __nv_bfloat16*>(mask), per);
   return cudaGetLastError();
@@ -399,6 +489,20 @@ int pgbp_adam(void* stream, int64_t n, float* w, const float* g, float* m, float
       n, w, g, m, v, static_cast<__nv_bfloat16*>(w_bf16), lr, beta1, beta2, eps, c1, c2);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PGBP_OK : fail(PGBP_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int pgbp_potts_features(void* stream, int64_t n, int L, int K, const float* J, const float* u,
+                        void* x, float* m1) {
+  if (n <= 0 || L < 3 || K != 8) return fail(PGBP_ERR_INVALID_ARGUMENT, "supported: n > 0, L >= 3, K = 8");
+  if (!J || !u || !x || !m1) return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t total = n * (int64_t)L * L;
+  const int64_t blocks = std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+  potts_features_kernel<8><<<(unsigned)blocks, 256, 0, s>>>(
+      n, L, J, u, static_cast<__nv_bfloat16*>(x), m1);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(PGBP_ERR_CUDA, cudaGetErrorString(e));
+  return PGBP_OK;
 }
 
 }  // extern "C"

@@ -158,8 +158,8 @@ struct Plan {
   mutable std::mutex tune_mu;
   mutable std::map<std::pair<int64_t, bool>, int> tuned_path;
   // kernel variant per launch site of the multi-kernel path (tune_sites in pgbp_kernels.cu), per
-  // (batch, temperature == 0): site 0 the binary variable sums, 1 .. pairwise.size() the dense
-  // pairwise buckets, then OR and AND; -1 = the built-in rule
+  // (batch, temperature == 0): site 0 the binary variable sums, 1 the other variable sums,
+  // 2 .. pairwise.size() + 1 the dense pairwise buckets, then OR and AND; -1 = the built-in rule
   mutable std::map<std::pair<int64_t, bool>, std::vector<int>> tuned_sites;
   int64_t device_bytes = 0;
   std::vector<void*> allocations;

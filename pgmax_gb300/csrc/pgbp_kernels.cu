@@ -177,7 +177,9 @@ struct Fused {
       return;
     }
     float m = -INFINITY;
+#pragma unroll
     for (int i = 0; i < k; ++i) m = fmaxp(m, d * old[i] + omd * outv(i));
+#pragma unroll
     for (int i = 0; i < k; ++i) {
       const float n = d * old[i] + omd * outv(i);
       const float v = fmaxp(n - m, kMsgNegInf);
@@ -281,14 +283,18 @@ __device__ __forceinline__ void pairwise_refs(const PairwiseDev& p, int4 q, Edge
 }
 
 template <int N1, int N2, bool T0, class C>
-__global__ void __launch_bounds__(256, (N1 == 2 && N2 == 2) ? PairwiseMinBlocks<C>::value : 1)
+__global__ void __launch_bounds__(256, (N1 == 2 && N2 == 2)   ? PairwiseMinBlocks<C>::value
+                                      : (N1 == 8 && N2 == 8) ? 2
+                                                             : 1)
     pairwise_kernel(C c, PairwiseDev p, int64_t B, float t, unsigned* deltas) {
   const Lane l = lane(B);
   float dmax = 0.0f;
+  // two factors per step for tables of up to 16 entries: their loads are independent, so twice
+  // as many are in flight; larger tables keep one (two would double the live state)
+  constexpr bool kPairs = N1 > 0 && N1 * N2 <= 16;
   if (l.valid) {
     int64_t u = l.u0;
-    // two factors per step: their loads are independent, so twice as many are in flight
-    for (; u + l.ustep < p.count; u += 2 * l.ustep) {
+    for (; kPairs && u + l.ustep < p.count; u += 2 * l.ustep) {
       const int4 qa = __ldg(p.rec + u);
       const int4 qb = __ldg(p.rec + u + l.ustep);
       const int64_t ka = __ldg(p.cfg_begin + u), kb = __ldg(p.cfg_begin + u + l.ustep);
@@ -298,7 +304,7 @@ __global__ void __launch_bounds__(256, (N1 == 2 && N2 == 2) ? PairwiseMinBlocks<
       pairwise_body<N1, N2, T0>(c, a1, a2, ka, p.n1, p.n2, l.b, t, dmax);
       pairwise_body<N1, N2, T0>(c, b1, b2, kb, p.n1, p.n2, l.b, t, dmax);
     }
-    if (u < p.count) {
+    for (; u < p.count; u += l.ustep) {
       EdgeRef a1, a2;
       pairwise_refs(p, __ldg(p.rec + u), a1, a2);
       pairwise_body<N1, N2, T0>(c, a1, a2, __ldg(p.cfg_begin + u), p.n1, p.n2, l.b, t, dmax);
@@ -1599,9 +1605,11 @@ VarsumDev dev(const VarsumSet& v) {
 }
 
 // vb_variant: 0 one instance per thread for the binary variables, 1 four (B % 4 == 0), -1 the
-// built-in rule
+// built-in rule; vo_variant: the other variables' sums per state unit (0) or by variable (1, when
+// built; -1 the rule: by variable when built)
 void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, const float* ev,
-                   int64_t evs, int64_t evb, float* vsum, int vb_variant = -1) {
+                   int64_t evs, int64_t evb, float* vsum, int vb_variant = -1,
+                   int vo_variant = -1) {
   ProfileScope ps(kProfVarsum, s);
   const VarsumSet& vb = p.varsum_binary;
   // 4 instances per thread only when that still leaves >= 16 warps per SM: the per-variable sums
@@ -1618,7 +1626,7 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
                                                      B);
   }
   const VarsumSet& vo = p.varsum_other;
-  if (vo.byvar_groups > 0) {
+  if (vo.byvar_groups > 0 && vo_variant != 0) {
     const Launch2 l = launch2(vo.byvar_units, B, p.sm_count);
     varsum_byvar_kernel<<<l.grid, l.block, 0, s>>>(vo.byvar_grp, vo.byvar_groups, vo.byvar_units,
                                                     vo.byvar_vs0, vo.byvar_eoff, vo.byvar_eslot,
@@ -1653,7 +1661,7 @@ void launch_bucket(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const
   }
 }
 
-int num_sites(const Plan& p) { return 3 + (int)p.pairwise.size(); }
+int num_sites(const Plan& p) { return 4 + (int)p.pairwise.size(); }
 
 // sites: the tuned variant per launch site (tuned_sites' layout) or null for the built-in rules
 template <bool T0>
@@ -1668,16 +1676,16 @@ void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool lo
     c.cur = cur;
     c.nxt = nxt;
     unsigned* d = dacc + it * B;
-    launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum), site(0));
+    launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum), site(0), site(1));
     const float* tables = gemm_tables;
     for (int qi = 0; qi < nq; ++qi) {
       const PairwiseBucket& q = p.pairwise[qi];
-      launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(1 + qi));
+      launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(2 + qi));
       if (tables != nullptr) tables += q.gemm_floats;
     }
     launch_enum_generic<T0>(s, p, c, B, t, d);
-    launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d, site(1 + nq));
-    launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d, site(2 + nq));
+    launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d, site(2 + nq));
+    launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d, site(3 + nq));
     launch_pool<T0>(s, p, c, B, t, 1, d);
   }
 }
@@ -1732,10 +1740,12 @@ const int* tune_sites(const Plan& p, cudaStream_t s, int64_t B, Fused c, float t
     }
     return best;
   };
+  // the two variable-sum sites (binary, other) are timed with the other one's rule in place
   if (p.varsum_binary.count > 0 && B % 4 == 0)
-    choice[0] = pick(2, [&](int v) { launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, v); });
-  else
-    launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum);  // variable sums for the factor trials
+    choice[0] = pick(2, [&](int v) { launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, v, -1); });
+  if (p.varsum_other.byvar_groups > 0 && p.varsum_other.count > 0)
+    choice[1] = pick(2, [&](int v) { launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, -1, v); });
+  launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum);  // variable sums for the factor trials
   const float* tables = gemm_tables;
   for (int qi = 0; qi < nq; ++qi) {
     const PairwiseBucket& q = p.pairwise[qi];
@@ -1744,14 +1754,14 @@ const int* tune_sites(const Plan& p, cudaStream_t s, int64_t B, Fused c, float t
     // it stays the rule there (a host can still choose it through pgbp_plan_tuning_set)
     const bool two = q.n1 == 2 && q.n2 == 2 && B % 4 == 0 && q.count > 0;
     if (two)
-      choice[1 + qi] = pick(2, [&](int v) {
+      choice[2 + qi] = pick(2, [&](int v) {
         launch_bucket<T0>(s, p, q, c, B, t, dacc, tables, v);
       });
     if (tables != nullptr) tables += q.gemm_floats;
   }
   for (int w = 0; w < 2; ++w) {
     if (p.logical[w].count > 0)
-      choice[1 + nq + w] = pick(2, [&](int v) {
+      choice[2 + nq + w] = pick(2, [&](int v) {
         launch_logical<T0>(s, p, w, c, B, t, low_t, 1, dacc, v);
       });
   }

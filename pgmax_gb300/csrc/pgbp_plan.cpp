@@ -1042,7 +1042,7 @@ int pgbp_plan_tuning_set(const pgbp_plan* plan, const pgbp_tuning_entry* entries
                          int64_t num_entries) {
   if (!plan || (num_entries > 0 && !entries)) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
   const pgbp::Plan& p = plan->p;
-  const int sites = 3 + (int)p.pairwise.size();
+  const int sites = 4 + (int)p.pairwise.size();
   for (int64_t i = 0; i < num_entries; ++i) {
     const pgbp_tuning_entry& e = entries[i];
     if (e.batch <= 0 || e.path < -1 || e.path > 2 || (e.num_sites != 0 && e.num_sites != sites))

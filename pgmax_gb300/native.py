@@ -170,6 +170,7 @@ SIGNATURES = [
     ("pgbp_center_mse", ctypes.c_int, [_p, _i64, ctypes.c_int, _p, _p, _p, _p, ctypes.c_float]),
     ("pgbp_adam", ctypes.c_int, [_p, _i64, _p, _p, _p, _p, _p, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, ctypes.c_float, _i64]),
+    ("pgbp_potts_features", ctypes.c_int, [_p, _i64, ctypes.c_int, ctypes.c_int, _p, _p, _p, _p]),
     ("pgbp_profile_enable", ctypes.c_int, [ctypes.c_int]),
     ("pgbp_profile_read", ctypes.c_int, [ctypes.POINTER(Profile)]),
     ("pgbp_last_error", ctypes.c_char_p, []),

@@ -104,6 +104,27 @@ def features(J, u, L: int, K: int):
   return torch.cat(parts, -1)
 
 
+def features_and_messages(J, u, L: int, K: int):
+  """(features [n, L, L, FEATURES] BF16, one-step messages [n, L, L, 4 K] FP32) of CUDA tensors
+  J [n, 2 L^2] and u [n, L^2 K], in one pgbp_potts_features launch: the values of features() and
+  one_step_messages() above (which restate them in torch, for checking)."""
+  import ctypes  # pylint: disable=g-import-not-at-top
+  import torch  # pylint: disable=g-import-not-at-top
+  from .. import native  # pylint: disable=g-import-not-at-top
+  J = J.to(torch.float32).contiguous()
+  u = u.to(torch.float32).contiguous()
+  n = J.shape[0]
+  x = torch.empty((n, L, L, FEATURES), dtype=torch.bfloat16, device=J.device)
+  m1 = torch.empty((n, L, L, 4 * K), dtype=torch.float32, device=J.device)
+  stream = ctypes.c_void_p(torch.cuda.current_stream(J.device).cuda_stream)
+  native.check(native.load().pgbp_potts_features(stream, n, L, K, ctypes.c_void_p(J.data_ptr()),
+                                                 ctypes.c_void_p(u.data_ptr()),
+                                                 ctypes.c_void_p(x.data_ptr()),
+                                                 ctypes.c_void_p(m1.data_ptr())),
+               "pgbp_potts_features")
+  return x, m1
+
+
 def message_index(L: int, K: int) -> np.ndarray:
   """[L * L * 4 * K] flat edge state of output channel (k, s) of pixel (i, j): the message into
   variable (i, j), state s, from its down (k=0), right (1), up (2) and left (3) factor."""

@@ -6,7 +6,8 @@
                      converged messages minus the closed-form one-step messages as targets
   train              Adam on the mean-centred squared error of the predicted correction
   evaluate           held-out instances run to 1e-4 from the learned init and from a cold start:
-                     wall time, iterations, belief error against the converged solution, and the
+                     wall time (the warm start's features, one-step messages and network
+                     included), iterations, belief error against the converged solution, and the
                      fallback rate (warm starts that miss the tolerance are rerun cold)
 
 `python -m pgmax_gb300.warmstart.train --out weights.npz` trains on the GPU and saves the weights.
@@ -44,16 +45,27 @@ class Family:
     self.index = torch.as_tensor(potts.message_index(self.L, self.K), device="cuda")
     self.n_es = int(self.wiring["var_states_for_edge_states"].shape[0])
 
-  def instances(self, seed: int, n: int):
-    """(features [n, L, L, 64] BF16, one-step messages [n, L, L, 32], potentials [n, P],
-    evidence [n, N_vs]) on the GPU."""
+  def problems(self, seed: int, n: int):
+    """(couplings J [n, 2 L^2], unaries u [n, L^2 K], potentials [n, P], evidence [n, N_vs]) of n
+    instances, on the GPU."""
     torch = _torch()
     J, u = potts.sample(seed, n, self.L, self.K, SIGMA)
     J = torch.as_tensor(J, device="cuda")
     u = torch.as_tensor(u, device="cuda")
-    x = potts.features(J, u, self.L, self.K).to(torch.bfloat16).contiguous()
-    m1 = potts.one_step_messages(J, u, self.L, self.K).contiguous()
-    return x, m1, potts.potentials(J, self.K).contiguous(), u
+    return J, u, potts.potentials(J, self.K).contiguous(), u
+
+  def warm_inputs(self, J, u):
+    """The network's input features [n, L, L, 64] (BF16) and the closed-form one-step messages
+    [n, L, L, 32] it corrects (one pgbp_potts_features launch): the part of a warm start computed
+    before the network runs."""
+    return potts.features_and_messages(J, u, self.L, self.K)
+
+  def instances(self, seed: int, n: int):
+    """(features [n, L, L, 64] BF16, one-step messages [n, L, L, 32], potentials [n, P],
+    evidence [n, N_vs]) on the GPU."""
+    J, u, lp, ev = self.problems(seed, n)
+    x, m1 = self.warm_inputs(J, u)
+    return x, m1, lp, ev
 
   def to_channels(self, msgs):
     """Flat messages [n, E_s] -> network layout [n, L, L, 4 K]."""
@@ -132,7 +144,7 @@ def evaluate(fam: Family, net: Optional[convnet.ConvNet], seed: int, n: int, bat
          "onestep_iters": []}
   for k in range(0, n, batch):
     m = min(batch, n - k)
-    x, m1, lp, ev = fam.instances(seed * 1_000_003 + k, m)
+    J, u, lp, ev = fam.problems(seed * 1_000_003 + k, m)
     zeros = torch.zeros((m, fam.n_es), device="cuda")
     # the converged plain solution (the judge of belief error)
     ref, ref_first, _ = run_to_tolerance(fam.plan, lp, ev, zeros, 1e-5, max_iters, chunk=10)
@@ -145,12 +157,20 @@ def evaluate(fam: Family, net: Optional[convnet.ConvNet], seed: int, n: int, bat
     cold, cold_first, _ = run_to_tolerance(fam.plan, lp, ev, zeros, tol, max_iters, chunk)
     torch.cuda.synchronize()
     res["cold_ms"] += 1e3 * (time.perf_counter() - t0)
-    # learned warm start; instances that miss the tolerance fall back to a cold start
-    _, one_first, _ = run_to_tolerance(fam.plan, lp, ev, fam.from_channels(m1), tol, max_iters,
-                                       chunk)
+    # one-step init alone (iterations only)
+    _, m1_only = fam.warm_inputs(J, u)
+    _, one_first, _ = run_to_tolerance(fam.plan, lp, ev, fam.from_channels(m1_only), tol,
+                                       max_iters, chunk)
     res["onestep_iters"].append(one_first[ok & (one_first >= 0)])
+    # learned warm start, its inputs included; instances that miss the tolerance fall back to a
+    # cold start
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    init = fam.from_channels(m1 + net.messages(x)) if net is not None else zeros
+    if net is not None:
+      x, m1 = fam.warm_inputs(J, u)
+      init = fam.from_channels(m1 + net.messages(x))
+    else:
+      init = zeros
     warm, warm_first, _ = run_to_tolerance(fam.plan, lp, ev, init, tol, max_iters, chunk)
     miss = warm_first < 0
     if bool(miss.any()):

@@ -148,3 +148,18 @@ def test_packaged_weights_give_a_warm_start_on_the_96_family():
   res = train.evaluate(fam, net, seed=9, n=32, batch=32, max_iters=2000)
   assert res["warm_iters_mean"] < res["cold_iters_mean"], res
   assert res["warm_iters_mean"] <= res["onestep_iters_mean"], res
+
+
+def test_feature_kernel_matches_the_torch_restatement():
+  torch = _torch()
+  from pgmax_gb300.warmstart import potts  # pylint: disable=g-import-not-at-top
+  for L in (3, 16, 96):
+    J, u = potts.sample(L, 4, L, 8, 0.7)
+    J = torch.as_tensor(J, device="cuda")
+    u = torch.as_tensor(u, device="cuda")
+    x, m1 = potts.features_and_messages(J, u, L, 8)
+    want_m1 = potts.one_step_messages(J, u, L, 8)
+    want_x = potts.features(J, u, L, 8)
+    assert _rel(m1.cpu(), want_m1.cpu()) < 1e-5
+    # BF16 features: one rounding of values within 1e-5 of each other
+    assert _rel(x.float().cpu(), want_x.to(torch.bfloat16).float().cpu()) < 1e-2
