@@ -46,6 +46,16 @@ __device__ __forceinline__ float fmaxp(float a, float b) {
   asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
   return r;
 }
+// Programmatic dependent launch. A kernel launched with launch_pdl may be scheduled while the
+// kernel before it in the stream is still finishing; pdl_begin(), its first statement, waits
+// until that kernel has completed and its writes are visible (for a normal launch it returns at
+// once) and then lets the kernel after it be scheduled the same way. Only the launch latency
+// between the kernels of an iteration is hidden; no two dependent kernels overlap.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ float fminp(float a, float b) {
   float r;
   asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
@@ -287,6 +297,7 @@ __global__ void __launch_bounds__(256, (N1 == 2 && N2 == 2)   ? PairwiseMinBlock
                                       : (N1 == 8 && N2 == 8) ? 2
                                                              : 1)
     pairwise_kernel(C c, PairwiseDev p, int64_t B, float t, unsigned* deltas) {
+  pdl_begin();
   const Lane l = lane(B);
   float dmax = 0.0f;
   // two factors per step for tables of up to 16 entries: their loads are independent, so twice
@@ -384,6 +395,7 @@ __device__ __forceinline__ void enum_generic_unit(const C& c, const EnumGenericD
 template <int MAXES, bool T0, class C>
 __global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g, int64_t B,
                                                            float t, unsigned* deltas) {
+  pdl_begin();
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
@@ -498,6 +510,7 @@ __device__ __forceinline__ void logical_unit(const C& c, const LogicalDev& g, in
 template <bool T0, class C>
 __global__ void __launch_bounds__(256) logical_kernel(C c, LogicalDev g, int64_t B, float t,
                                                       bool low_t, int normalize, unsigned* deltas) {
+  pdl_begin();
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
@@ -618,6 +631,7 @@ template <bool T0, class C>
 __global__ void __launch_bounds__(256) logical_warp_kernel(C c, LogicalDev g, int64_t B, float t,
                                                            bool low_t, int normalize,
                                                            unsigned* deltas) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t wstep = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -737,6 +751,7 @@ __device__ __forceinline__ void pool_unit(const C& c, const PoolDev& g, int64_t 
 template <bool T0, class C>
 __global__ void __launch_bounds__(256) pool_kernel(C c, PoolDev g, int64_t B, float t,
                                                    int normalize, unsigned* deltas) {
+  pdl_begin();
   const Lane l = lane(B);
   float dmax = 0.0f;
   if (l.valid) {
@@ -854,6 +869,7 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 template <bool T0>
 __global__ void __launch_bounds__(256, 4) pairwise22_x4_kernel(Fused c, PairwiseDev p, float t,
                                                             unsigned* deltas) {
+  pdl_begin();
   const int64_t B = c.B;
   const Lane4 l = lane4(B);
   float4 dm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1014,6 +1030,7 @@ __global__ void __launch_bounds__(256) varsum_binary_kernel(VarsumDev v, bool us
                                                             const float* __restrict__ ev,
                                                             int64_t evs, int64_t evb,
                                                             float* __restrict__ vsum, int64_t B) {
+  pdl_begin();
   const Lane l = lane(B);
   if (!l.valid) return;
   for (int64_t u = l.u0; u < v.count; u += l.ustep)
@@ -1025,6 +1042,7 @@ __global__ void __launch_bounds__(256) varsum_other_kernel(VarsumDev v, bool use
                                                            const float* __restrict__ ev,
                                                            int64_t evs, int64_t evb,
                                                            float* __restrict__ vsum, int64_t B) {
+  pdl_begin();
   const Lane l = lane(B);
   if (!l.valid) return;
   for (int64_t u = l.u0; u < v.count; u += l.ustep)
@@ -1040,6 +1058,7 @@ __global__ void __launch_bounds__(256) varsum_byvar_kernel(
     const int32_t* __restrict__ eoff, const int32_t* __restrict__ eslot,
     const float* __restrict__ msgs, const float* __restrict__ ev, int64_t evs, int64_t evb,
     float* __restrict__ vsum, int64_t B) {
+  pdl_begin();
   const Lane l = lane(B);
   if (!l.valid) return;
   const int64_t b = l.b;
@@ -1063,6 +1082,7 @@ __global__ void __launch_bounds__(256) varsum_binary_x4_kernel(VarsumDev v, bool
                                                                const float* __restrict__ ev,
                                                                int64_t evs, int64_t evb,
                                                                float* __restrict__ vsum, int64_t B) {
+  pdl_begin();
   const Lane4 l = lane4(B);
   if (!l.valid) return;
   const int64_t b = l.b;
@@ -1532,6 +1552,23 @@ PoolDev dev(const PoolSet& g) { return PoolDev{g.ch_begin, g.ch, g.ind, g.count}
 // x4 launch: lanes over groups of 4 instances.
 Launch2 launch2_x4(int64_t units, int64_t B, int sm_count) { return launch2(units, B / 4, sm_count); }
 
+// Launches a kernel that begins with pdl_begin() as a programmatic dependent of the previous
+// kernel in the stream.
+template <class... KArgs, class... Args>
+void launch_pdl(cudaStream_t s, dim3 grid, dim3 block, void (*kernel)(KArgs...), Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <bool T0, class C>
 void launch_pairwise(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const C& c, int64_t B,
                      float t, unsigned* deltas) {
@@ -1540,13 +1577,13 @@ void launch_pairwise(cudaStream_t s, const Plan& p, const PairwiseBucket& q, con
   const Launch2 l = launch2(q.count, B, p.sm_count);
   const PairwiseDev d = dev(q);
   if (q.n1 == 2 && q.n2 == 2) {
-    pairwise_kernel<2, 2, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, pairwise_kernel<2, 2, T0, C>, c, d, B, t, deltas);
   } else if (q.n1 == 4 && q.n2 == 4) {
-    pairwise_kernel<4, 4, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, pairwise_kernel<4, 4, T0, C>, c, d, B, t, deltas);
   } else if (q.n1 == 8 && q.n2 == 8) {
-    pairwise_kernel<8, 8, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, pairwise_kernel<8, 8, T0, C>, c, d, B, t, deltas);
   } else {
-    pairwise_kernel<0, 0, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, pairwise_kernel<0, 0, T0, C>, c, d, B, t, deltas);
   }
 }
 
@@ -1559,13 +1596,13 @@ void launch_enum_generic(cudaStream_t s, const Plan& p, const C& c, int64_t B, f
   const Launch2 l = launch2(g.count, B, p.sm_count);
   const EnumGenericDev d = dev(g);
   if (g.max_es <= 8) {
-    enum_generic_kernel<8, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, enum_generic_kernel<8, T0, C>, c, d, B, t, deltas);
   } else if (g.max_es <= 32) {
-    enum_generic_kernel<32, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, enum_generic_kernel<32, T0, C>, c, d, B, t, deltas);
   } else if (g.max_es <= 128) {
-    enum_generic_kernel<128, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, enum_generic_kernel<128, T0, C>, c, d, B, t, deltas);
   } else {
-    enum_generic_kernel<512, T0><<<l.grid, l.block, 0, s>>>(c, d, B, t, deltas);
+    launch_pdl(s, l.grid, l.block, enum_generic_kernel<512, T0, C>, c, d, B, t, deltas);
   }
 }
 
@@ -1582,12 +1619,12 @@ void launch_logical(cudaStream_t s, const Plan& p, int which, const C& c, int64_
     const int64_t warps = g.count * B;
     const int64_t blocks = std::max<int64_t>(
         1, std::min<int64_t>((warps + 7) / 8, (int64_t)p.sm_count * 16));
-    logical_warp_kernel<T0><<<(unsigned)blocks, 256, 0, s>>>(c, dev(g), B, t, low_t, normalize,
-                                                             deltas);
+    launch_pdl(s, dim3((unsigned)blocks), dim3(256), logical_warp_kernel<T0, C>, c, dev(g), B, t,
+               low_t, normalize, deltas);
     return;
   }
   const Launch2 l = launch2(g.count, B, p.sm_count);
-  logical_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(g), B, t, low_t, normalize, deltas);
+  launch_pdl(s, l.grid, l.block, logical_kernel<T0, C>, c, dev(g), B, t, low_t, normalize, deltas);
 }
 
 template <bool T0, class C>
@@ -1597,7 +1634,7 @@ void launch_pool(cudaStream_t s, const Plan& p, const C& c, int64_t B, float t, 
   if (g.count == 0) return;
   ProfileScope ps(kProfPool, s);
   const Launch2 l = launch2(g.count, B, p.sm_count);
-  pool_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(g), B, t, normalize, deltas);
+  launch_pdl(s, l.grid, l.block, pool_kernel<T0, C>, c, dev(g), B, t, normalize, deltas);
 }
 
 VarsumDev dev(const VarsumSet& v) {
@@ -1618,23 +1655,23 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
                                                  : vb.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32);
   if (vb.count > 0 && x4) {
     const Launch2 l = launch2_x4(vb.count, B, p.sm_count);
-    varsum_binary_x4_kernel<<<l.grid, l.block, 0, s>>>(dev(vb), vb.use_runs, cur, ev, evs, evb,
-                                                        vsum, B);
+    launch_pdl(s, l.grid, l.block, varsum_binary_x4_kernel, dev(vb), vb.use_runs, cur, ev, evs, evb,
+               vsum, B);
   } else if (vb.count > 0) {
     const Launch2 l = launch2(vb.count, B, p.sm_count);
-    varsum_binary_kernel<<<l.grid, l.block, 0, s>>>(dev(vb), vb.use_runs, cur, ev, evs, evb, vsum,
-                                                     B);
+    launch_pdl(s, l.grid, l.block, varsum_binary_kernel, dev(vb), vb.use_runs, cur, ev, evs, evb,
+               vsum, B);
   }
   const VarsumSet& vo = p.varsum_other;
   if (vo.byvar_groups > 0 && vo_variant != 0) {
     const Launch2 l = launch2(vo.byvar_units, B, p.sm_count);
-    varsum_byvar_kernel<<<l.grid, l.block, 0, s>>>(vo.byvar_grp, vo.byvar_groups, vo.byvar_units,
-                                                    vo.byvar_vs0, vo.byvar_eoff, vo.byvar_eslot,
-                                                    cur, ev, evs, evb, vsum, B);
+    launch_pdl(s, l.grid, l.block, varsum_byvar_kernel, vo.byvar_grp, vo.byvar_groups,
+               vo.byvar_units, vo.byvar_vs0, vo.byvar_eoff, vo.byvar_eslot, cur, ev, evs, evb, vsum,
+               B);
   } else if (vo.count > 0) {
     const Launch2 l = launch2(vo.count, B, p.sm_count);
-    varsum_other_kernel<<<l.grid, l.block, 0, s>>>(dev(vo), vo.use_runs, cur, ev, evs, evb, vsum,
-                                                    B);
+    launch_pdl(s, l.grid, l.block, varsum_other_kernel, dev(vo), vo.use_runs, cur, ev, evs, evb,
+               vsum, B);
   }
 }
 
@@ -1655,7 +1692,7 @@ void launch_bucket(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const
   if (x4) {
     ProfileScope ps(kProfPairwise, s);
     const Launch2 l = launch2_x4(q.count, B, p.sm_count);
-    pairwise22_x4_kernel<T0><<<l.grid, l.block, 0, s>>>(c, dev(q), t, d);
+    launch_pdl(s, l.grid, l.block, pairwise22_x4_kernel<T0>, c, dev(q), t, d);
   } else {
     launch_pairwise<T0>(s, p, q, c, B, t, d);
   }
