@@ -345,6 +345,14 @@ typedef struct {
 int pgbp_profile_enable(int enable);
 int pgbp_profile_read(pgbp_profile* out);
 
+/* Bounded device-side waits. Kernels that wait for their own asynchronous copies (the shared
+ * K x K table of the exp-domain pairwise kernel arrives by one bulk copy on an mbarrier) give up
+ * after 2 s instead of hanging, count the wait, and continue with wrong values. This returns the
+ * count on the current device since the last call in *count and resets it: PGBP_OK when it is
+ * zero, PGBP_ERR_TIMEOUT otherwise. Synchronises the device. No reference counterpart (JAX has no
+ * device-side waits to bound). */
+int pgbp_wait_timeouts(int64_t* count);
+
 const char* pgbp_last_error(void);
 int pgbp_version(void); /* major * 10000 + minor * 100 + patch */
 

@@ -64,6 +64,63 @@ __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) 
   lo = to_tf32(x - __uint_as_float(hi));
 }
 
+// ---- bulk copies into shared memory (cp.async.bulk, completion on an mbarrier)
+// A wait that has not seen its copy land after kWaitLimitNs is counted in g_wait_timeouts and
+// returns; the host reads the count (pgbp_wait_timeouts), so a lost copy is an error status, not a
+// hang.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+__device__ unsigned long long g_wait_timeouts = 0;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from global to shared
+// memory, completing the current phase of `bar`. Shared-memory reads issued before it (by any
+// thread, ordered by a barrier) complete before the copy writes.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_addr(bar);
+  uint64_t t0 = 0;
+  for (uint32_t i = 0;; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return;
+    if ((i & 63) == 0) {
+      uint64_t now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      if (t0 == 0) {
+        t0 = now;
+      } else if (now - t0 > kWaitLimitNs) {
+        atomicAdd(&g_wait_timeouts, 1ull);
+        return;
+      }
+    }
+  }
+}
+
 // D = A B + D, A 16x8 (row), B 8x8 (col), tf32 in, fp32 accumulate.
 __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4],
                                          const uint32_t (&b)[2]) {
@@ -75,16 +132,21 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4],
 }
 
 
-// Run-time tables of one group: E [K][K] (row i, column j), E' [K][K] (row j, column i), row
-// maxima r [K], column maxima c [K]. One CTA per group.
+// Position of table column j in the permuted order of its 8-block.
+__device__ __forceinline__ int perm8(int j) { return (j & ~7) + ((j & 3) << 1) + ((j >> 2) & 1); }
+
+// Run-time tables of one group in the pairwise kernel's shared-memory layout (one bulk copy moves
+// them there): E [K][K + 8] (row i, column perm8(j)), E' [K][K + 8] (row j, column perm8(i)), zero
+// padding, row maxima r [K], column maxima c [K]. One CTA per group.
 template <int K>
 __global__ void __launch_bounds__(kThreads) expgemm_tables_kernel(
     const int32_t* __restrict__ grp_table, const float* __restrict__ lpc, float t,
     float* __restrict__ tables) {
+  constexpr int kLde = K + 8;
   const int g = blockIdx.x;
   const float* psi = lpc + grp_table[g];
   float* out = tables + (int64_t)g * expgemm_table_floats(K);
-  float *e = out, *f = out + K * K, *rmax = out + 2 * K * K, *cmax = rmax + K;
+  float *e = out, *f = out + K * kLde, *rmax = out + 2 * K * kLde, *cmax = rmax + K;
   __shared__ float rs[K], cs[K];
   for (int i = threadIdx.x; i < K; i += blockDim.x) {
     float m = -INFINITY, n = -INFINITY;
@@ -100,8 +162,12 @@ __global__ void __launch_bounds__(kThreads) expgemm_tables_kernel(
   __syncthreads();
   for (int x = threadIdx.x; x < K * K; x += blockDim.x) {
     const int i = x / K, j = x % K;
-    e[x] = expf(div_t(psi[x] - rs[i], t));
-    f[j * K + i] = expf(div_t(psi[x] - cs[j], t));
+    e[i * kLde + perm8(j)] = expf(div_t(psi[x] - rs[i], t));
+    f[j * kLde + perm8(i)] = expf(div_t(psi[x] - cs[j], t));
+  }
+  for (int x = threadIdx.x; x < 2 * K * 8; x += blockDim.x) {  // padding columns
+    const int r = x / 8, j = K + x % 8;
+    (r < K ? e : f)[(r % K) * kLde + j] = 0.0f;
   }
 }
 
@@ -142,8 +208,6 @@ struct Smem {
   static constexpr size_t kBytes = sizeof(float) * kFloats + sizeof(unsigned) * kMaxB;
 };
 
-// Position of table column j in the permuted order of its 8-block.
-__device__ __forceinline__ int perm8(int j) { return (j & ~7) + ((j & 3) << 1) + ((j >> 2) & 1); }
 
 // State of slot i (0 .. K / 4 - 1) of the thread that owns quarter `part` of a column: the pair
 // (8 kb + part, 8 kb + part + 4) for kb = i / 2, the pair the B fragment layout stores together.
@@ -253,6 +317,7 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
   unsigned* s_res = reinterpret_cast<unsigned*>(s_w + Smem<K>::kXWords / 4);
   __shared__ int s_group;
   __shared__ int64_t s_tile0;
+  __shared__ __align__(8) uint64_t s_bar;  // completion of the table copy
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = threadIdx.x >> 2, part = threadIdx.x & 3;  // column of the tile, quarter of it
@@ -263,9 +328,12 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
   const int64_t t_begin = (int64_t)blockIdx.x * a.tiles_per_cta;
   const int64_t t_end = t_begin + a.tiles_per_cta < a.n_tiles ? t_begin + a.tiles_per_cta : a.n_tiles;
   int loaded = -1;
+  uint32_t phase = 0;    // parity of s_bar's current phase
+  bool pending = false;  // a table copy this thread has not yet waited for
   if (threadIdx.x == 0) {
     s_group = 0;
     s_tile0 = 0;
+    mbar_init(&s_bar);
   }
   __syncthreads();
   for (int64_t tile = t_begin; tile < t_end; ++tile) {
@@ -290,13 +358,12 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
     const int ncols = (int)(cols - c0 < kCols ? cols - c0 : kCols);
     const int64_t table = a.grp_table[g];
     if (g != loaded) {
-      const float* src = a.tables + (int64_t)g * expgemm_table_floats(K);
-      for (int x = threadIdx.x; x < K * K; x += kThreads) {
-        const int at = (x / K) * kLde + perm8(x % K);
-        s_e[at] = src[x];
-        s_f[at] = src[K * K + x];
-      }
-      for (int x = threadIdx.x; x < 2 * K; x += kThreads) s_r[x] = src[2 * K * K + x];
+      // E, E', r, c of the group land in s_e .. s_c with one bulk copy (the table block is laid
+      // out as they are), overlapping this tile's message loads; waited for before the GEMMs
+      if (threadIdx.x == 0)
+        bulk_load(s_e, a.tables + (int64_t)g * expgemm_table_floats(K),
+                  (uint32_t)(sizeof(float) * expgemm_table_floats(K)), &s_bar);
+      pending = true;
       loaded = g;
     }
     // ---- load: every message and variable sum of this thread's states first, then the maxima
@@ -345,6 +412,11 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
       split_tf32(active ? __expf(div_t(v2[2 * kb] - m2, a.t)) : 0.0f, h0, l0);
       split_tf32(active ? __expf(div_t(v2[2 * kb + 1] - m2, a.t)) : 0.0f, h1, l1);
       s_u[(kb * 4 + part) * kLdx + c] = make_uint4(h0, h1, l0, l1);
+    }
+    if (pending) {
+      mbar_wait(&s_bar, phase);
+      phase ^= 1u;
+      pending = false;
     }
     __syncthreads();
     // ---- F1 = E U, F2 = E' W on the tensor cores, one accumulator set live at a time (each
@@ -450,6 +522,13 @@ cudaError_t launch(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const
 }  // namespace
 
 bool expgemm_eligible(const PairwiseBucket& q) { return q.n_groups > 0; }
+
+cudaError_t read_wait_timeouts(unsigned long long* count) {
+  unsigned long long zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(count, g_wait_timeouts, sizeof(*count));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_wait_timeouts, &zero, sizeof(zero));
+  return e;
+}
 
 cudaError_t expgemm_prepare(const Plan& p, const PairwiseBucket& q, cudaStream_t s,
                             const float* lpc, float t, float* tables) {

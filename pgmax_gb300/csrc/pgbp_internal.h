@@ -39,12 +39,13 @@ struct PairwiseBucket {
   int64_t gemm_floats = 0;
 };
 
-// Floats of run-time tables one group of a shared-table bucket with K x K tables needs:
-// E and E' (2 K^2) plus the row and column maxima (2 K).
+// Floats of run-time tables one group of a shared-table bucket with K x K tables needs: E and E'
+// as K rows of K + 8 floats each (the exp-domain kernel's shared-memory layout, copied there as
+// one block) plus the row and column maxima (2 K).
 #ifdef __CUDACC__
 __host__ __device__
 #endif
-inline int64_t expgemm_table_floats(int K) { return 2LL * K * K + 2LL * K; }
+inline int64_t expgemm_table_floats(int K) { return 2LL * K * (K + 8) + 2LL * K; }
 
 // Every other EnumFactor: per factor its edge-state range, edges and config rows. Rows of config
 // k of factor f are row_begin[f] + k * n_vars[f] + i (i = variable), holding the edge state local to
@@ -221,6 +222,8 @@ cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* bel
 // potentials once per run; expgemm_iterate runs one iteration of the bucket (fused damping,
 // normalisation, clipping, residual), the counterpart of the dense pairwise kernel.
 bool expgemm_eligible(const PairwiseBucket& q);
+// Reads and resets the count of bounded device waits that gave up (pgbp_wait_timeouts).
+cudaError_t read_wait_timeouts(unsigned long long* count);
 cudaError_t expgemm_prepare(const Plan& p, const PairwiseBucket& q, cudaStream_t s,
                             const float* lpc, float t, float* tables);
 cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t s, int64_t B,

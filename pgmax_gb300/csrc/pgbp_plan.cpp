@@ -146,6 +146,16 @@ int pgbp_profile_read(pgbp_profile* out) {
   return rc;
 }
 
+int pgbp_wait_timeouts(int64_t* count) {
+  if (!count) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
+  unsigned long long n = 0;
+  const cudaError_t e = pgbp::read_wait_timeouts(&n);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_wait_timeouts");
+  *count = (int64_t)n;
+  if (n != 0) return fail(PGBP_ERR_TIMEOUT, "%lld bounded device waits gave up", (long long)n);
+  return PGBP_OK;
+}
+
 const char* pgbp_last_error(void) { return g_last_error.c_str(); }
 
 int pgbp_version(void) { return 200; }

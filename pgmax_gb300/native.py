@@ -173,6 +173,7 @@ SIGNATURES = [
     ("pgbp_potts_features", ctypes.c_int, [_p, _i64, ctypes.c_int, ctypes.c_int, _p, _p, _p, _p]),
     ("pgbp_profile_enable", ctypes.c_int, [ctypes.c_int]),
     ("pgbp_profile_read", ctypes.c_int, [ctypes.POINTER(Profile)]),
+    ("pgbp_wait_timeouts", ctypes.c_int, [ctypes.POINTER(_i64)]),
     ("pgbp_last_error", ctypes.c_char_p, []),
     ("pgbp_version", ctypes.c_int, []),
 ]
@@ -218,6 +219,15 @@ TUNE_MAX_SITES = 64
 class TuningEntry(ctypes.Structure):
   _fields_ = [("batch", _i64), ("temperature0", ctypes.c_int32), ("path", ctypes.c_int32),
               ("num_sites", ctypes.c_int32), ("site", ctypes.c_int32 * TUNE_MAX_SITES)]
+
+
+def wait_timeouts():
+  """Bounded device waits that gave up since the last call (pgbp_wait_timeouts); 0 normally."""
+  n = _i64(0)
+  rc = load().pgbp_wait_timeouts(ctypes.byref(n))
+  if rc not in (0, 6):  # PGBP_OK, PGBP_ERR_TIMEOUT
+    check(rc, "pgbp_wait_timeouts")
+  return int(n.value)
 
 
 def profile_read():

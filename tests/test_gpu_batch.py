@@ -160,6 +160,9 @@ def test_exp_domain_kernel_over_many_tables_and_instances():
                         np.zeros(wp["var_states_for_edge_states"].shape, np.float32), 20, 0.5,
                         1.0)[0]
       np.testing.assert_allclose(part, want, atol=ATOL, rtol=0)
+  # every group's table reached shared memory by its bulk copy within the wait limit
+  from pgmax_gb300 import native  # pylint: disable=g-import-not-at-top
+  assert native.wait_timeouts() == 0
 
 
 def test_exp_domain_underflow_falls_back_to_the_direct_formula():
