@@ -355,8 +355,11 @@ def run_energy(args):
       "e2e": {"value": terms * args.steps / (e2e_ms / 1e3), "unit": "energy terms/s",
               "h2d_bytes_per_step": int(maps_pinned.numel() * 4 + ev_pinned.numel() * 4),
               "d2h_bytes_per_step": int(en_host.numel() * 4)},
-      "gpu_launches": 2 * args.steps,
-      "roofline": {"bound": "hbm", "kernel": "energy_partial_kernel", "achieved": achieved,
+      # per call: the decodings' transpose, the partial kernel (variables, unary factors), the
+      # dense pairwise kernel (one bucket) and the final per-instance sum
+      "gpu_launches": 4 * args.steps,
+      "roofline": {"bound": "hbm", "kernel": "pgbp_energy (all four launches of one call)",
+                   "achieved": achieved,
                    "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                    "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
                    "algorithmic_bytes_per_launch": algo_bytes, "traffic": None},

@@ -176,9 +176,83 @@ __device__ __forceinline__ void warp_reduce(double& u, double& e, long long& cnt
   }
 }
 
-// grid (chunks of this launch, min(B, 65535)); partials [B][a.chunks].
+// Decoded states with the instances innermost: map_t[v * B + b] = map[b * ms + v] (the bits as
+// given), 32 x 32 tiles through shared memory.
+__global__ void transpose_states_kernel(const int32_t* __restrict__ map, int64_t ms, int64_t nv,
+                                        int64_t B, int32_t* __restrict__ map_t) {
+  __shared__ int32_t tile[32][33];
+  const int64_t v0 = (int64_t)blockIdx.x * 32, b0 = (int64_t)blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t b = b0 + r, v = v0 + threadIdx.x;
+    if (b < B && v < nv) tile[r][threadIdx.x] = map[b * ms + v];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t v = v0 + r, b = b0 + threadIdx.x;
+    if (v < nv && b < B) map_t[v * B + b] = tile[threadIdx.x][r];
+  }
+}
+
+// Dense pairwise segments with the instances on the lanes: grid (chunks of the segment,
+// ceil(B / 32)). Warp w of a CTA takes factors w, w + 8, ... of the chunk for 32 instances, so a
+// factor's record, variables and state counts are loaded once per 32 instances and the decoded
+// states are read as coalesced rows of map_t; each lane sums its instance in double in factor
+// order and the eight warps are added in warp order (a fixed order: the result does not depend
+// on timing).
+__global__ void __launch_bounds__(kEnergyThreads) energy_pairwise_kernel(
+    Args a, SegDev sg, const int32_t* __restrict__ map_t, EnergyPartial* part) {
+  __shared__ double s_e[kEnergyThreads / 32][32];
+  __shared__ long long s_c[kEnergyThreads / 32][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t chunk = sg.chunk_begin + blockIdx.x;
+  const int64_t i0 = (int64_t)blockIdx.x * kEnergyChunk;
+  const int64_t i1 = i0 + kEnergyChunk < sg.items ? i0 + kEnergyChunk : sg.items;
+  const int64_t b = (int64_t)blockIdx.y * 32 + lane;
+  const bool valid = b < a.B;
+  const float* __restrict__ lp_b = a.lp + (valid ? b : 0) * a.lps;
+  const int4* __restrict__ rec = static_cast<const int4*>(sg.p0);
+  const int32_t* __restrict__ cfg = static_cast<const int32_t*>(sg.p1);
+  double e = 0.0;
+  long long cnt = 0;
+  for (int64_t i = i0 + warp; i < i1; i += kEnergyThreads / 32) {
+    const int4 r = __ldg(rec + i);
+    const int va = __ldg(a.var_of_vs + r.z), vb = __ldg(a.var_of_vs + r.w);
+    const int ka = __ldg(a.var_off + va + 1) - __ldg(a.var_off + va);
+    const int kb = __ldg(a.var_off + vb + 1) - __ldg(a.var_off + vb);
+    const int k0 = __ldg(cfg + i);
+    if (valid) {
+      int sa = map_t[(int64_t)va * a.B + b], sb = map_t[(int64_t)vb * a.B + b];
+      if (sa < 0) sa += ka;
+      if (sb < 0) sb += kb;
+      if (sa >= 0 && sa < ka && sb >= 0 && sb < kb) {
+        ++cnt;
+        e += (double)lp_b[k0 + sa * sg.b + sb];
+      }
+    }
+  }
+  s_e[warp][lane] = e;
+  s_c[warp][lane] = cnt;
+  __syncthreads();
+  if (warp == 0 && valid) {
+    for (int w = 1; w < kEnergyThreads / 32; ++w) {
+      e += s_e[w][lane];
+      cnt += s_c[w][lane];
+    }
+    EnergyPartial q;
+    q.u = 0.0;
+    q.e = e;
+    q.cnt = cnt;
+    q.flags = 0;
+    q.pad = 0;
+    part[b * a.chunks + chunk] = q;
+  }
+}
+
+// grid (chunks of this launch, min(B, 65535)); partials [B][a.chunks]. With skip_pairwise the
+// dense pairwise chunks are left to energy_pairwise_kernel.
 __global__ void __launch_bounds__(kEnergyThreads) energy_partial_kernel(Args a, Launch L,
                                                                          int64_t first_chunk,
+                                                                         int skip_pairwise,
                                                                          EnergyPartial* part) {
   __shared__ double s_u[kEnergyThreads / 32], s_e[kEnergyThreads / 32];
   __shared__ long long s_c[kEnergyThreads / 32];
@@ -187,6 +261,7 @@ __global__ void __launch_bounds__(kEnergyThreads) energy_partial_kernel(Args a, 
   int si = 0;
   while (si + 1 < L.nseg && L.seg[si + 1].chunk_begin <= chunk) ++si;
   const SegDev sg = L.seg[si];
+  if (skip_pairwise && sg.kind == kEnergyPairwise) return;
   const int64_t i0 = (chunk - sg.chunk_begin) * kEnergyChunk;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t b = blockIdx.y; b < a.B; b += gridDim.y) {
@@ -280,8 +355,19 @@ void energy_plan(Plan& p) {
   p.energy_chunks = c;
 }
 
+namespace {
+// Batches from this size on run the dense pairwise terms with the instances on the lanes.
+constexpr int64_t kLanesMinBatch = 16;
+size_t partial_bytes(const Plan& p, int64_t B) {
+  const size_t n = (size_t)std::max<int64_t>(1, B * p.energy_chunks) * sizeof(EnergyPartial);
+  return (n + 255) & ~(size_t)255;
+}
+}  // namespace
+
 size_t energy_workspace_bytes(const Plan& p, int64_t B) {
-  return (size_t)std::max<int64_t>(1, B * p.energy_chunks) * sizeof(EnergyPartial);
+  size_t n = partial_bytes(p, B);
+  if (B >= kLanesMinBatch && !p.pairwise.empty()) n += sizeof(int32_t) * (size_t)(p.num_variables * B);
+  return n;
 }
 
 cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
@@ -303,6 +389,15 @@ cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   a.chunks = p.energy_chunks;
   a.gen = p.enum_generic;
   const unsigned gy = (unsigned)std::min<int64_t>(B, 65535);
+  bool lanes = false;
+  for (const EnergySeg& es : p.energy_segs) lanes |= es.kind == kEnergyPairwise;
+  lanes = lanes && B >= kLanesMinBatch && lp != nullptr;
+  int32_t* map_t = nullptr;
+  if (lanes) {
+    map_t = reinterpret_cast<int32_t*>(static_cast<char*>(ws) + partial_bytes(p, B));
+    const dim3 tg((unsigned)((p.num_variables + 31) / 32), (unsigned)((B + 31) / 32));
+    transpose_states_kernel<<<tg, dim3(32, 8), 0, s>>>(map, map_stride, p.num_variables, B, map_t);
+  }
   for (size_t s0 = 0; s0 < p.energy_segs.size(); s0 += kMaxSegsPerLaunch) {
     Launch L;
     L.nseg = (int)std::min<size_t>(kMaxSegsPerLaunch, p.energy_segs.size() - s0);
@@ -342,7 +437,16 @@ cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
     const EnergySeg& last = p.energy_segs[s0 + L.nseg - 1];
     const int64_t first = p.energy_segs[s0].chunk_begin;
     const int64_t n = last.chunk_begin + chunks_of(last.items) - first;
-    energy_partial_kernel<<<dim3((unsigned)n, gy), kEnergyThreads, 0, s>>>(a, L, first, part);
+    energy_partial_kernel<<<dim3((unsigned)n, gy), kEnergyThreads, 0, s>>>(a, L, first,
+                                                                            lanes ? 1 : 0, part);
+    if (lanes) {
+      for (int k = 0; k < L.nseg; ++k) {
+        const SegDev& d = L.seg[k];
+        if (d.kind != kEnergyPairwise) continue;
+        const dim3 g((unsigned)chunks_of(d.items), (unsigned)((B + 31) / 32));
+        energy_pairwise_kernel<<<g, kEnergyThreads, 0, s>>>(a, d, map_t, part);
+      }
+    }
   }
   const int present = (p.num_enum_factors > 0 ? 1 : 0) | (p.logical[0].count > 0 ? 2 : 0) |
                       (p.logical[1].count > 0 ? 4 : 0) | (p.pool.count > 0 ? 8 : 0);

@@ -128,6 +128,26 @@ def test_one_decoding_for_every_instance_and_determinism():
     assert_energy_close(float(got[b]), want, np.abs(ev[b]).sum() + np.abs(lp).sum())
 
 
+def test_large_batch_is_deterministic():
+  """Batches of 16 or more score the dense pairwise terms with the instances on the lanes:
+  repeated calls give the same bits, and every instance matches its single-instance call."""
+  torch = _torch()
+  _, _, _, w = _case_wiring("rbm", nh=20, nv=30, seed=6, sample=0)
+  plan = _plan(w)
+  rng = np.random.default_rng(8)
+  maps = _decodings(w, rng, 45)
+  nvs = int(w["num_var_states"])
+  npot = int(np.asarray(w["potentials_ranges"])[:, 1].max())
+  ev = rng.normal(size=(nvs,)).astype(np.float32)
+  lp = rng.normal(size=(npot,)).astype(np.float32)
+  got = plan.energy(torch.as_tensor(lp), torch.as_tensor(ev), torch.as_tensor(maps))
+  assert torch.equal(got, plan.energy(torch.as_tensor(lp), torch.as_tensor(ev),
+                                      torch.as_tensor(maps)))
+  for b in (0, 31, 32, 44):
+    one = plan.energy(torch.as_tensor(lp), torch.as_tensor(ev), torch.as_tensor(maps[b:b + 1]))
+    assert_energy_close(float(got[b]), float(one[0]), np.abs(ev).sum() + np.abs(lp).sum())
+
+
 def test_shared_tables_and_implicit_rows_match_explicit_plan():
   """A K = 16 grid with one shared table and implied rows against the same grid with per-factor
   tables and explicit rows (the potentials expanded), for the same decodings."""
