@@ -2359,7 +2359,7 @@ struct Sdlp {
   float* __restrict__ upd;         // optional: factor updates, caller layout [B][E_s]
   float* __restrict__ grad;        // optional: gradient, caller layout [B][E_s]
   int64_t B, n_es;
-  float t, step, coef;
+  float t, rt, step, coef;  // rt = 1 / t (T > 0)
   bool t0;
 
   __device__ __forceinline__ float pot(int64_t k, int64_t b) const {
@@ -2376,7 +2376,9 @@ struct Sdlp {
 
   // The epilogue of one edge with data d[i] = bp - ftov and e[i] = t exp((d[i] - m) / t)
   // materialised once (edges of up to kMaxK states; registers once the factor kernel's state count
-  // is a compile-time constant).
+  // is a compile-time constant). At T > 0 the divisions by t and by the sum are products with the
+  // reciprocal (within 2 ulp of the quotient; T > 0 is compared within a tolerance, T = 0 stays
+  // bit-exact and divides nothing).
   static constexpr int kMaxK = 64;
 
   template <class F>
@@ -2398,15 +2400,16 @@ struct Sdlp {
       for (int i = 0; i < k; ++i) arg = d[i] == m ? i : arg;
     } else {
       for (int i = 0; i < k; ++i) {
-        e[i] = t * expf((d[i] - m) / t);
+        e[i] = t * expf((d[i] - m) * rt);
         sum = sum + e[i];
       }
     }
-    lse[r.slot * B + b] = t0 ? m : m + t * logf(sum / t);
+    lse[r.slot * B + b] = t0 ? m : m + t * logf(sum * rt);
+    const float rs = t0 ? 0.0f : 1.0f / sum;
     for (int i = 0; i < k; ++i) {
       const int64_t at = (r.es0 + i) * B + b;
       const float sv = svar[(r.vs0 + i) * B + b];
-      const float g = t0 ? sv + (i == arg ? -1.0f : 0.0f) : sv - e[i] / sum;
+      const float g = t0 ? sv + (i == arg ? -1.0f : 0.0f) : sv - e[i] * rs;
       if (upd != nullptr) upd[b * n_es + r.es0 + i] = outv(i);
       if (grad != nullptr) grad[b * n_es + r.es0 + i] = g;
       if (nxt != nullptr) {
@@ -2428,14 +2431,15 @@ struct Sdlp {
     if (t0) {
       for (int i = 0; i < k; ++i) arg = (outv(i) - old[i] == m) ? i : arg;
     } else {
-      for (int i = 0; i < k; ++i) sum = sum + t * expf((outv(i) - old[i] - m) / t);
+      for (int i = 0; i < k; ++i) sum = sum + t * expf((outv(i) - old[i] - m) * rt);
     }
-    lse[r.slot * B + b] = t0 ? m : m + t * logf(sum / t);
+    lse[r.slot * B + b] = t0 ? m : m + t * logf(sum * rt);
+    const float rs = t0 ? 0.0f : 1.0f / sum;
     for (int i = 0; i < k; ++i) {
       const int64_t at = (r.es0 + i) * B + b;
       const float sv = svar[(r.vs0 + i) * B + b];
       const float g = t0 ? sv + (i == arg ? -1.0f : 0.0f)
-                         : sv - (t * expf((outv(i) - old[i] - m) / t)) / sum;
+                         : sv - (t * expf((outv(i) - old[i] - m) * rt)) * rs;
       if (upd != nullptr) upd[b * n_es + r.es0 + i] = outv(i);
       if (grad != nullptr) grad[b * n_es + r.es0 + i] = g;
       if (nxt != nullptr) {
@@ -2498,10 +2502,12 @@ __global__ void __launch_bounds__(256) sdlp_var_kernel(
       for (int64_t s = s0; s < s1; ++s) svar[s * B + b] = s == arg ? 1.0f : 0.0f;
       obj = m;
     } else {
+      const float rt = 1.0f / t;
       float sum = 0.0f;
-      for (int64_t s = s0; s < s1; ++s) sum = sum + t * expf((vsum[s * B + b] - m) / t);
-      for (int64_t s = s0; s < s1; ++s) svar[s * B + b] = (t * expf((vsum[s * B + b] - m) / t)) / sum;
-      obj = m + t * logf(sum / t);
+      for (int64_t s = s0; s < s1; ++s) sum = sum + t * expf((vsum[s * B + b] - m) * rt);
+      const float rs = 1.0f / sum;
+      for (int64_t s = s0; s < s1; ++s) svar[s * B + b] = (t * expf((vsum[s * B + b] - m) * rt)) * rs;
+      obj = m + t * logf(sum * rt);
     }
     acc += (double)obj;
   }
@@ -2689,6 +2695,7 @@ Sdlp sdlp_access(const Plan& p, int64_t B, const float* cur, const SdlpIn& in, c
   c.B = B;
   c.n_es = p.num_edge_states;
   c.t = t;
+  c.rt = t > 0.0f ? 1.0f / t : 0.0f;
   c.step = 0.0f;
   c.coef = 0.0f;
   c.t0 = t == 0.0f;
