@@ -39,6 +39,7 @@ NH, NV, BATCH, ITERS, DAMPING, TEMPERATURE = 500, 784, 128, 200, 0.5, 0.0
 NUM_EDGES = 2 * NH * NV + NH + NV
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "pairwise_kernel_rbm_b128.md")
+ENERGY_TRAFFIC_FILE = os.path.join(ROOT, "profiles", "energy_pairwise_rbm_b128.md")
 
 
 def rbm_params(seed=0):
@@ -362,7 +363,10 @@ def run_energy(args):
                    "achieved": achieved,
                    "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                    "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
-                   "algorithmic_bytes_per_launch": algo_bytes, "traffic": None},
+                   "algorithmic_bytes_per_launch": algo_bytes,
+                   "traffic": read_traffic(ENERGY_TRAFFIC_FILE, "traffic_bytes_per_launch:"),
+                   "traffic_kernel": "energy_pairwise_kernel (ncu, one launch; the transpose, "
+                                     "partial and final launches move about 2 MB more)"},
       "clocks": clocks.summary(),
   }
   if not args.no_cpu_baseline:
@@ -823,11 +827,12 @@ class ClockSampler:
             "samples": len(self.samples)}
 
 
-def read_traffic():
-  """Per-launch DRAM bytes of the pairwise kernel from the committed ncu summary, if any."""
+def read_traffic(path=None, key="traffic_bytes_per_full_launch:"):
+  """Per-launch DRAM bytes of a kernel from its committed ncu summary (default: the RBM
+  pairwise kernel), if any."""
   try:
-    for line in open(TRAFFIC_FILE):
-      if line.startswith("traffic_bytes_per_full_launch:"):
+    for line in open(path or TRAFFIC_FILE):
+      if line.startswith(key):
         return float(line.split(":")[1].split()[0])
   except OSError:
     pass

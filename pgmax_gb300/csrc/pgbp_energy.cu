@@ -212,21 +212,44 @@ __global__ void __launch_bounds__(kEnergyThreads) energy_pairwise_kernel(
   const float* __restrict__ lp_b = a.lp + (valid ? b : 0) * a.lps;
   const int4* __restrict__ rec = static_cast<const int4*>(sg.p0);
   const int32_t* __restrict__ cfg = static_cast<const int32_t*>(sg.p1);
+  // a bucket's factors all have n1 and n2 states (sg.a, sg.b); four factors per step, their
+  // loads issued level by level (record, variables, decoded states, potential) so the four
+  // dependent chains overlap; the sums still run in factor order
+  constexpr int kStep = 4, kWarps = kEnergyThreads / 32;
+  const int ka = sg.a, kb = sg.b;
   double e = 0.0;
   long long cnt = 0;
-  for (int64_t i = i0 + warp; i < i1; i += kEnergyThreads / 32) {
-    const int4 r = __ldg(rec + i);
-    const int va = __ldg(a.var_of_vs + r.z), vb = __ldg(a.var_of_vs + r.w);
-    const int ka = __ldg(a.var_off + va + 1) - __ldg(a.var_off + va);
-    const int kb = __ldg(a.var_off + vb + 1) - __ldg(a.var_off + vb);
-    const int k0 = __ldg(cfg + i);
-    if (valid) {
-      int sa = map_t[(int64_t)va * a.B + b], sb = map_t[(int64_t)vb * a.B + b];
-      if (sa < 0) sa += ka;
-      if (sb < 0) sb += kb;
-      if (sa >= 0 && sa < ka && sb >= 0 && sb < kb) {
+  for (int64_t i = i0 + warp; i < i1; i += kStep * kWarps) {
+    int4 r[kStep];
+    int k0[kStep], va[kStep], vb[kStep], sa[kStep], sb[kStep];
+    bool in[kStep];
+    float pv[kStep];
+#pragma unroll
+    for (int u = 0; u < kStep; ++u) {
+      const int64_t f = i + (int64_t)u * kWarps;
+      in[u] = f < i1;
+      r[u] = in[u] ? __ldg(rec + f) : make_int4(0, 0, 0, 0);
+      k0[u] = in[u] ? __ldg(cfg + f) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kStep; ++u) {
+      va[u] = in[u] ? __ldg(a.var_of_vs + r[u].z) : 0;
+      vb[u] = in[u] ? __ldg(a.var_of_vs + r[u].w) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kStep; ++u) {
+      sa[u] = (valid && in[u]) ? map_t[(int64_t)va[u] * a.B + b] : -1 - ka;
+      sb[u] = (valid && in[u]) ? map_t[(int64_t)vb[u] * a.B + b] : -1 - kb;
+      if (sa[u] < 0) sa[u] += ka;
+      if (sb[u] < 0) sb[u] += kb;
+      in[u] = sa[u] >= 0 && sa[u] < ka && sb[u] >= 0 && sb[u] < kb;
+      pv[u] = in[u] ? lp_b[k0[u] + sa[u] * kb + sb[u]] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < kStep; ++u) {
+      if (in[u]) {
         ++cnt;
-        e += (double)lp_b[k0 + sa * sg.b + sb];
+        e += (double)pv[u];
       }
     }
   }
