@@ -1025,7 +1025,10 @@ __device__ __forceinline__ void varsum_other_unit(const VarsumDev& v, bool use_r
   vsum[vv * B + b] = s;
 }
 
-__global__ void __launch_bounds__(256) varsum_binary_kernel(VarsumDev v, bool use_runs,
+// At least three blocks per SM, i.e. up to 85 registers: the compiler then keeps the 16-slot
+// load batches of both buffers in flight (72 registers), which beat four blocks per SM at 64
+// registers on the RBM's 784- and 500-slot chains (about 1 ms per 200-iteration step).
+__global__ void __launch_bounds__(256, 3) varsum_binary_kernel(VarsumDev v, bool use_runs,
                                                             const float* __restrict__ msgs,
                                                             const float* __restrict__ ev,
                                                             int64_t evs, int64_t evb,
