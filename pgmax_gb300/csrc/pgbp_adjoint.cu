@@ -60,6 +60,29 @@ __device__ __forceinline__ float div_t(float x, float t) {
 
 __device__ __forceinline__ float clip_lp(float x) { return fminf(fmaxf(x, -kLpClip), kLpClip); }
 
+// The per-iteration kernels below are launched as programmatic dependents of the kernel before
+// them in the stream (launch_pdl): each first waits until that kernel has completed and its writes
+// are visible, then lets the next one be scheduled, so only launch latency is hidden.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <class... KArgs, class... Args>
+void launch_pdl(cudaStream_t s, dim3 grid, void (*kernel)(KArgs...), Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // vsum[b, v] = ev[b, v] + sum of m[b, e] over the edge states e of v, in increasing e (the
 // reference's scatter order).
 __global__ void __launch_bounds__(256) vsum_kernel(const int32_t* __restrict__ vs_off,
@@ -68,6 +91,7 @@ __global__ void __launch_bounds__(256) vsum_kernel(const int32_t* __restrict__ v
                                                    int64_t n_es, const float* __restrict__ ev,
                                                    int64_t evs, float* __restrict__ vsum,
                                                    int64_t B) {
+  pdl_begin();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvs * B;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / nvs, v = i % nvs;
@@ -198,6 +222,7 @@ struct PairArgs {
 template <int M>
 __global__ void __launch_bounds__(256) pairwise_forward_kernel(PairArgs a, const float* m,
                                                                const float* vsum, float* out) {
+  pdl_begin();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count * a.B;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / a.count, u = i % a.count;
@@ -227,6 +252,7 @@ __global__ void __launch_bounds__(256) pairwise_backward_kernel(PairArgs a, cons
                                                                 float* __restrict__ gdir,
                                                                 float* __restrict__ gvtof,
                                                                 float* __restrict__ glp) {
+  pdl_begin();
   constexpr int U = M <= 8 ? M : 1;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count * a.B;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -294,6 +320,7 @@ __global__ void __launch_bounds__(256) gvsum_kernel(const int32_t* __restrict__ 
                                                     int64_t nvs, const float* __restrict__ gvtof,
                                                     int64_t n_es, float* __restrict__ gvsum,
                                                     float* __restrict__ gev, int64_t B) {
+  pdl_begin();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvs * B;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / nvs, v = i % nvs;
@@ -398,15 +425,15 @@ PairArgs pair_args(const Plan& p, const PairwiseBucket& q, int64_t B, const floa
 template <int M>
 void launch_forward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m, const float* vsum,
                       float* out) {
-  pairwise_forward_kernel<M><<<grid_for(a.count * a.B, sm), 256, 0, s>>>(a, m, vsum, out);
+  launch_pdl(s, grid_for(a.count * a.B, sm), pairwise_forward_kernel<M>, a, m, vsum, out);
 }
 
 template <int M>
 void launch_backward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m,
                        const float* vsum, const GradIn& gin, float* gdir, float* gvtof,
                        float* glp) {
-  pairwise_backward_kernel<M><<<grid_for(a.count * a.B, sm), 256, 0, s>>>(a, m, vsum, gin, gdir,
-                                                                         gvtof, glp);
+  launch_pdl(s, grid_for(a.count * a.B, sm), pairwise_backward_kernel<M>, a, m, vsum, gin, gdir,
+             gvtof, glp);
 }
 
 // One chunk's trajectory: messages [len][B][E_s] (normalised) and variable sums [len][B][N_vs].
@@ -427,8 +454,8 @@ void recompute(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_
   for (int64_t j = 0; j < len; ++j) {
     const float* mj = tr.m + j * tr.m_step;
     float* vj = tr.vs + j * tr.vs_step;
-    vsum_kernel<<<grid_for(nvs * B, p.sm_count), 256, 0, s>>>(p.vs_off, p.vs_edges, nvs, mj, n_es,
-                                                              ev, evs, vj, B);
+    launch_pdl(s, grid_for(nvs * B, p.sm_count), vsum_kernel, p.vs_off, p.vs_edges, nvs, mj, n_es,
+               ev, evs, vj, B);
     if (j + 1 == len) break;
     float* next = tr.m + (j + 1) * tr.m_step;
     for (const PairwiseBucket& q : p.pairwise) {
@@ -466,8 +493,8 @@ void backward_step(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
         break;
     }
   }
-  gvsum_kernel<<<grid_for(p.num_var_states * B, p.sm_count), 256, 0, s>>>(
-      p.vs_off, p.vs_edges, p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
+  launch_pdl(s, grid_for(p.num_var_states * B, p.sm_count), gvsum_kernel, p.vs_off, p.vs_edges,
+             p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
 }
 
 // A second stream per device for the recomputation, created on first use and kept.
