@@ -60,28 +60,8 @@ __device__ __forceinline__ float div_t(float x, float t) {
 
 __device__ __forceinline__ float clip_lp(float x) { return fminf(fmaxf(x, -kLpClip), kLpClip); }
 
-// The per-iteration kernels below are launched as programmatic dependents of the kernel before
-// them in the stream (launch_pdl): each first waits until that kernel has completed and its writes
-// are visible, then lets the next one be scheduled, so only launch latency is hidden.
-__device__ __forceinline__ void pdl_begin() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-template <class... KArgs, class... Args>
-void launch_pdl(cudaStream_t s, dim3 grid, void (*kernel)(KArgs...), Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
+// The per-iteration kernels below (variable sums, forward and backward pairwise passes,
+// gradient sums) begin with pdl_begin() and are launched with launch_pdl (pgbp_internal.h).
 
 // vsum[b, v] = ev[b, v] + sum of m[b, e] over the edge states e of v, in increasing e (the
 // reference's scatter order).
@@ -425,15 +405,16 @@ PairArgs pair_args(const Plan& p, const PairwiseBucket& q, int64_t B, const floa
 template <int M>
 void launch_forward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m, const float* vsum,
                       float* out) {
-  launch_pdl(s, grid_for(a.count * a.B, sm), pairwise_forward_kernel<M>, a, m, vsum, out);
+  launch_pdl(s, grid_for(a.count * a.B, sm), dim3(256), pairwise_forward_kernel<M>, a, m, vsum,
+             out);
 }
 
 template <int M>
 void launch_backward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m,
                        const float* vsum, const GradIn& gin, float* gdir, float* gvtof,
                        float* glp) {
-  launch_pdl(s, grid_for(a.count * a.B, sm), pairwise_backward_kernel<M>, a, m, vsum, gin, gdir,
-             gvtof, glp);
+  launch_pdl(s, grid_for(a.count * a.B, sm), dim3(256), pairwise_backward_kernel<M>, a, m, vsum,
+             gin, gdir, gvtof, glp);
 }
 
 // One chunk's trajectory: messages [len][B][E_s] (normalised) and variable sums [len][B][N_vs].
@@ -454,8 +435,8 @@ void recompute(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_
   for (int64_t j = 0; j < len; ++j) {
     const float* mj = tr.m + j * tr.m_step;
     float* vj = tr.vs + j * tr.vs_step;
-    launch_pdl(s, grid_for(nvs * B, p.sm_count), vsum_kernel, p.vs_off, p.vs_edges, nvs, mj, n_es,
-               ev, evs, vj, B);
+    launch_pdl(s, grid_for(nvs * B, p.sm_count), dim3(256), vsum_kernel, p.vs_off, p.vs_edges, nvs,
+               mj, n_es, ev, evs, vj, B);
     if (j + 1 == len) break;
     float* next = tr.m + (j + 1) * tr.m_step;
     for (const PairwiseBucket& q : p.pairwise) {
@@ -493,8 +474,8 @@ void backward_step(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
         break;
     }
   }
-  launch_pdl(s, grid_for(p.num_var_states * B, p.sm_count), gvsum_kernel, p.vs_off, p.vs_edges,
-             p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
+  launch_pdl(s, grid_for(p.num_var_states * B, p.sm_count), dim3(256), gvsum_kernel, p.vs_off,
+             p.vs_edges, p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
 }
 
 // A second stream per device for the recomputation, created on first use and kept.

@@ -262,6 +262,35 @@ cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
                    const float* ev, int64_t ev_stride, const int32_t* map, int64_t map_stride,
                    float* out, void* ws, size_t ws_bytes);
 
+#ifdef __CUDACC__
+// Programmatic dependent launch. A kernel launched with launch_pdl may be scheduled while the
+// kernel before it in the stream is still finishing; pdl_begin(), its first statement, waits
+// until that kernel has completed and its writes are visible (for a normal launch it returns at
+// once) and then lets the kernel after it be scheduled the same way. Only the launch latency
+// between dependent kernels is hidden; their work never overlaps.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches `kernel` (which must begin with pdl_begin()) as a programmatic dependent of the
+// previous kernel in stream s.
+template <class... KArgs, class... Args>
+void launch_pdl(cudaStream_t s, dim3 grid, dim3 block, void (*kernel)(KArgs...), Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+#endif
+
 }  // namespace pgbp
 
 // The opaque handle of include/pgbp.h.

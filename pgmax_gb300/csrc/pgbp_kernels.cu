@@ -46,16 +46,6 @@ __device__ __forceinline__ float fmaxp(float a, float b) {
   asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
   return r;
 }
-// Programmatic dependent launch. A kernel launched with launch_pdl may be scheduled while the
-// kernel before it in the stream is still finishing; pdl_begin(), its first statement, waits
-// until that kernel has completed and its writes are visible (for a normal launch it returns at
-// once) and then lets the kernel after it be scheduled the same way. Only the launch latency
-// between the kernels of an iteration is hidden; no two dependent kernels overlap.
-__device__ __forceinline__ void pdl_begin() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 __device__ __forceinline__ float fminp(float a, float b) {
   float r;
   asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
@@ -1554,23 +1544,6 @@ PoolDev dev(const PoolSet& g) { return PoolDev{g.ch_begin, g.ch, g.ind, g.count}
 
 // x4 launch: lanes over groups of 4 instances.
 Launch2 launch2_x4(int64_t units, int64_t B, int sm_count) { return launch2(units, B / 4, sm_count); }
-
-// Launches a kernel that begins with pdl_begin() as a programmatic dependent of the previous
-// kernel in the stream.
-template <class... KArgs, class... Args>
-void launch_pdl(cudaStream_t s, dim3 grid, dim3 block, void (*kernel)(KArgs...), Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
 
 template <bool T0, class C>
 void launch_pairwise(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const C& c, int64_t B,
