@@ -20,7 +20,9 @@
 //
 // Work split: factors of a bucket are sorted by table (plan time); a column is (factor, instance)
 // with the instance innermost, and a tile is 64 consecutive columns of one group. CTAs are
-// persistent over a contiguous range of tiles, reloading the table only when the group changes.
+// persistent over a contiguous range of tiles, reloading the table only when the group changes,
+// by one bulk copy (cp.async.bulk on an mbarrier) of the run-time tables, which are built in the
+// kernel's shared-memory layout.
 // Four threads own a column (K / 4 states of each edge each), so a thread issues all its message
 // and variable-sum loads before it uses any, and keeps the old messages in registers until the
 // epilogue. The residual is folded per CTA in shared memory and written once per instance.
