@@ -6,13 +6,17 @@ N(0, 0.5^2), a PairwiseFactorGroup of 392,000 2x2 tables [[0, 0], [0, W_ij]] wit
 samples, each with fresh Gumbel(0, 1) evidence on every unary state. One step runs BP for 200
 iterations at temperature 0, damping 0.5 over the whole batch, then computes beliefs and MAP-decodes
 every sample (the reference benchmark's timed region, rbm_lib.py:180-187, minus JAX compilation).
+Every step draws fresh noise: BP.run_perturbed generates it on the GPU inside the run
+(pgbp_run_perturbed) from a new seed.
 Data are synthetic and seeded (the reference's own numbers are for other RBM sizes on a V100).
 
 Metric: edge-message updates per second = batch x num_edges x iterations / time, num_edges =
 2*392,000 + 1,284 = 785,284.
   value  device-resident inputs; CUDA events on the launching stream around K steps.
-  e2e    the public API (pgmax_gb300.infer.BP) with host buffers: every step copies the step's
-         Gumbel evidence from pinned host memory, runs BP, decodes, and copies the MAP states back.
+  e2e    the public API (pgmax_gb300.infer.BP): every step runs BP.run_perturbed from a new seed
+         (nothing is copied in: the noise is made on the GPU), decodes, and copies the MAP states
+         back to pinned host memory. `e2e_host_noise` is the same with the Gumbel evidence drawn
+         on the host and copied in from pinned memory every step (BP.run).
 Roofline: the dense pairwise Enum kernel dominates; its per-launch algorithmic bytes are
   B*4*(2*E_pairwise) message reads + writes + B*4*N_vs variable sums + 4*P_pairwise shared potentials,
 timed per launch with CUDA events (pgbp_profile_*) inside the timed region.
@@ -976,12 +980,15 @@ def main():
 
   ev_host = gumbel_evidence(nvs, BATCH, 1000 + rank)
   lp_dev = torch.as_tensor(np.asarray(fg.fg_state.log_potentials, np.float32), device=dev)
-  ev_dev = torch.as_tensor(ev_host, device=dev)
   msgs0 = torch.zeros(n_es, dtype=torch.float32, device=dev)
-  arrays = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_dev)
+  # the unperturbed evidence (zero: the biases are in the unary factors' potentials)
+  base = bp.init()
+  seeds = iter(range((rank + 1) << 40, 1 << 62))
 
   def step_device():
-    out = bp.run(arrays, num_iters=ITERS, damping=DAMPING, temperature=TEMPERATURE)
+    # fresh Gumbel noise on every unary state of every sample, generated inside the run
+    out = bp.run_perturbed(base, ITERS, next(seeds), BATCH, damping=DAMPING,
+                           temperature=TEMPERATURE)
     beliefs = bp.get_beliefs(out)
     return infer.decode_map_states(beliefs)
 
@@ -1023,12 +1030,22 @@ def main():
   native.profile_enable(False)
   prof = native.profile_read()
 
-  # end to end through the public API with host buffers
-  ev_pinned = torch.as_tensor(ev_host).pin_memory()
+  # end to end through the public API: the seed in (the noise is made on the GPU), every
+  # sample's MAP states copied back to pinned host memory
   map_h = torch.empty((BATCH, NH), dtype=torch.int32).pin_memory()
   map_v = torch.empty((BATCH, NV), dtype=torch.int32).pin_memory()
 
   def step_e2e():
+    out = bp.run_perturbed(base, ITERS, next(seeds), BATCH, damping=DAMPING,
+                           temperature=TEMPERATURE)
+    dec = infer.decode_map_states(bp.get_beliefs(out))
+    map_h.copy_(dec[hidden], non_blocking=True)
+    map_v.copy_(dec[visible], non_blocking=True)
+
+  # the same with the noise drawn on the host and copied in every step (bp.run on host evidence)
+  ev_pinned = torch.as_tensor(ev_host).pin_memory()
+
+  def step_e2e_host_noise():
     ev_d = ev_pinned.to(dev, non_blocking=True)
     a = infer.BPArrays(log_potentials=lp_dev, ftov_msgs=msgs0, evidence=ev_d)
     out = bp.run(a, num_iters=ITERS, damping=DAMPING, temperature=TEMPERATURE)
@@ -1036,17 +1053,21 @@ def main():
     map_h.copy_(dec[hidden], non_blocking=True)
     map_v.copy_(dec[visible], non_blocking=True)
 
-  for _ in range(args.warmup):
-    step_e2e()
-  barrier()
-  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-  e0.record(stream)
-  for _ in range(args.steps):
-    step_e2e()
-  e1.record(stream)
-  barrier()
-  e2e_ms = max_over_ranks(e0.elapsed_time(e1))
+  def timed(fn):
+    for _ in range(args.warmup):
+      fn()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+      fn()
+    e1.record(stream)
+    barrier()
+    return max_over_ranks(e0.elapsed_time(e1))
+
+  e2e_ms = timed(step_e2e)
   e2e_value = units / (e2e_ms / 1e3)
+  host_noise_ms = timed(step_e2e_host_noise)
 
   # roofline of the dominant kernel (dense pairwise Enum, binary edges stored as one slot each):
   # its average launch time comes from the profiled repetition of the timed steps.
@@ -1086,8 +1107,13 @@ def main():
                  "edge_states": n_es, "parallelism": "replicas" if world > 1 else "single",
                  "l2": "inputs larger than L2 (804 MB of messages per buffer)"},
       "e2e": {"value": e2e_value, "unit": "edge-msg updates/s",
-              "h2d_bytes_per_step": int(ev_pinned.numel() * 4),
-              "d2h_bytes_per_step": int((map_h.numel() + map_v.numel()) * 4)},
+              "h2d_bytes_per_step": 0,
+              "d2h_bytes_per_step": int((map_h.numel() + map_v.numel()) * 4),
+              "noise": "Gumbel(0,1) generated on the GPU inside the run (pgbp_run_perturbed)"},
+      "e2e_host_noise": {"value": units / (host_noise_ms / 1e3), "unit": "edge-msg updates/s",
+                         "h2d_bytes_per_step": int(ev_pinned.numel() * 4),
+                         "d2h_bytes_per_step": int((map_h.numel() + map_v.numel()) * 4),
+                         "noise": "drawn on the host, copied in every step (bp.run)"},
       "gpu_launches": gpu_launches,
       "roofline": {
           "bound": "hbm",

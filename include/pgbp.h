@@ -14,6 +14,7 @@
  *   pgbp_beliefs        InfererContext.get_beliefs (flat part)   pgmax/infer/inferer.py:211-222
  *   pgbp_decode         decode_map_states                        pgmax/infer/inferer.py:251-264
  *   pgbp_marginals      get_marginals                            pgmax/infer/bp.py:263-288
+ *   pgbp_softmax_rows / pgbp_argmax_rows   get_marginals / decode_map_states of any belief arrays
  *   pgbp_energy         compute_energy                           pgmax/infer/energy.py:53-148
  *   pgbp_sdlp_run       SDLP(...).run_with_objvals               pgmax/infer/dual_lp.py:238-313
  *   pgbp_sdlp_objective smooth_dual_objval_and_grad / get_bp_updates  dual_lp.py:65-236, 419-448
@@ -160,9 +161,11 @@ int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch,
  * start-up). No counterpart in the reference, which leaves memory to XLA.
  * Scratch is one static device array of PGBP_STATIC_SCRATCH_BYTES per GPU that loads this library,
  * held until the process exits; a run needing more (pgbp_workspace_size) fails with
- * PGBP_ERR_WORKSPACE. The first call on a device looks up the array's address: make it before any
- * stream capture. All calls share the array, so calls that overlap on the GPU race; each call
- * clears what must start at zero. Arguments and results are those of pgbp_run. */
+ * PGBP_ERR_WORKSPACE. The first call on a device looks up the array's address and keeps it: make
+ * that call before any stream capture. A device reset (cudaDeviceReset) frees the array with
+ * every plan, so neither this entry point nor any plan may be used across one. All calls share
+ * the array, so calls that overlap on the GPU race; each call clears what must start at zero.
+ * Arguments and results are those of pgbp_run, bit for bit. */
 #define PGBP_STATIC_SCRATCH_BYTES (32u << 20)
 int pgbp_run_static_scratch(const pgbp_plan* plan, void* stream, int64_t batch,
                             const float* log_potentials, int64_t lp_stride,
@@ -170,6 +173,31 @@ int pgbp_run_static_scratch(const pgbp_plan* plan, void* stream, int64_t batch,
                             const float* msgs_in, int64_t msgs_stride,
                             float* msgs_out, float* deltas,
                             int64_t num_iters, double damping, double temperature);
+
+/* Perturb-and-MAP without a noise array: pgbp_run with the evidence of instance b
+ *   evidence[b][i] = evidence_base[b * ev_stride + i] + (float)noise_scale * G[b * N_vs + i]
+ * where G is the Gumbel(0, 1) stream of `seed` (pgbp_gumbel), generated inside the run's evidence
+ * transpose: nothing is copied from the host and no noise array is stored. evidence_base may be
+ * NULL (a zero base, ev_stride 0) or [batch, N_vs] (ev_stride 0 shares one base). evidence_out
+ * (NULL or [batch, N_vs], contiguous) receives the perturbed evidence, for pgbp_beliefs. The same
+ * result, bit for bit, as pgbp_run on that evidence. This is the loop the reference's perturb-and-MAP
+ * users write around run (fresh Gumbel evidence per sample through update_evidence under
+ * jax.vmap: benchmark/rbm_lib.py:173-184, pgmax/infer/bp_state.py:292-342), fused into the run. */
+int pgbp_run_perturbed(const pgbp_plan* plan, void* stream, int64_t batch,
+                       const float* log_potentials, int64_t lp_stride,
+                       const float* evidence_base, int64_t ev_stride,
+                       uint64_t seed, double noise_scale,
+                       const float* msgs_in, int64_t msgs_stride,
+                       float* msgs_out, float* deltas, float* evidence_out,
+                       int64_t num_iters, double damping, double temperature,
+                       void* workspace, size_t workspace_bytes);
+
+/* The noise stream of pgbp_run_perturbed: out[c] = G[c] for c < count, on the current device.
+ * G[c] = -ln(-ln(u_c)), u_c in (0, 1) from output c + 1 of SplitMix64 seeded with mix64(seed)
+ * (23 bits, u = (2k + 1) 2^-24), ln evaluated with correctly rounded float32 operations only (the
+ * exact steps are in pgmax_gb300/csrc/pgbp_gumbel.h), so the stream can be reproduced bit for bit
+ * on a host. No reference counterpart (jax.random.gumbel uses its own generator). */
+int pgbp_gumbel(void* stream, uint64_t seed, int64_t count, float* out);
 
 /* Runs BP until every instance's max message residual is below `tolerance` (the convergence loop
  * PGMax users write around run_with_diffs, bp.py:63-155, checking its msgs_deltas), or
@@ -250,6 +278,15 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
 /* Per-variable softmax of the flat beliefs: marginals[b] has the layout of beliefs[b]. */
 int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const float* beliefs,
                    int64_t beliefs_stride, float* marginals);
+
+/* get_marginals (pgmax/infer/bp.py:263-288) and decode_map_states (pgmax/infer/inferer.py:251-264)
+ * of belief arrays that did not come from a plan: `in` is a dense [rows, k] float32 array on the
+ * current device (a VarGroup's unflattened beliefs, padded states at -inf). pgbp_softmax_rows writes
+ * exp(x - logsumexp(x)) of every row ([rows, k]; padded states get 0, a row of -inf gets nan, as in
+ * the reference); pgbp_argmax_rows the index of each row's first maximum, or of its first NaN
+ * ([rows] int32). */
+int pgbp_softmax_rows(void* stream, int64_t rows, int64_t k, const float* in, float* out);
+int pgbp_argmax_rows(void* stream, int64_t rows, int64_t k, const float* in, int32_t* out);
 
 /* Autotuner decisions. pgbp_run times, once per (batch, temperature == 0), the eligible execution
  * paths and then, on the multi-kernel path, the kernel variants of each launch site (the binary
@@ -346,12 +383,36 @@ int pgbp_profile_enable(int enable);
 int pgbp_profile_read(pgbp_profile* out);
 
 /* Bounded device-side waits. Kernels that wait for their own asynchronous copies (the shared
- * K x K table of the exp-domain pairwise kernel arrives by one bulk copy on an mbarrier) give up
- * after 2 s instead of hanging, count the wait, and continue with wrong values. This returns the
- * count on the current device since the last call in *count and resets it: PGBP_OK when it is
- * zero, PGBP_ERR_TIMEOUT otherwise. Synchronises the device. No reference counterpart (JAX has no
- * device-side waits to bound). */
+ * K x K table of the exp-domain pairwise kernels arrives by one bulk copy on an mbarrier) give up
+ * after 2 s instead of hanging: the CTA that gave up stops (its part of the messages is left
+ * unwritten, so the launch's results are invalid), counts the wait on the device and sets the
+ * plan's fault word, which lives in mapped host memory.
+ *   pgbp_plan_check     PGBP_ERR_TIMEOUT when a completed launch on `plan` gave up a wait since
+ *                       the last report, else PGBP_OK; clears the word. It reads host memory
+ *                       only and does not synchronise: synchronise the stream first to cover the
+ *                       launches in it. Every entry point that enqueues work on a plan makes
+ *                       the same check first and fails with PGBP_ERR_TIMEOUT, enqueueing
+ *                       nothing, while the word is set.
+ *   pgbp_wait_timeouts  the device-wide count since the last call in *count, reset to zero:
+ *                       PGBP_OK when it is zero, PGBP_ERR_TIMEOUT otherwise. Synchronises the
+ *                       current device.
+ * No reference counterpart (JAX has no device-side waits to bound). */
+int pgbp_plan_check(const pgbp_plan* plan);
 int pgbp_wait_timeouts(int64_t* count);
+
+/* Debug settings, process-wide, read when a launch is enqueued. No reference counterpart.
+ *   PGBP_DEBUG_WAIT_LIMIT_NS     limit of the bounded device waits in ns (0 = the built-in 2 s;
+ *                                at most 10 s)
+ *   PGBP_DEBUG_SKIP_TABLE_COPY   1: the exp-domain pairwise kernels arm their table barrier for
+ *                                the copy's bytes but issue no copy, so their wait runs out with
+ *                                nothing in flight (tests the timeout path); 0: normal
+ *   PGBP_DEBUG_LEGACY_MMA        1: shared 64 x 64 tables of a single instance run on the
+ *                                warp-level mma.sync kernel instead of the tcgen05 one (for
+ *                                comparison); 0: normal */
+#define PGBP_DEBUG_WAIT_LIMIT_NS 1
+#define PGBP_DEBUG_SKIP_TABLE_COPY 2
+#define PGBP_DEBUG_LEGACY_MMA 3
+int pgbp_debug_set(int knob, int64_t value);
 
 const char* pgbp_last_error(void);
 int pgbp_version(void); /* major * 10000 + minor * 100 + patch */

@@ -439,3 +439,46 @@ int bpo_beliefs(const bpo_wiring* w, const float* evidence, const float* msgs, f
     beliefs[w->var_states_for_edge_states[i]] += msgs[i];
   return 0;
 }
+
+/* ---- the Gumbel stream of perturb-and-MAP runs (bpo_gumbel, see bp_oracle.h) */
+static uint64_t g_mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+/* ln(x) for a positive normal float: x = m 2^e with m in [sqrt(2)/2, sqrt(2)], then
+ * ln(m) = 2 atanh((m - 1) / (m + 1)) by its series up to the z^4 / 9 term. */
+static float g_ln(float x) {
+  uint32_t bits;
+  memcpy(&bits, &x, sizeof(bits));
+  int e = (int)((bits >> 23) & 0xffu) - 127;
+  const uint32_t mb = (bits & 0x007fffffu) | 0x3f800000u;
+  float m;
+  memcpy(&m, &mb, sizeof(m));
+  if (m > 0x1.6a09e6p+0f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float z = s * s;
+  float p = 0x1.c71c72p-4f;
+  p = p * z + 0x1.24924ap-3f;
+  p = p * z + 0x1.99999ap-3f;
+  p = p * z + 0x1.555556p-2f;
+  p = p * z + 1.0f;
+  const float lm = (s * p) * 2.0f;
+  return (float)e * 0x1.62e430p-1f + lm;
+}
+
+void bpo_gumbel(uint64_t seed, int64_t first, int64_t count, float* out) {
+  const uint64_t key = g_mix64(seed);
+  for (int64_t i = 0; i < count; ++i) {
+    const uint64_t c = (uint64_t)(first + i);
+    const uint64_t r = g_mix64(key + (c + 1ull) * 0x9E3779B97F4A7C15ull);
+    const uint32_t k = (uint32_t)(r >> 41);
+    const float u = (float)(2u * k + 1u) * 0x1.0p-24f;
+    const float w = -g_ln(u);
+    out[i] = -g_ln(w);
+  }
+}

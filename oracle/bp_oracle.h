@@ -70,6 +70,13 @@ int bpo_run_batch(const bpo_wiring* w, int64_t batch, const float* log_potential
 /* Flat beliefs evidence.at[var_states_for_edge_states].add(msgs), pgmax/infer/inferer.py:218-222. */
 int bpo_beliefs(const bpo_wiring* w, const float* evidence, const float* msgs, float* beliefs);
 
+/* Draws first .. first + count - 1 of the Gumbel(0, 1) stream of `seed` that the engine's
+ * perturb-and-MAP runs add to the evidence (pgbp_gumbel / pgbp_run_perturbed of include/pgbp.h),
+ * restated from its specification: SplitMix64 output c + 1 from state mix64(seed), 23 bits to
+ * u = (2k + 1) 2^-24, then -ln(-ln(u)) with ln by range reduction and the atanh series in
+ * float32 (no fused operations). */
+void bpo_gumbel(uint64_t seed, int64_t first, int64_t count, float* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,8 @@ def lib():
     L.bpo_beliefs.argtypes = [W, _pf, _pf, _pf]
     for f in (L.bpo_factor_update, L.bpo_run, L.bpo_run_batch, L.bpo_beliefs):
       f.restype = ctypes.c_int
+    L.bpo_gumbel.argtypes = [ctypes.c_uint64, _i64, _i64, _pf]
+    L.bpo_gumbel.restype = None
     _lib = L
   return _lib
 
@@ -196,4 +198,12 @@ def beliefs(wiring, evidence, msgs):
   ev, m = _f32(evidence), _f32(msgs)
   out = np.empty(wiring.num_var_states, np.float32)
   lib().bpo_beliefs(wiring.ptr, _fp(ev), _fp(m), _fp(out))
+  return out
+
+
+def gumbel(seed, count, first=0):
+  """Draws first .. first + count - 1 of the engine's Gumbel(0, 1) noise stream of `seed`
+  (pgbp_gumbel), restated on the CPU."""
+  out = np.empty(int(count), np.float32)
+  lib().bpo_gumbel(int(seed) & (2**64 - 1), int(first), int(count), _fp(out))
   return out

@@ -67,9 +67,10 @@ __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) 
 }
 
 // ---- bulk copies into shared memory (cp.async.bulk, completion on an mbarrier)
-// A wait that has not seen its copy land after kWaitLimitNs is counted in g_wait_timeouts and
-// returns; the host reads the count (pgbp_wait_timeouts), so a lost copy is an error status, not a
-// hang.
+// A wait that has not seen its copy land after the launch's limit (kWaitLimitNs unless the debug
+// setting changes it) gives up: the CTA counts it in g_wait_timeouts, sets the plan's fault word
+// (mapped host memory, read by pgbp_plan_check and the entry points) and stops, so a lost copy is
+// an error status, not a hang and not silently wrong tables.
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 __device__ unsigned long long g_wait_timeouts = 0;
 
@@ -84,13 +85,16 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar) {
 
 // One copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from global to shared
 // memory, completing the current phase of `bar`. Shared-memory reads issued before it (by any
-// thread, ordered by a barrier) complete before the copy writes.
+// thread, ordered by a barrier) complete before the copy writes. With `skip_copy` (a debug
+// setting) the barrier is armed for the bytes but no copy is issued: its phase never completes
+// and the wait for it runs out with nothing in flight.
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
-                                          uint64_t* bar) {
+                                          uint64_t* bar, bool skip_copy) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
                "r"(bytes)
                : "memory");
+  if (skip_copy) return;
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
           smem_addr(dst)),
@@ -98,7 +102,10 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
       : "memory");
 }
 
-__device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t parity) {
+// Waits for the phase of `bar` with parity `parity` to complete; false when `limit_ns` passed
+// first (measured on %globaltimer).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned long long limit_ns) {
   const uint32_t addr = smem_addr(bar);
   uint64_t t0 = 0;
   for (uint32_t i = 0;; ++i) {
@@ -109,15 +116,14 @@ __device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t parity) {
         : "=r"(done)
         : "r"(addr), "r"(parity)
         : "memory");
-    if (done) return;
+    if (done) return true;
     if ((i & 63) == 0) {
       uint64_t now;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
       if (t0 == 0) {
         t0 = now;
-      } else if (now - t0 > kWaitLimitNs) {
-        atomicAdd(&g_wait_timeouts, 1ull);
-        return;
+      } else if (now - t0 > limit_ns) {
+        return false;
       }
     }
   }
@@ -190,6 +196,9 @@ struct ExpArgs {
   const float* __restrict__ tables;
   float d, omd, t;
   unsigned* __restrict__ dacc;            // residual of this iteration, [B] float bits
+  unsigned* fault;                        // the plan's fault word (mapped host memory)
+  unsigned long long wait_ns;             // limit of the table wait
+  int skip_copy;                          // debug: arm the table barrier, issue no copy
 };
 
 // Shared-memory layout of one CTA.
@@ -364,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
       // out as they are), overlapping this tile's message loads; waited for before the GEMMs
       if (threadIdx.x == 0)
         bulk_load(s_e, a.tables + (int64_t)g * expgemm_table_floats(K),
-                  (uint32_t)(sizeof(float) * expgemm_table_floats(K)), &s_bar);
+                  (uint32_t)(sizeof(float) * expgemm_table_floats(K)), &s_bar, a.skip_copy != 0);
       pending = true;
       loaded = g;
     }
@@ -415,12 +424,25 @@ __global__ void __launch_bounds__(kThreads, 2) expgemm_pairwise_kernel(ExpArgs a
       split_tf32(active ? __expf(div_t(v2[2 * kb + 1] - m2, a.t)) : 0.0f, h1, l1);
       s_u[(kb * 4 + part) * kLdx + c] = make_uint4(h0, h1, l0, l1);
     }
+    int lost = 0;
     if (pending) {
-      mbar_wait(&s_bar, phase);
+      lost = mbar_wait(&s_bar, phase, a.wait_ns) ? 0 : 1;
       phase ^= 1u;
       pending = false;
     }
-    __syncthreads();
+    if (__syncthreads_or(lost)) {
+      // the tables never arrived: record the fault and stop without touching them; a copy that
+      // may still be in flight gets one more bounded wait before the CTA's shared memory goes
+      if (threadIdx.x == 0) {
+        atomicAdd(&g_wait_timeouts, 1ull);
+        if (a.fault != nullptr) {
+          *reinterpret_cast<volatile unsigned*>(a.fault) = 1u;
+          __threadfence_system();
+        }
+        if (!a.skip_copy) mbar_wait(&s_bar, phase ^ 1u, a.wait_ns);
+      }
+      return;
+    }
     // ---- F1 = E U, F2 = E' W on the tensor cores, one accumulator set live at a time (each
     // result overwrites its own operand once every warp is done reading it)
     {
@@ -566,6 +588,10 @@ cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t
   a.omd = omd;
   a.t = t;
   a.dacc = dacc;
+  const DebugKnobs knobs = debug_knobs();
+  a.fault = p.fault_dev;
+  a.wait_ns = knobs.wait_limit_ns != 0 ? knobs.wait_limit_ns : kWaitLimitNs;
+  a.skip_copy = knobs.skip_table_copy;
   switch (q.n1) {
     case 16: return launch<16>(p, q, s, a);
     case 32: return launch<32>(p, q, s, a);

@@ -164,11 +164,55 @@ struct Plan {
   mutable std::map<std::pair<int64_t, bool>, std::vector<int>> tuned_sites;
   int64_t device_bytes = 0;
   std::vector<void*> allocations;
+  // Fault word of the plan's launches, in mapped pinned host memory: a kernel whose bounded wait
+  // gave up sets it (fault_dev is its device alias); the entry points and pgbp_plan_check read
+  // it on the host without synchronising and report PGBP_ERR_TIMEOUT.
+  unsigned* fault_host = nullptr;
+  unsigned* fault_dev = nullptr;
   int64_t num_enum_factors = 0, num_enum_pairwise = 0;
 };
 
 // Records `message` as the calling thread's pgbp_last_error() and returns `code`.
 int set_last_error(int code, const char* message);
+
+// Makes `device` current for the guard's lifetime and gives the calling thread its previous
+// current device back on destruction, so no entry point leaves the caller on another device.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    err_ = cudaGetDevice(&prev_);
+    if (err_ == cudaSuccess && prev_ != device) {
+      err_ = cudaSetDevice(device);
+      switched_ = err_ == cudaSuccess;
+    }
+  }
+  ~DeviceGuard() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+  cudaError_t status() const { return err_; }
+
+ private:
+  int prev_ = 0;
+  bool switched_ = false;
+  cudaError_t err_ = cudaSuccess;
+};
+
+// PGBP_ERR_TIMEOUT (and clears the plan's fault word) when a launch on this plan recorded a
+// bounded device wait that gave up, else PGBP_OK. Reads host memory only: it sees the launches
+// that have completed.
+int take_plan_fault(const Plan& p);
+
+// Debug settings (pgbp_debug_set): the bounded waits' limit in ns (0 = the built-in 2 s),
+// whether the exp-domain kernels arm their table barrier without issuing the copy, so their wait
+// runs out with nothing in flight, and whether K = 64 at B = 1 runs the mma.sync kernel.
+struct DebugKnobs {
+  unsigned long long wait_limit_ns = 0;
+  int skip_table_copy = 0;
+  int legacy_mma = 0;  // K = 64 at B = 1 on the mma.sync kernel instead of the tcgen05 one
+};
+DebugKnobs debug_knobs();
 
 size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batched, bool lp_batched);
 
@@ -201,12 +245,23 @@ struct ToleranceRun {
   int64_t* iters_run;    // host
 };
 
+// pgbp_run_perturbed: evidence = base + scale * the Gumbel stream of `seed` (pgbp_gumbel.h),
+// generated in the run's evidence transpose; evidence_out (optional) receives it [B][N_vs].
+struct Perturbation {
+  uint64_t seed;
+  float scale;
+  float* evidence_out;
+};
+
 // Kernel launchers (pgbp_kernels.cu). They return cudaGetLastError() of their launches.
 cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
                    const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
                    float* msgs_out, float* deltas, int64_t iters, double damping, double temperature,
                    void* ws, size_t ws_bytes, int64_t checkpoint_every = 0,
-                   float* checkpoints = nullptr, const ToleranceRun* tol_run = nullptr);
+                   float* checkpoints = nullptr, const ToleranceRun* tol_run = nullptr,
+                   const Perturbation* pert = nullptr);
+// out[c] = draw c of the Gumbel stream of `seed`, c < count (pgbp_gumbel)
+cudaError_t gumbel(cudaStream_t s, uint64_t seed, int64_t count, float* out, int sm_count);
 cudaError_t factor_update(const Plan& p, cudaStream_t s, int type, int64_t B, const float* vtof,
                           int64_t vtof_stride, const float* lp, int64_t lp_stride, double temperature,
                           int normalize, float* out, int64_t out_stride);
@@ -216,6 +271,11 @@ cudaError_t decode(const Plan& p, cudaStream_t s, int64_t B, const float* belief
                    int32_t* map);
 cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* beliefs, int64_t stride,
                       float* out);
+// decode / marginals of a dense [rows, k] array (pgbp_argmax_rows / pgbp_softmax_rows)
+cudaError_t rows_argmax(cudaStream_t s, int64_t rows, int64_t k, const float* in, int32_t* out,
+                        int sm_count);
+cudaError_t rows_softmax(cudaStream_t s, int64_t rows, int64_t k, const float* in, float* out,
+                         int sm_count);
 
 // Shared-table exp-domain pairwise update (pgbp_expgemm.cu), multi-kernel path, T > 0, potentials
 // shared by the batch. expgemm_prepare fills the bucket's run-time tables from the clipped

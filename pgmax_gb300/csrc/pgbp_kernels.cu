@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "pgbp_gumbel.h"
 #include "pgbp_internal.h"
 
 namespace pgbp {
@@ -1406,6 +1407,39 @@ __global__ void to_inner_kernel(const float* __restrict__ src, int64_t sstride, 
   }
 }
 
+// Perturbed evidence of pgbp_run_perturbed: v = base + scale * G[b * n + i], G the Gumbel stream
+// of `key` (pgbp_gumbel.h) and base = src[b * sstride + i] (0 when src is null), written to
+// dst[i * B + b] (the run layout) and, when out is not null, to out[b * n + i] (the caller's),
+// via 32x32 tiles. Every draw is computed once.
+__global__ void to_inner_gumbel_kernel(const float* __restrict__ src, int64_t sstride, int64_t n,
+                                       int64_t B, uint64_t key, float scale,
+                                       float* __restrict__ dst, float* __restrict__ out) {
+  __shared__ float tile[32][33];
+  const int64_t i0 = (int64_t)blockIdx.x * 32, b0 = (int64_t)blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t b = b0 + r, i = i0 + threadIdx.x;
+    if (b < B && i < n) {
+      const float base = src != nullptr ? src[b * sstride + i] : 0.0f;
+      const float v = base + scale * gumbel_draw(key, (uint64_t)(b * n + i));
+      tile[r][threadIdx.x] = v;
+      if (out != nullptr) out[b * n + i] = v;
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t i = i0 + r, b = b0 + threadIdx.x;
+    if (b < B && i < n) dst[i * B + b] = tile[threadIdx.x][r];
+  }
+}
+
+// out[c] = G[c0 + c], c < count: the Gumbel stream of `key` (pgbp_gumbel).
+__global__ void gumbel_fill_kernel(uint64_t key, int64_t c0, int64_t count,
+                                   float* __restrict__ out) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < count;
+       c += (int64_t)gridDim.x * blockDim.x)
+    out[c] = gumbel_draw(key, (uint64_t)(c0 + c));
+}
+
 // dst[b * dstride + i] = src[i * B + b]
 __global__ void to_outer_kernel(const float* __restrict__ src, int64_t n, int64_t B,
                                 float* __restrict__ dst, int64_t dstride) {
@@ -1440,14 +1474,28 @@ __global__ void deltas_out_kernel(const unsigned* __restrict__ acc, int64_t iter
   }
 }
 
+// States s0 .. s1 - 1 of variable v: from the plan's var_off, or, for dense [rows, k] arrays
+// (var_off null), the k states of row v.
+__device__ __forceinline__ void var_states(const int32_t* __restrict__ var_off, int64_t k,
+                                           int64_t v, int64_t& s0, int64_t& s1) {
+  if (var_off != nullptr) {
+    s0 = var_off[v];
+    s1 = var_off[v + 1];
+  } else {
+    s0 = v * k;
+    s1 = s0 + k;
+  }
+}
+
 // decode_map_states (inferer.py:251-264): jnp.argmax, first maximum (or first NaN) wins.
-__global__ void decode_kernel(const int32_t* __restrict__ var_off, int64_t nv,
+__global__ void decode_kernel(const int32_t* __restrict__ var_off, int64_t k, int64_t nv,
                               const float* __restrict__ bel, int64_t bs, int32_t* __restrict__ map,
                               int64_t B) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv * B;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / nv, v = i % nv;
-    const int64_t s0 = var_off[v], s1 = var_off[v + 1];
+    int64_t s0, s1;
+    var_states(var_off, k, v, s0, s1);
     float best = s1 > s0 ? bel[b * bs + s0] : 0.0f;
     int32_t arg = 0;
     for (int64_t s = s0 + 1; s < s1; ++s) {
@@ -1462,14 +1510,16 @@ __global__ void decode_kernel(const int32_t* __restrict__ var_off, int64_t nv,
   }
 }
 
-// get_marginals (bp.py:263-288): exp(x - logsumexp(x)) per variable.
-__global__ void marginals_kernel(const int32_t* __restrict__ var_off, int64_t nv,
+// get_marginals (bp.py:263-288): exp(x - logsumexp(x)) per variable, the maximum taken as 0 when
+// it is not finite (so a variable whose states are all -inf gets nan, as in the reference).
+__global__ void marginals_kernel(const int32_t* __restrict__ var_off, int64_t k, int64_t nv,
                                  const float* __restrict__ bel, int64_t bs, float* __restrict__ out,
                                  int64_t B, int64_t nvs) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv * B;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / nv, v = i % nv;
-    const int64_t s0 = var_off[v], s1 = var_off[v + 1];
+    int64_t s0, s1;
+    var_states(var_off, k, v, s0, s1);
     float m = -INFINITY;
     for (int64_t s = s0; s < s1; ++s) m = fmaxp(m, bel[b * bs + s]);
     const float shift = isfinite(m) ? m : 0.0f;
@@ -2032,9 +2082,10 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
                    const float* ev, int64_t ev_stride, const float* msgs_in, int64_t msgs_stride,
                    float* msgs_out, float* deltas, int64_t num_iters, double damping,
                    double temperature, void* ws, size_t ws_bytes, int64_t checkpoint_every,
-                   float* checkpoints, const ToleranceRun* tol_run) {
+                   float* checkpoints, const ToleranceRun* tol_run, const Perturbation* pert) {
   const int64_t iters = std::max<int64_t>(num_iters, 1);
-  const bool ev_b = ev_stride != 0, lp_b = lp_stride != 0;
+  // perturbed evidence differs per instance even when its base is shared
+  const bool ev_b = ev_stride != 0 || pert != nullptr, lp_b = lp_stride != 0;
   char* w = static_cast<char*>(ws);
   auto take = [&](size_t bytes) {
     char* r = w;
@@ -2060,7 +2111,18 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   // evidence and potentials in the run layout; potentials clipped (bp.py:85-87)
   const float* evp = ev;
   int64_t evs = 1, evb = 0;
-  if (ev_b) {
+  if (pert != nullptr) {
+    if (p.num_var_states > 0) {
+      ProfileScope ps(kProfLayout, s);
+      dim3 grid((unsigned)((p.num_var_states + 31) / 32), (unsigned)((B + 31) / 32));
+      to_inner_gumbel_kernel<<<grid, dim3(32, 8), 0, s>>>(
+          ev, ev_stride, p.num_var_states, B, gumbel_key(pert->seed), pert->scale, evt,
+          pert->evidence_out);
+    }
+    evp = evt;
+    evs = B;
+    evb = 1;
+  } else if (ev_b) {
     to_inner(s, ev, ev_stride, p.num_var_states, B, evt, false, p.sm_count);
     evp = evt;
     evs = B;
@@ -2289,7 +2351,7 @@ cudaError_t decode(const Plan& p, cudaStream_t s, int64_t B, const float* bel, i
   if (p.num_variables == 0) return cudaSuccess;
   ProfileScope ps(kProfReadout, s);
   decode_kernel<<<flat_grid(p.num_variables * B, p.sm_count), 256, 0, s>>>(
-      p.var_off, p.num_variables, bel, stride, map, B);
+      p.var_off, 0, p.num_variables, bel, stride, map, B);
   return cudaGetLastError();
 }
 
@@ -2298,7 +2360,30 @@ cudaError_t marginals(const Plan& p, cudaStream_t s, int64_t B, const float* bel
   if (p.num_variables == 0) return cudaSuccess;
   ProfileScope ps(kProfReadout, s);
   marginals_kernel<<<flat_grid(p.num_variables * B, p.sm_count), 256, 0, s>>>(
-      p.var_off, p.num_variables, bel, stride, out, B, p.num_var_states);
+      p.var_off, 0, p.num_variables, bel, stride, out, B, p.num_var_states);
+  return cudaGetLastError();
+}
+
+cudaError_t gumbel(cudaStream_t s, uint64_t seed, int64_t count, float* out, int sm_count) {
+  if (count == 0) return cudaSuccess;
+  ProfileScope ps(kProfLayout, s);
+  gumbel_fill_kernel<<<flat_grid(count, sm_count), 256, 0, s>>>(gumbel_key(seed), 0, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t rows_argmax(cudaStream_t s, int64_t rows, int64_t k, const float* in, int32_t* out,
+                        int sm_count) {
+  if (rows == 0) return cudaSuccess;
+  ProfileScope ps(kProfReadout, s);
+  decode_kernel<<<flat_grid(rows, sm_count), 256, 0, s>>>(nullptr, k, rows, in, 0, out, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t rows_softmax(cudaStream_t s, int64_t rows, int64_t k, const float* in, float* out,
+                         int sm_count) {
+  if (rows == 0) return cudaSuccess;
+  ProfileScope ps(kProfReadout, s);
+  marginals_kernel<<<flat_grid(rows, sm_count), 256, 0, s>>>(nullptr, k, rows, in, 0, out, 1, 0);
   return cudaGetLastError();
 }
 

@@ -45,6 +45,8 @@ int cuda_fail(cudaError_t e, const char* what) {
   return fail(PGBP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+pgbp::DebugKnobs g_debug;
+
 struct Builder {
   pgbp::Plan& p;
   int err = PGBP_OK;
@@ -75,6 +77,8 @@ struct Builder {
 void free_plan(pgbp::Plan& p) {
   for (void* a : p.allocations) cudaFree(a);
   p.allocations.clear();
+  if (p.fault_host) cudaFreeHost(p.fault_host);
+  p.fault_host = p.fault_dev = nullptr;
 }
 
 bool in_range(int64_t x, int64_t lo, int64_t hi) { return x >= lo && x < hi; }
@@ -104,6 +108,18 @@ cudaEvent_t prof_event() {
 
 namespace pgbp {
 int set_last_error(int code, const char* message) { return fail(code, "%s", message); }
+
+int take_plan_fault(const Plan& p) {
+  if (!p.fault_host) return PGBP_OK;
+  volatile unsigned* w = p.fault_host;
+  if (*w == 0u) return PGBP_OK;
+  *w = 0u;
+  return fail(PGBP_ERR_TIMEOUT,
+              "a bounded device wait of an earlier launch on this plan gave up; that launch's "
+              "results are invalid");
+}
+
+DebugKnobs debug_knobs() { return g_debug; }
 bool profiling_enabled() { return g_prof_on; }
 void profile_record(int cls, cudaStream_t s, bool start) {
   cudaEvent_t e = prof_event();
@@ -156,6 +172,32 @@ int pgbp_wait_timeouts(int64_t* count) {
   return PGBP_OK;
 }
 
+int pgbp_plan_check(const pgbp_plan* plan) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  return pgbp::take_plan_fault(plan->p);
+}
+
+int pgbp_debug_set(int knob, int64_t value) {
+  switch (knob) {
+    case PGBP_DEBUG_WAIT_LIMIT_NS:
+      if (value < 0 || value > 10000000000LL)
+        return fail(PGBP_ERR_INVALID_ARGUMENT, "wait limit %lld ns outside [0, 1e10]",
+                    (long long)value);
+      g_debug.wait_limit_ns = (unsigned long long)value;
+      return PGBP_OK;
+    case PGBP_DEBUG_SKIP_TABLE_COPY:
+      if (value != 0 && value != 1) return fail(PGBP_ERR_INVALID_ARGUMENT, "expected 0 or 1");
+      g_debug.skip_table_copy = (int)value;
+      return PGBP_OK;
+    case PGBP_DEBUG_LEGACY_MMA:
+      if (value != 0 && value != 1) return fail(PGBP_ERR_INVALID_ARGUMENT, "expected 0 or 1");
+      g_debug.legacy_mma = (int)value;
+      return PGBP_OK;
+    default:
+      return fail(PGBP_ERR_INVALID_ARGUMENT, "unknown debug knob %d", knob);
+  }
+}
+
 const char* pgbp_last_error(void) { return g_last_error.c_str(); }
 
 int pgbp_version(void) { return 200; }
@@ -204,10 +246,21 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     return code;
   };
 
-  cudaError_t ce = cudaSetDevice(device);
-  if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaSetDevice"));
-  ce = cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, device);
+  pgbp::DeviceGuard guard(device);
+  if (guard.status() != cudaSuccess) return bail(cuda_fail(guard.status(), "cudaSetDevice"));
+  cudaError_t ce = cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, device);
   if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaDeviceGetAttribute"));
+  {
+    void* h = nullptr;
+    ce = cudaHostAlloc(&h, sizeof(unsigned), cudaHostAllocMapped | cudaHostAllocPortable);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaHostAlloc(fault word)"));
+    p.fault_host = static_cast<unsigned*>(h);
+    *p.fault_host = 0u;
+    void* dptr = nullptr;
+    ce = cudaHostGetDevicePointer(&dptr, h, 0);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaHostGetDevicePointer(fault word)"));
+    p.fault_dev = static_cast<unsigned*>(dptr);
+  }
 
   const int32_t* vs = d->var_states_for_edge_states;
   const int32_t* ei = d->edge_indices_for_edge_states;
@@ -760,7 +813,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
 
 int pgbp_plan_destroy(pgbp_plan* plan) {
   if (!plan) return PGBP_OK;
-  cudaSetDevice(plan->p.device);
+  pgbp::DeviceGuard guard(plan->p.device);
   free_plan(plan->p);
   delete plan;
   return PGBP_OK;
@@ -802,7 +855,8 @@ int run_checked(const pgbp_plan* plan, void* stream, int64_t batch, const float*
                 int64_t msgs_stride, float* msgs_out, float* deltas, int64_t num_iters,
                 double damping, double temperature, void* workspace, size_t workspace_bytes,
                 int64_t checkpoint_every, float* checkpoints,
-                const pgbp::ToleranceRun* tol_run = nullptr) {
+                const pgbp::ToleranceRun* tol_run = nullptr,
+                const pgbp::Perturbation* pert = nullptr) {
   if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
   const pgbp::Plan& p = plan->p;
   if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
@@ -815,21 +869,25 @@ int run_checked(const pgbp_plan* plan, void* stream, int64_t batch, const float*
     return fail(PGBP_ERR_INVALID_ARGUMENT, "evidence stride too small");
   if (msgs_stride != 0 && msgs_stride < p.num_edge_states)
     return fail(PGBP_ERR_INVALID_ARGUMENT, "messages stride too small");
-  if ((p.num_potentials > 0 && !log_potentials) || (p.num_var_states > 0 && !evidence) ||
+  if ((p.num_potentials > 0 && !log_potentials) ||
+      (p.num_var_states > 0 && !evidence && pert == nullptr) ||
       (p.num_edge_states > 0 && (!msgs_in || !msgs_out)))
     return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
   if (!(damping == damping) || !(temperature == temperature) || temperature < 0.0)
     return fail(PGBP_ERR_INVALID_ARGUMENT, "damping and temperature must be numbers, temperature >= 0");
-  const size_t need = pgbp::workspace_bytes(p, batch, num_iters, ev_stride != 0, lp_stride != 0);
+  const size_t need = pgbp::workspace_bytes(p, batch, num_iters, ev_stride != 0 || pert != nullptr,
+                                            lp_stride != 0);
   if (!workspace || workspace_bytes < need)
     return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
     return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::run_bp(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
                    ev_stride, msgs_in, msgs_stride, msgs_out, deltas, num_iters, damping, temperature,
-                   workspace, workspace_bytes, checkpoint_every, checkpoints, tol_run);
+                   workspace, workspace_bytes, checkpoint_every, checkpoints, tol_run, pert);
   if (e == cudaErrorStreamCaptureUnsupported && tol_run)
     return fail(PGBP_ERR_UNSUPPORTED, "pgbp_run_to_tolerance reads a count on the host: "
                 "it cannot run inside a stream capture");
@@ -848,6 +906,32 @@ int pgbp_run(const pgbp_plan* plan, void* stream, int64_t batch, const float* lo
   return run_checked(plan, stream, batch, log_potentials, lp_stride, evidence, ev_stride, msgs_in,
                      msgs_stride, msgs_out, deltas, num_iters, damping, temperature, workspace,
                      workspace_bytes, 0, nullptr);
+}
+
+int pgbp_run_perturbed(const pgbp_plan* plan, void* stream, int64_t batch,
+                       const float* log_potentials, int64_t lp_stride, const float* evidence_base,
+                       int64_t ev_stride, uint64_t seed, double noise_scale, const float* msgs_in,
+                       int64_t msgs_stride, float* msgs_out, float* deltas, float* evidence_out,
+                       int64_t num_iters, double damping, double temperature, void* workspace,
+                       size_t workspace_bytes) {
+  if (!(noise_scale == noise_scale) || noise_scale - noise_scale != 0.0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "noise_scale must be finite");
+  if (!evidence_base && ev_stride != 0)
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "a null evidence base takes ev_stride 0");
+  const pgbp::Perturbation pert{seed, (float)noise_scale, evidence_out};
+  return run_checked(plan, stream, batch, log_potentials, lp_stride, evidence_base, ev_stride,
+                     msgs_in, msgs_stride, msgs_out, deltas, num_iters, damping, temperature,
+                     workspace, workspace_bytes, 0, nullptr, nullptr, &pert);
+}
+
+int pgbp_gumbel(void* stream, uint64_t seed, int64_t count, float* out) {
+  if (count < 0 || (count > 0 && !out)) return fail(PGBP_ERR_INVALID_ARGUMENT, "bad count or null");
+  int dev = 0, sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = pgbp::gumbel(static_cast<cudaStream_t>(stream), seed, count, out, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_gumbel");
+  return PGBP_OK;
 }
 
 int pgbp_run_checkpointed(const pgbp_plan* plan, void* stream, int64_t batch,
@@ -919,8 +1003,10 @@ int pgbp_run_vjp(const pgbp_plan* plan, void* stream, int64_t batch, const float
     return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
     return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::run_vjp(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride,
                     evidence, ev_stride, checkpoints, num_iters, checkpoint_every, damping,
                     temperature, g_msgs_out, g_log_potentials, g_evidence, g_msgs_in, workspace,
@@ -937,8 +1023,10 @@ int pgbp_beliefs_vjp(const pgbp_plan* plan, void* stream, int64_t batch, const f
     return fail(PGBP_ERR_INVALID_ARGUMENT, "bad batch or stride");
   if (p.num_edge_states > 0 && (!g_beliefs || !g_msgs))
     return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::beliefs_vjp(p, static_cast<cudaStream_t>(stream), batch, g_beliefs, gb_stride, g_msgs);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_beliefs_vjp launch");
   return PGBP_OK;
@@ -963,8 +1051,10 @@ int pgbp_factor_update(const pgbp_plan* plan, void* stream, int type, int64_t ba
     return fail(PGBP_ERR_INVALID_ARGUMENT, "bad stride");
   if (!(temperature == temperature) || temperature < 0.0)
     return fail(PGBP_ERR_INVALID_ARGUMENT, "temperature must be >= 0");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // every output slot not written by a factor (the "other" states when normalizing) must be zero
   for (int64_t b = 0; b < batch; ++b) {
@@ -985,8 +1075,10 @@ int pgbp_beliefs(const pgbp_plan* plan, void* stream, int64_t batch, const float
     return fail(PGBP_ERR_INVALID_ARGUMENT, "bad batch or stride");
   if (p.num_var_states > 0 && (!evidence || !beliefs)) return fail(PGBP_ERR_INVALID_ARGUMENT, "null");
   if (p.num_edge_states > 0 && !msgs) return fail(PGBP_ERR_INVALID_ARGUMENT, "null msgs");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::beliefs(p, static_cast<cudaStream_t>(stream), batch, evidence, ev_stride, msgs,
                     msgs_stride, beliefs);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_beliefs launch");
@@ -1000,8 +1092,10 @@ int pgbp_decode(const pgbp_plan* plan, void* stream, int64_t batch, const float*
   if (!p.var_off) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
   if (batch <= 0 || beliefs_stride < 0 || !beliefs || !map)
     return fail(PGBP_ERR_INVALID_ARGUMENT, "bad argument");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::decode(p, static_cast<cudaStream_t>(stream), batch, beliefs, beliefs_stride, map);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_decode launch");
   return PGBP_OK;
@@ -1137,8 +1231,10 @@ int pgbp_sdlp_objective(const pgbp_plan* plan, void* stream, int64_t batch,
                       logsumexp_temp, workspace, workspace_bytes);
   if (rc) return rc;
   if (!objval) return fail(PGBP_ERR_INVALID_ARGUMENT, "null objval");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::sdlp_objective(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride,
                            evidence, ev_stride, msgs, msgs_stride, logsumexp_temp, objval, grad,
                            bp_updates, edge_lse, workspace);
@@ -1163,8 +1259,10 @@ int pgbp_sdlp_run(const pgbp_plan* plan, void* stream, int64_t batch, const floa
     return fail(PGBP_ERR_INVALID_ARGUMENT,
                 "For gradient descent, the learning rate must be smaller than the log sum-exp "
                 "temperature.");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::sdlp_run(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride,
                      evidence, ev_stride, msgs_in, msgs_stride, msgs_out, objvals, num_iters,
                      logsumexp_temp, lr, workspace);
@@ -1197,11 +1295,44 @@ int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch, const float*
     return fail(PGBP_ERR_WORKSPACE, "workspace of %zu bytes needed, got %zu", need, workspace_bytes);
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
     return fail(PGBP_ERR_WORKSPACE, "workspace must be 256-byte aligned");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::energy(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
                    ev_stride, map, map_stride, energy, workspace, workspace_bytes);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_energy launch");
+  return PGBP_OK;
+}
+
+namespace {
+
+// Arguments of pgbp_softmax_rows / pgbp_argmax_rows; the current device's SM count in *sm.
+int rows_check(int64_t rows, int64_t k, const void* in, const void* out, int* sm) {
+  if (rows < 0 || k < 0 || (rows > 0 && k == 0) || (rows > 0 && (!in || !out)))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad rows, k or null pointer");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(sm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  return PGBP_OK;
+}
+
+}  // namespace
+
+int pgbp_softmax_rows(void* stream, int64_t rows, int64_t k, const float* in, float* out) {
+  int sm = 0;
+  if (const int rc = rows_check(rows, k, in, out, &sm)) return rc;
+  const cudaError_t e = pgbp::rows_softmax(static_cast<cudaStream_t>(stream), rows, k, in, out, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_softmax_rows launch");
+  return PGBP_OK;
+}
+
+int pgbp_argmax_rows(void* stream, int64_t rows, int64_t k, const float* in, int32_t* out) {
+  int sm = 0;
+  if (const int rc = rows_check(rows, k, in, out, &sm)) return rc;
+  const cudaError_t e = pgbp::rows_argmax(static_cast<cudaStream_t>(stream), rows, k, in, out, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_argmax_rows launch");
   return PGBP_OK;
 }
 
@@ -1212,8 +1343,10 @@ int pgbp_marginals(const pgbp_plan* plan, void* stream, int64_t batch, const flo
   if (!p.var_off) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
   if (batch <= 0 || beliefs_stride < 0 || !beliefs || !marginals)
     return fail(PGBP_ERR_INVALID_ARGUMENT, "bad argument");
-  cudaError_t e = cudaSetDevice(p.device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  cudaError_t e;
   e = pgbp::marginals(p, static_cast<cudaStream_t>(stream), batch, beliefs, beliefs_stride, marginals);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_marginals launch");
   return PGBP_OK;

@@ -14,7 +14,10 @@
 //     PGBP_ERR_WORKSPACE before anything is enqueued;
 //   * no cudaMalloc, cudaFree or allocating library routine is called;
 //   * the first call on a device looks up the array's device address with cudaGetSymbolAddress
-//     (with that device current) and caches it; make that first call before any stream capture;
+//     (with that device current) and caches it; make that first call before any stream capture.
+//     A device reset frees the array together with every plan, so the cached address, like the
+//     plans, must not be used across a cudaDeviceReset;
+//   * the caller's current device is the same after the call as before it;
 //   * every call shares the one array: calls that overlap on the GPU (different streams, or
 //     different host threads without ordering) race on it. The part that must start at zero (the
 //     per-iteration residual accumulators) is cleared by every call; everything else is written
@@ -78,8 +81,10 @@ extern "C" int pgbp_run_static_scratch(const pgbp_plan* plan, void* stream, int6
              need, (size_t)PGBP_STATIC_SCRATCH_BYTES);
     return pgbp::set_last_error(PGBP_ERR_WORKSPACE, msg);
   }
-  cudaError_t e = cudaSetDevice(plan->p.device);
-  if (e != cudaSuccess) return pgbp::set_last_error(PGBP_ERR_CUDA, cudaGetErrorString(e));
+  // the caller's current device is given back when the call returns
+  pgbp::DeviceGuard guard(plan->p.device);
+  if (guard.status() != cudaSuccess)
+    return pgbp::set_last_error(PGBP_ERR_CUDA, cudaGetErrorString(guard.status()));
   void* scratch = nullptr;
   const int rc = scratch_address(plan->p.device, &scratch);
   if (rc != PGBP_OK) return rc;

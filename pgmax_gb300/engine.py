@@ -124,6 +124,15 @@ class Plan:
         pass
       self.handle = None
 
+  def check(self, synchronize=True):
+    """Raises PgbpError (a RuntimeError, status PGBP_ERR_TIMEOUT) when a launch on this plan gave
+    up a bounded device wait since the last check (pgbp_plan_check): that launch's results are
+    invalid. Synchronises the plan's device first unless `synchronize` is False, in which case
+    only launches that have already completed are seen."""
+    if synchronize:
+      _torch().cuda.synchronize(self.device)
+    native.check(self.lib.pgbp_plan_check(self.handle), "pgbp_plan_check")
+
   # ------------------------------------------------------------------------- autotuner
   def signature(self) -> str:
     buf = ctypes.create_string_buffer(1024)
@@ -231,6 +240,41 @@ class Plan:
       out = out[0]
       deltas = deltas[0] if deltas is not None else None
     return out, deltas
+
+  def run_perturbed(self, log_potentials, evidence, ftov_msgs, num_iters, seed, batch,
+                    noise_scale=1.0, damping=0.5, temperature=0.0, with_deltas=True):
+    """Perturb-and-MAP in one call (pgbp_run_perturbed): run() on `batch` instances whose evidence
+    is `evidence` (the base: [N_vs] shared, [batch, N_vs], or None for zeros) plus noise_scale times
+    the Gumbel(0, 1) stream of `seed`, generated inside the run. Returns (msgs [batch, E_s],
+    deltas [batch, iters] or None, the perturbed evidence [batch, N_vs])."""
+    torch = _torch()
+    B = int(batch)
+    if B < 1:
+      raise ValueError(f"batch must be >= 1, got {B}")
+    dev = f"cuda:{self.device}"
+    lp = self._dev(log_potentials) if self.num_potentials > 0 else torch.zeros(1, device=dev)
+    lp_t, b1, lps = self._rows(lp, self.num_potentials) if self.num_potentials > 0 else (lp, 1, 0)
+    m_t, b3, ms = self._rows(self._dev(ftov_msgs), self.num_edge_states)
+    if evidence is None:
+      b2, evs, ev_ptr = B, 0, None
+    else:
+      ev_t, b2, evs = self._rows(self._dev(evidence), self.num_var_states)
+      ev_ptr = ev_t.data_ptr()
+    for name, b, stride in (("log_potentials", b1, lps), ("evidence", b2, evs), ("ftov_msgs", b3, ms)):
+      if stride != 0 and b != B:
+        raise ValueError(f"{name} holds {b} instances, batch is {B}")
+    iters = max(int(num_iters), 1)
+    out = torch.empty((B, self.num_edge_states), dtype=torch.float32, device=dev)
+    deltas = torch.empty((B, iters), dtype=torch.float32, device=dev) if with_deltas else None
+    ev_out = torch.empty((B, self.num_var_states), dtype=torch.float32, device=dev)
+    ws_bytes = int(self.lib.pgbp_workspace_size(self.handle, B, iters))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    native.check(self.lib.pgbp_run_perturbed(
+        self.handle, self._stream(), B, lp_t.data_ptr(), lps, ev_ptr, evs,
+        int(seed) & (2**64 - 1), float(noise_scale), m_t.data_ptr(), ms, out.data_ptr(),
+        deltas.data_ptr() if deltas is not None else None, ev_out.data_ptr(), int(num_iters),
+        float(damping), float(temperature), ws.data_ptr(), ws_bytes), "pgbp_run_perturbed")
+    return out, deltas, ev_out
 
   def run_checkpointed(self, log_potentials, evidence, ftov_msgs, num_iters, damping=0.5,
                        temperature=0.0, checkpoint_every=10):
@@ -448,6 +492,61 @@ class Plan:
     native.check(self.lib.pgbp_marginals(self.handle, self._stream(), B, b_t.data_ptr(), bs,
                                          out.data_ptr()), "pgbp_marginals")
     return out if b.ndim == 2 else out[0]
+
+
+def gumbel(seed, count, device=None):
+  """Draws 0 .. count - 1 of the Gumbel(0, 1) stream of `seed` that run_perturbed adds to the
+  evidence (pgbp_gumbel), as a float32 CUDA tensor."""
+  torch = _require_cuda()
+  dev = torch.device("cuda", torch.cuda.current_device() if device is None else int(device))
+  out = torch.empty(int(count), dtype=torch.float32, device=dev)
+  with torch.cuda.device(dev):
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    native.check(native.load().pgbp_gumbel(stream, int(seed) & (2**64 - 1), int(count),
+                                           out.data_ptr()), "pgbp_gumbel")
+  return out
+
+
+def _dense_rows(x):
+  """x (torch or NumPy, shape (..., k)) as a contiguous float32 CUDA tensor, detached."""
+  torch = _require_cuda()
+  t = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, dtype=np.float32))
+  dev = t.device if t.is_cuda else torch.device("cuda", torch.cuda.current_device())
+  return t.detach().to(device=dev, dtype=torch.float32).contiguous()
+
+
+def softmax_last(x):
+  """get_marginals of one belief array of any shape (..., k) that did not come from a plan:
+  exp(x - logsumexp(x)) over the last axis by the pgbp_softmax_rows kernel (padded -inf states
+  get 0). Returns a CUDA tensor."""
+  torch = _torch()
+  t = _dense_rows(x)
+  if t.numel() == 0:
+    return t.clone()
+  k = int(t.shape[-1])
+  out = torch.empty_like(t)
+  with torch.cuda.device(t.device):
+    stream = ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+    native.check(native.load().pgbp_softmax_rows(stream, t.numel() // k, k, t.data_ptr(),
+                                                 out.data_ptr()), "pgbp_softmax_rows")
+  return out
+
+
+def argmax_last(x):
+  """decode_map_states of one belief array of any shape (..., k) that did not come from a plan:
+  the first maximum (or first NaN) over the last axis by the pgbp_argmax_rows kernel, int32; an
+  empty array decodes to zeros of shape (...) as in the reference. Returns a CUDA tensor."""
+  torch = _torch()
+  t = _dense_rows(x)
+  if t.numel() == 0:
+    return torch.zeros(t.shape[:-1], dtype=torch.float32, device=t.device)
+  k = int(t.shape[-1])
+  out = torch.empty(t.shape[:-1], dtype=torch.int32, device=t.device)
+  with torch.cuda.device(t.device):
+    stream = ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+    native.check(native.load().pgbp_argmax_rows(stream, t.numel() // k, k, t.data_ptr(),
+                                                out.data_ptr()), "pgbp_argmax_rows")
+  return out
 
 
 def _read_cache(path: str) -> Dict:

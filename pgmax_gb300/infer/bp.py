@@ -13,7 +13,7 @@ from typing import Any, Callable, Dict, Hashable, Optional, Tuple
 
 import numpy as np
 
-from .. import autodiff
+from .. import autodiff, engine
 from .bp_state import BPArrays, BPState
 from .inferer import Beliefs, Inferer, InfererContext, unflatten_beliefs
 
@@ -27,6 +27,7 @@ class BeliefPropagation(Inferer):
   run_bp: Callable[..., BPArrays]
   run_with_diffs: Callable[..., Tuple[BPArrays, Any]]
   context: Any = None
+  run_perturbed: Optional[Callable[..., BPArrays]] = None
 
 
 def BP(bp_state: BPState, temperature: Optional[float] = 0.0,  # pylint: disable=invalid-name
@@ -66,27 +67,41 @@ def BP(bp_state: BPState, temperature: Optional[float] = 0.0,  # pylint: disable
     warnings.warn("BP.run_bp is deprecated. Please consider using BP.run instead.")
     return run(bp_arrays, num_iters, damping, default_t)
 
+  def run_perturbed(bp_arrays: BPArrays, num_iters: int, seed: int, batch: int,
+                    noise_scale: float = 1.0, damping: float = 0.5,
+                    temperature: float = default_t) -> BPArrays:
+    """Perturb-and-MAP: `run` over `batch` samples whose evidence is bp_arrays.evidence plus
+    noise_scale times fresh Gumbel(0, 1) noise (the stream of `seed`, pgmax_gb300.engine.gumbel)
+    on every variable state, generated on the GPU inside the run. The returned BPArrays hold the
+    batch's messages and its perturbed evidence [batch, N_vs], ready for get_beliefs. Not in
+    PGMax, whose users draw the noise themselves and vmap run over update(evidence_updates=...)."""
+    msgs, _, ev = ctx.plan.run_perturbed(bp_arrays.log_potentials, bp_arrays.evidence,
+                                         bp_arrays.ftov_msgs, num_iters, seed, batch,
+                                         noise_scale, damping, temperature, with_deltas=False)
+    lp = bp_arrays.log_potentials
+    return BPArrays(log_potentials=lp if _is_torch(lp) else ctx.plan._dev(lp),  # pylint: disable=protected-access
+                    ftov_msgs=msgs, evidence=ev)
+
   return BeliefPropagation(init=ctx.init, update=ctx.update, to_bp_state=ctx.to_bp_state,
                            get_beliefs=ctx.get_beliefs, run=run, run_bp=run_bp,
-                           run_with_diffs=run_with_diffs, context=ctx)
+                           run_with_diffs=run_with_diffs, context=ctx,
+                           run_perturbed=run_perturbed)
 
 
 def _softmax_last(x):
-  if _is_torch(x):
+  if autodiff.wants_grad(x):
+    # differentiable beliefs (torch autograd reaches them): torch's softmax carries the gradient
     if x.numel() == 0:
       return x
     return (x - x.logsumexp(dim=-1, keepdim=True)).exp()
-  x = np.asarray(x)
-  if x.size == 0:
-    return x
-  m = np.max(x, axis=-1, keepdims=True)
-  m = np.where(np.isfinite(m), m, 0)
-  return np.exp(x - (np.log(np.sum(np.exp(x - m), axis=-1, keepdims=True)) + m))
+  return engine.softmax_last(x)
 
 
 def get_marginals(beliefs: Dict[Hashable, Any]) -> Dict[Hashable, Any]:
-  """Per-variable softmax of the beliefs (pgmax/infer/bp.py:263-288). Beliefs from get_beliefs
-  are normalised by the pgbp_marginals kernel; padded states get probability 0."""
+  """Per-variable softmax of the beliefs (pgmax/infer/bp.py:263-288) on the GPU. Beliefs from
+  get_beliefs are normalised by the pgbp_marginals kernel over the flat array, any other belief
+  arrays by pgbp_softmax_rows; padded states get probability 0. Beliefs that require grad go
+  through torch's softmax so that autograd reaches them."""
   ctx = getattr(beliefs, "context", None)
   flat = getattr(beliefs, "flat", None)
   if (ctx is not None and flat is not None and ctx.num_variables > 0 and
@@ -97,7 +112,7 @@ def get_marginals(beliefs: Dict[Hashable, Any]) -> Dict[Hashable, Any]:
     def zero_pad(x):
       if isinstance(x, dict):
         return {k: zero_pad(v) for k, v in x.items()}
-      return x.nan_to_num(neginf=0.0) if _is_torch(x) else np.nan_to_num(x, neginf=0.0)
+      return x.nan_to_num(nan=float("nan"), posinf=float("inf"), neginf=0.0)
 
     return {k: zero_pad(v) for k, v in out.items()}
 

@@ -198,18 +198,14 @@ def _tree_map(fn, tree):
 
 
 def _argmax_last(x):
-  if _is_torch(x):
-    if x.numel() == 0:
-      import torch  # pylint: disable=g-import-not-at-top
-      return torch.zeros(x.shape[:-1], device=x.device)
-    return x.argmax(dim=-1)
-  x = np.asarray(x)
-  return np.argmax(x, axis=-1) if x.size > 0 else np.zeros(x.shape[:-1])
+  from .. import engine  # pylint: disable=g-import-not-at-top
+  return engine.argmax_last(x)
 
 
 def decode_map_states(beliefs: Dict[Hashable, Any]) -> Dict[Hashable, Any]:
   """MAP states: argmax over each variable's states, first maximum wins (inferer.py:251-264).
-  Beliefs from get_beliefs are decoded by the pgbp_decode kernel."""
+  Beliefs from get_beliefs are decoded by the pgbp_decode kernel over the flat array, any other
+  belief arrays by pgbp_argmax_rows."""
   ctx = getattr(beliefs, "context", None)
   if ctx is not None and getattr(beliefs, "flat", None) is not None and ctx.num_variables > 0:
     flat_map = ctx.plan.decode(beliefs.flat, ctx.num_variables)

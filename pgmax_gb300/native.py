@@ -135,6 +135,10 @@ SIGNATURES = [
                                 _p, ctypes.c_size_t]),
     ("pgbp_run_static_scratch", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p,
                                                _p, _i64, _d, _d]),
+    ("pgbp_run_perturbed", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, ctypes.c_uint64, _d,
+                                          _p, _i64, _p, _p, _p, _i64, _d, _d, _p,
+                                          ctypes.c_size_t]),
+    ("pgbp_gumbel", ctypes.c_int, [_p, ctypes.c_uint64, _i64, _p]),
     ("pgbp_factor_update", ctypes.c_int, [_p, _p, ctypes.c_int, _i64, _p, _i64, _p, _i64, _d,
                                           ctypes.c_int, _p, _i64]),
     ("pgbp_run_checkpointed", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p,
@@ -148,6 +152,8 @@ SIGNATURES = [
     ("pgbp_beliefs", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p]),
     ("pgbp_decode", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
     ("pgbp_marginals", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p]),
+    ("pgbp_softmax_rows", ctypes.c_int, [_p, _i64, _i64, _p, _p]),
+    ("pgbp_argmax_rows", ctypes.c_int, [_p, _i64, _i64, _p, _p]),
     ("pgbp_plan_tuning_count", _i64, [_p]),
     ("pgbp_plan_tuning_get", ctypes.c_int, [_p, _p, _i64]),
     ("pgbp_plan_tuning_set", ctypes.c_int, [_p, _p, _i64]),
@@ -174,6 +180,8 @@ SIGNATURES = [
     ("pgbp_profile_enable", ctypes.c_int, [ctypes.c_int]),
     ("pgbp_profile_read", ctypes.c_int, [ctypes.POINTER(Profile)]),
     ("pgbp_wait_timeouts", ctypes.c_int, [ctypes.POINTER(_i64)]),
+    ("pgbp_plan_check", ctypes.c_int, [_p]),
+    ("pgbp_debug_set", ctypes.c_int, [ctypes.c_int, _i64]),
     ("pgbp_last_error", ctypes.c_char_p, []),
     ("pgbp_version", ctypes.c_int, []),
 ]
@@ -228,6 +236,18 @@ def wait_timeouts():
   if rc not in (0, 6):  # PGBP_OK, PGBP_ERR_TIMEOUT
     check(rc, "pgbp_wait_timeouts")
   return int(n.value)
+
+
+DEBUG_WAIT_LIMIT_NS = 1
+DEBUG_SKIP_TABLE_COPY = 2
+DEBUG_LEGACY_MMA = 3
+
+
+def debug_set(knob, value):
+  """Process-wide debug setting (pgbp_debug_set): DEBUG_WAIT_LIMIT_NS (0 = the built-in 2 s),
+  DEBUG_SKIP_TABLE_COPY (1 = the exp-domain kernels' table wait runs out with no copy issued) or
+  DEBUG_LEGACY_MMA (1 = shared 64 x 64 tables of one instance on the mma.sync kernel)."""
+  check(load().pgbp_debug_set(int(knob), int(value)), "pgbp_debug_set")
 
 
 def profile_read():

@@ -11,7 +11,8 @@ FIXTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "f
 
 def run_fixture_paths():
   return sorted(p for p in glob.glob(os.path.join(FIXTURES, "*.npz"))
-                if not os.path.basename(p).startswith(("factor_updates", "energy_", "sdlp_")))
+                if not os.path.basename(p).startswith(("factor_updates", "energy_", "sdlp_",
+                                                       "marginals_")))
 
 
 def energy_fixture_paths():
@@ -35,3 +36,10 @@ def fixture_id(path):
 def sdlp_fixture_paths():
   """SDLP calls of the reference: wiring, BPArrays, call kind and its outputs."""
   return sorted(glob.glob(os.path.join(FIXTURES, "sdlp_*.npz")))
+
+
+def marginals_fixture_paths():
+  """get_marginals calls of the reference after seeded runs: wiring, evidence, messages, flat
+  beliefs and, leaf by leaf, the unflattened beliefs and the reference's marginals."""
+  return sorted(p for p in glob.glob(os.path.join(FIXTURES, "marginals_*.npz"))
+                if not p.endswith("marginals_direct.npz"))

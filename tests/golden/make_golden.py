@@ -28,7 +28,15 @@ The smooth dual LP-MAP solver (`infer.SDLP`, pgmax/infer/dual_lp.py) is recorded
 reference's tests/lp/test_bp_for_lp.py and of `sdlp_cases` (the seeded graphs of cases.py with
 cold and random initial messages, temperatures 0 to 1, default and explicit learning rates).
 
-`--energy-only` / `--sdlp-only` regenerate those fixtures alone and leave the others untouched.
+`get_marginals` (pgmax/infer/bp.py:263-288) is recorded as `marginals_*.npz`: for seeded graphs
+of cases.py (including the mixed graph, whose variables of 2, 3 and 4 states make the unflattened
+beliefs padded with -inf), the run's output messages, the flat and unflattened beliefs and the
+reference's marginals leaf by leaf; and `marginals_direct.npz`: get_marginals called on hand-made
+belief arrays (-inf states, a variable whose states are all -inf, large magnitudes, an empty
+array).
+
+`--energy-only` / `--sdlp-only` / `--marginals-only` regenerate those fixtures alone and leave the
+others untouched. `--reference` names the PGMax source tree (or set PGMAX_REFERENCE).
 """
 
 import argparse
@@ -373,6 +381,85 @@ def save_sdlp():
   return len(REC.sdlp)
 
 
+def _leaves(tree, prefix=()):
+  """(key path, array) of the leaves of a beliefs / marginals dict."""
+  out = []
+  for k, v in tree.items():
+    if isinstance(v, dict):
+      out += _leaves(v, prefix + (k,))
+    else:
+      out.append((prefix + (k,), np.asarray(v)))
+  return out
+
+
+def marginals_cases(api):
+  """get_marginals of the beliefs of seeded runs, and of hand-made belief arrays."""
+  sys.path.insert(0, HERE)
+  import cases  # pylint: disable=g-import-not-at-top
+  inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  bp_mod = importlib.import_module("pgmax.infer.bp")
+  plans = [
+      ("ising12_T1", "ising", dict(n=12, seed=3), dict(num_iters=50, damping=0.5, temperature=1.0)),
+      ("rbm_T0", "rbm", dict(nh=20, nv=30, seed=0, sample=0), dict(num_iters=40, damping=0.5, temperature=0.0)),
+      ("potts_K4", "potts", dict(L=8, K=4, seed=1), dict(num_iters=30, damping=0.5, temperature=1.0)),
+      ("potts_K16", "potts", dict(L=4, K=16, seed=3), dict(num_iters=20, damping=0.5, temperature=0.5)),
+      ("deconv_T1", "deconv", dict(seed=0), dict(num_iters=40, damping=0.5, temperature=1.0)),
+      ("mixed_T0", "mixed", dict(seed=0), dict(num_iters=7, damping=0.5, temperature=0.0)),
+      ("mixed_T1", "mixed", dict(seed=1), dict(num_iters=9, damping=0.5, temperature=1.0)),
+      ("mixed_T0.3", "mixed", dict(seed=2), dict(num_iters=9, damping=0.3, temperature=0.3)),
+  ]
+  n = 0
+  for name, builder, bkw, rkw in plans:
+    fg, groups, ev = cases.BUILDERS[builder](api, **bkw)
+    bp = api.infer.BP(fg.bp_state, temperature=rkw["temperature"])
+    arrays = bp.init(evidence_updates=ev)
+    out = bp.run(arrays, num_iters=rkw["num_iters"], damping=rkw["damping"],
+                 temperature=rkw["temperature"])
+    ctx = inferer_mod.InfererContext(fg.bp_state)
+    beliefs = bp.get_beliefs(out)
+    marg = bp_mod.get_marginals(beliefs)
+    keyed = lambda t: {groups.index(g): v for g, v in t.items()}
+    bl = sorted(_leaves(keyed(beliefs)), key=lambda x: str(x[0]))
+    md = dict(_leaves(keyed(marg)))
+    ml = [(path, md[path]) for path, _ in bl]
+    rec = {"w." + k: v for k, v in wiring_arrays(ctx, fg.bp_state.fg_state).items()}
+    rec["evidence"] = _np(out.evidence, np.float32)
+    rec["ftov_msgs"] = _np(out.ftov_msgs, np.float32)
+    rec["log_potentials"] = _np(out.log_potentials, np.float32)
+    rec["flat_beliefs"] = np.asarray(
+        importlib.import_module("jax").numpy.array(out.evidence)
+        .at[ctx.var_states_for_edge_states].add(out.ftov_msgs), dtype=np.float32)
+    for k, ((path, b), (_, m)) in enumerate(zip(bl, ml)):
+      rec[f"leaf{k}.beliefs"] = b.astype(np.float32)
+      rec[f"leaf{k}.marginals"] = m.astype(np.float32)
+    rec["num_leaves"] = np.int64(len(bl))
+    rec["meta"] = np.array(json.dumps({
+        "source": "get_marginals", "case": name, "builder": builder, "builder_kwargs": bkw,
+        "run_kwargs": rkw, "leaf_paths": [[p[0]] + [str(x) for x in p[1:]] for p, _ in bl]}))
+    np.savez_compressed(os.path.join(OUT, f"marginals_{name}.npz"), **rec)
+    n += 1
+  # hand-made beliefs: -inf states (probability 0), a variable with every state -inf (nan, as
+  # exp(-inf - logsumexp) is), magnitudes of 1e4, a row of equal values, an empty array
+  rng = np.random.default_rng(4)
+  a = (rng.normal(size=(6, 5)) * 3).astype(np.float32)
+  a[0, 1] = -np.inf
+  a[1, :3] = -np.inf
+  a[2, :] = -np.inf
+  a[3, :] = 7.0
+  b = (rng.normal(size=(4, 3, 2)) * 1e4).astype(np.float32)
+  c = np.zeros((0, 4), np.float32)
+  d = rng.normal(size=(7, 64)).astype(np.float32)
+  direct = {"in0": a, "in1": b, "in2": c, "in3": d}
+  res = bp_mod.get_marginals({k: importlib.import_module("jax").numpy.array(v)
+                              for k, v in direct.items()})
+  rec = dict(direct)
+  for k in direct:
+    rec["out" + k[2:]] = np.asarray(res[k], dtype=np.float32)
+  rec["meta"] = np.array(json.dumps({"source": "get_marginals", "case": "direct"}))
+  np.savez_compressed(os.path.join(OUT, "marginals_direct.npz"), **rec)
+  return n + 1
+
+
 def save_run(path, run, extra=None):
   arrays = {}
   for k, v in run["wiring"].items():
@@ -492,10 +579,14 @@ def factor_update_fixtures(api):
 
 def main():
   ap = argparse.ArgumentParser()
-  ap.add_argument("--reference", default=os.environ.get("PGMAX_REFERENCE", "/root/reference"))
+  ap.add_argument("--reference", default=os.environ.get("PGMAX_REFERENCE"),
+                  help="the PGMax source tree (default: $PGMAX_REFERENCE)")
   ap.add_argument("--energy-only", action="store_true")
   ap.add_argument("--sdlp-only", action="store_true")
+  ap.add_argument("--marginals-only", action="store_true")
   args = ap.parse_args()
+  if not args.reference:
+    ap.error("name the PGMax source tree with --reference or PGMAX_REFERENCE")
   sys.path.insert(0, HERE)
   import jax_shim  # pylint: disable=g-import-not-at-top
   jax_shim.install()
@@ -519,6 +610,13 @@ def main():
     sdlp_cases(api)
     n = save_sdlp()
     print(json.dumps({"sdlp_reference_tests": status, "sdlp_fixtures": n}, indent=1))
+    return
+  if args.marginals_only:
+    for f in os.listdir(OUT):
+      if f.startswith("marginals_") and f.endswith(".npz"):
+        os.remove(os.path.join(OUT, f))
+    n = marginals_cases(api)
+    print(json.dumps({"marginals_fixtures": n}, indent=1))
     return
   if args.energy_only:
     for f in os.listdir(OUT):
@@ -545,6 +643,9 @@ def main():
   status.update(run_reference_tests(args.reference, sdlp_tests))
   sdlp_cases(api)
   save_sdlp()
+  n_runs = len(REC.runs)
+  marginals_cases(api)
+  del REC.runs[n_runs:]  # the marginals cases' own runs are saved in their fixtures
 
   # Golden vector of tests/test_pgmax.py: the (messages, expected) pair of its allclose call.
   golden = [a for a in REC.allclose_args if a[0] == "test_pgmax::test_e2e_sanity_check"]

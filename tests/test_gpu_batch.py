@@ -183,3 +183,43 @@ def test_exp_domain_underflow_falls_back_to_the_direct_formula():
   want = oracle.run(oracle.Wiring(wp), np.tile(table, wp["num_factors"]), ev.reshape(-1),
                     np.zeros(2 * K * w["num_factors"], np.float32), 10, 0.5, 1.0)[0]
   np.testing.assert_allclose(out.cpu().numpy(), want, atol=1e-4, rtol=1e-6)
+
+
+def test_table_wait_that_runs_out_is_an_error_and_the_plan_recovers():
+  """The exp-domain kernels' bounded table wait. With the debug settings that arm the table
+  barrier without issuing the copy and cut the limit to 1 ms, every CTA's wait runs out with
+  nothing in flight: the kernel stops, the device count and the plan's fault word are set, the
+  plan reports PGBP_ERR_TIMEOUT (RuntimeError) and the next launch is refused until the fault has
+  been reported once. With the settings cleared the same plan runs normally and matches the
+  oracle."""
+  from pgmax_gb300 import engine, native  # pylint: disable=g-import-not-at-top
+  L, K = 5, 64
+  rng = np.random.default_rng(21)
+  table = rng.normal(0.0, 0.5, size=K * K).astype(np.float32)
+  ev = rng.normal(size=L * L * K).astype(np.float32)
+  w = batch.grid_wiring(L, K, shared_table=True, implicit_rows=True)
+  m = np.zeros(2 * K * w["num_factors"], np.float32)
+  plan = engine.Plan(w, flags=1)
+  plan.check()
+  native.wait_timeouts()
+  native.debug_set(native.DEBUG_WAIT_LIMIT_NS, 1_000_000)
+  native.debug_set(native.DEBUG_SKIP_TABLE_COPY, 1)
+  try:
+    plan.run(table, ev, m, 2, 0.5, 1.0)
+    with pytest.raises(RuntimeError, match="status 6"):
+      plan.check()
+    plan.run(table, ev, m, 2, 0.5, 1.0)
+    _torch().cuda.synchronize()
+    with pytest.raises(RuntimeError, match="gave up"):   # refused at entry: nothing enqueued
+      plan.run(table, ev, m, 2, 0.5, 1.0)
+  finally:
+    native.debug_set(native.DEBUG_SKIP_TABLE_COPY, 0)
+    native.debug_set(native.DEBUG_WAIT_LIMIT_NS, 0)
+  assert native.wait_timeouts() > 0
+  plan.check()
+  out, _ = plan.run(table, ev, m, 10, 0.5, 1.0)
+  plan.check()
+  assert native.wait_timeouts() == 0
+  wp = batch.grid_wiring(L, K)
+  want = oracle.run(oracle.Wiring(wp), np.tile(table, wp["num_factors"]), ev, m, 10, 0.5, 1.0)[0]
+  np.testing.assert_allclose(out.cpu().numpy(), want, atol=ATOL, rtol=0)

@@ -330,3 +330,16 @@ def test_run_to_tolerance_matches_one_run_of_the_same_length(check_every):
     assert ran % check_every == 0 and ran - int(first.max()) < check_every
   else:                      # some instance oscillates: the run went to max_iters
     assert ran == 500
+
+
+def test_entry_points_leave_the_callers_device_current():
+  """Every C ABI call makes the plan's device current for its work and gives the caller's current
+  device back (a caller inside a host framework must not find its device changed)."""
+  import torch  # pylint: disable=g-import-not-at-top
+  f = fixtures.load(f"{fixtures.FIXTURES}/case_mixed_T1.npz")
+  torch.cuda.set_device(0)
+  plan = _plan(f["wiring"])
+  out, _ = plan.run(f["log_potentials"], f["evidence"], f["ftov_msgs_in"], 3, 0.5, 1.0)
+  plan.beliefs(f["evidence"], out)
+  torch.cuda.synchronize()
+  assert torch.cuda.current_device() == 0

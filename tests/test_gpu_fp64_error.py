@@ -5,11 +5,14 @@ cannot run here).
 
 Each case prints one line `FP64 error | <case> | msgs <max abs> | beliefs <max abs> | ...` (run
 with -s to see them), with the float64 run's last residual (max |change| of its last iteration),
-and checks: when the float64 run has settled (last residual <= 1e-4), 1e-4 on messages and beliefs
-and, for max-product runs, identical MAP decodes except at ties within 1e-4. A run that has not
-settled (max-product on the full RBM keeps oscillating after 200 iterations) carries float32
-rounding into its trajectory in the reference as well; its error is reported, and only checked to
-be finite.
+and checks: when both the float64 run and the float32 run have settled (last residual <= 1e-4),
+1e-4 on messages and beliefs and, for max-product runs, identical MAP decodes except at ties
+within 1e-4. A run that has not settled carries float32 rounding into its trajectory in the
+reference as well; its error is reported, and only checked to be finite. Max-product on the full
+RBM is such a run: whether the float64 run settles within 200 iterations depends on its own
+summation order (torch's float64 scatter-adds on the GPU are not ordered), and when it does the
+float32 run, which equals the float32 reference bit for bit (test_gpu_bench_workloads.py), may
+still be oscillating or end at another fixed point of max-product.
 Configurations (synthetic, seeded, the shapes of the benchmarks):
   ising50_T1 / ising50_T0  50 x 50 toroidal Ising, 0.8 [[1, -1], [-1, 1]], Gumbel evidence,
                            1000 iterations
@@ -64,14 +67,14 @@ def _compare(name, wiring, lp, ev, msgs, iters, temperature, damping=0.5, plan=N
   lp32 = torch.as_tensor(np.asarray(lp, np.float32), device="cuda")
   ev32 = torch.as_tensor(np.asarray(ev, np.float32), device="cuda")
   m32 = torch.as_tensor(np.asarray(msgs, np.float32), device="cuda")
-  out32, _ = plan.run(lp32, ev32, m32, iters, damping, temperature)
+  out32, deltas32 = plan.run(lp32, ev32, m32, iters, damping, temperature)
   bel32 = plan.beliefs(ev32, out32)
   g = bp_torch.EnumGraph(wiring, device="cuda")
   with torch.no_grad():
     out64, last = g.run(lp32.double(), ev32.double(), m32.double(), iters, damping, temperature,
                         with_last_delta=True)
     bel64 = g.beliefs(ev32.double(), out64)
-  settled = float(last.max()) <= BOUND
+  settled = float(last.max()) <= BOUND and float(deltas32[..., -1].max()) <= BOUND
   out64 = out64.reshape(out32.shape)
   bel64 = bel64.reshape(bel32.shape)
   dm = float((out32.double() - out64).abs().max())
@@ -102,7 +105,8 @@ def _compare(name, wiring, lp, ev, msgs, iters, temperature, damping=0.5, plan=N
   else:
     map_ok = True
   print(f"FP64 error | {name} | msgs {dm:.3g} | beliefs {db:.3g}{extra} | float64 last residual "
-        f"{float(last.max()):.3g}", flush=True)
+        f"{float(last.max()):.3g} | float32 last residual {float(deltas32[..., -1].max()):.3g}",
+        flush=True)
   assert np.isfinite(dm) and np.isfinite(db)
   if settled:
     assert dm <= BOUND and db <= BOUND, (dm, db)

@@ -3,10 +3,11 @@
 Such callers (code inside a host framework that owns all device memory, services with a fixed
 budget reserved at start-up) get the run's scratch from one static device array instead of a
 workspace. This test calls the entry point through the C ABI twice in a row, on different inputs,
-and checks each result against pgbp_run with a caller workspace, within the tolerance the GPU
-parity tests use (here the same kernels run, so the results must be identical). It also checks
-that a run needing more scratch than the static array holds is refused with a clear error.
-The file is named to be collected last; it also passes when run on its own.
+and checks each result against pgbp_run with a caller workspace: the same kernels run on the same
+inputs, so messages and residuals must be identical bit for bit. It also checks that a run needing
+more scratch than the static array holds is refused with a clear error, and that the caller's
+current device is the same after a call as before it. The file is named to be collected last; it
+also passes when run on its own.
 """
 
 import ctypes
@@ -52,6 +53,7 @@ def _static_run(torch, native, plan, lp, ev, msgs, B, iters, damping, temperatur
 @pytest.mark.parametrize("name", ["case_mixed_T1", "case_deconv_T0"])
 def test_static_scratch_matches_workspace_run_twice(name):
   torch, native, plan, f = _setup(name)
+  torch.cuda.set_device(0)
   rng = np.random.default_rng(11)
   B, iters = 9, 12
   T = float(f["temperature"])
@@ -65,10 +67,10 @@ def test_static_scratch_matches_workspace_run_twice(name):
     want, want_d = _reference_run(torch, native, plan, lp, ev, msgs, B, iters, 0.5, T)
     got, got_d = _static_run(torch, native, plan, lp, ev, msgs, B, iters, 0.5, T)
     torch.cuda.synchronize()
-    np.testing.assert_allclose(got.cpu().numpy(), want.cpu().numpy(), atol=1e-5, rtol=0,
-                               err_msg=f"call {call}")
-    np.testing.assert_allclose(got_d.cpu().numpy(), want_d.cpu().numpy(), atol=1e-5, rtol=0,
-                               err_msg=f"call {call}")
+    assert torch.cuda.current_device() == 0
+    np.testing.assert_array_equal(got.cpu().numpy(), want.cpu().numpy(), err_msg=f"call {call}")
+    np.testing.assert_array_equal(got_d.cpu().numpy(), want_d.cpu().numpy(),
+                                  err_msg=f"call {call}")
 
 
 def test_static_scratch_rejects_runs_larger_than_the_array():
