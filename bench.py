@@ -652,9 +652,39 @@ def build_multigraph(seed=0, n_graphs=MG_GRAPHS):
   return wirings, tables, evs, fam
 
 
+def multigraph_cpu_baseline(wirings, tables, evs, sample, iters):
+  """The C oracle on a sample of the batch's graphs, one host thread per graph (ctypes releases
+  the GIL): edge-message updates per second over the sample."""
+  import concurrent.futures  # pylint: disable=g-import-not-at-top
+  from oracle import oracle  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import batch  # pylint: disable=g-import-not-at-top
+  jobs = []
+  for g in sample:
+    w = wirings[g]
+    if w.get("enum.implicit_rows"):   # the oracle reads explicit rows and per-factor tables
+      L = int(round(np.sqrt(w["num_variables"])))
+      K = int(round(np.sqrt(tables[g].shape[0])))
+      w, lp = batch.grid_wiring(L, K), np.tile(tables[g], 2 * L * (L - 1))
+    else:
+      lp = tables[g]
+    jobs.append((oracle.Wiring(w), lp, evs[g], int(w["num_edges"]),
+                 np.zeros(w["var_states_for_edge_states"].shape[0], np.float32)))
+  cores = len(os.sched_getaffinity(0))
+  t0 = time.perf_counter()
+  with concurrent.futures.ThreadPoolExecutor(min(cores, len(jobs))) as ex:
+    list(ex.map(lambda j: oracle.run(j[0], j[1], j[2], j[4], iters, 0.5, 1.0), jobs))
+  dt = time.perf_counter() - t0
+  edges = sum(j[3] for j in jobs)
+  return {"value": edges * iters / dt, "unit": "edge-msg updates/s", "cores": min(cores, len(jobs)),
+          "kind": "port",
+          "sample": f"graphs {list(sample)} of the batch (families a, b, c), {iters} of the "
+                    f"{MG_ITERS} iterations each, C oracle, one host thread per graph ({dt:.1f} s)"}
+
+
 def run_multigraph(args):
   """Config 3: the 256-graph uneven batch as one union plan, 200 iterations at T=1, damping 0.5
-  (one step = one run over every graph)."""
+  (one step = one run over every graph). The step is captured once in a CUDA graph and replayed
+  (value); the same step launched eagerly is reported beside it."""
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import batch, native  # pylint: disable=g-import-not-at-top
   t0 = time.perf_counter()
@@ -678,29 +708,45 @@ def run_multigraph(args):
     out, _ = gb.run(lp, ev, m0, iters, 0.5, 1.0)
     return out
 
-  for _ in range(args.warmup):
-    step()
-  torch.cuda.synchronize()
-  s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-  with ClockSampler(0) as clocks:
+  def timed(fn):
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s0.record(stream)
     for _ in range(args.steps):
-      step()
+      fn()
     s1.record(stream)
     torch.cuda.synchronize()
-  ms = s0.elapsed_time(s1) / args.steps
+    return s0.elapsed_time(s1) / args.steps
+
+  for _ in range(args.warmup):   # also settles the autotuner's choices for this batch
+    step()
+  eager_ms = timed(step)
+  # the whole 200-iteration step as one CUDA graph (captured on a side stream, as torch asks)
+  graph = torch.cuda.CUDAGraph()
+  side = torch.cuda.Stream(dev)
+  side.wait_stream(stream)
+  with torch.cuda.stream(side):
+    step()
+  stream.wait_stream(side)
+  with torch.cuda.graph(graph):
+    captured_out = step()
+  for _ in range(args.warmup):
+    graph.replay()
+  with ClockSampler(0) as clocks:
+    ms = timed(graph.replay)
+  ref_out = step()
+  torch.cuda.synchronize()
+  replay_equal = bool(torch.equal(captured_out, ref_out))
   # end to end: host evidence in, beliefs and MAP states out
   ev_host = torch.as_tensor(gb.concat(evs)).pin_memory()
   map_host = torch.empty(int(u["num_variables"]), dtype=torch.int32).pin_memory()
-  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-  e0.record(stream)
-  for _ in range(args.steps):
+
+  def step_e2e():
     evd = ev_host.to(dev, non_blocking=True)
     out, _ = gb.run(lp, evd, m0, iters, 0.5, 1.0)
     map_host.copy_(gb.decode(gb.beliefs(evd, out)), non_blocking=True)
-  e1.record(stream)
-  torch.cuda.synchronize()
-  e2e_ms = e0.elapsed_time(e1) / args.steps
+
+  e2e_ms = timed(step_e2e)
   native.profile_read()
   native.profile_enable(True)
   step()
@@ -710,6 +756,16 @@ def run_multigraph(args):
   peak, src = peaks()
   p_distinct = int(lp.numel())
   bytes_iter = 4 * (2 * n_es + n_vs) + 4 * p_distinct
+  # the K = 64 tcgen05 kernel (family b): per launch every factor's two 64-state messages read
+  # and written and each of its variables' 64 sums read once (distinct), plus the tables
+  fb = [g for g in range(len(wirings)) if g % 3 == 1]
+  side_b = [int(round(np.sqrt(wirings[g]["num_variables"]))) for g in fb]
+  f64 = sum(2 * L * (L - 1) for L in side_b)
+  v64 = sum(L * L for L in side_b)
+  k64_bytes = 4 * (2 * 2 * 64 * f64 + 64 * v64) + 4 * 64 * 64 * len(fb)
+  n_k64, k64_ms = prof["pairwise_exp"]
+  k64_launch_ms = k64_ms / max(n_k64, 1)
+  k64_gbs = k64_bytes / (k64_launch_ms / 1e3) / 1e9 if n_k64 else None
   line = {
       "metric": "edge-msg updates/s", "value": num_edges * iters / (ms / 1e3),
       "unit": "edge-msg updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -719,10 +775,21 @@ def run_multigraph(args):
                  "families": fam, "num_iters": iters, "temperature": 1.0, "damping": 0.5,
                  "num_edges": num_edges, "edge_states": n_es, "var_states": n_vs,
                  "shared_table_floats": p_distinct,
+                 "execution": "one CUDA graph per step (the 200 iterations captured once, replayed)",
                  "l2": "inputs larger than L2 (%d MB of messages)" % (4 * n_es >> 20)},
+      "eager": {"ms_per_step": eager_ms, "value": num_edges * iters / (eager_ms / 1e3)},
+      "captured_replay_equals_eager": replay_equal,
       "setup_s": {"generate": round(t_gen, 2), "plan": round(t_plan, 2)},
-      "kernel_time_share": {k: v[1] for k, v in prof.items() if v[0]},
+      "kernel_ms_per_step": {k: v[1] for k, v in prof.items() if v[0]},
       "gpu_launches": int(sum(v[0] for v in prof.values()) * args.steps),
+      "roofline": {"bound": "hbm",
+                   "kernel": "tc::pairwise_kernel (K = 64 shared tables, tcgen05.mma tf32, TMEM "
+                             "accumulators)",
+                   "achieved": k64_gbs, "peak": peak, "unit": "GB/s",
+                   "frac": k64_gbs / peak if k64_gbs else None,
+                   "peak_source": src, "traffic": None,
+                   "algorithmic_bytes_per_launch": k64_bytes, "launch_ms": k64_launch_ms,
+                   "factors": f64},
       "iteration_roofline": {"bytes_per_iter": bytes_iter,
                              "achieved_gbs": bytes_iter * iters / (ms / 1e3) / 1e9,
                              "peak_gbs": peak, "frac": bytes_iter * iters / (ms / 1e3) / 1e9 / peak,
@@ -732,6 +799,9 @@ def run_multigraph(args):
               "d2h_bytes_per_step": int(map_host.numel() * 4)},
       "clocks": clocks.summary(),
   }
+  if not args.no_cpu_baseline:
+    line["cpu_baseline"] = multigraph_cpu_baseline(wirings, tables, evs, range(min(6, len(wirings))),
+                                                   5)
   print(json.dumps(line))
   return 0
 

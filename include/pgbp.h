@@ -372,9 +372,11 @@ int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch,
  * 7 read-out (pgbp_beliefs, pgbp_decode, pgbp_marginals, pgbp_beliefs_vjp, pgbp_energy, the
  * SDLP per-variable and per-factor kernels; the SDLP factor passes count in classes 1-5), 8 the
  * one-CTA-per-instance small-graph kernel (all iterations in one launch), 9 the adjoint kernels of
- * pgbp_run_vjp (its forward recomputation is counted in the classes above). Process-wide, not
+ * pgbp_run_vjp (its forward recomputation is counted in the classes above), 10 the tcgen05
+ * kernel of shared 64 x 64 tables of one instance (class 1 counts every other dense pairwise
+ * launch, class 6 the building of the exp-domain run-time tables). Process-wide, not
  * thread-safe. */
-#define PGBP_PROFILE_CLASSES 10
+#define PGBP_PROFILE_CLASSES 11
 typedef struct {
   int64_t launches[PGBP_PROFILE_CLASSES];
   double milliseconds[PGBP_PROFILE_CLASSES];

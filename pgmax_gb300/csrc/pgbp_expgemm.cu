@@ -543,6 +543,546 @@ cudaError_t launch(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const
   return a.B == 1 ? launch_b<K, true>(p, q, s, a) : launch_b<K, false>(p, q, s, a);
 }
 
+// ============================================================================ tcgen05 path
+// K = 64, one instance (B = 1; batches keep the kernel above). The same arithmetic as above with
+// the products on the fifth-generation tensor cores: tcgen05.mma kind::tf32, A and B operands in
+// shared memory (128-byte swizzled, K-major), accumulators in tensor memory (TMEM), and the work
+// of a tile split over specialised warps so that loads, the products and the epilogue of
+// consecutive units overlap:
+//   unit u = (tile of up to 128 columns = consecutive factors of one group, direction d = u & 1):
+//     d = 0: the messages to variable 1, D[c][i] = sum_j U[c][j] E[i][j], U from variable 2;
+//     d = 1: the messages to variable 2, D[c][j] = sum_i W[c][i] E'[j][i], W from variable 1.
+//   M = 128 columns, N = 64 states, K = 64 states in 8 steps of 8; three products per step
+//   (hi x hi, hi x lo, lo x hi of the tf32 splits), float32 accumulation in TMEM.
+//   * producer warps 8-14: per column, lanes across states (coalesced loads of the other edge's
+//     message and variable sum, and of this edge's message; the loads of the next columns are in
+//     flight while a column is computed): vtof, its maximum (warp reduction), u = exp((vtof -
+//     max) / T) split into tf32 high and low parts written as the A operand; this edge's old
+//     message, the maximum and the message's slot go to a staging buffer of the unit's stage;
+//   * MMA warp 15: loads the group's four tables (E, E' high and low parts, built once per run in
+//     the swizzled layout) into shared memory with one bulk copy when the group changes, then
+//     issues the 24 tcgen05.mma of the unit into TMEM accumulator stage d and commits them to an
+//     mbarrier;
+//   * epilogue warps 0-7, two groups of four (group d takes the units of stage d; a thread per
+//     column = TMEM lane): tcgen05.ld of the sums, log, damping, normalisation, clipping and the
+//     residual (the arithmetic of the kernel above), the new message written to the staging row,
+//     then stored by the warp with lanes across states.
+// Handshakes: mbarriers a_full (producers -> MMA), mma_done[2] (tcgen05.commit -> producers,
+// epilogue, table reload), tmem_free[2] (epilogue -> MMA), stg_full[2] / stg_free[2] (producers
+// <-> epilogue). Every wait is bounded; the first that runs out sets a CTA abort flag that ends
+// every other wait, the CTA records the fault and stops, and TMEM is freed after the last
+// committed products have completed.
+namespace tc {
+
+constexpr int K = 64;
+constexpr int kM = 128;                  // columns per tile (the MMA's M)
+constexpr int kEpiWarps = 8;             // warps 0-3: stage 0 (d = 0), warps 4-7: stage 1 (d = 1)
+constexpr int kProdWarps = 7;            // warps 8-14
+constexpr int kMmaWarp = 15;
+constexpr int kThreads = 32 * 16;        // four warps per SM sub-partition: 128 registers each
+constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 19 columns per producer warp
+constexpr int kBatch = 4;                // columns whose loads a producer lane keeps in flight
+constexpr int kBatches = (kColsPerProd + kBatch - 1) / kBatch;   // 5
+constexpr int kStg = K + 1;              // staging row stride (floats): conflict-free both ways
+constexpr uint32_t kTmemCols = 128;      // two accumulator stages of 64 fp32 columns
+// instruction descriptor: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
+// K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(K >> 3) << 17) |
+                            ((uint32_t)(kM >> 4) << 24);
+
+// shared memory, byte offsets from a 1024-byte aligned base
+constexpr int kMatBytes = K * K * 4;                 // one 64 x 64 tf32 table: 16 KB
+constexpr int kTabBytes = 4 * kMatBytes;             // E hi, E lo, E' hi, E' lo
+constexpr int kABytes = kM * K * 4;                  // one 128 x 64 tf32 operand: 32 KB
+constexpr int kOffAhi = kTabBytes;
+constexpr int kOffAlo = kOffAhi + kABytes;
+constexpr int kOffStg = kOffAlo + kABytes;           // 2 x [kM][kStg] floats
+constexpr int kStgBytes = kM * kStg * 4;
+constexpr int kOffM = kOffStg + 2 * kStgBytes;       // 2 x [kM] maxima of the other vtof
+constexpr int kOffOwn = kOffM + 2 * kM * 4;          // 2 x [kM] slot of the message written
+constexpr int kOffR = kOffOwn + 2 * kM * 4;          // 2 x [K] table row / column maxima
+constexpr int kOffBar = kOffR + 2 * K * 4;
+enum { kBarTab = 0, kBarAFull, kBarMma0, kBarMma1, kBarTmem0, kBarTmem1, kBarStgFull0,
+       kBarStgFull1, kBarStgFree0, kBarStgFree1, kNumBars };
+constexpr int kOffMisc = kOffBar + kNumBars * 8;     // TMEM address, abort flags, residual
+constexpr int kSmemUsed = kOffMisc + 16;
+constexpr int kSmemBytes = kSmemUsed + 1024;         // + alignment of the dynamic base
+static_assert(kSmemBytes <= 227 * 1024, "shared memory");
+static_assert(kOffBar % 8 == 0 && kOffStg % 16 == 0, "alignment");
+
+// floats of one group's tables in the run workspace: the four matrices, then r [K], c [K]
+constexpr int64_t kTabFloats = 4LL * K * K + 2LL * K;
+
+// Byte offset of element (r, k) of an R x 64 tf32 matrix in the 128-byte swizzled K-major layout:
+// two 32-element-wide atoms along k, R x 128 B each; row r at r * 128 B (8-row groups 1024 B
+// apart); the 16-byte chunk k / 4 of a row XOR row % 8.
+__host__ __device__ __forceinline__ uint32_t sw128(int r, int k, int R) {
+  const int atom = k >> 5, kk = k & 31;
+  return (uint32_t)(atom * (R * 128) + r * 128 + ((((kk >> 2) ^ r) & 7) << 4) + ((kk & 3) << 2));
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address >> 4 (bits 0-13), leading byte offset
+// (bits 16-29; unused by swizzled K-major layouts), stride byte offset >> 4 (bits 32-45: 1024 B
+// between 8-row groups), version 1 (bits 46-47), layout 128-byte swizzle (bits 61-63 = 2).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Descriptor of k-step ks (elements 8 ks .. 8 ks + 7) of an R-row matrix at `base`.
+__device__ __forceinline__ uint64_t kstep_desc(uint32_t base, int ks, int R) {
+  return sdesc(base + (uint32_t)((ks >> 2) * (R * 128) + (ks & 3) * 32));
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 16 consecutive fp32 columns of the warp's 32 TMEM lanes (thread = lane).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void bar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Bounded wait for the phase of `bar` with parity `parity`: false when the flag `abort` is set or
+// the limit passes (then this wait sets the flag).
+__device__ __forceinline__ bool wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns,
+                                     volatile int* abort) {
+  const uint32_t addr = smem_addr(bar);
+  uint64_t t0 = 0;
+  for (uint32_t i = 0;; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 15) == 0) {
+      if (*abort) return false;
+      uint64_t now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      if (t0 == 0) {
+        t0 = now;
+      } else if (now - t0 > limit_ns) {
+        *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ float warp_max(float x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = maxn(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+// Run-time tables of one group for this path: E hi, E lo (rows i, k = j), E' hi, E' lo (rows j,
+// k = i) in the swizzled layout above, then the row maxima r [K] and the column maxima c [K].
+__global__ void __launch_bounds__(256) tables_kernel(const int32_t* __restrict__ grp_table,
+                                                     const float* __restrict__ lpc, float t,
+                                                     float* __restrict__ tables) {
+  const int g = blockIdx.x;
+  const float* psi = lpc + grp_table[g];
+  float* out = tables + (int64_t)g * kTabFloats;
+  char* mats = reinterpret_cast<char*>(out);
+  float* rmax = out + 4 * K * K;
+  float* cmax = rmax + K;
+  __shared__ float rs[K], cs[K];
+  for (int i = threadIdx.x; i < K; i += blockDim.x) {
+    float m = -INFINITY, n = -INFINITY;
+    for (int j = 0; j < K; ++j) {
+      m = maxn(m, psi[i * K + j]);
+      n = maxn(n, psi[j * K + i]);
+    }
+    rs[i] = m;
+    cs[i] = n;
+    rmax[i] = m;
+    cmax[i] = n;
+  }
+  __syncthreads();
+  for (int x = threadIdx.x; x < K * K; x += blockDim.x) {
+    const int i = x / K, j = x % K;
+    uint32_t h, l;
+    split_tf32(expf(div_t(psi[x] - rs[i], t)), h, l);
+    *reinterpret_cast<uint32_t*>(mats + 0 * kMatBytes + sw128(i, j, K)) = h;
+    *reinterpret_cast<uint32_t*>(mats + 1 * kMatBytes + sw128(i, j, K)) = l;
+    split_tf32(expf(div_t(psi[x] - cs[j], t)), h, l);
+    *reinterpret_cast<uint32_t*>(mats + 2 * kMatBytes + sw128(j, i, K)) = h;
+    *reinterpret_cast<uint32_t*>(mats + 3 * kMatBytes + sw128(j, i, K)) = l;
+  }
+}
+
+// Tile `tile` of the CTA's walk: its group (cursor g, first tile t0 of g).
+struct TileCursor {
+  int g = 0;
+  int64_t t0 = 0;
+  __device__ void seek(const ExpArgs& a, int64_t tile) {
+    while (g < a.n_groups) {
+      const int64_t nt = ((int64_t)a.grp_count[g] + kM - 1) / kM;
+      if (tile < t0 + nt) break;
+      t0 += nt;
+      ++g;
+    }
+  }
+};
+
+__global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const float* tc_tables) {
+  extern __shared__ unsigned char dyn[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(dyn) + 1023) & ~static_cast<uintptr_t>(1023));
+  const uint32_t s_base = smem_addr(sm);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kOffBar);
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + kOffMisc);
+  volatile int* s_abort = reinterpret_cast<volatile int*>(sm + kOffMisc + 4);
+  unsigned* s_res = reinterpret_cast<unsigned*>(sm + kOffMisc + 8);
+  volatile int* s_drain = reinterpret_cast<volatile int*>(sm + kOffMisc + 12);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned long long lim = a.wait_ns;
+
+  const int64_t t_begin = (int64_t)blockIdx.x * a.tiles_per_cta;
+  const int64_t t_end =
+      t_begin + a.tiles_per_cta < a.n_tiles ? t_begin + a.tiles_per_cta : a.n_tiles;
+  const int64_t n_units = 2 * (t_end - t_begin);
+
+  if (threadIdx.x == 0) {
+    bar_init(&bars[kBarTab], 1);
+    bar_init(&bars[kBarAFull], 32 * kProdWarps);
+    bar_init(&bars[kBarMma0], 1);
+    bar_init(&bars[kBarMma1], 1);
+    bar_init(&bars[kBarTmem0], 128);
+    bar_init(&bars[kBarTmem1], 128);
+    bar_init(&bars[kBarStgFull0], 32 * kProdWarps);
+    bar_init(&bars[kBarStgFull1], 32 * kProdWarps);
+    bar_init(&bars[kBarStgFree0], 128);
+    bar_init(&bars[kBarStgFree1], 128);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *s_abort = 0;
+    *s_res = 0u;
+    *s_drain = 0;
+  }
+  if (warp == kMmaWarp) {  // the whole warp allocates (and later frees) the TMEM columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(s_tmem)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    fence_before_sync();
+  }
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *s_tmem;
+  const float* tab_g0 = tc_tables;  // group g's block: tc_tables + g * kTabFloats
+
+  if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
+    // ------------------------------------------------------------------ producers
+    // warp p owns columns p, p + 7, ... (< 128) of every tile; a lane keeps the six loads of
+    // kBatch columns in flight while it computes the previous batch, and a unit's first loads
+    // are issued before the wait for the operand buffer to be free
+    const int p = warp - kEpiWarps;
+    TileCursor cur;
+    for (int64_t u = 0; u < n_units; ++u) {
+      const int64_t tile = t_begin + (u >> 1);
+      const int d = (int)(u & 1), s = (int)(u & 1);
+      cur.seek(a, tile);
+      const int g = cur.g;
+      const int64_t c0 = (tile - cur.t0) * kM;
+      const int64_t left = (int64_t)a.grp_count[g] - c0;
+      const int ncols = (int)(left < kM ? left : kM);
+      const int64_t first = a.grp_first[g] + c0;
+      // lane j (< 19) holds the record of the warp's column j
+      int4 myq = make_int4(0, 0, 0, 0);
+      if (lane < kColsPerProd && p + kProdWarps * lane < ncols)
+        myq = a.rec[first + p + kProdWarps * lane];
+      float va[kBatch][6], vb[kBatch][6];
+      int own_a[kBatch], own_b[kBatch];
+      // the loads of batch b: per column the other edge's message, the other variable's sums and
+      // this edge's message, states lane and lane + 32
+      auto issue = [&](int b, float (&v)[kBatch][6], int (&own)[kBatch]) {
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+          const int j = b * kBatch + i;
+          const int col = p + kProdWarps * j;
+          const int qy = __shfl_sync(0xffffffffu, myq.y, j);
+          const int qz = __shfl_sync(0xffffffffu, myq.z, j);
+          const int qw = __shfl_sync(0xffffffffu, myq.w, j);
+          const int other = qy + (d == 0 ? K : 0), var = d == 0 ? qw : qz;
+          own[i] = qy + (d == 0 ? 0 : K);
+          if (col < ncols) {
+            v[i][0] = a.cur[other + lane];
+            v[i][1] = a.cur[other + lane + 32];
+            v[i][2] = a.vsum[var + lane];
+            v[i][3] = a.vsum[var + lane + 32];
+            v[i][4] = a.cur[own[i] + lane];
+            v[i][5] = a.cur[own[i] + lane + 32];
+          }
+        }
+      };
+      float* stg = reinterpret_cast<float*>(sm + kOffStg + s * kStgBytes);
+      float* stg_m = reinterpret_cast<float*>(sm + kOffM) + s * kM;
+      int* stg_own = reinterpret_cast<int*>(sm + kOffOwn) + s * kM;
+      // u (or w) and the staging of batch b
+      auto compute = [&](int b, const float (&v)[kBatch][6], const int (&own)[kBatch]) {
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+          const int c = p + kProdWarps * (b * kBatch + i);
+          if (c >= kM) continue;
+          uint32_t h0 = 0, l0 = 0, h1 = 0, l1 = 0;
+          if (c < ncols) {
+            const float t0 = v[i][2] - v[i][0], t1 = v[i][3] - v[i][1];
+            const float m = warp_max(maxn(t0, t1));
+            split_tf32(__expf(div_t(t0 - m, a.t)), h0, l0);
+            split_tf32(__expf(div_t(t1 - m, a.t)), h1, l1);
+            stg[c * kStg + lane] = v[i][4];
+            stg[c * kStg + lane + 32] = v[i][5];
+            if (lane == 0) {
+              stg_m[c] = m;
+              stg_own[c] = own[i];
+            }
+          }
+          *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane, kM)) = h0;
+          *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane + 32, kM)) = h1;
+          *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane, kM)) = l0;
+          *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane + 32, kM)) = l1;
+        }
+      };
+      static_assert(kBatches == 5, "the batch sequence below");
+      issue(0, va, own_a);
+      // a warp leaves together (its shuffles need every lane)
+      bool ok = u < 1 || wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1), lim,
+                              s_abort);
+      ok = ok && (u < 2 || wait(&bars[kBarStgFree0 + s], (uint32_t)(((u - 2) >> 1) & 1), lim,
+                                s_abort));
+      if (!__all_sync(0xffffffffu, ok)) break;
+      if (p == 0) {  // this direction's table maxima: r (to variable 1) or c (to variable 2)
+        float* stg_r = reinterpret_cast<float*>(sm + kOffR) + s * K;
+        const float* mx = tab_g0 + (int64_t)g * kTabFloats + 4 * K * K + d * K;
+        stg_r[lane] = mx[lane];
+        stg_r[lane + 32] = mx[lane + 32];
+      }
+      issue(1, vb, own_b);
+      compute(0, va, own_a);
+      issue(2, va, own_a);
+      compute(1, vb, own_b);
+      issue(3, vb, own_b);
+      compute(2, va, own_a);
+      issue(4, va, own_a);
+      compute(3, vb, own_b);
+      compute(4, va, own_a);
+      // the operand's generic-proxy writes become visible to the tensor cores' async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bar_arrive(&bars[kBarAFull]);
+      bar_arrive(&bars[kBarStgFull0 + s]);
+    }
+  } else if (warp == kMmaWarp) {
+    // ------------------------------------------------------------------ MMA issue
+    if (lane == 0) {
+      TileCursor cur;
+      int loaded = -1;
+      uint32_t tab_phase = 0;
+      int64_t last_commit[2] = {-1, -1};
+      for (int64_t u = 0; u < n_units; ++u) {
+        const int64_t tile = t_begin + (u >> 1);
+        const int d = (int)(u & 1), s = (int)(u & 1);
+        cur.seek(a, tile);
+        if (cur.g != loaded) {
+          // the old tables' last reader is the previous unit's products
+          if (u >= 1 && !wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1),
+                              lim, s_abort))
+            break;
+          bulk_load(sm, tab_g0 + (int64_t)cur.g * kTabFloats, (uint32_t)kTabBytes, &bars[kBarTab],
+                    a.skip_copy != 0);
+          if (!wait(&bars[kBarTab], tab_phase, lim, s_abort)) break;
+          tab_phase ^= 1u;
+          loaded = cur.g;
+        }
+        if (!wait(&bars[kBarAFull], (uint32_t)(u & 1), lim, s_abort)) break;
+        if (u >= 2 && !wait(&bars[kBarTmem0 + s], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort))
+          break;
+        fence_after_sync();
+        const uint32_t d_tmem = tmem + (uint32_t)(s * K);
+        const uint32_t b_hi = s_base + (uint32_t)((2 * d) * kMatBytes);
+        const uint32_t b_lo = b_hi + (uint32_t)kMatBytes;
+        const uint32_t a_hi = s_base + kOffAhi, a_lo = s_base + kOffAlo;
+#pragma unroll
+        for (int ks = 0; ks < K / 8; ++ks) {
+          const uint64_t ah = kstep_desc(a_hi, ks, kM), al = kstep_desc(a_lo, ks, kM);
+          const uint64_t bh = kstep_desc(b_hi, ks, K), bl = kstep_desc(b_lo, ks, K);
+          mma_tf32(d_tmem, ah, bh, ks > 0 ? 1u : 0u);
+          mma_tf32(d_tmem, ah, bl, 1u);
+          mma_tf32(d_tmem, al, bh, 1u);
+        }
+        mma_commit(&bars[kBarMma0 + s]);
+        last_commit[s] = u;
+      }
+      if (*s_abort) {
+        // products committed but never waited for by the epilogue may still be running: wait
+        // (bounded, apart from the abort flag) for the last commit of each accumulator stage
+        // before the columns are freed
+        for (int st = 0; st < 2; ++st)
+          if (last_commit[st] >= 0)
+            wait(&bars[kBarMma0 + st], (uint32_t)((last_commit[st] >> 1) & 1), lim, s_drain);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------------ epilogue
+    // group eg (warps 4 eg .. 4 eg + 3) takes the units of accumulator stage eg, i.e. direction
+    // eg; thread e of the group is TMEM lane e = column e of the tile
+    const int eg = warp >> 2, wq = warp & 3;
+    const int e = threadIdx.x & 127;
+    const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
+    TileCursor cur;
+    unsigned res = 0u;
+    for (int64_t u = eg; u < n_units; u += 2) {
+      const int64_t tile = t_begin + (u >> 1);
+      const int d = eg, s = eg;
+      cur.seek(a, tile);
+      const int g = cur.g;
+      const int64_t c0 = (tile - cur.t0) * kM;
+      const int64_t left = (int64_t)a.grp_count[g] - c0;
+      const int ncols = (int)(left < kM ? left : kM);
+      const uint32_t ph = (uint32_t)((u >> 1) & 1);
+      // a warp leaves together (tcgen05.ld is a warp-wide instruction)
+      bool ok = wait(&bars[kBarStgFull0 + s], ph, lim, s_abort);
+      ok = ok && wait(&bars[kBarMma0 + s], ph, lim, s_abort);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      fence_after_sync();
+      float* stg = reinterpret_cast<float*>(sm + kOffStg + s * kStgBytes);
+      const float mo = reinterpret_cast<float*>(sm + kOffM)[s * kM + e];
+      const float* rr = reinterpret_cast<float*>(sm + kOffR) + s * K;
+      const bool active = e < ncols;
+      float y[K];
+      float x = -INFINITY;
+#pragma unroll
+      for (int c4 = 0; c4 < K / 16; ++c4) {
+        float acc[16];
+        tmem_ld16(tmem + lane_base + (uint32_t)(s * K + 16 * c4), acc);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int st = 16 * c4 + j;
+          const float o = stg[e * kStg + st];
+          float f = 0.0f;
+          if (active) {
+            // sums >= 1e-30: the fast logarithm's absolute error is about 4e-7
+            f = acc[j] >= 1e-30f
+                    ? (a.t * __logf(acc[j]) + mo) + rr[st]
+                    : direct_message<K>(a, a.rec[a.grp_first[g] + c0 + e], 0, st, d == 0,
+                                        a.grp_table[g]);
+          }
+          y[st] = a.d * o + a.omd * f;
+          x = maxn(x, y[st]);
+        }
+      }
+      fence_before_sync();
+      bar_arrive(&bars[kBarTmem0 + s]);
+      float dmax = 0.0f;
+      if (active) {
+#pragma unroll
+        for (int st = 0; st < K; ++st) {
+          const float nv = maxn(y[st] - x, kMsgNegInf);
+          dmax = maxn(dmax, fabsf(nv - stg[e * kStg + st]));
+          stg[e * kStg + st] = nv;
+        }
+      }
+      __syncwarp();
+      const int* stg_own = reinterpret_cast<int*>(sm + kOffOwn) + s * kM;
+      for (int r = 0; r < 32; ++r) {
+        const int col = 32 * wq + r;
+        if (col < ncols) {
+          const int own = stg_own[col];
+          a.nxt[own + lane] = stg[col * kStg + lane];
+          a.nxt[own + lane + 32] = stg[col * kStg + lane + 32];
+        }
+      }
+      __syncwarp();
+      bar_arrive(&bars[kBarStgFree0 + s]);
+      res = __float_as_uint(maxn(__uint_as_float(res), dmax));
+    }
+    res = __float_as_uint(warp_max(__uint_as_float(res)));
+    if (lane == 0 && res != 0u) atomicMax(s_res, res);
+  }
+
+  // ---------------------------------------------------------------- teardown
+  fence_before_sync();
+  __syncthreads();
+  if (warp == kMmaWarp) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+  if (threadIdx.x == 0) {
+    if (*s_abort) {
+      atomicAdd(&g_wait_timeouts, 1ull);
+      if (a.fault != nullptr) {
+        *reinterpret_cast<volatile unsigned*>(a.fault) = 1u;
+        __threadfence_system();
+      }
+    } else if (a.dacc != nullptr && *s_res != 0u) {
+      atomicMax(a.dacc, *s_res);
+    }
+  }
+}
+
+}  // namespace tc
+
+// One iteration of a K = 64 bucket at B = 1 on the tcgen05 path: one CTA per SM, each over a
+// contiguous range of 128-column tiles.
+cudaError_t launch_tc(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const ExpArgs& base,
+                      const float* tc_tables) {
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      tc::pairwise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmemBytes);
+  if (attr != cudaSuccess) return attr;
+  ExpArgs a = base;
+  int64_t tiles = 0;
+  for (int64_t c : q.grp_count_host) tiles += (c + tc::kM - 1) / tc::kM;
+  if (tiles == 0) return cudaSuccess;
+  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)p.sm_count));
+  a.n_tiles = tiles;
+  a.tiles_per_cta = (tiles + ctas - 1) / ctas;
+  const int64_t grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
+  tc::pairwise_kernel<<<(unsigned)grid, tc::kThreads, tc::kSmemBytes, s>>>(a, tc_tables);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 bool expgemm_eligible(const PairwiseBucket& q) { return q.n_groups > 0; }
@@ -554,15 +1094,22 @@ cudaError_t read_wait_timeouts(unsigned long long* count) {
   return e;
 }
 
+int64_t expgemm_tc_table_floats(int K) { return K == tc::K ? tc::kTabFloats : 0; }
+
 cudaError_t expgemm_prepare(const Plan& p, const PairwiseBucket& q, cudaStream_t s,
                             const float* lpc, float t, float* tables) {
   (void)p;
   if (q.n_groups == 0) return cudaSuccess;
-  ProfileScope ps(kProfPairwise, s);
+  ProfileScope ps(kProfLayout, s);
   switch (q.n1) {
     case 16: expgemm_tables_kernel<16><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables); break;
     case 32: expgemm_tables_kernel<32><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables); break;
-    case 64: expgemm_tables_kernel<64><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables); break;
+    case 64:
+      expgemm_tables_kernel<64><<<q.n_groups, kThreads, 0, s>>>(q.grp_table, lpc, t, tables);
+      // the tcgen05 path's tables follow the n_groups blocks of the layout above
+      tc::tables_kernel<<<q.n_groups, 256, 0, s>>>(
+          q.grp_table, lpc, t, tables + (int64_t)q.n_groups * expgemm_table_floats(64));
+      break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -571,7 +1118,6 @@ cudaError_t expgemm_prepare(const Plan& p, const PairwiseBucket& q, cudaStream_t
 cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t s, int64_t B,
                             const float* cur, float* nxt, const float* vsum, const float* lpc,
                             const float* tables, float d, float omd, float t, unsigned* dacc) {
-  ProfileScope ps(kProfPairwise, s);
   ExpArgs a{};
   a.rec = q.rec;
   a.grp_first = q.grp_first;
@@ -592,6 +1138,11 @@ cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t
   a.fault = p.fault_dev;
   a.wait_ns = knobs.wait_limit_ns != 0 ? knobs.wait_limit_ns : kWaitLimitNs;
   a.skip_copy = knobs.skip_table_copy;
+  if (q.n1 == 64 && B == 1 && !knobs.legacy_mma) {
+    ProfileScope ps(kProfPairwiseExp, s);
+    return launch_tc(p, q, s, a, tables + (int64_t)q.n_groups * expgemm_table_floats(64));
+  }
+  ProfileScope ps(kProfPairwise, s);
   switch (q.n1) {
     case 16: return launch<16>(p, q, s, a);
     case 32: return launch<32>(p, q, s, a);

@@ -46,6 +46,10 @@ struct PairwiseBucket {
 __host__ __device__
 #endif
 inline int64_t expgemm_table_floats(int K) { return 2LL * K * (K + 8) + 2LL * K; }
+// Floats of the tcgen05 path's tables of one group (K = 64 only, else 0): E and E' split into
+// tf32 high and low parts in the 128-byte swizzled layout of its shared memory, then the row
+// and column maxima. A K = 64 bucket keeps both layouts (n_groups blocks of each).
+int64_t expgemm_tc_table_floats(int K);
 
 // Every other EnumFactor: per factor its edge-state range, edges and config rows. Rows of config
 // k of factor f are row_begin[f] + k * n_vars[f] + i (i = variable), holding the edge state local to
@@ -222,7 +226,7 @@ cudaError_t prepare_small_graph(Plan& p);
 
 // Kernel-class timing (pgbp_profile_*): RAII bracket around one launch when profiling is on.
 enum ProfileClass { kProfVarsum = 0, kProfPairwise, kProfEnumGeneric, kProfOr, kProfAnd, kProfPool,
-                    kProfLayout, kProfReadout, kProfSmallGraph, kProfAdjoint };
+                    kProfLayout, kProfReadout, kProfSmallGraph, kProfAdjoint, kProfPairwiseExp };
 bool profiling_enabled();
 void profile_record(int cls, cudaStream_t s, bool start);
 struct ProfileScope {

@@ -521,38 +521,37 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_eslot, g_evs, g_rb, g_ncfg, g_nv, g_cfg,
         g_les;
     int max_es = 0;
+    std::vector<int32_t> esz, estart;  // per factor, reused
     for (size_t k = 0; k < facs.size(); ++k) {
       const int64_t f = facs[k];
       const int64_t fb = fac_es_begin[f], fe = fac_es_end[f];
-      // edges of the factor
-      std::vector<int32_t> esz;
-      for (int64_t i = fb; i < fe; ++i)
-        if (i == fb || ei[i] != ei[i - 1]) esz.push_back(0), esz.back() = 0;
-      {
-        size_t j = 0;
-        for (int64_t i = fb; i < fe; ++i) {
-          if (i > fb && ei[i] != ei[i - 1]) ++j;
-          esz[j]++;
-        }
-      }
+      // edges of the factor: a factor starts at an edge boundary and holds whole edges
+      esz.clear();
+      for (int64_t i = fb; i < fe; i = edge_start[ei[i] + 1])
+        esz.push_back(edge_start[ei[i] + 1] - (int32_t)i);
       const int nv = (int)esz.size();
-      std::vector<int32_t> estart(nv + 1, 0);
+      estart.assign(nv + 1, 0);
       for (int j = 0; j < nv; ++j) estart[j + 1] = estart[j] + esz[j];
       int64_t nc = 0, cfg0 = 0;
       std::vector<int32_t> les;
+      // implied rows of a pairwise factor of at most 64 x 64 states are the dense row-major
+      // table: such a factor goes to its bucket without its rows being spelled out
+      const bool implicit_dense = implicit && nv == 2 && esz[0] <= 64 && esz[1] <= 64;
       if (implicit) {
         if (nv > 2)
           return bail(fail(PGBP_ERR_UNSUPPORTED, "implicit enum rows need unary or pairwise factors"));
         nc = nv == 1 ? esz[0] : (int64_t)esz[0] * esz[1];
         cfg0 = implicit_cfg;
         implicit_cfg += nc;
-        les.resize((size_t)(nc * nv));
-        for (int64_t c = 0; c < nc; ++c) {
-          if (nv == 1) {
-            les[(size_t)c] = (int32_t)c;
-          } else {
-            les[(size_t)(2 * c)] = (int32_t)(c / esz[1]);
-            les[(size_t)(2 * c + 1)] = (int32_t)(esz[0] + c % esz[1]);
+        if (!implicit_dense) {
+          les.resize((size_t)(nc * nv));
+          for (int64_t c = 0; c < nc; ++c) {
+            if (nv == 1) {
+              les[(size_t)c] = (int32_t)c;
+            } else {
+              les[(size_t)(2 * c)] = (int32_t)(c / esz[1]);
+              les[(size_t)(2 * c + 1)] = (int32_t)(esz[0] + c % esz[1]);
+            }
           }
         }
       }
@@ -585,7 +584,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         pot_first = pot0 + alias[k];
       }
       bool dense = nv == 2 && nc == (int64_t)esz[0] * esz[1] && esz[0] <= 64 && esz[1] <= 64;
-      for (int64_t c = 0; dense && c < nc; ++c) {
+      for (int64_t c = 0; dense && !implicit_dense && c < nc; ++c) {
         if (les[(size_t)(2 * c)] != c / esz[1] || les[(size_t)(2 * c + 1)] != esz[0] + c % esz[1])
           dense = false;
       }
@@ -653,7 +652,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         q.grp_count = bd.upload(gc);
         q.grp_table = bd.upload(gt);
         q.grp_count_host.assign(gc.begin(), gc.end());
-        q.gemm_floats = (int64_t)q.n_groups * pgbp::expgemm_table_floats(q.n1);
+        q.gemm_floats = (int64_t)q.n_groups * (pgbp::expgemm_table_floats(q.n1) +
+                                                pgbp::expgemm_tc_table_floats(q.n1));
       }
       q.rec = bd.upload(kv.second.first);
       q.cfg_begin = bd.upload(kv.second.second);

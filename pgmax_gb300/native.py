@@ -117,12 +117,13 @@ FLAG_PATH_MULTI = 8
 FLAG_ENUM_IMPLICIT_ROWS = 16
 
 
-class Profile(ctypes.Structure):
-  _fields_ = [("launches", _i64 * 10), ("milliseconds", ctypes.c_double * 10)]
-
-
 PROFILE_CLASSES = ("varsum", "pairwise", "enum_generic", "or", "and", "pool", "layout", "readout",
-                   "small_graph", "adjoint")
+                   "small_graph", "adjoint", "pairwise_exp")
+
+
+class Profile(ctypes.Structure):
+  _fields_ = [("launches", _i64 * len(PROFILE_CLASSES)),
+              ("milliseconds", ctypes.c_double * len(PROFILE_CLASSES))]
 
 # (name, restype, argtypes) of every symbol include/pgbp.h declares
 SIGNATURES = [

@@ -223,3 +223,57 @@ def test_table_wait_that_runs_out_is_an_error_and_the_plan_recovers():
   wp = batch.grid_wiring(L, K)
   want = oracle.run(oracle.Wiring(wp), np.tile(table, wp["num_factors"]), ev, m, 10, 0.5, 1.0)[0]
   np.testing.assert_allclose(out.cpu().numpy(), want, atol=ATOL, rtol=0)
+
+
+@pytest.mark.parametrize("temperature", [1.0, 0.7, 0.3])
+def test_tcgen05_path_for_shared_64x64_tables(temperature):
+  """Shared 64 x 64 tables of a single instance run the tcgen05 kernel (products on the
+  fifth-generation tensor cores, accumulators in tensor memory, warp-specialised pipeline). A
+  union of grids whose groups end in partial 128-column tiles, with more tiles than SMs so that
+  CTAs walk several tiles and change groups inside their range, must match every graph's oracle
+  run within 1e-5 and the warp-level mma.sync kernel (the debug setting) within 1e-5."""
+  from pgmax_gb300 import native  # pylint: disable=g-import-not-at-top
+  specs = [(5, 64), (90, 64), (3, 64), (23, 64), (2, 64), (12, 64)]
+  ws = [batch.grid_wiring(L, K, shared_table=True, implicit_rows=True) for L, K in specs]
+  gb = batch.GraphBatch(ws, flags=1)
+  rng = np.random.default_rng(int(temperature * 10) + 40)
+  tables = [rng.normal(0.0, 0.5, size=K * K).astype(np.float32) for _, K in specs]
+  evs = [rng.normal(size=L * L * K).astype(np.float32) for L, K in specs]
+  m0 = np.zeros(gb.layout.perm.shape[0], np.float32)
+  iters = 12
+  out, d_tc = gb.run(gb.concat(tables), gb.concat(evs), m0, iters, 0.5, temperature)
+  got = out.cpu().numpy()
+  native.debug_set(native.DEBUG_LEGACY_MMA, 1)
+  try:
+    out_mma, d_mma = gb.run(gb.concat(tables), gb.concat(evs), m0, iters, 0.5, temperature)
+  finally:
+    native.debug_set(native.DEBUG_LEGACY_MMA, 0)
+  np.testing.assert_allclose(got, out_mma.cpu().numpy(), atol=ATOL, rtol=0)
+  np.testing.assert_allclose(d_tc.cpu().numpy(), d_mma.cpu().numpy(), atol=ATOL, rtol=0)
+  parts = gb.layout.split(gb.layout.union_to_graph_major(got), "msgs")
+  for (L, K), t, e, part in zip(specs, tables, evs, parts):
+    wp = batch.grid_wiring(L, K)
+    want = oracle.run(oracle.Wiring(wp), np.tile(t, wp["num_factors"]), e,
+                      np.zeros(wp["var_states_for_edge_states"].shape, np.float32), iters, 0.5,
+                      temperature)[0]
+    np.testing.assert_allclose(part, want, atol=ATOL, rtol=0, err_msg=f"L={L}")
+  assert native.wait_timeouts() == 0
+
+
+def test_tcgen05_path_underflow_falls_back_to_the_direct_formula():
+  """K = 64, one instance: where E u underflows the epilogue recomputes the message directly."""
+  L, K = 4, 64
+  rng = np.random.default_rng(12)
+  table = np.where(rng.random(K * K) < 0.5, -300.0, 0.0).astype(np.float32)
+  table[::K + 1] = -300.0
+  ev = np.full((L * L, K), -200.0, np.float32)
+  ev[np.arange(L * L), rng.integers(0, K, L * L)] = 0.0
+  w = batch.grid_wiring(L, K, shared_table=True, implicit_rows=True)
+  from pgmax_gb300 import engine  # pylint: disable=g-import-not-at-top
+  plan = engine.Plan(w, flags=1)
+  out, _ = plan.run(table, ev.reshape(-1), np.zeros(2 * K * w["num_factors"], np.float32), 10,
+                    0.5, 1.0)
+  wp = batch.grid_wiring(L, K)
+  want = oracle.run(oracle.Wiring(wp), np.tile(table, wp["num_factors"]), ev.reshape(-1),
+                    np.zeros(2 * K * w["num_factors"], np.float32), 10, 0.5, 1.0)[0]
+  np.testing.assert_allclose(out.cpu().numpy(), want, atol=1e-4, rtol=1e-6)
