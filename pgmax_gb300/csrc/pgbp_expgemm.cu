@@ -30,6 +30,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "pgbp_internal.h"
 
@@ -581,8 +582,6 @@ constexpr int kProdWarps = 7;            // warps 8-14
 constexpr int kMmaWarp = 15;
 constexpr int kThreads = 32 * 16;        // four warps per SM sub-partition: 128 registers each
 constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 19 columns per producer warp
-constexpr int kBatch = 4;                // columns whose loads a producer lane keeps in flight
-constexpr int kBatches = (kColsPerProd + kBatch - 1) / kBatch;   // 5
 constexpr int kStg = K + 1;              // staging row stride (floats): conflict-free both ways
 constexpr uint32_t kTmemCols = 128;      // two accumulator stages of 64 fp32 columns
 // instruction descriptor: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
@@ -680,9 +679,10 @@ __device__ __forceinline__ void bar_arrive(uint64_t* bar) {
 }
 
 // Bounded wait for the phase of `bar` with parity `parity`: false when the flag `abort` is set or
-// the limit passes (then this wait sets the flag).
+// the limit passes (then this wait sets the flag). A role that is rarely on the critical path
+// passes `sleep_ns` > 0 to sleep between polls, leaving the issue slots to the warps that work.
 __device__ __forceinline__ bool wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns,
-                                     volatile int* abort) {
+                                     volatile int* abort, unsigned sleep_ns = 0) {
   const uint32_t addr = smem_addr(bar);
   uint64_t t0 = 0;
   for (uint32_t i = 0;; ++i) {
@@ -694,6 +694,7 @@ __device__ __forceinline__ bool wait(uint64_t* bar, uint32_t parity, unsigned lo
         : "r"(addr), "r"(parity)
         : "memory");
     if (done) return true;
+    if (sleep_ns != 0) __nanosleep(sleep_ns);
     if ((i & 15) == 0) {
       if (*abort) return false;
       uint64_t now;
@@ -712,6 +713,13 @@ __device__ __forceinline__ float warp_max(float x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x = maxn(x, __shfl_xor_sync(0xffffffffu, x, o));
   return x;
+}
+
+// Maximum over the warp in one instruction, NaN-propagating like maxn.
+__device__ __forceinline__ float warp_max_redux(float x) {
+  float r;
+  asm volatile("redux.sync.max.NaN.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(x));
+  return r;
 }
 
 // Run-time tables of one group for this path: E hi, E lo (rows i, k = j), E' hi, E' lo (rows j,
@@ -748,6 +756,47 @@ __global__ void __launch_bounds__(256) tables_kernel(const int32_t* __restrict__
     *reinterpret_cast<uint32_t*>(mats + 2 * kMatBytes + sw128(j, i, K)) = h;
     *reinterpret_cast<uint32_t*>(mats + 3 * kMatBytes + sw128(j, i, K)) = l;
   }
+}
+
+// One fp32 column of the warp's 32 TMEM lanes (thread = lane).
+__device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
+  uint32_t r;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  return __uint_as_float(r);
+}
+
+// The epilogue of one column when some of its sums (E u) fell below 1e-30 in some lane of the
+// warp: those messages are recomputed with the reference's formula (direct_message). Kept out of
+// line so that the common path stays compact. Called by every lane of the warp (it reads TMEM
+// with warp-wide loads); `small` marks this lane's states to recompute, `row` is its staging row
+// (the old message in, the new one out). Returns the column's residual.
+__device__ __noinline__ float epilogue_slow(const ExpArgs& a, uint32_t taddr, float* row, float mo,
+                                            const float* rr, uint64_t small, bool active, int4 q,
+                                            int64_t table, bool first_edge) {
+  float y[K];
+  float x = -INFINITY;
+#pragma unroll 1
+  for (int st = 0; st < K; ++st) {
+    const float sum = tmem_ld1(taddr + (uint32_t)st);
+    float f = 0.0f;
+    if (active) {
+      f = (small >> st) & 1ull ? direct_message<K>(a, q, 0, st, first_edge, table)
+                               : (a.t * __logf(sum) + mo) + rr[st];
+    }
+    y[st] = a.d * row[st] + a.omd * f;
+    x = maxn(x, y[st]);
+  }
+  float dmax = 0.0f;
+  if (active) {
+#pragma unroll 1
+    for (int st = 0; st < K; ++st) {
+      const float nv = maxn(y[st] - x, kMsgNegInf);
+      dmax = maxn(dmax, fabsf(nv - row[st]));
+      row[st] = nv;
+    }
+  }
+  return dmax;
 }
 
 // Tile `tile` of the CTA's walk: its group (cursor g, first tile t0 of g).
@@ -813,99 +862,153 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
 
   if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
     // ------------------------------------------------------------------ producers
-    // warp p owns columns p, p + 7, ... (< 128) of every tile; a lane keeps the six loads of
-    // kBatch columns in flight while it computes the previous batch, and a unit's first loads
-    // are issued before the wait for the operand buffer to be free
+    // Warp p owns columns p + 7 j (j < 19, column < 128) of every tile, split into two halves
+    // (j < 10, j >= 10). A lane keeps the other edge's message and the other variable's sums of
+    // one half in registers (states lane and lane + 32) while it computes the other half, and the
+    // loads of the next unit's first half are issued before this unit's second half is computed,
+    // so the memory latency is hidden behind the arithmetic. This edge's old message goes straight
+    // to the staging row by cp.async, without passing through registers.
     const int p = warp - kEpiWarps;
+    constexpr int kHalf = 10;   // columns of the first half (the second has 9)
+    struct Unit {               // what a lane needs of a unit
+      int d, ncols, g, qy, qz, qw;  // qy/qz/qw: the record of the warp's column `lane` (< 19)
+    };
+    // the tile's group, width and records (loaded one tile ahead, while the tile before it runs)
     TileCursor cur;
-    for (int64_t u = 0; u < n_units; ++u) {
-      const int64_t tile = t_begin + (u >> 1);
-      const int d = (int)(u & 1), s = (int)(u & 1);
+    auto tile_info = [&](int64_t tile) {
+      Unit x;
       cur.seek(a, tile);
-      const int g = cur.g;
+      x.d = 0;
+      x.g = cur.g;
       const int64_t c0 = (tile - cur.t0) * kM;
-      const int64_t left = (int64_t)a.grp_count[g] - c0;
-      const int ncols = (int)(left < kM ? left : kM);
-      const int64_t first = a.grp_first[g] + c0;
-      // lane j (< 19) holds the record of the warp's column j
-      int4 myq = make_int4(0, 0, 0, 0);
-      if (lane < kColsPerProd && p + kProdWarps * lane < ncols)
-        myq = a.rec[first + p + kProdWarps * lane];
-      float va[kBatch][6], vb[kBatch][6];
-      int own_a[kBatch], own_b[kBatch];
-      // the loads of batch b: per column the other edge's message, the other variable's sums and
-      // this edge's message, states lane and lane + 32
-      auto issue = [&](int b, float (&v)[kBatch][6], int (&own)[kBatch]) {
+      const int64_t left = (int64_t)a.grp_count[x.g] - c0;
+      x.ncols = (int)(left < kM ? left : kM);
+      int4 q = make_int4(0, 0, 0, 0);
+      if (lane < kColsPerProd && p + kProdWarps * lane < x.ncols)
+        q = a.rec[a.grp_first[x.g] + c0 + p + kProdWarps * lane];
+      x.qy = q.y;
+      x.qz = q.z;
+      x.qw = q.w;
+      return x;
+    };
+    float ra[kHalf][4], rb[kColsPerProd - kHalf][4];
+    // register loads of columns j0 .. j0 + n - 1 of unit x: other message and other sums (zero
+    // for columns past the tile's end)
+    auto load = [&](const Unit& x, int j0, auto& r) {
+      constexpr int n = sizeof(r) / sizeof(r[0]);
 #pragma unroll
-        for (int i = 0; i < kBatch; ++i) {
-          const int j = b * kBatch + i;
-          const int col = p + kProdWarps * j;
-          const int qy = __shfl_sync(0xffffffffu, myq.y, j);
-          const int qz = __shfl_sync(0xffffffffu, myq.z, j);
-          const int qw = __shfl_sync(0xffffffffu, myq.w, j);
-          const int other = qy + (d == 0 ? K : 0), var = d == 0 ? qw : qz;
-          own[i] = qy + (d == 0 ? 0 : K);
-          if (col < ncols) {
-            v[i][0] = a.cur[other + lane];
-            v[i][1] = a.cur[other + lane + 32];
-            v[i][2] = a.vsum[var + lane];
-            v[i][3] = a.vsum[var + lane + 32];
-            v[i][4] = a.cur[own[i] + lane];
-            v[i][5] = a.cur[own[i] + lane + 32];
-          }
+      for (int i = 0; i < n; ++i) {
+        const int j = j0 + i;
+        const int qy = __shfl_sync(0xffffffffu, x.qy, j);
+        const int qv = __shfl_sync(0xffffffffu, x.d == 0 ? x.qw : x.qz, j);
+        const bool act = p + kProdWarps * j < x.ncols;
+        const int other = qy + (x.d == 0 ? K : 0);
+        r[i][0] = act ? a.cur[other + lane] : 0.0f;
+        r[i][1] = act ? a.cur[other + lane + 32] : 0.0f;
+        r[i][2] = act ? a.vsum[qv + lane] : 0.0f;
+        r[i][3] = act ? a.vsum[qv + lane + 32] : 0.0f;
+      }
+    };
+    // (x - m) / T as div_t computes it, with the power-of-two test made once per kernel: the
+    // column bodies below are then branch-free, so the compiler interleaves them
+    const float t_inv = __uint_as_float((254u - ((__float_as_uint(a.t) >> 23) & 0xffu)) << 23);
+    const bool t_pow2 = [&] {
+      const unsigned ub = __float_as_uint(a.t), eb = (ub >> 23) & 0xffu;
+      return (ub & 0x807fffffu) == 0u && eb >= 2u && eb <= 252u;
+    }();
+    // u (or w) of columns j0 .. j0 + n - 1 into the operand; the maximum and slot to staging
+    auto compute = [&](auto pow2, const Unit& x, int j0, const auto& r, float* stg_m,
+                       int* stg_own) {
+      constexpr int n = sizeof(r) / sizeof(r[0]);
+#pragma unroll
+      for (int i = 0; i < n; ++i) {
+        const int j = j0 + i;
+        const int c = p + kProdWarps * j;
+        if (c >= kM) continue;
+        const int qy = __shfl_sync(0xffffffffu, x.qy, j);
+        const bool act = c < x.ncols;
+        const float t0 = r[i][2] - r[i][0], t1 = r[i][3] - r[i][1];
+        const float m = warp_max_redux(maxn(t0, t1));
+        float z0, z1;
+        if constexpr (decltype(pow2)::value) {
+          z0 = (t0 - m) * t_inv;
+          z1 = (t1 - m) * t_inv;
+        } else {
+          z0 = (t0 - m) / a.t;
+          z1 = (t1 - m) / a.t;
         }
-      };
+        uint32_t h0, l0, h1, l1;
+        split_tf32(__expf(z0), h0, l0);
+        split_tf32(__expf(z1), h1, l1);
+        if (!act) h0 = l0 = h1 = l1 = 0u;
+        if (lane == 0 && act) {
+          stg_m[c] = m;
+          stg_own[c] = qy + (x.d == 0 ? 0 : K);
+        }
+        *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane, kM)) = h0;
+        *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane + 32, kM)) = h1;
+        *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane, kM)) = l0;
+        *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane + 32, kM)) = l1;
+      }
+    };
+    Unit x = n_units > 0 ? tile_info(t_begin) : Unit{};   // the unit being produced
+    Unit next_tile = x;
+    if (n_units > 0) load(x, 0, ra);
+    for (int64_t u = 0; u < n_units; ++u) {
+      if ((u & 1) == 0 && u + 2 < n_units) next_tile = tile_info(t_begin + (u >> 1) + 1);
+      const int s = (int)(u & 1);
       float* stg = reinterpret_cast<float*>(sm + kOffStg + s * kStgBytes);
       float* stg_m = reinterpret_cast<float*>(sm + kOffM) + s * kM;
       int* stg_own = reinterpret_cast<int*>(sm + kOffOwn) + s * kM;
-      // u (or w) and the staging of batch b
-      auto compute = [&](int b, const float (&v)[kBatch][6], const int (&own)[kBatch]) {
-#pragma unroll
-        for (int i = 0; i < kBatch; ++i) {
-          const int c = p + kProdWarps * (b * kBatch + i);
-          if (c >= kM) continue;
-          uint32_t h0 = 0, l0 = 0, h1 = 0, l1 = 0;
-          if (c < ncols) {
-            const float t0 = v[i][2] - v[i][0], t1 = v[i][3] - v[i][1];
-            const float m = warp_max(maxn(t0, t1));
-            split_tf32(__expf(div_t(t0 - m, a.t)), h0, l0);
-            split_tf32(__expf(div_t(t1 - m, a.t)), h1, l1);
-            stg[c * kStg + lane] = v[i][4];
-            stg[c * kStg + lane + 32] = v[i][5];
-            if (lane == 0) {
-              stg_m[c] = m;
-              stg_own[c] = own[i];
-            }
-          }
-          *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane, kM)) = h0;
-          *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane + 32, kM)) = h1;
-          *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane, kM)) = l0;
-          *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane + 32, kM)) = l1;
-        }
-      };
-      static_assert(kBatches == 5, "the batch sequence below");
-      issue(0, va, own_a);
       // a warp leaves together (its shuffles need every lane)
-      bool ok = u < 1 || wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1), lim,
+      bool ok = u < 2 || wait(&bars[kBarStgFree0 + s], (uint32_t)(((u - 2) >> 1) & 1), lim,
                               s_abort);
-      ok = ok && (u < 2 || wait(&bars[kBarStgFree0 + s], (uint32_t)(((u - 2) >> 1) & 1), lim,
-                                s_abort));
       if (!__all_sync(0xffffffffu, ok)) break;
+      // this edge's old messages of every column of the warp into the staging rows
+#pragma unroll
+      for (int j = 0; j < kColsPerProd; ++j) {
+        const int c = p + kProdWarps * j;
+        const int qy = __shfl_sync(0xffffffffu, x.qy, j);
+        if (c < x.ncols) {
+          const float* src = a.cur + qy + (x.d == 0 ? 0 : K);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                           smem_addr(stg + c * kStg + lane)),
+                       "l"(src + lane)
+                       : "memory");
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                           smem_addr(stg + c * kStg + lane + 32)),
+                       "l"(src + lane + 32)
+                       : "memory");
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      load(x, kHalf, rb);
+      ok = u < 1 || wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1), lim,
+                         s_abort);
+      if (!__all_sync(0xffffffffu, ok)) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        break;
+      }
       if (p == 0) {  // this direction's table maxima: r (to variable 1) or c (to variable 2)
         float* stg_r = reinterpret_cast<float*>(sm + kOffR) + s * K;
-        const float* mx = tab_g0 + (int64_t)g * kTabFloats + 4 * K * K + d * K;
+        const float* mx = tab_g0 + (int64_t)x.g * kTabFloats + 4 * K * K + x.d * K;
         stg_r[lane] = mx[lane];
         stg_r[lane + 32] = mx[lane + 32];
       }
-      issue(1, vb, own_b);
-      compute(0, va, own_a);
-      issue(2, va, own_a);
-      compute(1, vb, own_b);
-      issue(3, vb, own_b);
-      compute(2, va, own_a);
-      issue(4, va, own_a);
-      compute(3, vb, own_b);
-      compute(4, va, own_a);
+      if (t_pow2) compute(std::true_type{}, x, 0, ra, stg_m, stg_own);
+      else compute(std::false_type{}, x, 0, ra, stg_m, stg_own);
+      const Unit cur_x = x;
+      if (u + 1 < n_units) {
+        if ((u & 1) == 0) {
+          x.d = 1;          // the other direction of the same tile
+        } else {
+          x = next_tile;    // the next tile, direction 0
+        }
+        load(x, 0, ra);
+      }
+      if (t_pow2) compute(std::true_type{}, cur_x, kHalf, rb, stg_m, stg_own);
+      else compute(std::false_type{}, cur_x, kHalf, rb, stg_m, stg_own);
+      asm volatile("cp.async.wait_all;" ::: "memory");
       // the operand's generic-proxy writes become visible to the tensor cores' async proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       bar_arrive(&bars[kBarAFull]);
@@ -981,8 +1084,8 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       const int ncols = (int)(left < kM ? left : kM);
       const uint32_t ph = (uint32_t)((u >> 1) & 1);
       // a warp leaves together (tcgen05.ld is a warp-wide instruction)
-      bool ok = wait(&bars[kBarStgFull0 + s], ph, lim, s_abort);
-      ok = ok && wait(&bars[kBarMma0 + s], ph, lim, s_abort);
+      bool ok = wait(&bars[kBarStgFull0 + s], ph, lim, s_abort, 256);
+      ok = ok && wait(&bars[kBarMma0 + s], ph, lim, s_abort, 256);
       if (!__all_sync(0xffffffffu, ok)) break;
       fence_after_sync();
       float* stg = reinterpret_cast<float*>(sm + kOffStg + s * kStgBytes);
@@ -991,6 +1094,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       const bool active = e < ncols;
       float y[K];
       float x = -INFINITY;
+      uint64_t small = 0;  // states whose sum fell below 1e-30
 #pragma unroll
       for (int c4 = 0; c4 < K / 16; ++c4) {
         float acc[16];
@@ -999,31 +1103,37 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         for (int j = 0; j < 16; ++j) {
           const int st = 16 * c4 + j;
           const float o = stg[e * kStg + st];
-          float f = 0.0f;
-          if (active) {
-            // sums >= 1e-30: the fast logarithm's absolute error is about 4e-7
-            f = acc[j] >= 1e-30f
-                    ? (a.t * __logf(acc[j]) + mo) + rr[st]
-                    : direct_message<K>(a, a.rec[a.grp_first[g] + c0 + e], 0, st, d == 0,
-                                        a.grp_table[g]);
-          }
+          // sums >= 1e-30: the fast logarithm's absolute error is about 4e-7
+          if (!(acc[j] >= 1e-30f)) small |= 1ull << st;
+          const float f = (a.t * __logf(acc[j]) + mo) + rr[st];
           y[st] = a.d * o + a.omd * f;
           x = maxn(x, y[st]);
         }
       }
-      fence_before_sync();
-      bar_arrive(&bars[kBarTmem0 + s]);
+      if (!active) small = 0;
+      const bool slow = __any_sync(0xffffffffu, small != 0);
       float dmax = 0.0f;
-      if (active) {
+      if (slow) {  // rare: a table row spanning more than about 69 T underflowed somewhere
+        const int4 q = active ? a.rec[a.grp_first[g] + c0 + e] : make_int4(0, 0, 0, 0);
+        dmax = epilogue_slow(a, tmem + lane_base + (uint32_t)(s * K), stg + e * kStg, mo, rr,
+                             small, active, q, a.grp_table[g], d == 0);
+        fence_before_sync();
+        bar_arrive(&bars[kBarTmem0 + s]);
+      } else {
+        fence_before_sync();
+        bar_arrive(&bars[kBarTmem0 + s]);
+        if (active) {
 #pragma unroll
-        for (int st = 0; st < K; ++st) {
-          const float nv = maxn(y[st] - x, kMsgNegInf);
-          dmax = maxn(dmax, fabsf(nv - stg[e * kStg + st]));
-          stg[e * kStg + st] = nv;
+          for (int st = 0; st < K; ++st) {
+            const float nv = maxn(y[st] - x, kMsgNegInf);
+            dmax = maxn(dmax, fabsf(nv - stg[e * kStg + st]));
+            stg[e * kStg + st] = nv;
+          }
         }
       }
       __syncwarp();
       const int* stg_own = reinterpret_cast<int*>(sm + kOffOwn) + s * kM;
+#pragma unroll 8
       for (int r = 0; r < 32; ++r) {
         const int col = 32 * wq + r;
         if (col < ncols) {
