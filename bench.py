@@ -44,6 +44,7 @@ NUM_EDGES = 2 * NH * NV + NH + NV
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "pairwise_kernel_rbm_b128.md")
 ENERGY_TRAFFIC_FILE = os.path.join(ROOT, "profiles", "energy_pairwise_rbm_b128.md")
+TC_TRAFFIC_FILE = os.path.join(ROOT, "profiles", "tc_pairwise_k64_multigraph64.md")
 
 
 def rbm_params(seed=0):
@@ -787,7 +788,11 @@ def run_multigraph(args):
                              "accumulators)",
                    "achieved": k64_gbs, "peak": peak, "unit": "GB/s",
                    "frac": k64_gbs / peak if k64_gbs else None,
-                   "peak_source": src, "traffic": None,
+                   "peak_source": src,
+                   "traffic": (lambda r: r * k64_bytes if r else None)(
+                       read_traffic(TC_TRAFFIC_FILE, "traffic_per_algorithmic_byte:")),
+                   "traffic_note": "ncu DRAM bytes per algorithmic byte of a 64-graph launch "
+                                   "(profiles/tc_pairwise_k64_multigraph64.md) x this launch's",
                    "algorithmic_bytes_per_launch": k64_bytes, "launch_ms": k64_launch_ms,
                    "factors": f64},
       "iteration_roofline": {"bytes_per_iter": bytes_iter,

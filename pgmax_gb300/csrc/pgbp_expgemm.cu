@@ -577,8 +577,9 @@ namespace tc {
 
 constexpr int K = 64;
 constexpr int kM = 128;                  // columns per tile (the MMA's M)
-constexpr int kEpiWarps = 8;             // warps 0-3: stage 0 (d = 0), warps 4-7: stage 1 (d = 1)
-constexpr int kProdWarps = 7;            // warps 8-14
+constexpr int kEpiGroups = 1;            // epilogue groups of 4 warps; group g takes units u = g mod it
+constexpr int kEpiWarps = 4 * kEpiGroups;
+constexpr int kProdWarps = 15 - kEpiWarps;  // the warps after the epilogue's
 constexpr int kMmaWarp = 15;
 constexpr int kThreads = 32 * 16;        // four warps per SM sub-partition: 128 registers each
 constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 19 columns per producer warp
@@ -869,7 +870,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     // so the memory latency is hidden behind the arithmetic. This edge's old message goes straight
     // to the staging row by cp.async, without passing through registers.
     const int p = warp - kEpiWarps;
-    constexpr int kHalf = 10;   // columns of the first half (the second has 9)
+    constexpr int kHalf = (kColsPerProd + 1) / 2;   // columns of the first half
     struct Unit {               // what a lane needs of a unit
       int d, ncols, g, qy, qz, qw;  // qy/qz/qw: the record of the warp's column `lane` (< 19)
     };
@@ -1067,16 +1068,16 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     __syncwarp();
   } else {
     // ------------------------------------------------------------------ epilogue
-    // group eg (warps 4 eg .. 4 eg + 3) takes the units of accumulator stage eg, i.e. direction
-    // eg; thread e of the group is TMEM lane e = column e of the tile
-    const int eg = warp >> 2, wq = warp & 3;
+    // group eg (warps 4 eg .. 4 eg + 3) takes the units u = eg mod kEpiGroups; thread e of the
+    // group is TMEM lane e = column e of the tile
+    const int eg = kEpiGroups == 1 ? 0 : warp >> 2, wq = warp & 3;
     const int e = threadIdx.x & 127;
     const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
     TileCursor cur;
     unsigned res = 0u;
-    for (int64_t u = eg; u < n_units; u += 2) {
+    for (int64_t u = eg; u < n_units; u += kEpiGroups) {
       const int64_t tile = t_begin + (u >> 1);
-      const int d = eg, s = eg;
+      const int d = (int)(u & 1), s = (int)(u & 1);
       cur.seek(a, tile);
       const int g = cur.g;
       const int64_t c0 = (tile - cur.t0) * kM;
