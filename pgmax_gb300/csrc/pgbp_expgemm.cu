@@ -48,6 +48,12 @@ __device__ __forceinline__ float maxn(float a, float b) {
   return r;
 }
 
+__device__ __forceinline__ float minn(float a, float b) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+
 // x / t; a power-of-two t multiplies by its exact reciprocal (the same correctly rounded value).
 __device__ __forceinline__ float div_t(float x, float t) {
   const unsigned u = __float_as_uint(t);
@@ -549,41 +555,46 @@ cudaError_t launch(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const
 // the products on the fifth-generation tensor cores: tcgen05.mma kind::tf32, A and B operands in
 // shared memory (128-byte swizzled, K-major), accumulators in tensor memory (TMEM), and the work
 // of a tile split over specialised warps so that loads, the products and the epilogue of
-// consecutive units overlap:
-//   unit u = (tile of up to 128 columns = consecutive factors of one group, direction d = u & 1):
-//     d = 0: the messages to variable 1, D[c][i] = sum_j U[c][j] E[i][j], U from variable 2;
-//     d = 1: the messages to variable 2, D[c][j] = sum_i W[c][i] E'[j][i], W from variable 1.
+// consecutive units overlap.
+//   The CTAs come in pairs over the same range of tiles (a tile = up to 128 consecutive factors
+//   of one group); CTA 2 r computes the messages to variable 1 of range r, CTA 2 r + 1 those to
+//   variable 2, so a CTA holds one direction's tables and the two CTAs of a pair read each
+//   message row at about the same time (one DRAM read, one L2 hit). Unit u of a CTA = its tile u:
+//     direction 0: D[c][i] = sum_j U[c][j] E[i][j], U from variable 2 (the messages to 1);
+//     direction 1: D[c][j] = sum_i W[c][i] E'[j][i], W from variable 1 (the messages to 2).
 //   M = 128 columns, N = 64 states, K = 64 states in 8 steps of 8; three products per step
 //   (hi x hi, hi x lo, lo x hi of the tf32 splits), float32 accumulation in TMEM.
-//   * producer warps 8-14: per column, lanes across states (coalesced loads of the other edge's
-//     message and variable sum, and of this edge's message; the loads of the next columns are in
-//     flight while a column is computed): vtof, its maximum (warp reduction), u = exp((vtof -
-//     max) / T) split into tf32 high and low parts written as the A operand; this edge's old
-//     message, the maximum and the message's slot go to a staging buffer of the unit's stage;
-//   * MMA warp 15: loads the group's four tables (E, E' high and low parts, built once per run in
-//     the swizzled layout) into shared memory with one bulk copy when the group changes, then
-//     issues the 24 tcgen05.mma of the unit into TMEM accumulator stage d and commits them to an
-//     mbarrier;
-//   * epilogue warps 0-7, two groups of four (group d takes the units of stage d; a thread per
-//     column = TMEM lane): tcgen05.ld of the sums, log, damping, normalisation, clipping and the
-//     residual (the arithmetic of the kernel above), the new message written to the staging row,
-//     then stored by the warp with lanes across states.
-// Handshakes: mbarriers a_full (producers -> MMA), mma_done[2] (tcgen05.commit -> producers,
-// epilogue, table reload), tmem_free[2] (epilogue -> MMA), stg_full[2] / stg_free[2] (producers
-// <-> epilogue). Every wait is bounded; the first that runs out sets a CTA abort flag that ends
-// every other wait, the CTA records the fault and stops, and TMEM is freed after the last
-// committed products have completed.
+//   * producer warps 4-14, two steps per unit, the operand double-buffered so that the copies
+//     of unit u are in flight while unit u - 1 is converted and multiplied:
+//       copy u: cp.async of each column's other-edge message into the high part of A buffer
+//       u & 1 and of the other variable's sums into its low part, at the operand positions;
+//       convert u - 1 (after a barrier of the producers): a thread per (column, half of the
+//       states) turns the pair in place into u = exp((vtof - max) / T) split into tf32 parts,
+//       and leaves the column maxima and the group's table maxima for the epilogue;
+//   * MMA warp 15: loads the group's two tables of its direction (high and low tf32 parts, built
+//     once per run in the swizzled layout) with one bulk copy when the group changes, then
+//     issues the 24 tcgen05.mma of the unit into TMEM accumulator stage u & 1 and commits them;
+//   * epilogue warps 0-3 (a thread per column = TMEM lane): fetch the columns' old messages of
+//     the next unit by cp.async into a staging buffer while this unit is finished: tcgen05.ld of
+//     the sums, log, damping, normalisation, clipping and the residual; the new messages are
+//     written to the staging rows and stored by the warp with lanes across states.
+// Handshakes (mbarriers): a_full[2] (producers -> MMA), mma_done[2] (tcgen05.commit ->
+// producers, epilogue, table reload), tmem_free[2] (epilogue -> MMA), meta_full[2] / meta_free[2]
+// (producers <-> epilogue: column and table maxima). Every wait is bounded; the first that runs
+// out sets a CTA abort flag that ends every other wait, the CTA records the fault and stops, and
+// TMEM is freed after the last committed products have completed.
 namespace tc {
 
 constexpr int K = 64;
 constexpr int kM = 128;                  // columns per tile (the MMA's M)
-constexpr int kEpiGroups = 1;            // epilogue groups of 4 warps; group g takes units u = g mod it
-constexpr int kEpiWarps = 4 * kEpiGroups;
-constexpr int kProdWarps = 15 - kEpiWarps;  // the warps after the epilogue's
+constexpr int kEpiWarps = 4;             // warps 0-3: thread e of the four = TMEM lane = column e
+constexpr int kProdWarps = 11;           // warps 4-14
 constexpr int kMmaWarp = 15;
 constexpr int kThreads = 32 * 16;        // four warps per SM sub-partition: 128 registers each
-constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 19 columns per producer warp
-constexpr int kStg = K + 1;              // staging row stride (floats): conflict-free both ways
+constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 12 columns per producer warp
+constexpr int kCvtWarps = kM / 16;       // producer warps that convert: 16 columns x 2 halves each
+static_assert(kCvtWarps <= kProdWarps, "converting warps");
+static_assert(kColsPerProd % 2 == 0, "producer columns come in half-warp pairs");
 constexpr uint32_t kTmemCols = 128;      // two accumulator stages of 64 fp32 columns
 // instruction descriptor: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
 // K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
@@ -592,23 +603,27 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(K >
 
 // shared memory, byte offsets from a 1024-byte aligned base
 constexpr int kMatBytes = K * K * 4;                 // one 64 x 64 tf32 table: 16 KB
-constexpr int kTabBytes = 4 * kMatBytes;             // E hi, E lo, E' hi, E' lo
-constexpr int kABytes = kM * K * 4;                  // one 128 x 64 tf32 operand: 32 KB
-constexpr int kOffAhi = kTabBytes;
-constexpr int kOffAlo = kOffAhi + kABytes;
-constexpr int kOffStg = kOffAlo + kABytes;           // 2 x [kM][kStg] floats
-constexpr int kStgBytes = kM * kStg * 4;
+constexpr int kTabBytes = 2 * kMatBytes;             // this direction's table: high, low parts
+constexpr int kABytes = kM * K * 4;                  // one 128 x 64 tf32 matrix: 32 KB
+constexpr int kABufBytes = 2 * kABytes;              // an operand buffer: high part, low part
+constexpr int kOffA = kTabBytes;                     // 2 operand buffers
+constexpr int kOffStg = kOffA + 2 * kABufBytes;      // 2 x [kM][K] floats, rows XOR-swizzled
+constexpr int kStgBytes = kM * K * 4;
 constexpr int kOffM = kOffStg + 2 * kStgBytes;       // 2 x [kM] maxima of the other vtof
-constexpr int kOffOwn = kOffM + 2 * kM * 4;          // 2 x [kM] slot of the message written
-constexpr int kOffR = kOffOwn + 2 * kM * 4;          // 2 x [K] table row / column maxima
+constexpr int kOffR = kOffM + 2 * kM * 4;            // 2 x [K] table row / column maxima
 constexpr int kOffBar = kOffR + 2 * K * 4;
-enum { kBarTab = 0, kBarAFull, kBarMma0, kBarMma1, kBarTmem0, kBarTmem1, kBarStgFull0,
-       kBarStgFull1, kBarStgFree0, kBarStgFree1, kNumBars };
+enum { kBarTab = 0, kBarAFull0, kBarAFull1, kBarMma0, kBarMma1, kBarTmem0, kBarTmem1,
+       kBarMetaFull0, kBarMetaFull1, kBarMetaFree0, kBarMetaFree1, kNumBars };
 constexpr int kOffMisc = kOffBar + kNumBars * 8;     // TMEM address, abort flags, residual
 constexpr int kSmemUsed = kOffMisc + 16;
 constexpr int kSmemBytes = kSmemUsed + 1024;         // + alignment of the dynamic base
 static_assert(kSmemBytes <= 227 * 1024, "shared memory");
-static_assert(kOffBar % 8 == 0 && kOffStg % 16 == 0, "alignment");
+static_assert(kOffBar % 8 == 0 && kOffStg % 16 == 0 && kOffA % 1024 == 0, "alignment");
+
+// Staging rows: the 16-byte chunk q (states 4 q .. 4 q + 3) of row c at float c * K + 4 (q ^ (c &
+// 7)), so that eight threads reading chunk q of eight consecutive rows, and a half-warp reading
+// the 16 chunks of one row, each take the fewest shared-memory wavefronts.
+__device__ __forceinline__ int stg_chunk(int c, int q) { return c * K + ((q ^ (c & 7)) << 2); }
 
 // floats of one group's tables in the run workspace: the four matrices, then r [K], c [K]
 constexpr int64_t kTabFloats = 4LL * K * K + 2LL * K;
@@ -655,9 +670,9 @@ __device__ __forceinline__ void fence_after_sync() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// 16 consecutive fp32 columns of the warp's 32 TMEM lanes (thread = lane).
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 16 consecutive fp32 columns of the warp's 32 TMEM lanes (thread = lane), without the wait: a
+// batch of loads completes at one tcgen05.wait::ld, which must come before `r` is read.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
       "%15}, [%16];"
@@ -665,9 +680,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
         "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 __device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count) {
@@ -716,11 +728,16 @@ __device__ __forceinline__ float warp_max(float x) {
   return x;
 }
 
-// Maximum over the warp in one instruction, NaN-propagating like maxn.
-__device__ __forceinline__ float warp_max_redux(float x) {
-  float r;
-  asm volatile("redux.sync.max.NaN.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(x));
-  return r;
+// AND of `pred` over the `count` threads of named barrier `id`; each of them gets the result.
+__device__ __forceinline__ bool named_bar_and(int id, int count, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n"
+      " selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(id), "r"(count)
+      : "memory");
+  return r != 0u;
 }
 
 // Run-time tables of one group for this path: E hi, E lo (rows i, k = j), E' hi, E' lo (rows j,
@@ -767,34 +784,50 @@ __device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
   return __uint_as_float(r);
 }
 
-// The epilogue of one column when some of its sums (E u) fell below 1e-30 in some lane of the
-// warp: those messages are recomputed with the reference's formula (direct_message). Kept out of
-// line so that the common path stays compact. Called by every lane of the warp (it reads TMEM
-// with warp-wide loads); `small` marks this lane's states to recompute, `row` is its staging row
-// (the old message in, the new one out). Returns the column's residual.
-__device__ __noinline__ float epilogue_slow(const ExpArgs& a, uint32_t taddr, float* row, float mo,
-                                            const float* rr, uint64_t small, bool active, int4 q,
+// The epilogue's message for state st from the sum E u (>= 1e-30): f = T log(sum) + max of the
+// other vtof + table maximum, damped with the old message o.
+__device__ __forceinline__ float epi_message(const ExpArgs& a, float tl2, float sum, float mo_rr,
+                                             float o) {
+  const float f = __fmaf_rn(tl2, __log2f(sum), mo_rr);
+  return __fmaf_rn(a.d, o, a.omd * f);
+}
+
+// The epilogue of one column when some sum (E u) of a lane of the warp fell below 1e-30 or is not
+// a number: those messages are recomputed with the reference's formula (direct_message). Kept out
+// of line so that the common path stays compact. Called by every lane of the warp (it reads TMEM
+// with warp-wide loads); `row` is the lane's staging row (state st in chunk (st / 4) ^ key: the
+// old message in, the new one out). Returns the column's residual.
+__device__ __noinline__ float epilogue_slow(const ExpArgs& a, uint32_t taddr, float* row, int key,
+                                            float mo, const float* rr, bool active, int4 q,
                                             int64_t table, bool first_edge) {
+  const float tl2 = a.t * 0.693147180559945309f;
   float y[K];
   float x = -INFINITY;
 #pragma unroll 1
   for (int st = 0; st < K; ++st) {
     const float sum = tmem_ld1(taddr + (uint32_t)st);
+    const float o = row[(((st >> 2) ^ key) << 2) + (st & 3)];
     float f = 0.0f;
     if (active) {
-      f = (small >> st) & 1ull ? direct_message<K>(a, q, 0, st, first_edge, table)
-                               : (a.t * __logf(sum) + mo) + rr[st];
+      if (sum >= 1e-30f) {
+        y[st] = epi_message(a, tl2, sum, mo + rr[st], o);
+      } else {
+        f = direct_message<K>(a, q, 0, st, first_edge, table);
+        y[st] = a.d * o + a.omd * f;
+      }
+    } else {
+      y[st] = 0.0f;
     }
-    y[st] = a.d * row[st] + a.omd * f;
     x = maxn(x, y[st]);
   }
   float dmax = 0.0f;
   if (active) {
 #pragma unroll 1
     for (int st = 0; st < K; ++st) {
+      const int at = (((st >> 2) ^ key) << 2) + (st & 3);
       const float nv = maxn(y[st] - x, kMsgNegInf);
-      dmax = maxn(dmax, fabsf(nv - row[st]));
-      row[st] = nv;
+      dmax = maxn(dmax, fabsf(nv - row[at]));
+      row[at] = nv;
     }
   }
   return dmax;
@@ -827,22 +860,25 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned long long lim = a.wait_ns;
 
-  const int64_t t_begin = (int64_t)blockIdx.x * a.tiles_per_cta;
+  // the pair of CTAs over range blockIdx.x / 2: direction blockIdx.x & 1
+  const int dir = (int)(blockIdx.x & 1u);
+  const int64_t t_begin = (int64_t)(blockIdx.x >> 1) * a.tiles_per_cta;
   const int64_t t_end =
       t_begin + a.tiles_per_cta < a.n_tiles ? t_begin + a.tiles_per_cta : a.n_tiles;
-  const int64_t n_units = 2 * (t_end - t_begin);
+  const int64_t n_units = t_end > t_begin ? t_end - t_begin : 0;
 
   if (threadIdx.x == 0) {
     bar_init(&bars[kBarTab], 1);
-    bar_init(&bars[kBarAFull], 32 * kProdWarps);
+    bar_init(&bars[kBarAFull0], 32 * kProdWarps);
+    bar_init(&bars[kBarAFull1], 32 * kProdWarps);
     bar_init(&bars[kBarMma0], 1);
     bar_init(&bars[kBarMma1], 1);
     bar_init(&bars[kBarTmem0], 128);
     bar_init(&bars[kBarTmem1], 128);
-    bar_init(&bars[kBarStgFull0], 32 * kProdWarps);
-    bar_init(&bars[kBarStgFull1], 32 * kProdWarps);
-    bar_init(&bars[kBarStgFree0], 128);
-    bar_init(&bars[kBarStgFree1], 128);
+    bar_init(&bars[kBarMetaFull0], 32 * kProdWarps);
+    bar_init(&bars[kBarMetaFull1], 32 * kProdWarps);
+    bar_init(&bars[kBarMetaFree0], 128);
+    bar_init(&bars[kBarMetaFree1], 128);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *s_abort = 0;
     *s_res = 0u;
@@ -863,23 +899,19 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
 
   if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
     // ------------------------------------------------------------------ producers
-    // Warp p owns columns p + 7 j (j < 19, column < 128) of every tile, split into two halves
-    // (j < 10, j >= 10). A lane keeps the other edge's message and the other variable's sums of
-    // one half in registers (states lane and lane + 32) while it computes the other half, and the
-    // loads of the next unit's first half are issued before this unit's second half is computed,
-    // so the memory latency is hidden behind the arithmetic. This edge's old message goes straight
-    // to the staging row by cp.async, without passing through registers.
+    // Step u copies unit u (warp p takes columns p, p + 11, ... of the tile, lanes across
+    // states; nothing passes through registers) and converts unit u - 1 in place (warps 0-7 of
+    // the producers, a thread per (column cc = 16 p + lane % 16, half ch = lane / 16 of the
+    // states)).
     const int p = warp - kEpiWarps;
-    constexpr int kHalf = (kColsPerProd + 1) / 2;   // columns of the first half
-    struct Unit {               // what a lane needs of a unit
-      int d, ncols, g, qy, qz, qw;  // qy/qz/qw: the record of the warp's column `lane` (< 19)
+    struct Unit {       // a tile as the producers see it
+      int ncols, g;     // columns, group
+      int qy, qv;       // the record of column p + 11 lane (lane < 12): message pair, other sums
     };
-    // the tile's group, width and records (loaded one tile ahead, while the tile before it runs)
     TileCursor cur;
     auto tile_info = [&](int64_t tile) {
       Unit x;
       cur.seek(a, tile);
-      x.d = 0;
       x.g = cur.g;
       const int64_t c0 = (tile - cur.t0) * kM;
       const int64_t left = (int64_t)a.grp_count[x.g] - c0;
@@ -888,132 +920,131 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       if (lane < kColsPerProd && p + kProdWarps * lane < x.ncols)
         q = a.rec[a.grp_first[x.g] + c0 + p + kProdWarps * lane];
       x.qy = q.y;
-      x.qz = q.z;
-      x.qw = q.w;
+      x.qv = dir == 0 ? q.w : q.z;
       return x;
     };
-    float ra[kHalf][4], rb[kColsPerProd - kHalf][4];
-    // register loads of columns j0 .. j0 + n - 1 of unit x: other message and other sums (zero
-    // for columns past the tile's end)
-    auto load = [&](const Unit& x, int j0, auto& r) {
-      constexpr int n = sizeof(r) / sizeof(r[0]);
-#pragma unroll
-      for (int i = 0; i < n; ++i) {
-        const int j = j0 + i;
-        const int qy = __shfl_sync(0xffffffffu, x.qy, j);
-        const int qv = __shfl_sync(0xffffffffu, x.d == 0 ? x.qw : x.qz, j);
-        const bool act = p + kProdWarps * j < x.ncols;
-        const int other = qy + (x.d == 0 ? K : 0);
-        r[i][0] = act ? a.cur[other + lane] : 0.0f;
-        r[i][1] = act ? a.cur[other + lane + 32] : 0.0f;
-        r[i][2] = act ? a.vsum[qv + lane] : 0.0f;
-        r[i][3] = act ? a.vsum[qv + lane + 32] : 0.0f;
-      }
-    };
-    // (x - m) / T as div_t computes it, with the power-of-two test made once per kernel: the
-    // column bodies below are then branch-free, so the compiler interleaves them
+    // (x - m) / T as div_t computes it, with the power-of-two test made once per kernel
     const float t_inv = __uint_as_float((254u - ((__float_as_uint(a.t) >> 23) & 0xffu)) << 23);
     const bool t_pow2 = [&] {
       const unsigned ub = __float_as_uint(a.t), eb = (ub >> 23) & 0xffu;
       return (ub & 0x807fffffu) == 0u && eb >= 2u && eb <= 252u;
     }();
-    // u (or w) of columns j0 .. j0 + n - 1 into the operand; the maximum and slot to staging
-    auto compute = [&](auto pow2, const Unit& x, int j0, const auto& r, float* stg_m,
-                       int* stg_own) {
-      constexpr int n = sizeof(r) / sizeof(r[0]);
+    const int cc = 16 * p + (lane & 15), ch = lane >> 4;
+    const uint32_t cvt_off = (uint32_t)(ch * (kM * 128) + cc * 128);
+    // vtof = sums - message of the pair at (cc, ch) of buffer `buf`, its column maximum, and
+    // u = exp((vtof - max) / T) split into tf32 parts written over the pair
+    auto convert = [&](auto pow2, unsigned char* buf, int ncols, float* meta_m) {
+      float t[32];
+      float mx = -INFINITY;
 #pragma unroll
-      for (int i = 0; i < n; ++i) {
-        const int j = j0 + i;
-        const int c = p + kProdWarps * j;
-        if (c >= kM) continue;
-        const int qy = __shfl_sync(0xffffffffu, x.qy, j);
-        const bool act = c < x.ncols;
-        const float t0 = r[i][2] - r[i][0], t1 = r[i][3] - r[i][1];
-        const float m = warp_max_redux(maxn(t0, t1));
-        float z0, z1;
-        if constexpr (decltype(pow2)::value) {
-          z0 = (t0 - m) * t_inv;
-          z1 = (t1 - m) * t_inv;
-        } else {
-          z0 = (t0 - m) / a.t;
-          z1 = (t1 - m) / a.t;
-        }
-        uint32_t h0, l0, h1, l1;
-        split_tf32(__expf(z0), h0, l0);
-        split_tf32(__expf(z1), h1, l1);
-        if (!act) h0 = l0 = h1 = l1 = 0u;
-        if (lane == 0 && act) {
-          stg_m[c] = m;
-          stg_own[c] = qy + (x.d == 0 ? 0 : K);
-        }
-        *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane, kM)) = h0;
-        *reinterpret_cast<uint32_t*>(sm + kOffAhi + sw128(c, lane + 32, kM)) = h1;
-        *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane, kM)) = l0;
-        *reinterpret_cast<uint32_t*>(sm + kOffAlo + sw128(c, lane + 32, kM)) = l1;
+      for (int jj = 0; jj < 8; ++jj) {
+        const uint32_t off = cvt_off + (uint32_t)(((jj ^ cc) & 7) << 4);
+        const float4 o = *reinterpret_cast<const float4*>(buf + off);
+        const float4 v = *reinterpret_cast<const float4*>(buf + kABytes + off);
+        t[4 * jj + 0] = v.x - o.x;
+        t[4 * jj + 1] = v.y - o.y;
+        t[4 * jj + 2] = v.z - o.z;
+        t[4 * jj + 3] = v.w - o.w;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) mx = maxn(mx, t[4 * jj + q]);
       }
-    };
-    Unit x = n_units > 0 ? tile_info(t_begin) : Unit{};   // the unit being produced
-    Unit next_tile = x;
-    if (n_units > 0) load(x, 0, ra);
-    for (int64_t u = 0; u < n_units; ++u) {
-      if ((u & 1) == 0 && u + 2 < n_units) next_tile = tile_info(t_begin + (u >> 1) + 1);
-      const int s = (int)(u & 1);
-      float* stg = reinterpret_cast<float*>(sm + kOffStg + s * kStgBytes);
-      float* stg_m = reinterpret_cast<float*>(sm + kOffM) + s * kM;
-      int* stg_own = reinterpret_cast<int*>(sm + kOffOwn) + s * kM;
-      // a warp leaves together (its shuffles need every lane)
-      bool ok = u < 2 || wait(&bars[kBarStgFree0 + s], (uint32_t)(((u - 2) >> 1) & 1), lim,
-                              s_abort);
-      if (!__all_sync(0xffffffffu, ok)) break;
-      // this edge's old messages of every column of the warp into the staging rows
+      const float m = maxn(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+      const bool act = cc < ncols;
 #pragma unroll
-      for (int j = 0; j < kColsPerProd; ++j) {
-        const int c = p + kProdWarps * j;
-        const int qy = __shfl_sync(0xffffffffu, x.qy, j);
-        if (c < x.ncols) {
-          const float* src = a.cur + qy + (x.d == 0 ? 0 : K);
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                           smem_addr(stg + c * kStg + lane)),
-                       "l"(src + lane)
-                       : "memory");
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                           smem_addr(stg + c * kStg + lane + 32)),
-                       "l"(src + lane + 32)
-                       : "memory");
+      for (int jj = 0; jj < 8; ++jj) {
+        const uint32_t off = cvt_off + (uint32_t)(((jj ^ cc) & 7) << 4);
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float z;
+          if constexpr (decltype(pow2)::value) z = (t[4 * jj + q] - m) * t_inv;
+          else z = (t[4 * jj + q] - m) / a.t;
+          split_tf32(__expf(z), h[q], l[q]);
+          if (!act) h[q] = l[q] = 0u;
+        }
+        *reinterpret_cast<uint4*>(buf + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4*>(buf + kABytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
+      }
+      if (ch == 0 && act) meta_m[cc] = m;
+    };
+    auto cp4 = [&](unsigned char* dst, const float* src) {
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src)
+                   : "memory");
+    };
+    auto cp16 = [&](unsigned char* dst, const float* src) {
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
+                   : "memory");
+    };
+    Unit x = n_units > 0 ? tile_info(t_begin) : Unit{};   // the unit copied at this step
+    Unit xc = x;                                           // the unit converted at this step
+    for (int64_t u = 0; u <= n_units; ++u) {
+      Unit xn = x;
+      if (u + 1 < n_units) xn = tile_info(t_begin + u + 1);
+      const int b = (int)(u & 1);
+      unsigned char* abuf = sm + kOffA + b * kABufBytes;
+      // operand buffer u & 1 was last read by the products of unit u - 2; the maxima slot of
+      // unit u - 1 by the epilogue of unit u - 3
+      bool ok = u >= n_units || u < 2 ||
+                wait(&bars[kBarMma0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort);
+      ok = ok && (u < 3 || wait(&bars[kBarMetaFree0 + ((u - 1) & 1)],
+                                (uint32_t)(((u - 3) >> 1) & 1), lim, s_abort));
+      if (u < n_units && ok) {
+        // half-warp h of the warp takes column p + 11 (2 i + h); lane l16 the 16-byte chunk l16
+        // of the other message's row (16-byte aligned: the plan starts such rows at multiples of
+        // 4 slots) and of the sums' row when that is aligned too, else four single states
+        const int h = lane >> 4, l16 = lane & 15;
+#pragma unroll
+        for (int i = 0; i < kColsPerProd / 2; ++i) {
+          const int j = 2 * i + h;
+          const int c = p + kProdWarps * j;
+          const int qy = __shfl_sync(0xffffffffu, x.qy, j);
+          const int qv = __shfl_sync(0xffffffffu, x.qv, j);
+          if (c < x.ncols) {
+            const float* other = a.cur + qy + (dir == 0 ? K : 0);
+            const float* sums = a.vsum + qv;
+            const uint32_t o = sw128(c, 4 * l16, kM);
+            cp16(abuf + o, other + 4 * l16);
+            if ((qv & 3) == 0) {
+              cp16(abuf + kABytes + o, sums + 4 * l16);
+            } else {
+#pragma unroll
+              for (int k4 = 0; k4 < 4; ++k4)
+                cp4(abuf + kABytes + sw128(c, l16 + 16 * k4, kM), sums + l16 + 16 * k4);
+            }
+          }
         }
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
-      load(x, kHalf, rb);
-      ok = u < 1 || wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1), lim,
-                         s_abort);
-      if (!__all_sync(0xffffffffu, ok)) {
+      if (u >= 1) {
+        // this thread's copies of unit u - 1 have landed; the barrier makes every thread's
+        // visible and, with the and of the waits above, lets the producers leave together
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+      }
+      if (!named_bar_and(1, 32 * kProdWarps, ok)) {
         asm volatile("cp.async.wait_all;" ::: "memory");
         break;
       }
-      if (p == 0) {  // this direction's table maxima: r (to variable 1) or c (to variable 2)
-        float* stg_r = reinterpret_cast<float*>(sm + kOffR) + s * K;
-        const float* mx = tab_g0 + (int64_t)x.g * kTabFloats + 4 * K * K + x.d * K;
-        stg_r[lane] = mx[lane];
-        stg_r[lane + 32] = mx[lane + 32];
-      }
-      if (t_pow2) compute(std::true_type{}, x, 0, ra, stg_m, stg_own);
-      else compute(std::false_type{}, x, 0, ra, stg_m, stg_own);
-      const Unit cur_x = x;
-      if (u + 1 < n_units) {
-        if ((u & 1) == 0) {
-          x.d = 1;          // the other direction of the same tile
-        } else {
-          x = next_tile;    // the next tile, direction 0
+      if (u >= 1) {
+        const int mb = (int)((u - 1) & 1);
+        unsigned char* cbuf = sm + kOffA + mb * kABufBytes;
+        float* meta_m = reinterpret_cast<float*>(sm + kOffM) + mb * kM;
+        if (p < kCvtWarps) {
+          if (t_pow2) convert(std::true_type{}, cbuf, xc.ncols, meta_m);
+          else convert(std::false_type{}, cbuf, xc.ncols, meta_m);
+        } else if (p == kCvtWarps) {
+          // this direction's table maxima: r (to variable 1) or c (to variable 2)
+          float* meta_r = reinterpret_cast<float*>(sm + kOffR) + mb * K;
+          const float* mx = tab_g0 + (int64_t)xc.g * kTabFloats + 4 * K * K + dir * K;
+          meta_r[lane] = mx[lane];
+          meta_r[lane + 32] = mx[lane + 32];
         }
-        load(x, 0, ra);
+        // the operand's generic-proxy writes become visible to the tensor cores' async proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        bar_arrive(&bars[kBarAFull0 + mb]);
+        bar_arrive(&bars[kBarMetaFull0 + mb]);
       }
-      if (t_pow2) compute(std::true_type{}, cur_x, kHalf, rb, stg_m, stg_own);
-      else compute(std::false_type{}, cur_x, kHalf, rb, stg_m, stg_own);
-      asm volatile("cp.async.wait_all;" ::: "memory");
-      // the operand's generic-proxy writes become visible to the tensor cores' async proxy
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      bar_arrive(&bars[kBarAFull]);
-      bar_arrive(&bars[kBarStgFull0 + s]);
+      xc = x;
+      x = xn;
     }
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------------------------ MMA issue
@@ -1023,28 +1054,27 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       uint32_t tab_phase = 0;
       int64_t last_commit[2] = {-1, -1};
       for (int64_t u = 0; u < n_units; ++u) {
-        const int64_t tile = t_begin + (u >> 1);
-        const int d = (int)(u & 1), s = (int)(u & 1);
-        cur.seek(a, tile);
+        const int s = (int)(u & 1);
+        cur.seek(a, t_begin + u);
         if (cur.g != loaded) {
           // the old tables' last reader is the previous unit's products
           if (u >= 1 && !wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1),
                               lim, s_abort))
             break;
-          bulk_load(sm, tab_g0 + (int64_t)cur.g * kTabFloats, (uint32_t)kTabBytes, &bars[kBarTab],
-                    a.skip_copy != 0);
+          bulk_load(sm, tab_g0 + (int64_t)cur.g * kTabFloats + (int64_t)dir * 2 * K * K,
+                    (uint32_t)kTabBytes, &bars[kBarTab], a.skip_copy != 0);
           if (!wait(&bars[kBarTab], tab_phase, lim, s_abort)) break;
           tab_phase ^= 1u;
           loaded = cur.g;
         }
-        if (!wait(&bars[kBarAFull], (uint32_t)(u & 1), lim, s_abort)) break;
+        if (!wait(&bars[kBarAFull0 + s], (uint32_t)((u >> 1) & 1), lim, s_abort)) break;
         if (u >= 2 && !wait(&bars[kBarTmem0 + s], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort))
           break;
         fence_after_sync();
         const uint32_t d_tmem = tmem + (uint32_t)(s * K);
-        const uint32_t b_hi = s_base + (uint32_t)((2 * d) * kMatBytes);
-        const uint32_t b_lo = b_hi + (uint32_t)kMatBytes;
-        const uint32_t a_hi = s_base + kOffAhi, a_lo = s_base + kOffAlo;
+        const uint32_t b_hi = s_base, b_lo = s_base + (uint32_t)kMatBytes;
+        const uint32_t a_hi = s_base + (uint32_t)(kOffA + s * kABufBytes);
+        const uint32_t a_lo = a_hi + (uint32_t)kABytes;
 #pragma unroll
         for (int ks = 0; ks < K / 8; ++ks) {
           const uint64_t ah = kstep_desc(a_hi, ks, kM), al = kstep_desc(a_lo, ks, kM);
@@ -1068,83 +1098,144 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     __syncwarp();
   } else {
     // ------------------------------------------------------------------ epilogue
-    // group eg (warps 4 eg .. 4 eg + 3) takes the units u = eg mod kEpiGroups; thread e of the
-    // group is TMEM lane e = column e of the tile
-    const int eg = kEpiGroups == 1 ? 0 : warp >> 2, wq = warp & 3;
-    const int e = threadIdx.x & 127;
+    // thread e of warps 0-3 is TMEM lane e = column e of the tile; warp wq owns columns (and
+    // staging rows) 32 wq .. 32 wq + 31, so the warps never wait for one another
+    const int wq = warp, e = threadIdx.x;
+    const int h = lane >> 4, l16 = lane & 15;
     const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
-    TileCursor cur;
+    const float tl2 = a.t * 0.693147180559945309f;
+    float* stg0 = reinterpret_cast<float*>(sm + kOffStg);
+    TileCursor fcur, cur;
+    // the old messages of unit f's columns 32 wq .. 32 wq + 31 into staging buffer f & 1
+    // (cp.async of 16-byte chunks, a half-warp per row); returns the slot of the lane's column
+    auto fetch = [&](int64_t f) {
+      fcur.seek(a, t_begin + f);
+      const int g = fcur.g;
+      const int64_t c0 = (t_begin + f - fcur.t0) * kM;
+      const int64_t left = (int64_t)a.grp_count[g] - c0;
+      const int ncols = (int)(left < kM ? left : kM);
+      int own = 0;
+      if (e < ncols) own = a.rec[a.grp_first[g] + c0 + e].y + (dir == 0 ? 0 : K);
+      float* stg = stg0 + (f & 1) * (kM * K);
+#pragma unroll 4
+      for (int i = 0; i < 16; ++i) {
+        const int r = 2 * i + h, c = 32 * wq + r;
+        const int ow = __shfl_sync(0xffffffffu, own, r);
+        if (c < ncols) {
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                           smem_addr(stg + stg_chunk(c, l16))),
+                       "l"(a.cur + ow + 4 * l16)
+                       : "memory");
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      return own;
+    };
     unsigned res = 0u;
-    for (int64_t u = eg; u < n_units; u += kEpiGroups) {
-      const int64_t tile = t_begin + (u >> 1);
-      const int d = (int)(u & 1), s = (int)(u & 1);
-      cur.seek(a, tile);
+    int own_next = n_units > 0 ? fetch(0) : 0;
+    for (int64_t u = 0; u < n_units; ++u) {
+      const int s = (int)(u & 1);
+      const int own = own_next;
+      if (u + 1 < n_units) {
+        own_next = fetch(u + 1);
+      } else {
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      }
+      cur.seek(a, t_begin + u);
       const int g = cur.g;
-      const int64_t c0 = (tile - cur.t0) * kM;
+      const int64_t c0 = (t_begin + u - cur.t0) * kM;
       const int64_t left = (int64_t)a.grp_count[g] - c0;
       const int ncols = (int)(left < kM ? left : kM);
       const uint32_t ph = (uint32_t)((u >> 1) & 1);
       // a warp leaves together (tcgen05.ld is a warp-wide instruction)
-      bool ok = wait(&bars[kBarStgFull0 + s], ph, lim, s_abort, 256);
-      ok = ok && wait(&bars[kBarMma0 + s], ph, lim, s_abort, 256);
-      if (!__all_sync(0xffffffffu, ok)) break;
+      bool ok = wait(&bars[kBarMetaFull0 + s], ph, lim, s_abort, 32);
+      ok = ok && wait(&bars[kBarMma0 + s], ph, lim, s_abort, 32);
+      if (!__all_sync(0xffffffffu, ok)) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        break;
+      }
+      asm volatile("cp.async.wait_group 1;" ::: "memory");   // this unit's old messages
+      __syncwarp();
       fence_after_sync();
-      float* stg = reinterpret_cast<float*>(sm + kOffStg + s * kStgBytes);
-      const float mo = reinterpret_cast<float*>(sm + kOffM)[s * kM + e];
-      const float* rr = reinterpret_cast<float*>(sm + kOffR) + s * K;
+      float* stg = stg0 + s * (kM * K);
+      float* row = stg + e * K;
+      const int key = e & 7;
+      const float mo = reinterpret_cast<const float*>(sm + kOffM)[s * kM + e];
+      const float* rr = reinterpret_cast<const float*>(sm + kOffR) + s * K;
       const bool active = e < ncols;
+      // the 64 sums of the column in one batch of TMEM loads, turned into y in place
+      uint32_t raw[K / 16][16];
+#pragma unroll
+      for (int c4 = 0; c4 < K / 16; ++c4)
+        tmem_ld16_nowait(tmem + lane_base + (uint32_t)(s * K + 16 * c4), raw[c4]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       float y[K];
-      float x = -INFINITY;
-      uint64_t small = 0;  // states whose sum fell below 1e-30
 #pragma unroll
-      for (int c4 = 0; c4 < K / 16; ++c4) {
-        float acc[16];
-        tmem_ld16(tmem + lane_base + (uint32_t)(s * K + 16 * c4), acc);
+      for (int st = 0; st < K; ++st) y[st] = __uint_as_float(raw[st >> 4][st & 15]);
+      float x4[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+      float amin = INFINITY;   // the smallest sum (NaN if any is not a number)
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int st = 16 * c4 + j;
-          const float o = stg[e * kStg + st];
-          // sums >= 1e-30: the fast logarithm's absolute error is about 4e-7
-          if (!(acc[j] >= 1e-30f)) small |= 1ull << st;
-          const float f = (a.t * __logf(acc[j]) + mo) + rr[st];
-          y[st] = a.d * o + a.omd * f;
-          x = maxn(x, y[st]);
+      for (int q = 0; q < K / 4; ++q) {
+        const float4 o = *reinterpret_cast<const float4*>(row + ((q ^ key) << 2));
+        const float4 r4 = *reinterpret_cast<const float4*>(rr + 4 * q);
+        const float ov[4] = {o.x, o.y, o.z, o.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int st = 4 * q + k;
+          amin = minn(amin, y[st]);
+          y[st] = epi_message(a, tl2, y[st], mo + rv[k], ov[k]);
+          x4[k] = maxn(x4[k], y[st]);
         }
       }
-      if (!active) small = 0;
-      const bool slow = __any_sync(0xffffffffu, small != 0);
+      const float x = maxn(maxn(x4[0], x4[1]), maxn(x4[2], x4[3]));
+      const bool slow = __any_sync(0xffffffffu, active && !(amin >= 1e-30f));
       float dmax = 0.0f;
       if (slow) {  // rare: a table row spanning more than about 69 T underflowed somewhere
-        const int4 q = active ? a.rec[a.grp_first[g] + c0 + e] : make_int4(0, 0, 0, 0);
-        dmax = epilogue_slow(a, tmem + lane_base + (uint32_t)(s * K), stg + e * kStg, mo, rr,
-                             small, active, q, a.grp_table[g], d == 0);
+        const int4 qr = active ? a.rec[a.grp_first[g] + c0 + e] : make_int4(0, 0, 0, 0);
+        dmax = epilogue_slow(a, tmem + lane_base + (uint32_t)(s * K), row, key, mo, rr, active,
+                             qr, a.grp_table[g], dir == 0);
         fence_before_sync();
         bar_arrive(&bars[kBarTmem0 + s]);
+        bar_arrive(&bars[kBarMetaFree0 + s]);
       } else {
         fence_before_sync();
         bar_arrive(&bars[kBarTmem0 + s]);
+        bar_arrive(&bars[kBarMetaFree0 + s]);
         if (active) {
 #pragma unroll
-          for (int st = 0; st < K; ++st) {
-            const float nv = maxn(y[st] - x, kMsgNegInf);
-            dmax = maxn(dmax, fabsf(nv - stg[e * kStg + st]));
-            stg[e * kStg + st] = nv;
+          for (int q4 = 0; q4 < K / 16; ++q4) {
+            float4 o[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              o[k] = *reinterpret_cast<const float4*>(row + (((4 * q4 + k) ^ key) << 2));
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int st = 16 * q4 + 4 * k;
+              float4 nv;
+              nv.x = maxn(y[st + 0] - x, kMsgNegInf);
+              nv.y = maxn(y[st + 1] - x, kMsgNegInf);
+              nv.z = maxn(y[st + 2] - x, kMsgNegInf);
+              nv.w = maxn(y[st + 3] - x, kMsgNegInf);
+              dmax = maxn(dmax, fabsf(nv.x - o[k].x));
+              dmax = maxn(dmax, fabsf(nv.y - o[k].y));
+              dmax = maxn(dmax, fabsf(nv.z - o[k].z));
+              dmax = maxn(dmax, fabsf(nv.w - o[k].w));
+              *reinterpret_cast<float4*>(row + (((4 * q4 + k) ^ key) << 2)) = nv;
+            }
           }
         }
       }
       __syncwarp();
-      const int* stg_own = reinterpret_cast<int*>(sm + kOffOwn) + s * kM;
-#pragma unroll 8
-      for (int r = 0; r < 32; ++r) {
-        const int col = 32 * wq + r;
-        if (col < ncols) {
-          const int own = stg_own[col];
-          a.nxt[own + lane] = stg[col * kStg + lane];
-          a.nxt[own + lane + 32] = stg[col * kStg + lane + 32];
-        }
+      // the new rows to their slots, a half-warp per row, 16-byte stores
+#pragma unroll 4
+      for (int i = 0; i < 16; ++i) {
+        const int r = 2 * i + h, c = 32 * wq + r;
+        const int ow = __shfl_sync(0xffffffffu, own, r);
+        if (c < ncols)
+          *reinterpret_cast<float4*>(a.nxt + ow + 4 * l16) =
+              *reinterpret_cast<const float4*>(stg + stg_chunk(c, l16));
       }
-      __syncwarp();
-      bar_arrive(&bars[kBarStgFree0 + s]);
+      __syncwarp();   // the rows are read before the next fetch into this buffer
       res = __float_as_uint(maxn(__uint_as_float(res), dmax));
     }
     res = __float_as_uint(warp_max(__uint_as_float(res)));
@@ -1175,8 +1266,8 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
 
 }  // namespace tc
 
-// One iteration of a K = 64 bucket at B = 1 on the tcgen05 path: one CTA per SM, each over a
-// contiguous range of 128-column tiles.
+// One iteration of a K = 64 bucket at B = 1 on the tcgen05 path: pairs of CTAs (one per SM),
+// each pair over a contiguous range of 128-column tiles, one CTA per message direction.
 cudaError_t launch_tc(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const ExpArgs& base,
                       const float* tc_tables) {
   static const cudaError_t attr = cudaFuncSetAttribute(
@@ -1186,10 +1277,10 @@ cudaError_t launch_tc(const Plan& p, const PairwiseBucket& q, cudaStream_t s, co
   int64_t tiles = 0;
   for (int64_t c : q.grp_count_host) tiles += (c + tc::kM - 1) / tc::kM;
   if (tiles == 0) return cudaSuccess;
-  const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)p.sm_count));
+  const int64_t ranges = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)p.sm_count / 2));
   a.n_tiles = tiles;
-  a.tiles_per_cta = (tiles + ctas - 1) / ctas;
-  const int64_t grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
+  a.tiles_per_cta = (tiles + ranges - 1) / ranges;
+  const int64_t grid = 2 * ((tiles + a.tiles_per_cta - 1) / a.tiles_per_cta);
   tc::pairwise_kernel<<<(unsigned)grid, tc::kThreads, tc::kSmemBytes, s>>>(a, tc_tables);
   return cudaGetLastError();
 }
@@ -1249,7 +1340,11 @@ cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t
   a.fault = p.fault_dev;
   a.wait_ns = knobs.wait_limit_ns != 0 ? knobs.wait_limit_ns : kWaitLimitNs;
   a.skip_copy = knobs.skip_table_copy;
-  if (q.n1 == 64 && B == 1 && !knobs.legacy_mma) {
+  // the tcgen05 kernel moves message rows as 16-byte chunks: every row and buffer aligned
+  const bool aligned16 =
+      q.rows16 && ((reinterpret_cast<uintptr_t>(cur) | reinterpret_cast<uintptr_t>(nxt) |
+                    reinterpret_cast<uintptr_t>(vsum)) & 15u) == 0;
+  if (q.n1 == 64 && B == 1 && aligned16 && !knobs.legacy_mma) {
     ProfileScope ps(kProfPairwiseExp, s);
     return launch_tc(p, q, s, a, tables + (int64_t)q.n_groups * expgemm_table_floats(64));
   }

@@ -37,6 +37,7 @@ struct PairwiseBucket {
   int32_t* grp_table = nullptr;
   std::vector<int64_t> grp_count_host;
   int64_t gemm_floats = 0;
+  bool rows16 = false;  // every factor's message pair starts at a multiple of 4 slots
 };
 
 // Floats of run-time tables one group of a shared-table bucket with K x K tables needs: E and E'

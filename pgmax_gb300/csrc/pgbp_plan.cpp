@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -316,11 +317,31 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
   }
   auto factor_of = [&](int64_t es) { return (int64_t)fi[es]; };
 
-  // --- slots: one per binary edge (compressed pair), one per state otherwise; edge order
+  // --- slots: one per binary edge (compressed pair), one per state otherwise; edge order. A
+  // factor whose edges all have a multiple of 4 states starts at a multiple of 4 slots, so that
+  // at B = 1 each of its messages is a 16-byte aligned row (the slots skipped are never read).
   std::vector<int32_t> edge_slot(ne + 1, 0);
-  for (int64_t e = 0; e < ne; ++e) {
-    const int32_t k = edge_start[e + 1] - edge_start[e];
-    edge_slot[e + 1] = edge_slot[e] + (k == 2 ? 1 : k);
+  {
+    std::vector<char> align4(ne, 0);
+    for (size_t f = 0; f < fac_es_begin.size(); ++f) {
+      bool all4 = true;
+      for (int64_t i = fac_es_begin[f]; i < fac_es_end[f] && all4;
+           i = edge_start[ei[i] + 1]) {
+        const int32_t k = edge_start[ei[i] + 1] - edge_start[ei[i]];
+        all4 = k >= 4 && k % 4 == 0;
+      }
+      if (all4) align4[ei[fac_es_begin[f]]] = 1;
+    }
+    int64_t next = 0;
+    for (int64_t e = 0; e < ne; ++e) {
+      const int32_t k = edge_start[e + 1] - edge_start[e];
+      if (align4[e]) next = (next + 3) & ~(int64_t)3;
+      edge_slot[e] = (int32_t)next;
+      next += (k == 2 ? 1 : k);
+    }
+    if (next > INT32_MAX)
+      return bail(fail(PGBP_ERR_UNSUPPORTED, "more than 2^31 message slots"));
+    edge_slot[ne] = (int32_t)next;
   }
   p.num_slots = edge_slot[ne];
   auto slot_of_es = [&](int64_t es) {  // slot holding edge state es (binary: the edge's slot)
@@ -652,6 +673,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         q.grp_count = bd.upload(gc);
         q.grp_table = bd.upload(gt);
         q.grp_count_host.assign(gc.begin(), gc.end());
+        q.rows16 = true;
+        for (const int4& r : recs) q.rows16 = q.rows16 && (r.y & 3) == 0;
         q.gemm_floats = (int64_t)q.n_groups * (pgbp::expgemm_table_floats(q.n1) +
                                                 pgbp::expgemm_tc_table_floats(q.n1));
       }
