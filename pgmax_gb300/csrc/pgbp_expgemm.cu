@@ -611,12 +611,15 @@ constexpr int kOffStg = kOffA + 2 * kABufBytes;      // 2 x [kM][K] floats, rows
 constexpr int kStgBytes = kM * K * 4;
 constexpr int kOffM = kOffStg + 2 * kStgBytes;       // 2 x [kM] maxima of the other vtof
 constexpr int kOffR = kOffM + 2 * kM * 4;            // 2 x [K] table row / column maxima
-constexpr int kOffBar = kOffR + 2 * K * 4;
+constexpr int kOffOwn = kOffR + 2 * K * 4;           // 2 x [kM] slot of each column's message
+constexpr int kOffBar = kOffOwn + 2 * kM * 4;
 enum { kBarTab = 0, kBarAFull0, kBarAFull1, kBarMma0, kBarMma1, kBarTmem0, kBarTmem1,
-       kBarMetaFull0, kBarMetaFull1, kBarMetaFree0, kBarMetaFree1, kNumBars };
+       kBarMetaFull0, kBarMetaFull1, kBarMetaFree0, kBarMetaFree1, kBarOwnFull0, kBarOwnFull1,
+       kBarOwnFree0, kBarOwnFree1, kNumBars };
 constexpr int kOffMisc = kOffBar + kNumBars * 8;     // TMEM address, abort flags, residual
-constexpr int kSmemUsed = kOffMisc + 16;
-constexpr int kSmemBytes = kSmemUsed + 1024;         // + alignment of the dynamic base
+constexpr int kSmemBytes = kOffMisc + 16;
+// the dynamic shared memory starts at the CTA's shared window (no static shared memory), which
+// the kernel checks to be 1024-byte aligned (the swizzled operands need it)
 static_assert(kSmemBytes <= 227 * 1024, "shared memory");
 static_assert(kOffBar % 8 == 0 && kOffStg % 16 == 0 && kOffA % 1024 == 0, "alignment");
 
@@ -834,24 +837,38 @@ __device__ __noinline__ float epilogue_slow(const ExpArgs& a, uint32_t taddr, fl
 }
 
 // Tile `tile` of the CTA's walk: its group (cursor g, first tile t0 of g).
+// (Tile indices fit in int32: the launcher takes this kernel only below 2^31 tiles.)
 struct TileCursor {
-  int g = 0;
-  int64_t t0 = 0;
-  __device__ void seek(const ExpArgs& a, int64_t tile) {
-    while (g < a.n_groups) {
-      const int64_t nt = ((int64_t)a.grp_count[g] + kM - 1) / kM;
-      if (tile < t0 + nt) break;
-      t0 += nt;
+  int g = -1;
+  int count = 0;        // columns of group g
+  int t0 = 0, t1 = 0;   // group g's tiles are t0 .. t1 - 1
+  // a group's column count is loaded once, when the walk enters the group
+  __device__ void seek(const ExpArgs& a, int tile) {
+    while (tile >= t1 && g + 1 < a.n_groups) {
       ++g;
+      t0 = t1;
+      count = a.grp_count[g];
+      t1 = t0 + (count + kM - 1) / kM;
     }
+  }
+  __device__ int c0(int tile) const { return (tile - t0) * kM; }
+  __device__ int ncols(int tile) const {
+    const int left = count - (tile - t0) * kM;
+    return left < kM ? left : kM;
   }
 };
 
 __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const float* tc_tables) {
-  extern __shared__ unsigned char dyn[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(dyn) + 1023) & ~static_cast<uintptr_t>(1023));
+  extern __shared__ __align__(1024) unsigned char dyn[];
+  unsigned char* sm = dyn;
   const uint32_t s_base = smem_addr(sm);
+  if ((s_base & 1023u) != 0u) {  // not expected: reported as a fault, nothing touched
+    if (threadIdx.x == 0 && a.fault != nullptr) {
+      *reinterpret_cast<volatile unsigned*>(a.fault) = 1u;
+      __threadfence_system();
+    }
+    return;
+  }
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kOffBar);
   uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + kOffMisc);
   volatile int* s_abort = reinterpret_cast<volatile int*>(sm + kOffMisc + 4);
@@ -879,6 +896,10 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     bar_init(&bars[kBarMetaFull1], 32 * kProdWarps);
     bar_init(&bars[kBarMetaFree0], 128);
     bar_init(&bars[kBarMetaFree1], 128);
+    bar_init(&bars[kBarOwnFull0], 32 * kProdWarps);
+    bar_init(&bars[kBarOwnFull1], 32 * kProdWarps);
+    bar_init(&bars[kBarOwnFree0], 128);
+    bar_init(&bars[kBarOwnFree1], 128);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *s_abort = 0;
     *s_res = 0u;
@@ -907,20 +928,27 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     struct Unit {       // a tile as the producers see it
       int ncols, g;     // columns, group
       int qy, qv;       // the record of column p + 11 lane (lane < 12): message pair, other sums
+      float r0, r1;     // warp 8: the group's table maxima of states lane, lane + 32
     };
     TileCursor cur;
-    auto tile_info = [&](int64_t tile) {
+    auto tile_info = [&](int64_t tile64) {
       Unit x;
+      const int tile = (int)tile64;
       cur.seek(a, tile);
       x.g = cur.g;
-      const int64_t c0 = (tile - cur.t0) * kM;
-      const int64_t left = (int64_t)a.grp_count[x.g] - c0;
-      x.ncols = (int)(left < kM ? left : kM);
+      const int64_t c0 = cur.c0(tile);
+      x.ncols = cur.ncols(tile);
       int4 q = make_int4(0, 0, 0, 0);
       if (lane < kColsPerProd && p + kProdWarps * lane < x.ncols)
         q = a.rec[a.grp_first[x.g] + c0 + p + kProdWarps * lane];
       x.qy = q.y;
       x.qv = dir == 0 ? q.w : q.z;
+      x.r0 = x.r1 = 0.0f;
+      if (p == kCvtWarps) {  // this direction's table maxima: r (to variable 1) or c (to 2)
+        const float* mx = tab_g0 + (int64_t)x.g * kTabFloats + 4 * K * K + dir * K;
+        x.r0 = mx[lane];
+        x.r1 = mx[lane + 32];
+      }
       return x;
     };
     // (x - m) / T as div_t computes it, with the power-of-two test made once per kernel
@@ -988,11 +1016,15 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
                 wait(&bars[kBarMma0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort);
       ok = ok && (u < 3 || wait(&bars[kBarMetaFree0 + ((u - 1) & 1)],
                                 (uint32_t)(((u - 3) >> 1) & 1), lim, s_abort));
+      // the slot list of unit u goes where the epilogue read unit u - 2's
+      ok = ok && (u >= n_units || u < 2 ||
+                  wait(&bars[kBarOwnFree0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort));
       if (u < n_units && ok) {
         // half-warp h of the warp takes column p + 11 (2 i + h); lane l16 the 16-byte chunk l16
         // of the other message's row (16-byte aligned: the plan starts such rows at multiples of
         // 4 slots) and of the sums' row when that is aligned too, else four single states
         const int h = lane >> 4, l16 = lane & 15;
+        int* meta_own = reinterpret_cast<int*>(sm + kOffOwn) + b * kM;
 #pragma unroll
         for (int i = 0; i < kColsPerProd / 2; ++i) {
           const int j = 2 * i + h;
@@ -1000,6 +1032,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
           const int qy = __shfl_sync(0xffffffffu, x.qy, j);
           const int qv = __shfl_sync(0xffffffffu, x.qv, j);
           if (c < x.ncols) {
+            if (l16 == 0) meta_own[c] = qy + (dir == 0 ? 0 : K);
             const float* other = a.cur + qy + (dir == 0 ? K : 0);
             const float* sums = a.vsum + qv;
             const uint32_t o = sw128(c, 4 * l16, kM);
@@ -1015,6 +1048,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         }
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
+      if (u < n_units) bar_arrive(&bars[kBarOwnFull0 + b]);
       if (u >= 1) {
         // this thread's copies of unit u - 1 have landed; the barrier makes every thread's
         // visible and, with the and of the waits above, lets the producers leave together
@@ -1032,11 +1066,9 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
           if (t_pow2) convert(std::true_type{}, cbuf, xc.ncols, meta_m);
           else convert(std::false_type{}, cbuf, xc.ncols, meta_m);
         } else if (p == kCvtWarps) {
-          // this direction's table maxima: r (to variable 1) or c (to variable 2)
           float* meta_r = reinterpret_cast<float*>(sm + kOffR) + mb * K;
-          const float* mx = tab_g0 + (int64_t)xc.g * kTabFloats + 4 * K * K + dir * K;
-          meta_r[lane] = mx[lane];
-          meta_r[lane + 32] = mx[lane + 32];
+          meta_r[lane] = xc.r0;
+          meta_r[lane + 32] = xc.r1;
         }
         // the operand's generic-proxy writes become visible to the tensor cores' async proxy
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -1055,7 +1087,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       int64_t last_commit[2] = {-1, -1};
       for (int64_t u = 0; u < n_units; ++u) {
         const int s = (int)(u & 1);
-        cur.seek(a, t_begin + u);
+        cur.seek(a, (int)(t_begin + u));
         if (cur.g != loaded) {
           // the old tables' last reader is the previous unit's products
           if (u >= 1 && !wait(&bars[kBarMma0 + ((u - 1) & 1)], (uint32_t)(((u - 1) >> 1) & 1),
@@ -1105,17 +1137,28 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
     const float tl2 = a.t * 0.693147180559945309f;
     float* stg0 = reinterpret_cast<float*>(sm + kOffStg);
-    TileCursor fcur, cur;
+    TileCursor fcur;
     // the old messages of unit f's columns 32 wq .. 32 wq + 31 into staging buffer f & 1
-    // (cp.async of 16-byte chunks, a half-warp per row); returns the slot of the lane's column
+    // (cp.async of 16-byte chunks, a half-warp per row), at the slots the producers listed;
+    // returns the slot of the lane's column, or -1 when the wait for the list gave up
+    struct EUnit {
+      int own, ncols, c0, g;  // own: the lane's column's slot, -1 when the wait gave up
+    };
     auto fetch = [&](int64_t f) {
-      fcur.seek(a, t_begin + f);
-      const int g = fcur.g;
-      const int64_t c0 = (t_begin + f - fcur.t0) * kM;
-      const int64_t left = (int64_t)a.grp_count[g] - c0;
-      const int ncols = (int)(left < kM ? left : kM);
-      int own = 0;
-      if (e < ncols) own = a.rec[a.grp_first[g] + c0 + e].y + (dir == 0 ? 0 : K);
+      EUnit x;
+      const int tile = (int)(t_begin + f);
+      fcur.seek(a, tile);
+      x.ncols = fcur.ncols(tile);
+      x.c0 = fcur.c0(tile);
+      x.g = fcur.g;
+      const int ncols = x.ncols;
+      const int fs = (int)(f & 1);
+      const bool ok = wait(&bars[kBarOwnFull0 + fs], (uint32_t)((f >> 1) & 1), lim, s_abort, 32);
+      x.own = -1;
+      if (!__all_sync(0xffffffffu, ok)) return x;
+      const int own = e < ncols ? reinterpret_cast<const int*>(sm + kOffOwn)[fs * kM + e] : 0;
+      x.own = own;
+      bar_arrive(&bars[kBarOwnFree0 + fs]);
       float* stg = stg0 + (f & 1) * (kM * K);
 #pragma unroll 4
       for (int i = 0; i < 16; ++i) {
@@ -1129,23 +1172,23 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         }
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
-      return own;
+      return x;
     };
     unsigned res = 0u;
-    int own_next = n_units > 0 ? fetch(0) : 0;
-    for (int64_t u = 0; u < n_units; ++u) {
+    EUnit nx = n_units > 0 ? fetch(0) : EUnit{-1, 0, 0, 0};   // own -1: the CTA is stopping
+    for (int64_t u = 0; u < n_units && nx.own >= 0; ++u) {
       const int s = (int)(u & 1);
-      const int own = own_next;
+      const int own = nx.own, ncols = nx.ncols, g = nx.g;
+      const int64_t c0 = nx.c0;
       if (u + 1 < n_units) {
-        own_next = fetch(u + 1);
+        nx = fetch(u + 1);
+        if (nx.own < 0) {
+          asm volatile("cp.async.wait_all;" ::: "memory");
+          break;
+        }
       } else {
         asm volatile("cp.async.commit_group;" ::: "memory");
       }
-      cur.seek(a, t_begin + u);
-      const int g = cur.g;
-      const int64_t c0 = (t_begin + u - cur.t0) * kM;
-      const int64_t left = (int64_t)a.grp_count[g] - c0;
-      const int ncols = (int)(left < kM ? left : kM);
       const uint32_t ph = (uint32_t)((u >> 1) & 1);
       // a warp leaves together (tcgen05.ld is a warp-wide instruction)
       bool ok = wait(&bars[kBarMetaFull0 + s], ph, lim, s_abort, 32);
@@ -1344,7 +1387,9 @@ cudaError_t expgemm_iterate(const Plan& p, const PairwiseBucket& q, cudaStream_t
   const bool aligned16 =
       q.rows16 && ((reinterpret_cast<uintptr_t>(cur) | reinterpret_cast<uintptr_t>(nxt) |
                     reinterpret_cast<uintptr_t>(vsum)) & 15u) == 0;
-  if (q.n1 == 64 && B == 1 && aligned16 && !knobs.legacy_mma) {
+  // its tile cursor counts tiles and columns in int32
+  const bool small = q.count + (int64_t)q.n_groups * tc::kM < (int64_t)INT32_MAX;
+  if (q.n1 == 64 && B == 1 && aligned16 && small && !knobs.legacy_mma) {
     ProfileScope ps(kProfPairwiseExp, s);
     return launch_tc(p, q, s, a, tables + (int64_t)q.n_groups * expgemm_table_floats(64));
   }
