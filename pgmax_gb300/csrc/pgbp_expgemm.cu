@@ -564,23 +564,27 @@ cudaError_t launch(const Plan& p, const PairwiseBucket& q, cudaStream_t s, const
 //     direction 1: D[c][j] = sum_i W[c][i] E'[j][i], W from variable 1 (the messages to 2).
 //   M = 128 columns, N = 64 states, K = 64 states in 8 steps of 8; three products per step
 //   (hi x hi, hi x lo, lo x hi of the tf32 splits), float32 accumulation in TMEM.
-//   * producer warps 4-14, two steps per unit, the operand double-buffered so that the copies
-//     of unit u are in flight while unit u - 1 is converted and multiplied:
-//       copy u: cp.async of each column's other-edge message into the high part of A buffer
-//       u & 1 and of the other variable's sums into its low part, at the operand positions;
-//       convert u - 1 (after a barrier of the producers): a thread per (column, half of the
-//       states) turns the pair in place into u = exp((vtof - max) / T) split into tf32 parts,
-//       and leaves the column maxima and the group's table maxima for the epilogue;
+//   * producer warps 4-14, two steps per unit, so that the copies of unit u are in flight while
+//     unit u - 1 is converted and unit u - 2 multiplied:
+//       copy u: cp.async of each column's other-edge message and of the other variable's sums
+//       into raw buffer u & 1 (16-byte chunks at the operand's swizzled positions);
+//       convert u - 1: a thread per (column cc, half of the states) in warps 4-11 (the TMEM lane
+//       quadrant of its warp): vtof = sums - message, the column maximum (the two halves swap
+//       theirs through their raw rows), u = exp((vtof - max) / T) split into tf32 high and low
+//       parts stored into TMEM operand buffer (u - 1) & 1 with tcgen05.st; the column maxima and
+//       the group's table maxima are left for the epilogue;
 //   * MMA warp 15: loads the group's two tables of its direction (high and low tf32 parts, built
 //     once per run in the swizzled layout) with one bulk copy when the group changes, then
-//     issues the 24 tcgen05.mma of the unit into TMEM accumulator stage u & 1 and commits them;
+//     issues the 24 tcgen05.mma of the unit (A from TMEM, B from shared memory) into TMEM
+//     accumulator stage u & 1 and commits them;
 //   * epilogue warps 0-3 (a thread per column = TMEM lane): fetch the columns' old messages of
 //     the next unit by cp.async into a staging buffer while this unit is finished: tcgen05.ld of
 //     the sums, log, damping, normalisation, clipping and the residual; the new messages are
 //     written to the staging rows and stored by the warp with lanes across states.
-// Handshakes (mbarriers): a_full[2] (producers -> MMA), mma_done[2] (tcgen05.commit ->
-// producers, epilogue, table reload), tmem_free[2] (epilogue -> MMA), meta_full[2] / meta_free[2]
-// (producers <-> epilogue: column and table maxima). Every wait is bounded; the first that runs
+// Handshakes (mbarriers): raw_full[2] (cp.async completion) / raw_free[2] (conversion done),
+// a_full[2] (producers -> MMA), mma_done[2] (tcgen05.commit -> producers, epilogue, table
+// reload), tmem_free[2] (epilogue -> MMA), meta_full[2] / meta_free[2] (producers <-> epilogue:
+// column and table maxima), own_full[2] / own_free[2] (producers <-> epilogue: message slots). Every wait is bounded; the first that runs
 // out sets a CTA abort flag that ends every other wait, the CTA records the fault and stops, and
 // TMEM is freed after the last committed products have completed.
 namespace tc {
@@ -595,7 +599,10 @@ constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 12 columns 
 constexpr int kCvtWarps = kM / 16;       // producer warps that convert: 16 columns x 2 halves each
 static_assert(kCvtWarps <= kProdWarps, "converting warps");
 static_assert(kColsPerProd % 2 == 0, "producer columns come in half-warp pairs");
-constexpr uint32_t kTmemCols = 128;      // two accumulator stages of 64 fp32 columns
+// tensor memory: accumulator stage s at columns 64 s (0-127); operand buffer b at 128 + 128 b,
+// high part then low part (64 columns each)
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kTmemA = 128;
 // instruction descriptor: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
 // K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(K >> 3) << 17) |
@@ -604,9 +611,9 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(K >
 // shared memory, byte offsets from a 1024-byte aligned base
 constexpr int kMatBytes = K * K * 4;                 // one 64 x 64 tf32 table: 16 KB
 constexpr int kTabBytes = 2 * kMatBytes;             // this direction's table: high, low parts
-constexpr int kABytes = kM * K * 4;                  // one 128 x 64 tf32 matrix: 32 KB
-constexpr int kABufBytes = 2 * kABytes;              // an operand buffer: high part, low part
-constexpr int kOffA = kTabBytes;                     // 2 operand buffers
+constexpr int kABytes = kM * K * 4;                  // one 128 x 64 float matrix: 32 KB
+constexpr int kABufBytes = 2 * kABytes;              // a raw buffer: other messages, sums
+constexpr int kOffA = kTabBytes;                     // 2 raw buffers (swizzled like an operand)
 constexpr int kOffStg = kOffA + 2 * kABufBytes;      // 2 x [kM][K] floats, rows XOR-swizzled
 constexpr int kStgBytes = kM * K * 4;
 constexpr int kOffM = kOffStg + 2 * kStgBytes;       // 2 x [kM] maxima of the other vtof
@@ -615,7 +622,8 @@ constexpr int kOffOwn = kOffR + 2 * K * 4;           // 2 x [kM] slot of each co
 constexpr int kOffBar = kOffOwn + 2 * kM * 4;
 enum { kBarTab = 0, kBarAFull0, kBarAFull1, kBarMma0, kBarMma1, kBarTmem0, kBarTmem1,
        kBarMetaFull0, kBarMetaFull1, kBarMetaFree0, kBarMetaFree1, kBarOwnFull0, kBarOwnFull1,
-       kBarOwnFree0, kBarOwnFree1, kNumBars };
+       kBarOwnFree0, kBarOwnFree1, kBarRawFull0, kBarRawFull1, kBarRawFree0, kBarRawFree1,
+       kNumBars };
 constexpr int kOffMisc = kOffBar + kNumBars * 8;     // TMEM address, abort flags, residual
 constexpr int kSmemBytes = kOffMisc + 16;
 // the dynamic shared memory starts at the CTA's shared window (no static shared memory), which
@@ -652,11 +660,27 @@ __device__ __forceinline__ uint64_t kstep_desc(uint32_t base, int ks, int R) {
   return sdesc(base + (uint32_t)((ks >> 2) * (R * 128) + (ks & 3) * 32));
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+// D (+)= A B^T for one k-step: A in tensor memory (128 lanes = rows, 8 columns = the k-step's
+// elements), B from a shared-memory descriptor, D in tensor memory.
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b,
+                                            uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+
+// 32 consecutive 32-bit columns of the warp's 32 TMEM lanes (thread = lane) from registers.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
+      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
+      "r"(r[29]), "r"(r[30]), "r"(r[31])
       : "memory");
 }
 
@@ -729,6 +753,11 @@ __device__ __forceinline__ float warp_max(float x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x = maxn(x, __shfl_xor_sync(0xffffffffu, x, o));
   return x;
+}
+
+// Named barrier `id` over `count` threads (a multiple of 32).
+__device__ __forceinline__ void named_bar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
 // AND of `pred` over the `count` threads of named barrier `id`; each of them gets the result.
@@ -900,6 +929,10 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     bar_init(&bars[kBarOwnFull1], 32 * kProdWarps);
     bar_init(&bars[kBarOwnFree0], 128);
     bar_init(&bars[kBarOwnFree1], 128);
+    bar_init(&bars[kBarRawFull0], 32 * kProdWarps);   // cp.async completion, one per thread
+    bar_init(&bars[kBarRawFull1], 32 * kProdWarps);
+    bar_init(&bars[kBarRawFree0], 32 * kCvtWarps);
+    bar_init(&bars[kBarRawFree1], 32 * kCvtWarps);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *s_abort = 0;
     *s_res = 0u;
@@ -957,11 +990,16 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       const unsigned ub = __float_as_uint(a.t), eb = (ub >> 23) & 0xffu;
       return (ub & 0x807fffffu) == 0u && eb >= 2u && eb <= 252u;
     }();
-    const int cc = 16 * p + (lane & 15), ch = lane >> 4;
+    // converting warp p (< 8) takes TMEM lane quadrant p % 4 (the one its warp may access):
+    // thread = (column cc = 32 (p % 4) + lane, half ch = p / 4 of the states)
+    const int cc = 32 * (p & 3) + lane, ch = (p >> 2) & 1;
     const uint32_t cvt_off = (uint32_t)(ch * (kM * 128) + cc * 128);
-    // vtof = sums - message of the pair at (cc, ch) of buffer `buf`, its column maximum, and
-    // u = exp((vtof - max) / T) split into tf32 parts written over the pair
-    auto convert = [&](auto pow2, unsigned char* buf, int ncols, float* meta_m) {
+    const uint32_t mx_off = (uint32_t)(cc * 128 + ((cc & 7) << 4));   // chunk 0 of the row
+    // vtof = sums - message of the pair at (cc, ch) of raw buffer `buf`, the column maximum (the
+    // two halves exchange theirs through their rows, dead once read), u = exp((vtof - max) / T)
+    // split into tf32 parts written to TMEM operand buffer `ab`; the raw rows are released
+    auto convert = [&](auto pow2, unsigned char* buf, int ab, int ncols, float* meta_m,
+                       uint64_t* raw_free) {
       float t[32];
       float mx = -INFINITY;
 #pragma unroll
@@ -976,23 +1014,24 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
 #pragma unroll
         for (int q = 0; q < 4; ++q) mx = maxn(mx, t[4 * jj + q]);
       }
-      const float m = maxn(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+      *reinterpret_cast<float*>(buf + ch * (kM * 128) + mx_off) = mx;
+      named_bar_sync(2, 32 * kCvtWarps);
+      const float m = maxn(mx, *reinterpret_cast<const float*>(buf + (ch ^ 1) * (kM * 128) + mx_off));
+      bar_arrive(raw_free);
       const bool act = cc < ncols;
+      uint32_t h[32], l[32];
 #pragma unroll
-      for (int jj = 0; jj < 8; ++jj) {
-        const uint32_t off = cvt_off + (uint32_t)(((jj ^ cc) & 7) << 4);
-        uint32_t h[4], l[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          float z;
-          if constexpr (decltype(pow2)::value) z = (t[4 * jj + q] - m) * t_inv;
-          else z = (t[4 * jj + q] - m) / a.t;
-          split_tf32(__expf(z), h[q], l[q]);
-          if (!act) h[q] = l[q] = 0u;
-        }
-        *reinterpret_cast<uint4*>(buf + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4*>(buf + kABytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
+      for (int k = 0; k < 32; ++k) {
+        float z;
+        if constexpr (decltype(pow2)::value) z = (t[k] - m) * t_inv;
+        else z = (t[k] - m) / a.t;
+        split_tf32(__expf(z), h[k], l[k]);
+        if (!act) h[k] = l[k] = 0u;
       }
+      const uint32_t ta = tmem + ((uint32_t)(32 * (p & 3)) << 16) + kTmemA + (uint32_t)(ab * 128 + 32 * ch);
+      tmem_st32(ta, h);
+      tmem_st32(ta + 64u, l);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       if (ch == 0 && act) meta_m[cc] = m;
     };
     auto cp4 = [&](unsigned char* dst, const float* src) {
@@ -1010,15 +1049,11 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       if (u + 1 < n_units) xn = tile_info(t_begin + u + 1);
       const int b = (int)(u & 1);
       unsigned char* abuf = sm + kOffA + b * kABufBytes;
-      // operand buffer u & 1 was last read by the products of unit u - 2; the maxima slot of
-      // unit u - 1 by the epilogue of unit u - 3
+      // copy u: raw buffer u & 1 was last read by the conversion of unit u - 2, the slot list
+      // ring's entry by the epilogue's fetch of unit u - 2
       bool ok = u >= n_units || u < 2 ||
-                wait(&bars[kBarMma0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort);
-      ok = ok && (u < 3 || wait(&bars[kBarMetaFree0 + ((u - 1) & 1)],
-                                (uint32_t)(((u - 3) >> 1) & 1), lim, s_abort));
-      // the slot list of unit u goes where the epilogue read unit u - 2's
-      ok = ok && (u >= n_units || u < 2 ||
-                  wait(&bars[kBarOwnFree0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort));
+                (wait(&bars[kBarRawFree0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort) &&
+                 wait(&bars[kBarOwnFree0 + b], (uint32_t)(((u - 2) >> 1) & 1), lim, s_abort));
       if (u < n_units && ok) {
         // half-warp h of the warp takes column p + 11 (2 i + h); lane l16 the 16-byte chunk l16
         // of the other message's row (16-byte aligned: the plan starts such rows at multiples of
@@ -1046,14 +1081,23 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
             }
           }
         }
+        // the raw buffer is full once every producer thread's copies have landed
+        asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(
+                         smem_addr(&bars[kBarRawFull0 + b]))
+                     : "memory");
+        bar_arrive(&bars[kBarOwnFull0 + b]);
       }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-      if (u < n_units) bar_arrive(&bars[kBarOwnFull0 + b]);
       if (u >= 1) {
-        // this thread's copies of unit u - 1 have landed; the barrier makes every thread's
-        // visible and, with the and of the waits above, lets the producers leave together
-        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        // convert u - 1: its copies have landed; TMEM operand buffer (u - 1) & 1 was last read
+        // by the products of unit u - 3, the maxima slot by the epilogue of unit u - 3
+        const int mb = (int)((u - 1) & 1);
+        ok = ok && wait(&bars[kBarRawFull0 + mb], (uint32_t)(((u - 1) >> 1) & 1), lim, s_abort);
+        ok = ok && (u < 3 || (wait(&bars[kBarMma0 + mb], (uint32_t)(((u - 3) >> 1) & 1), lim,
+                                   s_abort) &&
+                              wait(&bars[kBarMetaFree0 + mb], (uint32_t)(((u - 3) >> 1) & 1),
+                                   lim, s_abort)));
       }
+      // the producers leave together (the converting warps meet at a named barrier)
       if (!named_bar_and(1, 32 * kProdWarps, ok)) {
         asm volatile("cp.async.wait_all;" ::: "memory");
         break;
@@ -1063,15 +1107,16 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         unsigned char* cbuf = sm + kOffA + mb * kABufBytes;
         float* meta_m = reinterpret_cast<float*>(sm + kOffM) + mb * kM;
         if (p < kCvtWarps) {
-          if (t_pow2) convert(std::true_type{}, cbuf, xc.ncols, meta_m);
-          else convert(std::false_type{}, cbuf, xc.ncols, meta_m);
+          fence_after_sync();
+          if (t_pow2) convert(std::true_type{}, cbuf, mb, xc.ncols, meta_m, &bars[kBarRawFree0 + mb]);
+          else convert(std::false_type{}, cbuf, mb, xc.ncols, meta_m, &bars[kBarRawFree0 + mb]);
         } else if (p == kCvtWarps) {
           float* meta_r = reinterpret_cast<float*>(sm + kOffR) + mb * K;
           meta_r[lane] = xc.r0;
           meta_r[lane + 32] = xc.r1;
         }
-        // the operand's generic-proxy writes become visible to the tensor cores' async proxy
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        // the operand's TMEM writes are ordered before the MMA warp's products
+        fence_before_sync();
         bar_arrive(&bars[kBarAFull0 + mb]);
         bar_arrive(&bars[kBarMetaFull0 + mb]);
       }
@@ -1105,15 +1150,13 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         fence_after_sync();
         const uint32_t d_tmem = tmem + (uint32_t)(s * K);
         const uint32_t b_hi = s_base, b_lo = s_base + (uint32_t)kMatBytes;
-        const uint32_t a_hi = s_base + (uint32_t)(kOffA + s * kABufBytes);
-        const uint32_t a_lo = a_hi + (uint32_t)kABytes;
+        const uint32_t a_hi = tmem + kTmemA + (uint32_t)(s * 128), a_lo = a_hi + 64u;
 #pragma unroll
         for (int ks = 0; ks < K / 8; ++ks) {
-          const uint64_t ah = kstep_desc(a_hi, ks, kM), al = kstep_desc(a_lo, ks, kM);
           const uint64_t bh = kstep_desc(b_hi, ks, K), bl = kstep_desc(b_lo, ks, K);
-          mma_tf32(d_tmem, ah, bh, ks > 0 ? 1u : 0u);
-          mma_tf32(d_tmem, ah, bl, 1u);
-          mma_tf32(d_tmem, al, bh, 1u);
+          mma_tf32_ts(d_tmem, a_hi + 8u * ks, bh, ks > 0 ? 1u : 0u);
+          mma_tf32_ts(d_tmem, a_hi + 8u * ks, bl, 1u);
+          mma_tf32_ts(d_tmem, a_lo + 8u * ks, bh, 1u);
         }
         mma_commit(&bars[kBarMma0 + s]);
         last_commit[s] = u;
