@@ -591,18 +591,19 @@ namespace tc {
 
 constexpr int K = 64;
 constexpr int kM = 128;                  // columns per tile (the MMA's M)
-constexpr int kEpiWarps = 4;             // warps 0-3: thread e of the four = TMEM lane = column e
-constexpr int kProdWarps = 11;           // warps 4-14
-constexpr int kMmaWarp = 15;
-constexpr int kThreads = 32 * 16;        // four warps per SM sub-partition: 128 registers each
+constexpr int kEpiWarps = 8;             // warps 0-7: TMEM lane quadrant w % 4, states 32 (w / 4) ..
+constexpr int kProdWarps = 11;           // warps 8-18
+constexpr int kMmaWarp = 19;
+constexpr int kThreads = 32 * 20;        // five warps per SM sub-partition: 96 registers each
 constexpr int kColsPerProd = (kM + kProdWarps - 1) / kProdWarps;  // 12 columns per producer warp
 constexpr int kCvtWarps = kM / 16;       // producer warps that convert: 16 columns x 2 halves each
 static_assert(kCvtWarps <= kProdWarps, "converting warps");
 static_assert(kColsPerProd % 2 == 0, "producer columns come in half-warp pairs");
 // tensor memory: accumulator stage s at columns 64 s (0-127); operand buffer b at 128 + 128 b,
-// high part then low part (64 columns each)
+// high part then low part (64 columns each); the epilogue's half-row maxima at 384 + 2 s + half
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kTmemA = 128;
+constexpr uint32_t kTmemX = 384;
 // instruction descriptor: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
 // K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(K >> 3) << 17) |
@@ -671,17 +672,21 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, ui
       : "memory");
 }
 
-// 32 consecutive 32-bit columns of the warp's 32 TMEM lanes (thread = lane) from registers.
-__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+// 16 consecutive 32-bit columns of the warp's 32 TMEM lanes (thread = lane) from registers.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
   asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16};" ::"r"(taddr),
       "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
       "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
-      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
-      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
-      "r"(r[29]), "r"(r[30]), "r"(r[31])
+      "r"(r[15])
       : "memory");
+}
+
+// One 32-bit column of the warp's 32 TMEM lanes from a register.
+__device__ __forceinline__ void tmem_st1(uint32_t taddr, uint32_t r) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" ::"r"(taddr), "r"(r)
+               : "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -824,45 +829,12 @@ __device__ __forceinline__ float epi_message(const ExpArgs& a, float tl2, float 
   return __fmaf_rn(a.d, o, a.omd * f);
 }
 
-// The epilogue of one column when some sum (E u) of a lane of the warp fell below 1e-30 or is not
-// a number: those messages are recomputed with the reference's formula (direct_message). Kept out
-// of line so that the common path stays compact. Called by every lane of the warp (it reads TMEM
-// with warp-wide loads); `row` is the lane's staging row (state st in chunk (st / 4) ^ key: the
-// old message in, the new one out). Returns the column's residual.
-__device__ __noinline__ float epilogue_slow(const ExpArgs& a, uint32_t taddr, float* row, int key,
-                                            float mo, const float* rr, bool active, int4 q,
-                                            int64_t table, bool first_edge) {
-  const float tl2 = a.t * 0.693147180559945309f;
-  float y[K];
-  float x = -INFINITY;
-#pragma unroll 1
-  for (int st = 0; st < K; ++st) {
-    const float sum = tmem_ld1(taddr + (uint32_t)st);
-    const float o = row[(((st >> 2) ^ key) << 2) + (st & 3)];
-    float f = 0.0f;
-    if (active) {
-      if (sum >= 1e-30f) {
-        y[st] = epi_message(a, tl2, sum, mo + rr[st], o);
-      } else {
-        f = direct_message<K>(a, q, 0, st, first_edge, table);
-        y[st] = a.d * o + a.omd * f;
-      }
-    } else {
-      y[st] = 0.0f;
-    }
-    x = maxn(x, y[st]);
-  }
-  float dmax = 0.0f;
-  if (active) {
-#pragma unroll 1
-    for (int st = 0; st < K; ++st) {
-      const int at = (((st >> 2) ^ key) << 2) + (st & 3);
-      const float nv = maxn(y[st] - x, kMsgNegInf);
-      dmax = maxn(dmax, fabsf(nv - row[at]));
-      row[at] = nv;
-    }
-  }
-  return dmax;
+// The damped message of state st of a column whose sum E u fell below 1e-30 or is not a number:
+// the reference's formula (direct_message). Out of line, so that the common path stays compact.
+__device__ __noinline__ float epi_message_slow(const ExpArgs& a, int4 q, int st, bool first_edge,
+                                               int64_t table, float o) {
+  const float f = direct_message<K>(a, q, 0, st, first_edge, table);
+  return a.d * o + a.omd * f;
 }
 
 // Tile `tile` of the CTA's walk: its group (cursor g, first tile t0 of g).
@@ -919,16 +891,16 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     bar_init(&bars[kBarAFull1], 32 * kProdWarps);
     bar_init(&bars[kBarMma0], 1);
     bar_init(&bars[kBarMma1], 1);
-    bar_init(&bars[kBarTmem0], 128);
-    bar_init(&bars[kBarTmem1], 128);
+    bar_init(&bars[kBarTmem0], 32 * kEpiWarps);
+    bar_init(&bars[kBarTmem1], 32 * kEpiWarps);
     bar_init(&bars[kBarMetaFull0], 32 * kProdWarps);
     bar_init(&bars[kBarMetaFull1], 32 * kProdWarps);
-    bar_init(&bars[kBarMetaFree0], 128);
-    bar_init(&bars[kBarMetaFree1], 128);
+    bar_init(&bars[kBarMetaFree0], 32 * kEpiWarps);
+    bar_init(&bars[kBarMetaFree1], 32 * kEpiWarps);
     bar_init(&bars[kBarOwnFull0], 32 * kProdWarps);
     bar_init(&bars[kBarOwnFull1], 32 * kProdWarps);
-    bar_init(&bars[kBarOwnFree0], 128);
-    bar_init(&bars[kBarOwnFree1], 128);
+    bar_init(&bars[kBarOwnFree0], 32 * kEpiWarps);
+    bar_init(&bars[kBarOwnFree1], 32 * kEpiWarps);
     bar_init(&bars[kBarRawFull0], 32 * kProdWarps);   // cp.async completion, one per thread
     bar_init(&bars[kBarRawFull1], 32 * kProdWarps);
     bar_init(&bars[kBarRawFree0], 32 * kCvtWarps);
@@ -1019,18 +991,22 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       const float m = maxn(mx, *reinterpret_cast<const float*>(buf + (ch ^ 1) * (kM * 128) + mx_off));
       bar_arrive(raw_free);
       const bool act = cc < ncols;
-      uint32_t h[32], l[32];
+      const uint32_t ta =
+          tmem + ((uint32_t)(32 * (p & 3)) << 16) + kTmemA + (uint32_t)(ab * 128 + 32 * ch);
 #pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        float z;
-        if constexpr (decltype(pow2)::value) z = (t[k] - m) * t_inv;
-        else z = (t[k] - m) / a.t;
-        split_tf32(__expf(z), h[k], l[k]);
-        if (!act) h[k] = l[k] = 0u;
+      for (int k16 = 0; k16 < 2; ++k16) {
+        uint32_t h[16], l[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          float z;
+          if constexpr (decltype(pow2)::value) z = (t[16 * k16 + k] - m) * t_inv;
+          else z = (t[16 * k16 + k] - m) / a.t;
+          split_tf32(__expf(z), h[k], l[k]);
+          if (!act) h[k] = l[k] = 0u;
+        }
+        tmem_st16(ta + 16u * k16, h);
+        tmem_st16(ta + 64u + 16u * k16, l);
       }
-      const uint32_t ta = tmem + ((uint32_t)(32 * (p & 3)) << 16) + kTmemA + (uint32_t)(ab * 128 + 32 * ch);
-      tmem_st32(ta, h);
-      tmem_st32(ta + 64u, l);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       if (ch == 0 && act) meta_m[cc] = m;
     };
@@ -1173,20 +1149,21 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     __syncwarp();
   } else {
     // ------------------------------------------------------------------ epilogue
-    // thread e of warps 0-3 is TMEM lane e = column e of the tile; warp wq owns columns (and
-    // staging rows) 32 wq .. 32 wq + 31, so the warps never wait for one another
-    const int wq = warp, e = threadIdx.x;
-    const int h = lane >> 4, l16 = lane & 15;
-    const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
+    // warp w takes TMEM lane quadrant qd = w % 4 (columns 32 qd .. 32 qd + 31 of the tile, thread
+    // = column e) and states 32 eh .. 32 eh + 31, eh = w / 4; the two warps of a quadrant swap
+    // their half-row maxima through TMEM. Rows are fetched and stored a quarter-warp per row half.
+    const int qd = warp & 3, eh = warp >> 2;
+    const int e = 32 * qd + lane;
+    const int l8 = lane & 7, r4 = lane >> 3;
+    const uint32_t lane_base = (uint32_t)(32 * qd) << 16;
     const float tl2 = a.t * 0.693147180559945309f;
     float* stg0 = reinterpret_cast<float*>(sm + kOffStg);
     TileCursor fcur;
-    // the old messages of unit f's columns 32 wq .. 32 wq + 31 into staging buffer f & 1
-    // (cp.async of 16-byte chunks, a half-warp per row), at the slots the producers listed;
-    // returns the slot of the lane's column, or -1 when the wait for the list gave up
     struct EUnit {
       int own, ncols, c0, g;  // own: the lane's column's slot, -1 when the wait gave up
     };
+    // the old messages (this warp's state half) of unit f's rows into staging buffer f & 1, at
+    // the slots the producers listed
     auto fetch = [&](int64_t f) {
       EUnit x;
       const int tile = (int)(t_begin + f);
@@ -1194,23 +1171,22 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       x.ncols = fcur.ncols(tile);
       x.c0 = fcur.c0(tile);
       x.g = fcur.g;
-      const int ncols = x.ncols;
       const int fs = (int)(f & 1);
       const bool ok = wait(&bars[kBarOwnFull0 + fs], (uint32_t)((f >> 1) & 1), lim, s_abort, 32);
       x.own = -1;
       if (!__all_sync(0xffffffffu, ok)) return x;
-      const int own = e < ncols ? reinterpret_cast<const int*>(sm + kOffOwn)[fs * kM + e] : 0;
-      x.own = own;
+      x.own = e < x.ncols ? reinterpret_cast<const int*>(sm + kOffOwn)[fs * kM + e] : 0;
       bar_arrive(&bars[kBarOwnFree0 + fs]);
-      float* stg = stg0 + (f & 1) * (kM * K);
-#pragma unroll 4
-      for (int i = 0; i < 16; ++i) {
-        const int r = 2 * i + h, c = 32 * wq + r;
-        const int ow = __shfl_sync(0xffffffffu, own, r);
-        if (c < ncols) {
+      float* stg = stg0 + fs * (kM * K);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int r = 4 * i + r4, c = 32 * qd + r;
+        const int ow = __shfl_sync(0xffffffffu, x.own, r);
+        const int q = 8 * eh + l8;
+        if (c < x.ncols) {
           asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                           smem_addr(stg + stg_chunk(c, l16))),
-                       "l"(a.cur + ow + 4 * l16)
+                           smem_addr(stg + stg_chunk(c, q))),
+                       "l"(a.cur + ow + 4 * q)
                        : "memory");
         }
       }
@@ -1218,28 +1194,24 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       return x;
     };
     unsigned res = 0u;
-    EUnit nx = n_units > 0 ? fetch(0) : EUnit{-1, 0, 0, 0};   // own -1: the CTA is stopping
-    for (int64_t u = 0; u < n_units && nx.own >= 0; ++u) {
+    EUnit nx = n_units > 0 ? fetch(0) : EUnit{-1, 0, 0, 0};
+    for (int64_t u = 0; u < n_units; ++u) {
       const int s = (int)(u & 1);
       const int own = nx.own, ncols = nx.ncols, g = nx.g;
       const int64_t c0 = nx.c0;
+      bool ok = own >= 0;
       if (u + 1 < n_units) {
-        nx = fetch(u + 1);
-        if (nx.own < 0) {
-          asm volatile("cp.async.wait_all;" ::: "memory");
-          break;
+        if (ok) {
+          nx = fetch(u + 1);
+          ok = nx.own >= 0;
         }
       } else {
         asm volatile("cp.async.commit_group;" ::: "memory");
       }
       const uint32_t ph = (uint32_t)((u >> 1) & 1);
-      // a warp leaves together (tcgen05.ld is a warp-wide instruction)
-      bool ok = wait(&bars[kBarMetaFull0 + s], ph, lim, s_abort, 32);
+      ok = ok && wait(&bars[kBarMetaFull0 + s], ph, lim, s_abort, 32);
       ok = ok && wait(&bars[kBarMma0 + s], ph, lim, s_abort, 32);
-      if (!__all_sync(0xffffffffu, ok)) {
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        break;
-      }
+      ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-wide
       asm volatile("cp.async.wait_group 1;" ::: "memory");   // this unit's old messages
       __syncwarp();
       fence_after_sync();
@@ -1247,79 +1219,108 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       float* row = stg + e * K;
       const int key = e & 7;
       const float mo = reinterpret_cast<const float*>(sm + kOffM)[s * kM + e];
-      const float* rr = reinterpret_cast<const float*>(sm + kOffR) + s * K;
+      const float* rr = reinterpret_cast<const float*>(sm + kOffR) + s * K + 32 * eh;
       const bool active = e < ncols;
-      // the 64 sums of the column in one batch of TMEM loads, turned into y in place
-      uint32_t raw[K / 16][16];
-#pragma unroll
-      for (int c4 = 0; c4 < K / 16; ++c4)
-        tmem_ld16_nowait(tmem + lane_base + (uint32_t)(s * K + 16 * c4), raw[c4]);
+      // the 32 sums of the half row in one batch of TMEM loads, turned into y in place (after a
+      // failed wait the values are garbage and unused: the CTA stops at the barrier below)
+      uint32_t raw[2][16];
+      const uint32_t tacc = tmem + lane_base + (uint32_t)(s * K + 32 * eh);
+      tmem_ld16_nowait(tacc, raw[0]);
+      tmem_ld16_nowait(tacc + 16u, raw[1]);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      float y[K];
+      float y[32];
 #pragma unroll
-      for (int st = 0; st < K; ++st) y[st] = __uint_as_float(raw[st >> 4][st & 15]);
+      for (int k = 0; k < 32; ++k) y[k] = __uint_as_float(raw[k >> 4][k & 15]);
       float x4[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
       float amin = INFINITY;   // the smallest sum (NaN if any is not a number)
 #pragma unroll
-      for (int q = 0; q < K / 4; ++q) {
-        const float4 o = *reinterpret_cast<const float4*>(row + ((q ^ key) << 2));
-        const float4 r4 = *reinterpret_cast<const float4*>(rr + 4 * q);
-        const float ov[4] = {o.x, o.y, o.z, o.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
+      for (int q = 0; q < 8; ++q) {
+        const float4 o = *reinterpret_cast<const float4*>(row + (((8 * eh + q) ^ key) << 2));
+        const float4 r4v = *reinterpret_cast<const float4*>(rr + 4 * q);
+        const float ov[4] = {o.x, o.y, o.z, o.w}, rv[4] = {r4v.x, r4v.y, r4v.z, r4v.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const int st = 4 * q + k;
-          amin = minn(amin, y[st]);
-          y[st] = epi_message(a, tl2, y[st], mo + rv[k], ov[k]);
-          x4[k] = maxn(x4[k], y[st]);
+          const int j = 4 * q + k;
+          amin = minn(amin, y[j]);
+          y[j] = epi_message(a, tl2, y[j], mo + rv[k], ov[k]);
         }
       }
-      const float x = maxn(maxn(x4[0], x4[1]), maxn(x4[2], x4[3]));
-      const bool slow = __any_sync(0xffffffffu, active && !(amin >= 1e-30f));
-      float dmax = 0.0f;
-      if (slow) {  // rare: a table row spanning more than about 69 T underflowed somewhere
+      if (__any_sync(0xffffffffu, active && !(amin >= 1e-30f))) {
+        // rare: a table row spanning more than about 69 T underflowed somewhere in the warp;
+        // those states take the reference's formula
         const int4 qr = active ? a.rec[a.grp_first[g] + c0 + e] : make_int4(0, 0, 0, 0);
-        dmax = epilogue_slow(a, tmem + lane_base + (uint32_t)(s * K), row, key, mo, rr, active,
-                             qr, a.grp_table[g], dir == 0);
-        fence_before_sync();
-        bar_arrive(&bars[kBarTmem0 + s]);
-        bar_arrive(&bars[kBarMetaFree0 + s]);
-      } else {
-        fence_before_sync();
-        bar_arrive(&bars[kBarTmem0 + s]);
-        bar_arrive(&bars[kBarMetaFree0 + s]);
-        if (active) {
 #pragma unroll
-          for (int q4 = 0; q4 < K / 16; ++q4) {
-            float4 o[4];
+        for (int j = 0; j < 32; ++j) {
+          const float sum = tmem_ld1(tacc + (uint32_t)j);
+          if (active && !(sum >= 1e-30f)) {
+            const int st = 32 * eh + j;
+            y[j] = epi_message_slow(a, qr, st, dir == 0, a.grp_table[g],
+                                    row[(((st >> 2) ^ key) << 2) + (st & 3)]);
+          }
+        }
+      }
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-              o[k] = *reinterpret_cast<const float4*>(row + (((4 * q4 + k) ^ key) << 2));
+      for (int j = 0; j < 32; ++j) x4[j & 3] = maxn(x4[j & 3], y[j]);
+      const float xh = maxn(maxn(x4[0], x4[1]), maxn(x4[2], x4[3]));
+      // swap the half-row maxima with the other warp of the quadrant; the epilogue warps leave
+      // together here (the barrier ends the unit's waits)
+      tmem_st1(tmem + lane_base + kTmemX + (uint32_t)(2 * s + eh), __float_as_uint(xh));
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      fence_before_sync();
+      if (!named_bar_and(3, 32 * kEpiWarps, ok)) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        break;
+      }
+      fence_after_sync();
+      const float x = maxn(xh, __uint_as_float([&] {
+        uint32_t r;
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];"
+                     : "=r"(r)
+                     : "r"(tmem + lane_base + kTmemX + (uint32_t)(2 * s + (eh ^ 1))));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        return r;
+      }()));
+      fence_before_sync();
+      bar_arrive(&bars[kBarTmem0 + s]);
+      bar_arrive(&bars[kBarMetaFree0 + s]);
+      float dmax = 0.0f;
+      if (active) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int st = 16 * q4 + 4 * k;
-              float4 nv;
-              nv.x = maxn(y[st + 0] - x, kMsgNegInf);
-              nv.y = maxn(y[st + 1] - x, kMsgNegInf);
-              nv.z = maxn(y[st + 2] - x, kMsgNegInf);
-              nv.w = maxn(y[st + 3] - x, kMsgNegInf);
-              dmax = maxn(dmax, fabsf(nv.x - o[k].x));
-              dmax = maxn(dmax, fabsf(nv.y - o[k].y));
-              dmax = maxn(dmax, fabsf(nv.z - o[k].z));
-              dmax = maxn(dmax, fabsf(nv.w - o[k].w));
-              *reinterpret_cast<float4*>(row + (((4 * q4 + k) ^ key) << 2)) = nv;
-            }
+        for (int q4 = 0; q4 < 2; ++q4) {
+          float4 o[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            o[k] = *reinterpret_cast<const float4*>(row + (((8 * eh + 4 * q4 + k) ^ key) << 2));
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int j = 16 * q4 + 4 * k;
+            float4 nv;
+            nv.x = maxn(y[j + 0] - x, kMsgNegInf);
+            nv.y = maxn(y[j + 1] - x, kMsgNegInf);
+            nv.z = maxn(y[j + 2] - x, kMsgNegInf);
+            nv.w = maxn(y[j + 3] - x, kMsgNegInf);
+            dmax = maxn(dmax, fabsf(nv.x - o[k].x));
+            dmax = maxn(dmax, fabsf(nv.y - o[k].y));
+            dmax = maxn(dmax, fabsf(nv.z - o[k].z));
+            dmax = maxn(dmax, fabsf(nv.w - o[k].w));
+            *reinterpret_cast<float4*>(row + (((8 * eh + 4 * q4 + k) ^ key) << 2)) = nv;
           }
         }
       }
       __syncwarp();
-      // the new rows to their slots, a half-warp per row, 16-byte stores
-#pragma unroll 4
-      for (int i = 0; i < 16; ++i) {
-        const int r = 2 * i + h, c = 32 * wq + r;
-        const int ow = __shfl_sync(0xffffffffu, own, r);
-        if (c < ncols)
-          *reinterpret_cast<float4*>(a.nxt + ow + 4 * l16) =
-              *reinterpret_cast<const float4*>(stg + stg_chunk(c, l16));
+      // the new half rows to their slots, a quarter-warp per row, 16-byte stores
+      {
+        float4 v[8];
+        const int q = 8 * eh + l8;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          v[i] = *reinterpret_cast<const float4*>(stg + stg_chunk(32 * qd + 4 * i + r4, q));
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int r = 4 * i + r4, c = 32 * qd + r;
+          const int ow = __shfl_sync(0xffffffffu, own, r);
+          if (c < ncols) *reinterpret_cast<float4*>(a.nxt + ow + 4 * q) = v[i];
+        }
       }
       __syncwarp();   // the rows are read before the next fetch into this buffer
       res = __float_as_uint(maxn(__uint_as_float(res), dmax));
