@@ -48,6 +48,13 @@ __device__ __forceinline__ float maxn(float a, float b) {
   return r;
 }
 
+// 2^x, PTX ex2.approx (flushes subnormal results to zero; -inf gives 0).
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 __device__ __forceinline__ float minn(float a, float b) {
   float r;
   asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
@@ -821,12 +828,12 @@ __device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
   return __uint_as_float(r);
 }
 
-// The epilogue's message for state st from the sum E u (>= 1e-30): f = T log(sum) + max of the
-// other vtof + table maximum, damped with the old message o.
-__device__ __forceinline__ float epi_message(const ExpArgs& a, float tl2, float sum, float mo_rr,
-                                             float o) {
-  const float f = __fmaf_rn(tl2, __log2f(sum), mo_rr);
-  return __fmaf_rn(a.d, o, a.omd * f);
+// The epilogue's damped message for a state from the sum E u (>= 1e-30): d o + (1 - d) f with
+// f = T log(sum) + max of the other vtof + table maximum, as
+// fma(d, o, fma((1 - d) T ln 2, log2(sum), (1 - d) max + (1 - d) table maximum)).
+__device__ __forceinline__ float epi_message(const ExpArgs& a, float atl2, float sum,
+                                             float omd_mo_rr, float o) {
+  return __fmaf_rn(a.d, o, __fmaf_rn(atl2, __log2f(sum), omd_mo_rr));
 }
 
 // The damped message of state st of a column whose sum E u fell below 1e-30 or is not a number:
@@ -956,12 +963,8 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       }
       return x;
     };
-    // (x - m) / T as div_t computes it, with the power-of-two test made once per kernel
-    const float t_inv = __uint_as_float((254u - ((__float_as_uint(a.t) >> 23) & 0xffu)) << 23);
-    const bool t_pow2 = [&] {
-      const unsigned ub = __float_as_uint(a.t), eb = (ub >> 23) & 0xffu;
-      return (ub & 0x807fffffu) == 0u && eb >= 2u && eb <= 252u;
-    }();
+    // u = exp((t - m) / T) = 2^(t c2 - m c2), c2 = log2(e) / T: one fma and ex2.approx
+    const float c2 = 1.4426950408889634f / a.t;
     // converting warp p (< 8) takes TMEM lane quadrant p % 4 (the one its warp may access):
     // thread = (column cc = 32 (p % 4) + lane, half ch = p / 4 of the states)
     const int cc = 32 * (p & 3) + lane, ch = (p >> 2) & 1;
@@ -970,7 +973,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     // vtof = sums - message of the pair at (cc, ch) of raw buffer `buf`, the column maximum (the
     // two halves exchange theirs through their rows, dead once read), u = exp((vtof - max) / T)
     // split into tf32 parts written to TMEM operand buffer `ab`; the raw rows are released
-    auto convert = [&](auto pow2, unsigned char* buf, int ab, int ncols, float* meta_m,
+    auto convert = [&](unsigned char* buf, int ab, int ncols, float* meta_m,
                        uint64_t* raw_free) {
       float t[32];
       float mx = -INFINITY;
@@ -991,6 +994,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       const float m = maxn(mx, *reinterpret_cast<const float*>(buf + (ch ^ 1) * (kM * 128) + mx_off));
       bar_arrive(raw_free);
       const bool act = cc < ncols;
+      const float mc2 = -m * c2;
       const uint32_t ta =
           tmem + ((uint32_t)(32 * (p & 3)) << 16) + kTmemA + (uint32_t)(ab * 128 + 32 * ch);
 #pragma unroll
@@ -998,11 +1002,8 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         uint32_t h[16], l[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-          float z;
-          if constexpr (decltype(pow2)::value) z = (t[16 * k16 + k] - m) * t_inv;
-          else z = (t[16 * k16 + k] - m) / a.t;
-          split_tf32(__expf(z), h[k], l[k]);
-          if (!act) h[k] = l[k] = 0u;
+          const float z = act ? __fmaf_rn(t[16 * k16 + k], c2, mc2) : -INFINITY;
+          split_tf32(ex2_approx(z), h[k], l[k]);   // a column past the tile's end: zeros
         }
         tmem_st16(ta + 16u * k16, h);
         tmem_st16(ta + 64u + 16u * k16, l);
@@ -1084,12 +1085,12 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         float* meta_m = reinterpret_cast<float*>(sm + kOffM) + mb * kM;
         if (p < kCvtWarps) {
           fence_after_sync();
-          if (t_pow2) convert(std::true_type{}, cbuf, mb, xc.ncols, meta_m, &bars[kBarRawFree0 + mb]);
-          else convert(std::false_type{}, cbuf, mb, xc.ncols, meta_m, &bars[kBarRawFree0 + mb]);
+          convert(cbuf, mb, xc.ncols, meta_m, &bars[kBarRawFree0 + mb]);
         } else if (p == kCvtWarps) {
+          // the table maxima, times 1 - damping
           float* meta_r = reinterpret_cast<float*>(sm + kOffR) + mb * K;
-          meta_r[lane] = xc.r0;
-          meta_r[lane + 32] = xc.r1;
+          meta_r[lane] = a.omd * xc.r0;
+          meta_r[lane + 32] = a.omd * xc.r1;
         }
         // the operand's TMEM writes are ordered before the MMA warp's products
         fence_before_sync();
@@ -1156,7 +1157,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
     const int e = 32 * qd + lane;
     const int l8 = lane & 7, r4 = lane >> 3;
     const uint32_t lane_base = (uint32_t)(32 * qd) << 16;
-    const float tl2 = a.t * 0.693147180559945309f;
+    const float atl2 = a.omd * a.t * 0.693147180559945309f;
     float* stg0 = reinterpret_cast<float*>(sm + kOffStg);
     TileCursor fcur;
     struct EUnit {
@@ -1218,7 +1219,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       float* stg = stg0 + s * (kM * K);
       float* row = stg + e * K;
       const int key = e & 7;
-      const float mo = reinterpret_cast<const float*>(sm + kOffM)[s * kM + e];
+      const float mo = a.omd * reinterpret_cast<const float*>(sm + kOffM)[s * kM + e];
       const float* rr = reinterpret_cast<const float*>(sm + kOffR) + s * K + 32 * eh;
       const bool active = e < ncols;
       // the 32 sums of the half row in one batch of TMEM loads, turned into y in place (after a
@@ -1242,7 +1243,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
         for (int k = 0; k < 4; ++k) {
           const int j = 4 * q + k;
           amin = minn(amin, y[j]);
-          y[j] = epi_message(a, tl2, y[j], mo + rv[k], ov[k]);
+          y[j] = epi_message(a, atl2, y[j], mo + rv[k], ov[k]);
         }
       }
       if (__any_sync(0xffffffffu, active && !(amin >= 1e-30f))) {
