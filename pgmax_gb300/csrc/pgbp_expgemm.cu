@@ -833,7 +833,9 @@ __device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
 // fma(d, o, fma((1 - d) T ln 2, log2(sum), (1 - d) max + (1 - d) table maximum)).
 __device__ __forceinline__ float epi_message(const ExpArgs& a, float atl2, float sum,
                                              float omd_mo_rr, float o) {
-  return __fmaf_rn(a.d, o, __fmaf_rn(atl2, __log2f(sum), omd_mo_rr));
+  float lg;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(lg) : "f"(sum));   // sum is normal on this path
+  return __fmaf_rn(a.d, o, __fmaf_rn(atl2, lg, omd_mo_rr));
 }
 
 // The damped message of state st of a column whose sum E u fell below 1e-30 or is not a number:
@@ -1228,6 +1230,13 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       const uint32_t tacc = tmem + lane_base + (uint32_t)(s * K + 32 * eh);
       tmem_ld16_nowait(tacc, raw[0]);
       tmem_ld16_nowait(tacc + 16u, raw[1]);
+      // the first half's old messages and maxima load while the TMEM loads are in flight
+      float4 o4[4], rm4[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        o4[q] = *reinterpret_cast<const float4*>(row + (((8 * eh + q) ^ key) << 2));
+        rm4[q] = *reinterpret_cast<const float4*>(rr + 4 * q);
+      }
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       float y[32];
 #pragma unroll
@@ -1235,15 +1244,24 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
       float x4[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
       float amin = INFINITY;   // the smallest sum (NaN if any is not a number)
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float4 o = *reinterpret_cast<const float4*>(row + (((8 * eh + q) ^ key) << 2));
-        const float4 r4v = *reinterpret_cast<const float4*>(rr + 4 * q);
-        const float ov[4] = {o.x, o.y, o.z, o.w}, rv[4] = {r4v.x, r4v.y, r4v.z, r4v.w};
+      for (int h2 = 0; h2 < 2; ++h2) {
+        if (h2 == 1) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int j = 4 * q + k;
-          amin = minn(amin, y[j]);
-          y[j] = epi_message(a, atl2, y[j], mo + rv[k], ov[k]);
+          for (int q = 0; q < 4; ++q) {
+            o4[q] = *reinterpret_cast<const float4*>(row + (((8 * eh + 4 + q) ^ key) << 2));
+            rm4[q] = *reinterpret_cast<const float4*>(rr + 16 + 4 * q);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float ov[4] = {o4[q].x, o4[q].y, o4[q].z, o4[q].w};
+          const float rv[4] = {rm4[q].x, rm4[q].y, rm4[q].z, rm4[q].w};
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int j = 16 * h2 + 4 * q + k;
+            amin = minn(amin, y[j]);
+            y[j] = epi_message(a, atl2, y[j], mo + rv[k], ov[k]);
+          }
         }
       }
       if (__any_sync(0xffffffffu, active && !(amin >= 1e-30f))) {
@@ -1263,12 +1281,13 @@ __global__ void __launch_bounds__(kThreads, 1) pairwise_kernel(ExpArgs a, const 
 #pragma unroll
       for (int j = 0; j < 32; ++j) x4[j & 3] = maxn(x4[j & 3], y[j]);
       const float xh = maxn(maxn(x4[0], x4[1]), maxn(x4[2], x4[3]));
-      // swap the half-row maxima with the other warp of the quadrant; the epilogue warps leave
-      // together here (the barrier ends the unit's waits)
+      // swap the half-row maxima with the other warp of the quadrant (barrier 3 + quadrant, the
+      // two warps); they leave together here (the barrier ends the unit's waits); a pair that
+      // stops leaves the others' waits for its arrivals to run out and stop them too
       tmem_st1(tmem + lane_base + kTmemX + (uint32_t)(2 * s + eh), __float_as_uint(xh));
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       fence_before_sync();
-      if (!named_bar_and(3, 32 * kEpiWarps, ok)) {
+      if (!named_bar_and(3 + qd, 64, ok)) {
         asm volatile("cp.async.wait_all;" ::: "memory");
         break;
       }
