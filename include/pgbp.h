@@ -129,8 +129,6 @@ typedef struct {
   int64_t device_bytes;          /* device memory owned by the plan */
   int64_t num_slots;             /* message slots per instance: 1 per binary edge, else 1 per state */
   int64_t small_graph_smem_bytes; /* shared memory of the one-CTA-per-instance path, 0 if unused */
-  int64_t num_fused_rows;        /* rows of a 2 x 2 bucket whose first variables' sums the factor
-                                    pass forms (runs with a batch that is a multiple of 32) */
 } pgbp_plan_info;
 
 /* Compiles the wiring into device-resident schedules on `device`. Validates every index. */
@@ -412,14 +410,10 @@ int pgbp_wait_timeouts(int64_t* count);
  *                                nothing in flight (tests the timeout path); 0: normal
  *   PGBP_DEBUG_LEGACY_MMA        1: shared 64 x 64 tables of a single instance run on the
  *                                warp-level mma.sync kernel instead of the tcgen05 one (for
- *                                comparison); 0: normal
- *   PGBP_DEBUG_NO_ROWS           1: binary pairwise rows whose first variables' sums the factor
- *                                pass forms itself go through the variable-sum pass instead
- *                                (bit-identical results; for comparison); 0: normal */
+ *                                comparison); 0: normal */
 #define PGBP_DEBUG_WAIT_LIMIT_NS 1
 #define PGBP_DEBUG_SKIP_TABLE_COPY 2
 #define PGBP_DEBUG_LEGACY_MMA 3
-#define PGBP_DEBUG_NO_ROWS 4
 int pgbp_debug_set(int knob, int64_t value);
 
 const char* pgbp_last_error(void);

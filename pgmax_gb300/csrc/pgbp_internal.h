@@ -152,20 +152,6 @@ struct Plan {
   std::vector<EnergySeg> energy_segs;
   int64_t energy_chunks = 0;
   VarsumSet varsum_binary, varsum_other;
-  // Rows of a dense 2 x 2 bucket whose first variables' sums the factor pass itself can form
-  // (pairwise22_rows_kernel): row r = the bucket's records u0[r] .. u0[r + 1] - 1, all with first
-  // variable state vs[r], whose slot list in edge order is pre_slots[pre_off[r] ..
-  // pre_off[r + 1]) (edges of generic Enum factors, updated before the rows) followed by the
-  // records' first-edge slots. varsum_binary_rest: the binary variables that are no row's.
-  struct FusedRows {
-    int64_t count = 0;
-    int bucket = -1;
-    int32_t* vs = nullptr;
-    int32_t* u0 = nullptr;
-    int32_t* pre_off = nullptr;
-    int32_t* pre_slots = nullptr;
-  } rows;
-  VarsumSet varsum_binary_rest;
   std::vector<PairwiseBucket> pairwise;
   EnumGeneric enum_generic;
   LogicalSet logical[2];
@@ -230,7 +216,6 @@ struct DebugKnobs {
   unsigned long long wait_limit_ns = 0;
   int skip_table_copy = 0;
   int legacy_mma = 0;  // K = 64 at B = 1 on the mma.sync kernel instead of the tcgen05 one
-  int no_rows = 0;     // binary pairwise rows through the variable-sum pass, not fused
 };
 DebugKnobs debug_knobs();
 
@@ -355,22 +340,6 @@ __device__ __forceinline__ void pdl_begin() {
 
 // Launches `kernel` (which must begin with pdl_begin()) as a programmatic dependent of the
 // previous kernel in stream s.
-template <class... KArgs, class... Args>
-void launch_pdl_smem(cudaStream_t s, dim3 grid, dim3 block, size_t smem,
-                     void (*kernel)(KArgs...), Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
 template <class... KArgs, class... Args>
 void launch_pdl(cudaStream_t s, dim3 grid, dim3 block, void (*kernel)(KArgs...), Args... args) {
   cudaLaunchConfig_t cfg = {};

@@ -27,7 +27,6 @@
 #include <math.h>
 
 #include <algorithm>
-#include <utility>
 #include <type_traits>
 
 #include "pgbp_gumbel.h"
@@ -919,192 +918,6 @@ __global__ void __launch_bounds__(256, 4) pairwise22_x4_kernel(Fused c, Pairwise
   block_max4_to(deltas, l, dm);
 }
 
-// ----------------------------------------------------------------------------- fused rows
-// A dense 2 x 2 bucket whose factors come in rows of one first variable (Plan::rows, e.g. an
-// RBM's hidden variables, each with its 784 factors in a row): one CTA per (row, block of T
-// instances) walks the row's factors in order and, besides the new messages, forms the first
-// variable's sums for the next iteration: evidence, the new messages of its generic Enum edges
-// (updated earlier in the iteration), then each new message to it in edge order, the same float
-// additions in the same order as varsum_binary_unit, so the variable-sum pass skips that
-// variable. The rows' messages and the other variables' sums stream through a 3-stage
-// shared-memory ring, 8 factors per stage, filled by bulk copies (cp.async.bulk, completion on
-// an mbarrier) that lanes 0-7 of warp 0 issue two stages ahead, with each factor's record and
-// potentials. Every wait is bounded; one that runs out stops the CTA after its copies in flight
-// have landed and sets the plan's fault word.
-constexpr int kRowChunk = 8;
-constexpr int kRowStages = 3;
-
-struct RowsDev {
-  const int32_t* __restrict__ vs;
-  const int32_t* __restrict__ u0;
-  const int32_t* __restrict__ pre_off;
-  const int32_t* __restrict__ pre_slots;
-};
-
-__device__ __forceinline__ uint32_t rows_saddr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ bool rows_wait(uint64_t* bar, uint32_t parity,
-                                          unsigned long long limit_ns, volatile int* abort) {
-  const uint32_t addr = rows_saddr(bar);
-  uint64_t t0 = 0;
-  for (uint32_t i = 0;; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((i & 15) == 0) {
-      if (abort != nullptr && *abort) return false;
-      uint64_t now;
-      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-      if (t0 == 0) {
-        t0 = now;
-      } else if (now - t0 > limit_ns) {
-        if (abort != nullptr) *abort = 1;
-        return false;
-      }
-    }
-  }
-}
-
-template <bool T0>
-__global__ void __launch_bounds__(128, 4) pairwise22_rows_kernel(
-    Fused c, RowsDev r, PairwiseDev pw, float t, unsigned* deltas, float* __restrict__ vsum_next,
-    const float* __restrict__ ev, int64_t evs, int64_t evb, unsigned long long wait_ns,
-    unsigned* fault) {
-  pdl_begin();
-  extern __shared__ __align__(16) unsigned char rsm[];
-  const int T = (int)blockDim.x;
-  const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t B = c.B, row = blockIdx.x, b0 = (int64_t)blockIdx.y * T, b = b0 + tid;
-  const size_t data_bytes = (size_t)kRowChunk * 4 * T * sizeof(float);
-  const size_t stage_bytes = data_bytes + kRowChunk * 32;  // + records and potentials
-  uint64_t* bars = reinterpret_cast<uint64_t*>(rsm + kRowStages * stage_bytes);
-  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + kRowStages);
-  const int u0 = __ldg(r.u0 + row), n = __ldg(r.u0 + row + 1) - u0;
-  const int chunks = (n + kRowChunk - 1) / kRowChunk;
-  if (tid == 0) {
-    for (int st = 0; st < kRowStages; ++st)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(rows_saddr(&bars[st])) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    *s_abort = 0;
-  }
-  __syncthreads();
-
-  // lanes 0-7 of warp 0 keep the record, first potential and potentials of factor `lane` of the
-  // next chunk to issue (loaded one chunk ahead)
-  int4 q_n = make_int4(0, 0, 0, 0);
-  float4 p_n = make_float4(0.f, 0.f, 0.f, 0.f);
-  auto prefetch = [&](int ch) {
-    const int j = ch * kRowChunk + lane;
-    if (warp == 0 && lane < kRowChunk && ch < chunks && j < n) {
-      q_n = __ldg(pw.rec + u0 + j);
-      const int64_t k0 = __ldg(pw.cfg_begin + u0 + j);
-      if ((k0 & 3) == 0) {
-        p_n = __ldg(reinterpret_cast<const float4*>(c.lp + k0));
-      } else {
-        p_n = make_float4(__ldg(c.lp + k0), __ldg(c.lp + k0 + 1), __ldg(c.lp + k0 + 2),
-                          __ldg(c.lp + k0 + 3));
-      }
-    }
-  };
-  // chunk ch into stage ch % 3 (warp 0): the four rows of each factor's T instances
-  auto issue = [&](int ch) {
-    const int st = ch % kRowStages;
-    unsigned char* base = rsm + st * stage_bytes;
-    const int nf = min(kRowChunk, n - ch * kRowChunk);
-    if (lane < nf) {
-      reinterpret_cast<int4*>(base + data_bytes)[lane] = q_n;
-      reinterpret_cast<float4*>(base + data_bytes + kRowChunk * 16)[lane] = p_n;
-    }
-    const int4 q = q_n;
-    __syncwarp();
-    const uint32_t bar = rows_saddr(&bars[st]);
-    if (lane == 0)
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                   "r"((uint32_t)(nf * 4 * T * sizeof(float)))
-                   : "memory");
-    __syncwarp();
-    if (lane < nf) {
-      float* d = reinterpret_cast<float*>(base) + (size_t)lane * 4 * T;
-      const float* src[4] = {c.cur + (int64_t)q.y * B + b0, c.cur + ((int64_t)q.y + 1) * B + b0,
-                             c.vsum + (int64_t)q.w * B + b0, c.vsum + ((int64_t)q.w + 1) * B + b0};
-      // the two message rows (slots q.y, q.y + 1) and the two sum rows (states q.w, q.w + 1)
-      // are adjacent: with the whole batch in one CTA, one copy each
-      const int parts = T == B ? 2 : 4;
-      const uint32_t bytes = (uint32_t)((4 / parts) * T * sizeof(float));
-      for (int k = 0; k < parts; ++k)
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-            "[%3];" ::"r"(rows_saddr(d + k * (4 / parts) * T)),
-            "l"(src[k * (4 / parts)]), "r"(bytes), "r"(bar)
-            : "memory");
-    }
-    prefetch(ch + 1);
-  };
-
-  const int64_t v1 = __ldg(r.vs + row);
-  const float a0 = c.vsum[v1 * B + b], a1 = c.vsum[(v1 + 1) * B + b];
-  float s0 = ev[v1 * evs + b * evb], s1 = ev[(v1 + 1) * evs + b * evb];
-  for (int k = __ldg(r.pre_off + row); k < __ldg(r.pre_off + row + 1); ++k) {
-    float m0, m1;
-    decode2(c.nxt[(int64_t)__ldg(r.pre_slots + k) * B + b], m0, m1);
-    s0 += m0;
-    s1 += m1;
-  }
-  float dm = 0.0f;
-  prefetch(0);
-  if (warp == 0)
-    for (int ch = 0; ch < kRowStages - 1 && ch < chunks; ++ch) issue(ch);
-  int done = 0;
-  for (int ch = 0; ch < chunks; ++ch) {
-    const int st = ch % kRowStages;
-    const bool ok = rows_wait(&bars[st], (uint32_t)((ch / kRowStages) & 1), wait_ns, s_abort);
-    // every thread is done with chunk ch - 1, whose stage the next issue refills
-    if (__syncthreads_or(!ok)) break;
-    if (warp == 0 && ch + kRowStages - 1 < chunks) issue(ch + kRowStages - 1);
-    const unsigned char* base = rsm + st * stage_bytes;
-    const float* dat = reinterpret_cast<const float*>(base);
-    const int4* recs = reinterpret_cast<const int4*>(base + data_bytes);
-    const float4* pots = reinterpret_cast<const float4*>(base + data_bytes + kRowChunk * 16);
-    const int nf = min(kRowChunk, n - ch * kRowChunk);
-    for (int j = 0; j < nf; ++j) {
-      const float* dj = dat + (size_t)j * 4 * T;
-      const int4 q = recs[j];
-      const float4 pp = pots[j];
-      float n1, n2;
-      pair22<T0>(dj[tid], dj[T + tid], a0, a1, dj[2 * T + tid], dj[3 * T + tid], pp.x, pp.y,
-                 pp.z, pp.w, t, c.d, c.omd, n1, n2, dm);
-      c.nxt[(int64_t)q.y * B + b] = n1;
-      c.nxt[((int64_t)q.y + 1) * B + b] = n2;
-      float m0, m1;
-      decode2(n1, m0, m1);
-      s0 += m0;
-      s1 += m1;
-    }
-    done = ch + 1;
-  }
-  if (done == chunks) {
-    vsum_next[v1 * B + b] = s0;
-    vsum_next[(v1 + 1) * B + b] = s1;
-    if (deltas != nullptr) atomicMax(deltas + b, __float_as_uint(dm));
-  } else if (tid == 0) {
-    // stopped: the copies already issued land (bounded wait) before the CTA leaves
-    const int issued = min(chunks, done + kRowStages - 1);
-    for (int ch = done; ch < issued; ++ch)
-      rows_wait(&bars[ch % kRowStages], (uint32_t)((ch / kRowStages) & 1), wait_ns, nullptr);
-    if (fault != nullptr) {
-      *reinterpret_cast<volatile unsigned*>(fault) = 1u;
-      __threadfence_system();
-    }
-  }
-}
-
 // ----------------------------------------------------------------------------- variable sums
 // var_sums = evidence.at[var_states_for_edge_states].add(msgs) (bp.py:217): serial per variable
 // state over its edge states in increasing order. Binary variables read one compressed slot per
@@ -1859,10 +1672,9 @@ VarsumDev dev(const VarsumSet& v) {
 // built; -1 the rule: by variable when built)
 void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, const float* ev,
                    int64_t evs, int64_t evb, float* vsum, int vb_variant = -1,
-                   int vo_variant = -1, const VarsumSet* vb_set = nullptr) {
+                   int vo_variant = -1) {
   ProfileScope ps(kProfVarsum, s);
-  // vb_set: the binary variables to sum (default: all of them)
-  const VarsumSet& vb = vb_set != nullptr ? *vb_set : p.varsum_binary;
+  const VarsumSet& vb = p.varsum_binary;
   // 4 instances per thread only when that still leaves >= 16 warps per SM: the per-variable sums
   // are serial chains, so latency is hidden by warps, not by the work inside one thread
   const bool x4 = B % 4 == 0 && (vb_variant >= 0 ? vb_variant == 1
@@ -1887,30 +1699,6 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
     launch_pdl(s, l.grid, l.block, varsum_other_kernel, dev(vo), vo.use_runs, cur, ev, evs, evb,
                vsum, B);
   }
-}
-
-// The fused rows of bucket q (Plan::rows): the whole batch in one CTA per row up to 128
-// instances (each factor's rows in two bulk copies), else 64 or 32 instances per CTA.
-template <bool T0>
-void launch_rows(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const Fused& c,
-                 int64_t B, float t, unsigned* d, float* vsum_next, const float* ev, int64_t evs,
-                 int64_t evb) {
-  ProfileScope ps(kProfPairwise, s);
-  const int T = B <= 128 ? (int)B : B % 128 == 0 ? 128 : B % 64 == 0 ? 64 : 32;
-  const size_t smem = (size_t)kRowStages * ((size_t)kRowChunk * 4 * T * sizeof(float) +
-                                            kRowChunk * 32) +
-                      kRowStages * sizeof(uint64_t) + sizeof(int);
-  static const cudaError_t attr = cudaFuncSetAttribute(
-      pairwise22_rows_kernel<T0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      (int)((size_t)kRowStages * ((size_t)kRowChunk * 4 * 128 * sizeof(float) + kRowChunk * 32) +
-            kRowStages * sizeof(uint64_t) + sizeof(int)));
-  (void)attr;
-  const RowsDev rd{p.rows.vs, p.rows.u0, p.rows.pre_off, p.rows.pre_slots};
-  const DebugKnobs k = debug_knobs();
-  const unsigned long long lim = k.wait_limit_ns != 0 ? k.wait_limit_ns : 2000000000ull;
-  launch_pdl_smem(s, dim3((unsigned)p.rows.count, (unsigned)(B / T)), dim3((unsigned)T), smem,
-                  pairwise22_rows_kernel<T0>, c, rd, dev(q), t, d, vsum_next, ev, evs, evb, lim,
-                  p.fault_dev);
 }
 
 // One dense pairwise bucket of one iteration. variant: for 2 x 2 tables 0 one instance per
@@ -1939,47 +1727,29 @@ void launch_bucket(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const
 int num_sites(const Plan& p) { return 4 + (int)p.pairwise.size(); }
 
 // sites: the tuned variant per launch site (tuned_sites' layout) or null for the built-in rules
-// vsum_alt: a second variable-sum buffer (or null). With it, a plan with fused rows runs them:
-// the generic Enum factors first (the rows add their new messages), the rows' kernel, which
-// writes its variables' sums for the next iteration into the other buffer, and from the second
-// iteration a variable-sum pass over the remaining variables only. Every message and sum is the
-// same as without (the same operations in the same order).
 template <bool T0>
 void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool low_t, int64_t iters,
              float* msgs0, float* msgs1, const float* ev, int64_t evs, int64_t evb,
-             unsigned* dacc, const float* gemm_tables, const int* sites,
-             float* vsum_alt = nullptr) {
+             unsigned* dacc, const float* gemm_tables, const int* sites) {
   const int nq = (int)p.pairwise.size();
   auto site = [&](int i) { return sites != nullptr ? sites[i] : -1; };
-  const bool rows = vsum_alt != nullptr && p.rows.count > 0 && B % 32 == 0 && c.lpb == 0 &&
-                    p.rows.count <= 2147483647LL && B / 32 <= 65535 && !debug_knobs().no_rows;
-  float* vs_cur = const_cast<float*>(c.vsum);
-  float* vs_nxt = vsum_alt;
   for (int64_t it = 0; it < iters; ++it) {
     float* cur = (it & 1) ? msgs1 : msgs0;
     float* nxt = (it & 1) ? msgs0 : msgs1;
     c.cur = cur;
     c.nxt = nxt;
-    c.vsum = vs_cur;
     unsigned* d = dacc + it * B;
-    launch_varsum(s, p, B, cur, ev, evs, evb, vs_cur, site(0), site(1),
-                  rows && it > 0 ? &p.varsum_binary_rest : nullptr);
-    if (rows) launch_enum_generic<T0>(s, p, c, B, t, d);
+    launch_varsum(s, p, B, cur, ev, evs, evb, const_cast<float*>(c.vsum), site(0), site(1));
     const float* tables = gemm_tables;
     for (int qi = 0; qi < nq; ++qi) {
       const PairwiseBucket& q = p.pairwise[qi];
-      if (rows && qi == p.rows.bucket) {
-        launch_rows<T0>(s, p, q, c, B, t, d, vs_nxt, ev, evs, evb);
-      } else {
-        launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(2 + qi));
-      }
+      launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(2 + qi));
       if (tables != nullptr) tables += q.gemm_floats;
     }
-    if (!rows) launch_enum_generic<T0>(s, p, c, B, t, d);
+    launch_enum_generic<T0>(s, p, c, B, t, d);
     launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d, site(2 + nq));
     launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d, site(3 + nq));
     launch_pool<T0>(s, p, c, B, t, 1, d);
-    if (rows) std::swap(vs_cur, vs_nxt);
   }
 }
 
@@ -2280,7 +2050,6 @@ size_t workspace_bytes(const Plan& p, int64_t batch, int64_t iters, bool ev_batc
   n += align_up(sizeof(unsigned) * (size_t)(it * B));
   n += align_up(sizeof(float) * (size_t)gemm_table_floats(p));
   n += align_up(sizeof(int));  // convergence count of pgbp_run_to_tolerance
-  if (p.rows.count > 0) n += align_up(sizeof(float) * (size_t)(p.num_var_states * B));  // rows
   return n;
 }
 
@@ -2332,8 +2101,6 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   unsigned* dacc = (unsigned*)take(sizeof(unsigned) * (size_t)(iters * B));
   float* gemm_ws = (float*)take(sizeof(float) * (size_t)gemm_table_floats(p));
   int* unconverged = (int*)take(sizeof(int));
-  float* vsum_alt =
-      p.rows.count > 0 ? (float*)take(sizeof(float) * (size_t)(p.num_var_states * B)) : nullptr;
   (void)ws_bytes;
   if (tol_run != nullptr) {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -2449,13 +2216,8 @@ cudaError_t run_bp(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
       else launch_cluster<false>(s, p, g, B, n, t, low_t, m0, m1, vsum, dacc);
       return (n & 1) ? m1 : m0;
     }
-    if (t0) {
-      iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, nullptr, sites,
-                    vsum_alt);
-    } else {
-      iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, gemm, sites,
-                     vsum_alt);
-    }
+    if (t0) iterate<true>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, nullptr, sites);
+    else iterate<false>(s, p, B, c, t, low_t, n, m0, m1, evp, evs, evb, dacc, gemm, sites);
     return (n & 1) ? m1 : m0;
   };
   int path = kPathMulti;

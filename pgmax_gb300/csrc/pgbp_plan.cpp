@@ -194,10 +194,6 @@ int pgbp_debug_set(int knob, int64_t value) {
       if (value != 0 && value != 1) return fail(PGBP_ERR_INVALID_ARGUMENT, "expected 0 or 1");
       g_debug.legacy_mma = (int)value;
       return PGBP_OK;
-    case PGBP_DEBUG_NO_ROWS:
-      if (value != 0 && value != 1) return fail(PGBP_ERR_INVALID_ARGUMENT, "expected 0 or 1");
-      g_debug.no_rows = (int)value;
-      return PGBP_OK;
     default:
       return fail(PGBP_ERR_INVALID_ARGUMENT, "unknown debug knob %d", knob);
   }
@@ -704,62 +700,6 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       g.row_les = bd.upload(g_les);
     }
     if (bd.err) return bail(bd.err);
-
-    // fused rows: a 2 x 2 bucket whose factors come in runs of one first variable each, that
-    // variable binary with its slots in edge order = generic Enum edges, then the run's
-    // first-edge slots in record order (an RBM's hidden rows)
-    for (int qi = 0; qi < (int)p.pairwise.size() && p.rows.count == 0; ++qi) {
-      if (p.pairwise[qi].n1 != 2 || p.pairwise[qi].n2 != 2) continue;
-      const auto& recs = buckets.at(std::make_pair(2, 2)).first;
-      std::vector<int32_t> unit_of(nvs, -1);
-      for (size_t u = 0; u < vb_vs.size(); ++u) unit_of[vb_vs[u]] = (int32_t)u;
-      std::vector<char> generic_slot(p.num_slots, 0);
-      for (size_t j = 0; j < g_eslot.size(); ++j)
-        if (g_esz[j] == 2) generic_slot[g_eslot[j]] = 1;
-      std::vector<char> taken(vb_vs.size(), 0);
-      std::vector<int32_t> r_vs, r_u0, r_pre_off{0}, r_pre;
-      bool ok = !recs.empty();
-      for (size_t u = 0; u < recs.size() && ok;) {
-        const int32_t v1 = recs[u].z;
-        size_t e = u;
-        while (e < recs.size() && recs[e].z == v1) ++e;
-        const int32_t unit = unit_of[v1];
-        ok = unit >= 0 && !taken[unit];
-        if (ok) {
-          taken[unit] = 1;
-          const int32_t a = vb_off[unit], b = vb_off[unit + 1];
-          const int32_t n = (int32_t)(e - u), pre = b - a - n;
-          ok = pre >= 0;
-          for (int32_t k = 0; ok && k < n; ++k) ok = vb_slots[a + pre + k] == recs[u + k].y;
-          for (int32_t k = 0; ok && k < pre; ++k) ok = generic_slot[vb_slots[a + k]] != 0;
-          if (ok) {
-            r_vs.push_back(v1);
-            r_u0.push_back((int32_t)u);
-            r_pre.insert(r_pre.end(), vb_slots.begin() + a, vb_slots.begin() + a + pre);
-            r_pre_off.push_back((int32_t)r_pre.size());
-          }
-        }
-        u = e;
-      }
-      if (!ok || r_vs.size() < 16) break;
-      r_u0.push_back((int32_t)recs.size());
-      p.rows.count = (int64_t)r_vs.size();
-      p.rows.bucket = qi;
-      p.rows.vs = bd.upload(r_vs);
-      p.rows.u0 = bd.upload(r_u0);
-      p.rows.pre_off = bd.upload(r_pre_off);
-      p.rows.pre_slots = bd.upload(r_pre);
-      std::vector<int32_t> rest_vs, rest_off{0}, rest_slots;
-      for (size_t u = 0; u < vb_vs.size(); ++u) {
-        if (taken[u]) continue;
-        rest_vs.push_back(vb_vs[u]);
-        rest_slots.insert(rest_slots.end(), vb_slots.begin() + vb_off[u],
-                          vb_slots.begin() + vb_off[u + 1]);
-        rest_off.push_back((int32_t)rest_slots.size());
-      }
-      fill_varsum(p.varsum_binary_rest, rest_vs, rest_off, rest_slots);
-      if (bd.err) return bail(bd.err);
-    }
   }
 
   // --- OR / AND factors
@@ -919,7 +859,6 @@ int pgbp_plan_get_info(const pgbp_plan* plan, pgbp_plan_info* info) {
   info->device_bytes = p.device_bytes;
   info->num_slots = p.num_slots;
   info->small_graph_smem_bytes = p.small_graph_smem;
-  info->num_fused_rows = p.rows.count;
   return PGBP_OK;
 }
 

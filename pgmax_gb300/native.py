@@ -108,7 +108,7 @@ class PlanInfo(ctypes.Structure):
       "num_edge_states", "num_var_states", "num_edges", "num_variables", "num_potentials",
       "num_enum_factors", "num_enum_pairwise_factors", "num_or_factors", "num_and_factors",
       "num_pool_factors", "num_pairwise_buckets", "device_bytes", "num_slots",
-      "small_graph_smem_bytes", "num_fused_rows")]
+      "small_graph_smem_bytes")]
 
 FLAG_NO_SMALL_GRAPH = 1
 FLAG_PATH_SMALL = 2
@@ -242,14 +242,12 @@ def wait_timeouts():
 DEBUG_WAIT_LIMIT_NS = 1
 DEBUG_SKIP_TABLE_COPY = 2
 DEBUG_LEGACY_MMA = 3
-DEBUG_NO_ROWS = 4
 
 
 def debug_set(knob, value):
   """Process-wide debug setting (pgbp_debug_set): DEBUG_WAIT_LIMIT_NS (0 = the built-in 2 s),
-  DEBUG_SKIP_TABLE_COPY (1 = the exp-domain kernels' table wait runs out with no copy issued),
-  DEBUG_LEGACY_MMA (1 = shared 64 x 64 tables of one instance on the mma.sync kernel) or
-  DEBUG_NO_ROWS (1 = binary pairwise rows through the variable-sum pass, not fused)."""
+  DEBUG_SKIP_TABLE_COPY (1 = the exp-domain kernels' table wait runs out with no copy issued) or
+  DEBUG_LEGACY_MMA (1 = shared 64 x 64 tables of one instance on the mma.sync kernel)."""
   check(load().pgbp_debug_set(int(knob), int(value)), "pgbp_debug_set")
 
 
