@@ -16,6 +16,7 @@
  *   pgbp_marginals      get_marginals                            pgmax/infer/bp.py:263-288
  *   pgbp_softmax_rows / pgbp_argmax_rows   get_marginals / decode_map_states of any belief arrays
  *   pgbp_energy         compute_energy                           pgmax/infer/energy.py:53-148
+ *   pgbp_energy_terms   compute_energy(debug_mode=True)          pgmax/infer/energy.py:151-204
  *   pgbp_sdlp_run       SDLP(...).run_with_objvals               pgmax/infer/dual_lp.py:238-313
  *   pgbp_sdlp_objective smooth_dual_objval_and_grad / get_bp_updates  dual_lp.py:65-236, 419-448
  *
@@ -363,6 +364,23 @@ int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch,
                 const float* evidence, int64_t ev_stride,
                 const int32_t* map, int64_t map_stride, float* energy,
                 void* workspace, size_t workspace_bytes);
+
+/* The per-variable and per-factor terms of the energy of `batch` decodings: compute_energy's
+ * debug mode (pgmax/infer/energy.py:151-204), on the device. evidence and map as for pgbp_energy.
+ * Outputs, no workspace:
+ *   var_energy [batch, num_variables] (evidence_to_vars order): -evidence[state] of the decoded
+ *     state (a negative state s of a K-state variable is s + K), NaN when no state is decoded;
+ *   factor_config [batch, num_factors] (the flat wiring's factor order): for an EnumFactor the
+ *     index of the decoded config among the factor's configs (the last of equal configs, as the
+ *     reference's lookup keeps it), -1 when its variables decode no config (enum.py:326-360);
+ *     for an OR / AND / Pool factor 0 when the decoding satisfies it, -1 when it violates it
+ *     (logical.py:378-406, pool.py:242-272). The reference's factor energy is then
+ *     -potentials[config] of the factor object's own potentials (in their own precision), or
+ *     +inf for -1, 0 for a satisfied logical or Pool factor. */
+int pgbp_energy_terms(const pgbp_plan* plan, void* stream, int64_t batch,
+                      const float* evidence, int64_t ev_stride,
+                      const int32_t* map, int64_t map_stride,
+                      float* var_energy, int32_t* factor_config);
 
 /* Kernel timing. While enabled, pgbp_run brackets every kernel launch with CUDA events on its
  * stream (no synchronisation is added). pgbp_profile_read waits for the recorded events, returns

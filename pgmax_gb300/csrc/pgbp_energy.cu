@@ -55,6 +55,7 @@ struct SegDev {
   const void* p0;
   const void* p1;
   const void* p2;
+  const int32_t* fac;  // item -> factor index in the flat wiring (factor segments)
 };
 
 struct Launch {
@@ -325,6 +326,91 @@ __global__ void __launch_bounds__(kEnergyThreads) energy_partial_kernel(Args a, 
   }
 }
 
+// compute_energy's debug mode (pgmax/infer/energy.py:151-204) for B decodings: per variable
+// -evidence[state] (NaN when no state is decoded); per factor the decoded config, which the host
+// turns into the factor's energy with the factor's own potentials: an EnumFactor's index of the
+// decoded config among its configs, the last of equal configs as the reference's lookup keeps it
+// (-1 when none is decoded, enum.py:326-360); 0 / -1 for an OR / AND (logical.py:378-406) or Pool
+// (pool.py:242-272) factor that the decoding satisfies / violates. grid (chunks of this launch,
+// min(B, 65535)); var_e [B][num_variables], fac_cfg [B][num_factors].
+__global__ void __launch_bounds__(kEnergyThreads) energy_terms_kernel(Args a, Launch L,
+                                                                       int64_t first_chunk,
+                                                                       int64_t nv, int64_t nf,
+                                                                       float* __restrict__ var_e,
+                                                                       int32_t* __restrict__ fac_cfg) {
+  const int64_t chunk = first_chunk + blockIdx.x;
+  int si = 0;
+  while (si + 1 < L.nseg && L.seg[si + 1].chunk_begin <= chunk) ++si;
+  const SegDev sg = L.seg[si];
+  const int64_t i0 = (chunk - sg.chunk_begin) * kEnergyChunk;
+  for (int64_t b = blockIdx.y; b < a.B; b += gridDim.y) {
+    const int32_t* map_b = a.map + b * a.ms;
+    const float* ev_b = a.ev ? a.ev + b * a.evs : nullptr;
+    for (int k = 0; k < kEnergyChunk / kEnergyThreads; ++k) {
+      const int64_t i = i0 + (int64_t)k * kEnergyThreads + threadIdx.x;
+      if (i >= sg.items) continue;
+      int cfg = -1;
+      switch (sg.kind) {
+        case kEnergyVars: {
+          const int v = (int)i;
+          const int s = decoded_state(map_b, a.var_off, v);
+          var_e[b * nv + v] = s >= 0 ? -ev_b[__ldg(a.var_off + v) + s] : NAN;
+          continue;
+        }
+        case kEnergyPairwise: {
+          const int4 r = __ldg(static_cast<const int4*>(sg.p0) + i);
+          const int sa = state_of_vs(map_b, a, r.z), sb = state_of_vs(map_b, a, r.w);
+          if (sa >= 0 && sb >= 0) cfg = sa * sg.b + sb;   // row-major configs
+          break;
+        }
+        case kEnergyGeneric: {
+          const EnumGeneric& g = a.gen;
+          const int j0 = __ldg(g.edge_off + i), nvf = __ldg(g.n_vars + i), nc = __ldg(g.n_cfg + i);
+          const int rb = __ldg(g.row_begin + i);
+          for (int c = 0; c < nc; ++c) {
+            int est = 0;
+            bool ok = true;
+            for (int t = 0; t < nvf && ok; ++t) {
+              const int j = j0 + t;
+              const int s = state_of_vs(map_b, a, __ldg(g.edge_vs + j));
+              ok = s >= 0 && __ldg(g.row_les + rb + c * nvf + t) == est + s;
+              est += __ldg(g.edge_size + j);
+            }
+            if (ok) cfg = c;
+          }
+          break;
+        }
+        case kEnergyLogical: {
+          const int32_t* pb = static_cast<const int32_t*>(sg.p0);
+          const int4* par = static_cast<const int4*>(sg.p1);
+          const int4* ch = static_cast<const int4*>(sg.p2);
+          const int r = sg.a;
+          bool all = true;
+          for (int q = __ldg(pb + i), q1 = __ldg(pb + i + 1); q < q1 && all; ++q)
+            all = state_of_vs(map_b, a, __ldg(par + q).z) == r;
+          const bool child = state_of_vs(map_b, a, __ldg(ch + i).z) == r;
+          cfg = all != child ? -1 : 0;
+          break;
+        }
+        case kEnergyPool: {
+          const int32_t* cbg = static_cast<const int32_t*>(sg.p0);
+          const int4* chs = static_cast<const int4*>(sg.p1);
+          const int4* ind = static_cast<const int4*>(sg.p2);
+          int on = 0;
+          for (int q = __ldg(cbg + i), q1 = __ldg(cbg + i + 1); q < q1; ++q)
+            on += state_of_vs(map_b, a, __ldg(chs + q).z) == 1;
+          const int ind_on = state_of_vs(map_b, a, __ldg(ind + i).z) == 1;
+          cfg = on != ind_on ? -1 : 0;
+          break;
+        }
+        default:
+          continue;
+      }
+      fac_cfg[b * nf + __ldg(sg.fac + i)] = cfg;
+    }
+  }
+}
+
 // One warp per instance: adds its partials (lane c, c + 32, ... then a fixed butterfly) and
 // combines the terms in the reference's order.
 __global__ void energy_final_kernel(const EnergyPartial* __restrict__ part, int64_t chunks,
@@ -353,6 +439,46 @@ __global__ void energy_final_kernel(const EnergyPartial* __restrict__ part, int6
 }
 
 int64_t chunks_of(int64_t items) { return (items + kEnergyChunk - 1) / kEnergyChunk; }
+
+// A segment's pointers as the kernels see them.
+SegDev seg_dev(const Plan& p, const EnergySeg& es) {
+  SegDev d{};
+  d.kind = es.kind;
+  d.items = es.items;
+  d.chunk_begin = es.chunk_begin;
+  switch (es.kind) {
+    case kEnergyPairwise: {
+      const PairwiseBucket& q = p.pairwise[(size_t)es.param];
+      d.a = q.n1;
+      d.b = q.n2;
+      d.p0 = q.rec;
+      d.p1 = q.cfg_begin;
+      d.fac = q.fac;
+      break;
+    }
+    case kEnergyGeneric:
+      d.fac = p.enum_generic.fac;
+      break;
+    case kEnergyLogical: {
+      const LogicalSet& g = p.logical[es.param];
+      d.a = g.off == 1 ? 0 : 1;  // the relevant state: 0 for OR, 1 for AND
+      d.p0 = g.par_begin;
+      d.p1 = g.par;
+      d.p2 = g.child;
+      d.fac = g.fac;
+      break;
+    }
+    case kEnergyPool:
+      d.p0 = p.pool.ch_begin;
+      d.p1 = p.pool.ch;
+      d.p2 = p.pool.ind;
+      d.fac = p.pool.fac;
+      break;
+    default:
+      break;
+  }
+  return d;
+}
 
 }  // namespace
 
@@ -424,39 +550,7 @@ cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   for (size_t s0 = 0; s0 < p.energy_segs.size(); s0 += kMaxSegsPerLaunch) {
     Launch L;
     L.nseg = (int)std::min<size_t>(kMaxSegsPerLaunch, p.energy_segs.size() - s0);
-    for (int k = 0; k < L.nseg; ++k) {
-      const EnergySeg& es = p.energy_segs[s0 + k];
-      SegDev& d = L.seg[k];
-      d = SegDev{};
-      d.kind = es.kind;
-      d.items = es.items;
-      d.chunk_begin = es.chunk_begin;
-      switch (es.kind) {
-        case kEnergyPairwise: {
-          const PairwiseBucket& q = p.pairwise[(size_t)es.param];
-          d.a = q.n1;
-          d.b = q.n2;
-          d.p0 = q.rec;
-          d.p1 = q.cfg_begin;
-          break;
-        }
-        case kEnergyLogical: {
-          const LogicalSet& g = p.logical[es.param];
-          d.a = g.off == 1 ? 0 : 1;  // the relevant state: 0 for OR, 1 for AND
-          d.p0 = g.par_begin;
-          d.p1 = g.par;
-          d.p2 = g.child;
-          break;
-        }
-        case kEnergyPool:
-          d.p0 = p.pool.ch_begin;
-          d.p1 = p.pool.ch;
-          d.p2 = p.pool.ind;
-          break;
-        default:
-          break;
-      }
-    }
+    for (int k = 0; k < L.nseg; ++k) L.seg[k] = seg_dev(p, p.energy_segs[s0 + k]);
     const EnergySeg& last = p.energy_segs[s0 + L.nseg - 1];
     const int64_t first = p.energy_segs[s0].chunk_begin;
     const int64_t n = last.chunk_begin + chunks_of(last.items) - first;
@@ -476,6 +570,34 @@ cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   const int64_t threads = B * 32;
   energy_final_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
       part, p.energy_chunks, B, (long long)p.num_enum_factors, present, out);
+  return cudaGetLastError();
+}
+
+cudaError_t energy_terms(const Plan& p, cudaStream_t s, int64_t B, const float* ev,
+                         int64_t ev_stride, const int32_t* map, int64_t map_stride, float* var_e,
+                         int32_t* fac_cfg) {
+  ProfileScope ps(kProfReadout, s);
+  Args a{};
+  a.var_off = p.var_off;
+  a.var_of_vs = p.var_of_vs;
+  a.ev = ev;
+  a.evs = ev_stride;
+  a.map = map;
+  a.ms = map_stride;
+  a.B = B;
+  a.chunks = p.energy_chunks;
+  a.gen = p.enum_generic;
+  const unsigned gy = (unsigned)std::min<int64_t>(B, 65535);
+  for (size_t s0 = 0; s0 < p.energy_segs.size(); s0 += kMaxSegsPerLaunch) {
+    Launch L;
+    L.nseg = (int)std::min<size_t>(kMaxSegsPerLaunch, p.energy_segs.size() - s0);
+    for (int k = 0; k < L.nseg; ++k) L.seg[k] = seg_dev(p, p.energy_segs[s0 + k]);
+    const EnergySeg& last = p.energy_segs[s0 + L.nseg - 1];
+    const int64_t first = p.energy_segs[s0].chunk_begin;
+    const int64_t n = last.chunk_begin + chunks_of(last.items) - first;
+    energy_terms_kernel<<<dim3((unsigned)n, gy), kEnergyThreads, 0, s>>>(
+        a, L, first, p.num_variables, p.num_factors, var_e, fac_cfg);
+  }
   return cudaGetLastError();
 }
 

@@ -38,6 +38,7 @@ struct PairwiseBucket {
   std::vector<int64_t> grp_count_host;
   int64_t gemm_floats = 0;
   bool rows16 = false;  // every factor's message pair starts at a multiple of 4 slots
+  int32_t* fac = nullptr;  // [count] the record's factor index in the flat wiring
 };
 
 // Floats of run-time tables one group of a shared-table bucket with K x K tables needs: E and E'
@@ -59,6 +60,7 @@ int64_t expgemm_tc_table_floats(int K);
 struct EnumGeneric {
   int64_t count = 0;
   int max_es = 0;                 // largest number of edge states of one factor
+  int32_t* fac = nullptr;         // [count] factor index in the flat wiring
   int32_t* es_begin = nullptr;    // [count] absolute edge-state index
   int32_t* n_es = nullptr;        // [count]
   int32_t* edge_off = nullptr;    // [count + 1]
@@ -81,6 +83,7 @@ struct LogicalSet {
   int32_t* par_begin = nullptr;  // [count + 1]
   int4* par = nullptr;           // [num_parents] (es0, slot, vs0, 0)
   int4* child = nullptr;         // [count]
+  int32_t* fac = nullptr;        // [count] factor index in the flat wiring
 };
 
 // Pool factors: choices ch_begin[f] .. ch_begin[f + 1] - 1, binary edges as above (pool.py:62-83).
@@ -89,6 +92,7 @@ struct PoolSet {
   int32_t* ch_begin = nullptr;
   int4* ch = nullptr;            // [num_choices]
   int4* ind = nullptr;           // [count]
+  int32_t* fac = nullptr;        // [count] factor index in the flat wiring
 };
 
 // Variable sums: binary variables (both states from one compressed slot per edge) and the
@@ -323,6 +327,9 @@ cudaError_t sdlp_run(const Plan& p, cudaStream_t s, int64_t B, const float* lp, 
 // Energy of decodings (pgbp_energy.cu). energy_plan fills p.energy_segs / p.energy_chunks.
 void energy_plan(Plan& p);
 size_t energy_workspace_bytes(const Plan& p, int64_t B);
+cudaError_t energy_terms(const Plan& p, cudaStream_t s, int64_t B, const float* ev,
+                         int64_t ev_stride, const int32_t* map, int64_t map_stride, float* var_e,
+                         int32_t* fac_cfg);
 cudaError_t energy(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_t lp_stride,
                    const float* ev, int64_t ev_stride, const int32_t* map, int64_t map_stride,
                    float* out, void* ws, size_t ws_bytes);

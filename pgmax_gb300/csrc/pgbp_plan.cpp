@@ -539,6 +539,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     p.shared_potentials = alias != nullptr;
     int64_t implicit_cfg = 0;
     std::map<std::pair<int, int>, std::pair<std::vector<int4>, std::vector<int32_t>>> buckets;
+    std::map<std::pair<int, int>, std::vector<int32_t>> bucket_fac;  // factor index per record
+    std::vector<int32_t> g_fac;
     std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_eslot, g_evs, g_rb, g_ncfg, g_nv, g_cfg,
         g_les;
     int max_es = 0;
@@ -614,7 +616,9 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         const int4 r0 = edge_rec(fb);
         bk.first.push_back(make_int4(r0.x, r0.y, r0.z, vs[fb + esz[0]]));
         bk.second.push_back((int32_t)pot_first);
+        bucket_fac[{esz[0], esz[1]}].push_back((int32_t)factor_of(fb));
       } else {
+        g_fac.push_back((int32_t)factor_of(fb));
         g_es.push_back((int32_t)fb);
         g_nes.push_back((int32_t)(fe - fb));
         max_es = std::max<int>(max_es, (int)(fe - fb));
@@ -651,14 +655,17 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         for (size_t i = 0; i < order.size(); ++i) order[i] = i;
         std::stable_sort(order.begin(), order.end(),
                          [&](size_t a, size_t b) { return cfg[a] < cfg[b]; });
+        auto& fac = bucket_fac[kv.first];
         std::vector<int4> r2(recs.size());
-        std::vector<int32_t> c2(cfg.size());
+        std::vector<int32_t> c2(cfg.size()), f2(fac.size());
         for (size_t i = 0; i < order.size(); ++i) {
           r2[i] = recs[order[i]];
           c2[i] = cfg[order[i]];
+          f2[i] = fac[order[i]];
         }
         recs.swap(r2);
         cfg.swap(c2);
+        fac.swap(f2);
         std::vector<int32_t> gf, gc, gt;
         for (size_t i = 0; i < cfg.size(); ++i) {
           if (i == 0 || cfg[i] != cfg[i - 1]) {
@@ -680,6 +687,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       }
       q.rec = bd.upload(kv.second.first);
       q.cfg_begin = bd.upload(kv.second.second);
+      q.fac = bd.upload(bucket_fac[kv.first]);
       p.num_enum_pairwise += q.count;
       p.pairwise.push_back(q);
     }
@@ -698,6 +706,7 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       g.n_vars = bd.upload(g_nv);
       g.cfg_begin = bd.upload(g_cfg);
       g.row_les = bd.upload(g_les);
+      g.fac = bd.upload(g_fac);
     }
     if (bd.err) return bail(bd.err);
   }
@@ -748,6 +757,11 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     g.par_begin = bd.upload(pb);
     g.par = bd.upload(pes);
     g.child = bd.upload(ces);
+    {
+      std::vector<int32_t> fac(F);
+      for (int64_t f = 0; f < F; ++f) fac[f] = (int32_t)factor_of(m0 + ch[f]);
+      g.fac = bd.upload(fac);
+    }
     if (bd.err) return bail(bd.err);
   }
 
@@ -794,6 +808,9 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       g.ch_begin = bd.upload(cb);
       g.ch = bd.upload(ces);
       g.ind = bd.upload(ies);
+      std::vector<int32_t> fac(F);
+      for (int64_t f = 0; f < F; ++f) fac[f] = (int32_t)factor_of(m0 + ind[f]);
+      g.fac = bd.upload(fac);
       if (bd.err) return bail(bd.err);
     }
   }
@@ -1325,6 +1342,29 @@ int pgbp_energy(const pgbp_plan* plan, void* stream, int64_t batch, const float*
   e = pgbp::energy(p, static_cast<cudaStream_t>(stream), batch, log_potentials, lp_stride, evidence,
                    ev_stride, map, map_stride, energy, workspace, workspace_bytes);
   if (e != cudaSuccess) return cuda_fail(e, "pgbp_energy launch");
+  return PGBP_OK;
+}
+
+int pgbp_energy_terms(const pgbp_plan* plan, void* stream, int64_t batch, const float* evidence,
+                      int64_t ev_stride, const int32_t* map, int64_t map_stride,
+                      float* var_energy, int32_t* factor_config) {
+  if (!plan) return fail(PGBP_ERR_INVALID_ARGUMENT, "null plan");
+  const pgbp::Plan& p = plan->p;
+  if (!p.var_of_vs) return fail(PGBP_ERR_INVALID_ARGUMENT, "plan has no evidence_to_vars");
+  if (batch <= 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "batch must be positive");
+  if (ev_stride < 0 || map_stride < 0 ||
+      (ev_stride != 0 && ev_stride < p.num_var_states) ||
+      (map_stride != 0 && map_stride < p.num_variables))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "bad stride");
+  if (!map || (p.num_variables > 0 && !var_energy) || (p.num_factors > 0 && !factor_config) ||
+      (p.num_var_states > 0 && !evidence))
+    return fail(PGBP_ERR_INVALID_ARGUMENT, "null data pointer");
+  pgbp::DeviceGuard guard(p.device);
+  if (guard.status() != cudaSuccess) return cuda_fail(guard.status(), "cudaSetDevice");
+  if (const int rc = pgbp::take_plan_fault(p)) return rc;
+  const cudaError_t e = pgbp::energy_terms(p, static_cast<cudaStream_t>(stream), batch, evidence,
+                                           ev_stride, map, map_stride, var_energy, factor_config);
+  if (e != cudaSuccess) return cuda_fail(e, "pgbp_energy_terms launch");
   return PGBP_OK;
 }
 

@@ -484,6 +484,33 @@ class Plan:
         "pgbp_energy")
     return out if any(batched) else out[0]
 
+  def energy_terms(self, evidence, map_states):
+    """Per-variable energies and per-factor decoded configs of decodings (pgbp_energy_terms,
+    compute_energy's debug mode): map_states [num_variables] or [B, num_variables] (int),
+    evidence [n] or [B, n]. Returns (var_energy float32 [.., num_variables], factor_config int32
+    [.., num_factors]), with the batch axis when an input carries one."""
+    torch = _torch()
+    m = self._dev(map_states, torch.int32)
+    ev = self._dev(evidence)
+    nvars = int(self.info["num_variables"])
+    nf = sum(int(self.info[k]) for k in ("num_enum_factors", "num_or_factors", "num_and_factors",
+                                          "num_pool_factors"))
+    m_t, b1, mst = self._rows(m, nvars)
+    ev_t, b2, evs = self._rows(ev, self.num_var_states)
+    batched = [t.ndim == 2 for t in (m, ev)]
+    sizes = {b for b, bt in zip((b1, b2), batched) if bt}
+    if len(sizes) > 1:
+      raise ValueError(f"batch sizes differ: {sorted(sizes)}")
+    B = sizes.pop() if sizes else 1
+    var_e = torch.empty((B, nvars), dtype=torch.float32, device=ev.device)
+    fac_c = torch.empty((B, nf), dtype=torch.int32, device=ev.device)
+    native.check(self.lib.pgbp_energy_terms(
+        self.handle, self._stream(), B, ev_t.data_ptr(), evs, m_t.data_ptr(), mst,
+        var_e.data_ptr(), fac_c.data_ptr()), "pgbp_energy_terms")
+    if any(batched):
+      return var_e, fac_c
+    return var_e[0], fac_c[0]
+
   def marginals(self, flat_beliefs):
     torch = _torch()
     b = self._dev(flat_beliefs)

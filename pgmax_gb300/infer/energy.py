@@ -1,5 +1,5 @@
-"""Energy of MAP decodings: pgmax.infer.compute_energy (pgmax/infer/energy.py:53-148) on the
-pgbp_energy kernel.
+"""Energy of MAP decodings: pgmax.infer.compute_energy (pgmax/infer/energy.py:53-204) on the
+pgbp_energy / pgbp_energy_terms kernels.
 
 `compute_energy(bp_state, bp_arrays, map_states)` returns `(energy, None, None)` like the
 reference. The energy is a float32 device tensor: 0-d for one decoding, [B] when the decodings
@@ -7,12 +7,18 @@ reference. The energy is a float32 device tensor: 0-d for one decoding, [B] when
 `jax.vmap(compute_energy)` gives in the reference (examples/rbm.ipynb evaluates the energies of a
 batch of perturb-and-MAP samples this way). Lower is better; +inf marks a decoding that violates a
 factor.
+
+With `debug_mode=True` it returns `(energy, vars_energies, factors_energies)` as the reference's
+debug mode does (energy.py:151-204): the energy as a Python float summed over the variables, then
+the factors, in the reference's order; each variable's -evidence of its decoded state; each
+factor's energy keyed by the frozenset of its variables. The terms come from one kernel launch.
 """
 
 from typing import Any, Dict, Hashable, Tuple
 
 import numpy as np
 
+from .. import factor as factor_mod
 from .bp_state import BPArrays, BPState
 
 
@@ -59,15 +65,61 @@ def compute_energy(bp_state: BPState, bp_arrays: BPArrays, map_states: Dict[Hash
                    debug_mode: bool = False) -> Tuple[Any, Any, Any]:
   """Returns (energy, None, None): the energy of the decoding `map_states`, a dict from the
   VarGroups of the factor graph to their states, under the evidence and log potentials of
-  `bp_arrays` (energy.py:53-148). The per-variable and per-factor breakdown of the reference's
-  debug mode (energy.py:150-213, a host-side Python loop) is not provided."""
-  if debug_mode:
-    raise NotImplementedError(
-        "compute_energy(debug_mode=True) (per-variable and per-factor energies) is not provided; "
-        "the total energy is computed on the device with debug_mode=False")
+  `bp_arrays` (energy.py:53-148). With debug_mode, (energy, vars_energies, factors_energies)
+  (energy.py:151-204, see the module docstring)."""
   ctx = _context(bp_state)
   plan = ctx.plan
   groups = [vg for vg in bp_state.fg_state.variable_groups if int(np.prod(vg.num_states.shape)) > 0]
   states = _flat_states(groups, map_states, f"cuda:{plan.device}")
+  if debug_mode:
+    return _compute_energy_debug_mode(bp_state, bp_arrays, groups, states, plan)
   energy = plan.energy(bp_arrays.log_potentials, bp_arrays.evidence, states)
   return energy, None, None
+
+
+def _compute_energy_debug_mode(bp_state, bp_arrays, groups, states, plan):
+  """energy.py:151-204: the evidence of bp_arrays; the decoded configs from the device; the
+  potentials of the factor objects themselves (in their own precision), as the reference's
+  debug mode reads them."""
+  ev_ndim = getattr(bp_arrays.evidence, "ndim", None)
+  if states.ndim != 1 or (ev_ndim if ev_ndim is not None else np.ndim(bp_arrays.evidence)) != 1:
+    raise ValueError("compute_energy(debug_mode=True) takes one decoding, without a batch axis")
+  # states must be in [0, K): the reference raises for a state past the end (it indexes the
+  # evidence with it), and a negative one, which its evidence lookup would count from the end
+  # but its factor checks would not, is refused too
+  k = np.concatenate([np.asarray(vg.num_states).reshape(-1) for vg in groups]) if groups else (
+      np.zeros(0, np.int64))
+  s = states.cpu().numpy().astype(np.int64)
+  bad = np.nonzero((s < 0) | (s >= k))[0]
+  if bad.size:
+    raise IndexError(f"decoded state {int(s[bad[0]])} out of range for a variable with "
+                     f"{int(k[bad[0]])} states")
+  var_e, fac_c = plan.energy_terms(bp_arrays.evidence, states)
+  var_e, fac_c = var_e.cpu().numpy(), fac_c.cpu().numpy()
+  energy = 0.0
+  vars_energies = {}
+  i = 0
+  for vg in groups:
+    for var in vg.variables:
+      e = float(var_e[i])
+      vars_energies[var] = e
+      energy += e
+      i += 1
+  # the factor's energy from its decoded config and its own potentials (enum.py:326-360), or
+  # the verdict of an OR / AND / Pool factor (logical.py:378-406, pool.py:242-272)
+  factors_energies = {}
+  f = 0
+  for factor_group in bp_state.fg_state.factor_group_to_potentials_starts:
+    enum = factor_group.factor_type is factor_mod.EnumFactor
+    for this_factor in factor_group.factors:
+      c = int(fac_c[f])
+      if c < 0:
+        e = float(np.inf)
+      elif enum:
+        e = float(-np.asarray(this_factor.log_potentials)[c])
+      else:
+        e = 0.0
+      energy += e
+      factors_energies[frozenset(this_factor.variables)] = e
+      f += 1
+  return energy, vars_energies, factors_energies

@@ -167,6 +167,7 @@ SIGNATURES = [
     ("pgbp_energy_workspace_size", ctypes.c_size_t, [_p, _i64]),
     ("pgbp_energy", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p,
                                    ctypes.c_size_t]),
+    ("pgbp_energy_terms", ctypes.c_int, [_p, _p, _i64, _p, _i64, _p, _i64, _p, _p]),
     # include/pgbp_learn.h
     ("pgbp_conv3x3", ctypes.c_int, [_p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, _p, _p, _p, _p, ctypes.c_int, ctypes.c_int, _p]),

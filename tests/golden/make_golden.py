@@ -46,6 +46,7 @@ import os
 import sys
 import traceback
 import types
+import warnings
 
 import numpy as np
 
@@ -193,13 +194,14 @@ def install_energy_capture():
   """Wraps pgmax.infer.compute_energy so that every non-debug call is recorded."""
   energy_mod = importlib.import_module("pgmax.infer.energy")
   inferer_mod = importlib.import_module("pgmax.infer.inferer")
+  factor_mod = importlib.import_module("pgmax.factor")
   orig = energy_mod.compute_energy
 
   def compute_energy(bp_state, bp_arrays, map_states, debug_mode=False):
     res = orig(bp_state, bp_arrays, map_states, debug_mode)
     if not debug_mode:
       ctx = inferer_mod.InfererContext(bp_state)
-      REC.energies.append({
+      rec = {
           "source": REC.current,
           "meta": dict(REC.meta),
           "wiring": wiring_arrays(ctx, bp_state.fg_state),
@@ -207,7 +209,38 @@ def install_energy_capture():
           "evidence": _np(bp_arrays.evidence, np.float32),
           "map_flat": flat_map(bp_state.fg_state.variable_groups, map_states),
           "energy": np.float32(np.asarray(res[0])),
-      })
+      }
+      # the same decoding in debug mode (energy.py:151-204), when every state is in [0, K): the
+      # terms in variable order and in factor order, and the total as the reference sums it
+      nstates = np.bincount(np.asarray(rec["wiring"]["evidence_to_vars"], np.int64))
+      m = rec["map_flat"]
+      debug = None
+      if m.shape[0] == nstates.shape[0] and np.all((m >= 0) & (m < nstates)):
+        try:
+          with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            debug = orig(bp_state, bp_arrays, map_states, True)
+        except AttributeError:
+          # the reference's debug mode reads factor_configs, which a SingleFactorGroup (a factor
+          # added on its own) and the logical groups lack: such graphs get no debug record
+          debug = None
+      if debug is not None:
+        total, var_e, fac_e = debug
+        fg_state = bp_state.fg_state
+        rec["debug_var_terms"] = np.array(
+            [var_e[v] for vg in fg_state.variable_groups for v in vg.variables], np.float64)
+        rec["debug_fac_terms"] = np.array(
+            [fac_e[frozenset(f.variables)] for g in fg_state.factor_group_to_potentials_starts
+             for f in g.factors], np.float64)
+        rec["debug_energy"] = np.float64(total)
+        # the potentials debug mode reads: the Enum factor objects' own, in their own precision,
+        # concatenated in factor order (the flat wiring's Enum config order)
+        enum_pots = [np.asarray(f.log_potentials, np.float64).reshape(-1)
+                     for g in fg_state.factor_group_to_potentials_starts
+                     if g.factor_type is factor_mod.EnumFactor for f in g.factors]
+        rec["debug_factor_potentials"] = (np.concatenate(enum_pots) if enum_pots
+                                          else np.zeros(0, np.float64))
+      REC.energies.append(rec)
     return res
 
   energy_mod.compute_energy = compute_energy
@@ -269,8 +302,10 @@ def save_energies():
     src = rec["source"].replace("::", "__").replace(".", "_")
     counts[src] = counts.get(src, 0) + 1
     arrays = {"w." + k: v for k, v in rec["wiring"].items()}
-    for k in ("log_potentials", "evidence", "map_flat", "energy"):
-      arrays[k] = rec[k]
+    for k in ("log_potentials", "evidence", "map_flat", "energy", "debug_var_terms",
+              "debug_fac_terms", "debug_energy", "debug_factor_potentials"):
+      if k in rec:
+        arrays[k] = rec[k]
     arrays["meta"] = np.array(json.dumps({"source": rec["source"], **rec["meta"]}))
     np.savez_compressed(os.path.join(OUT, f"energy_{src}_{counts[src]:02d}.npz"), **arrays)
   return len(REC.energies)

@@ -61,3 +61,34 @@ def test_oracle_one_hot_wraps_negative_states_once():
   assert oh.tolist() == [0, 0, 1, 0, 0]
   oh = oracle_energy.var_state_onehot(e2v, np.array([-4, -2]))
   assert oh.tolist() == [0, 0, 0, 1, 0]
+
+
+DEBUG = [p for p in ENERGIES if "debug_energy" in np.load(p).files]
+
+
+def _same_terms(got, want):
+  """Bit-equal float32 values in float64, nan matching nan."""
+  got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+  return got.shape == want.shape and np.array_equal(got, want, equal_nan=True)
+
+
+def test_debug_fixtures_exist():
+  # the reference's debug mode fails on graphs with single factors; the rest are recorded
+  assert len(DEBUG) >= 100
+
+
+@pytest.mark.parametrize("path", DEBUG, ids=fixtures.fixture_id)
+def test_debug_terms_match_reference(path):
+  """compute_energy_terms against the reference's debug mode (energy.py:151-204): every variable
+  and factor term bit for bit, and the total summed as the reference sums it (variables, then
+  factors, in Python floats)."""
+  fx = fixtures.load(path)
+  var_t, fac_t = oracle_energy.compute_energy_terms(fx["wiring"], fx["debug_factor_potentials"],
+                                                    fx["evidence"], fx["map_flat"])
+  assert _same_terms(var_t, fx["debug_var_terms"])
+  assert _same_terms(fac_t, fx["debug_fac_terms"])
+  total = 0.0
+  for x in list(var_t) + list(fac_t):
+    total += float(x)
+  want = float(fx["debug_energy"])
+  assert (np.isnan(total) and np.isnan(want)) or total == want

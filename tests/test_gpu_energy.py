@@ -282,3 +282,99 @@ def test_host_api_or_factors_score_like_their_enum_form():
   assert np.isfinite(energies[0]) and np.isinf(energies[1])
   assert np.isinf(energies[3])
   assert abs(energies[0] - energies[2]) <= 1e-5
+
+
+DEBUG = [p for p in ENERGIES if "debug_energy" in np.load(p).files]
+
+
+def _bits_equal(got, want):
+  got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+  return got.shape == want.shape and np.array_equal(got, want, equal_nan=True)
+
+
+@pytest.mark.parametrize("path", DEBUG, ids=fixtures.fixture_id)
+def test_energy_terms_match_reference_debug_mode(path):
+  """pgbp_energy_terms against the reference's debug mode (energy.py:151-204): the variable
+  terms bit for bit, the decoded configs as the oracle finds them (pinned to the same fixtures),
+  and the factor terms and total they give with the factors' own potentials."""
+  fx = fixtures.load(path)
+  plan = _plan(fx["wiring"])
+  var_e, fac_c = plan.energy_terms(fx["evidence"], fx["map_flat"])
+  var_e, fac_c = var_e.cpu().numpy(), fac_c.cpu().numpy()
+  assert _bits_equal(var_e, fx["debug_var_terms"])
+  _, want_cfg = oracle_energy.compute_energy_configs(fx["wiring"], fx["evidence"], fx["map_flat"])
+  np.testing.assert_array_equal(fac_c, want_cfg)
+  _, fac_t = oracle_energy.compute_energy_terms(fx["wiring"], fx["debug_factor_potentials"],
+                                                fx["evidence"], fx["map_flat"])
+  assert _bits_equal(fac_t, fx["debug_fac_terms"])
+
+
+@pytest.mark.parametrize("builder,kw", [
+    ("mixed", dict(seed=0, vardict=False)),
+    ("mixed", dict(seed=3)),
+    ("deconv", dict(seed=1)),
+    ("potts", dict(L=7, K=5, seed=4)),
+])
+def test_energy_terms_batched_match_oracle(builder, kw):
+  """Batches of random, repaired, negative and out-of-range decodings: every instance's terms
+  and configs as the oracle's."""
+  torch = _torch()
+  _, _, _, w = _case_wiring(builder, **kw)
+  plan = _plan(w)
+  rng = np.random.default_rng(23)
+  B = 21
+  maps = _decodings(w, rng, B)
+  ev = rng.normal(size=(B, int(w["num_var_states"]))).astype(np.float32)
+  var_e, fac_c = plan.energy_terms(torch.as_tensor(ev), torch.as_tensor(maps))
+  var_e, fac_c = var_e.cpu().numpy(), fac_c.cpu().numpy()
+  for b in range(B):
+    want_v, want_c = oracle_energy.compute_energy_configs(w, ev[b], maps[b])
+    assert _bits_equal(var_e[b], want_v)
+    np.testing.assert_array_equal(fac_c[b], want_c)
+
+
+@pytest.mark.parametrize("builder,kw", [
+    ("mixed", dict(seed=1, vardict=False)),
+    ("mixed", dict(seed=2)),
+    ("rbm", dict(nh=12, nv=18, seed=3, sample=0)),
+])
+def test_compute_energy_debug_mode_through_the_api(builder, kw):
+  """infer.compute_energy(debug_mode=True) returns the reference's structure: the total as a
+  float summed over the variables then the factors, each variable's term keyed by the variable,
+  each factor's keyed by the frozenset of its variables, with the factors' own potentials."""
+  api = _api()
+  fg, groups, ev = cases.BUILDERS[builder](api, **kw)
+  bp = api.infer.BP(fg.bp_state, temperature=0.0)
+  arrays = bp.run(bp.init(evidence_updates=ev), num_iters=15)
+  decoded = api.infer.decode_map_states(bp.get_beliefs(arrays))
+  total, var_en, fac_en = api.infer.compute_energy(fg.bp_state, arrays, decoded, debug_mode=True)
+  assert isinstance(total, float)
+  w = bp.context.flat_wiring()
+  from pgmax_gb300.infer import energy as energy_mod  # pylint: disable=g-import-not-at-top
+  live = [vg for vg in fg.bp_state.fg_state.variable_groups
+          if int(np.prod(vg.num_states.shape)) > 0]
+  m = energy_mod._flat_states(live, decoded, "cpu").numpy()  # pylint: disable=protected-access
+  ev_flat = np.asarray(arrays.evidence.cpu() if hasattr(arrays.evidence, "cpu") else
+                       arrays.evidence, np.float32)
+  pots = [np.asarray(f.log_potentials, np.float64).reshape(-1)
+          for g in fg.bp_state.fg_state.factor_group_to_potentials_starts
+          if g.factor_type is api.factor.EnumFactor for f in g.factors]
+  pots = np.concatenate(pots) if pots else np.zeros(0)
+  want_v, want_f = oracle_energy.compute_energy_terms(w, pots, ev_flat, m)
+  variables = [v for vg in live for v in vg.variables]
+  assert list(var_en) == variables
+  assert _bits_equal([var_en[v] for v in variables], want_v)
+  factors = [f for g in fg.bp_state.fg_state.factor_group_to_potentials_starts for f in g.factors]
+  assert len(fac_en) == len({frozenset(f.variables) for f in factors})
+  got_f = [fac_en[frozenset(f.variables)] for f in factors]
+  assert _bits_equal(got_f, want_f)
+  want_total = 0.0
+  for x in list(want_v) + list(want_f):
+    want_total += float(x)
+  assert total == want_total or (np.isnan(total) and np.isnan(want_total))
+  # and the non-debug energy agrees with the total
+  e = float(api.infer.compute_energy(fg.bp_state, arrays, decoded)[0].cpu())
+  if np.isfinite(want_total):
+    assert abs(e - want_total) <= 2e-6 * (np.abs(want_v).sum() + np.abs(want_f).sum()) + 1e-6
+  else:
+    assert e == want_total
