@@ -158,6 +158,15 @@ struct Plan {
   VarsumSet varsum_binary, varsum_other;
   std::vector<PairwiseBucket> pairwise;
   EnumGeneric enum_generic;
+  // The multi-kernel iteration runs the generic Enum factors that are unary on a binary variable
+  // with configs (0), (1) in that order (unary evidence factors, e.g. an RBM's biases) with a
+  // kernel of their own: rec (first edge state, slot, first variable state, first potential);
+  // enum_generic_rest holds the other generic factors (every other path takes enum_generic).
+  struct Unary2Set {
+    int64_t count = 0;
+    int4* rec = nullptr;
+  } unary2;
+  EnumGeneric enum_generic_rest;
   LogicalSet logical[2];
   PoolSet pool;
   int64_t flags = 0;

@@ -918,6 +918,100 @@ __global__ void __launch_bounds__(256, 4) pairwise22_x4_kernel(Fused c, Pairwise
   block_max4_to(deltas, l, dm);
 }
 
+// ----------------------------------------------------------------------------- unary factors
+// A generic Enum factor that is unary on a binary variable with configs (0), (1) in that order
+// (Plan::unary2): the operations of enum_generic_unit for it, in the same order (s = (0 + v) + p,
+// its maximum with -inf, at T > 0 exp((s - max) / T) added to 0, then Fused::store's damping,
+// normalisation and clip), without its per-thread arrays. c is the compressed current message,
+// a0 / a1 the variable's sums, p0 / p1 the two potentials.
+template <bool T0>
+__device__ __forceinline__ void unary2(float c, float a0, float a1, float p0, float p1, float t,
+                                       float d, float omd, float& n, float& dmax) {
+  float o0, o1;
+  decode2(c, o0, o1);
+  const float v0 = a0 - o0, v1 = a1 - o1;
+  const float s0 = (0.0f + v0) + p0, s1 = (0.0f + v1) + p1;
+  const float mx0 = fmaxp(-INFINITY, s0), mx1 = fmaxp(-INFINITY, s1);
+  float f0, f1;
+  if (T0) {
+    f0 = mx0 - v0;
+    f1 = mx1 - v1;
+  } else {
+    const float se0 = 0.0f + expf(div_t(s0 - mx0, t));
+    const float se1 = 0.0f + expf(div_t(s1 - mx1, t));
+    f0 = (t * logf(se0) + mx0) - v0;
+    f1 = (t * logf(se1) + mx1) - v1;
+  }
+  const float q0 = d * o0 + omd * f0, q1 = d * o1 + omd * f1;
+  const float m = fmaxp(q0, q1);
+  const float w0 = fmaxp(q0 - m, kMsgNegInf), w1 = fmaxp(q1 - m, kMsgNegInf);
+  n = encode2(w0, w1);
+  dmax = fmaxp(dmax, fabsf(w0 - o0));
+  dmax = fmaxp(dmax, fabsf(w1 - o1));
+}
+
+struct Unary2Dev {
+  const int4* __restrict__ rec;  // (first edge state, slot, first variable state, potential)
+  int64_t count;
+};
+
+// 4 instances per thread (B % 4 == 0).
+template <bool T0>
+__global__ void __launch_bounds__(256) unary2_x4_kernel(Fused c, Unary2Dev g, float t,
+                                                        unsigned* deltas) {
+  pdl_begin();
+  const int64_t B = c.B;
+  const Lane4 l = lane4(B);
+  float4 dm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (l.valid) {
+    const int64_t b = l.b;
+    for (int64_t u = l.u0; u < g.count; u += l.ustep) {
+      const int4 q = __ldg(g.rec + u);
+      const float4 c4 = ld4(c.cur + (int64_t)q.y * B + b);
+      const float4 a0 = ld4(c.vsum + (int64_t)q.z * B + b);
+      const float4 a1 = ld4(c.vsum + ((int64_t)q.z + 1) * B + b);
+      float4 p0, p1;
+      if (c.lpb == 0) {
+        const float x0 = __ldg(c.lp + (int64_t)q.w * c.lps), x1 = __ldg(c.lp + ((int64_t)q.w + 1) * c.lps);
+        p0 = make_float4(x0, x0, x0, x0);
+        p1 = make_float4(x1, x1, x1, x1);
+      } else {
+        p0 = ld4(c.lp + (int64_t)q.w * c.lps + b);
+        p1 = ld4(c.lp + ((int64_t)q.w + 1) * c.lps + b);
+      }
+      float4 n;
+      unary2<T0>(c4.x, a0.x, a1.x, p0.x, p1.x, t, c.d, c.omd, n.x, dm.x);
+      unary2<T0>(c4.y, a0.y, a1.y, p0.y, p1.y, t, c.d, c.omd, n.y, dm.y);
+      unary2<T0>(c4.z, a0.z, a1.z, p0.z, p1.z, t, c.d, c.omd, n.z, dm.z);
+      unary2<T0>(c4.w, a0.w, a1.w, p0.w, p1.w, t, c.d, c.omd, n.w, dm.w);
+      st4(c.nxt + (int64_t)q.y * B + b, n);
+    }
+  }
+  block_max4_to(deltas, l, dm);
+}
+
+// One instance per thread.
+template <bool T0>
+__global__ void __launch_bounds__(256) unary2_kernel(Fused c, Unary2Dev g, float t,
+                                                     unsigned* deltas) {
+  pdl_begin();
+  const int64_t B = c.B;
+  const Lane l = lane(B);
+  float dm = 0.0f;
+  if (l.valid) {
+    const int64_t b = l.b;
+    for (int64_t u = l.u0; u < g.count; u += l.ustep) {
+      const int4 q = __ldg(g.rec + u);
+      float n;
+      unary2<T0>(c.cur[(int64_t)q.y * B + b], c.vsum[(int64_t)q.z * B + b],
+                 c.vsum[((int64_t)q.z + 1) * B + b], c.pot(q.w, b), c.pot((int64_t)q.w + 1, b),
+                 t, c.d, c.omd, n, dm);
+      c.nxt[(int64_t)q.y * B + b] = n;
+    }
+  }
+  block_max_to(deltas, l, dm);
+}
+
 // ----------------------------------------------------------------------------- variable sums
 // var_sums = evidence.at[var_states_for_edge_states].add(msgs) (bp.py:217): serial per variable
 // state over its edge states in increasing order. Binary variables read one compressed slot per
@@ -1615,8 +1709,8 @@ void launch_pairwise(cudaStream_t s, const Plan& p, const PairwiseBucket& q, con
 
 template <bool T0, class C>
 void launch_enum_generic(cudaStream_t s, const Plan& p, const C& c, int64_t B, float t,
-                         unsigned* deltas) {
-  const EnumGeneric& g = p.enum_generic;
+                         unsigned* deltas, const EnumGeneric* set = nullptr) {
+  const EnumGeneric& g = set != nullptr ? *set : p.enum_generic;
   if (g.count == 0) return;
   ProfileScope ps(kProfEnumGeneric, s);
   const Launch2 l = launch2(g.count, B, p.sm_count);
@@ -1629,6 +1723,23 @@ void launch_enum_generic(cudaStream_t s, const Plan& p, const C& c, int64_t B, f
     launch_pdl(s, l.grid, l.block, enum_generic_kernel<128, T0, C>, c, d, B, t, deltas);
   } else {
     launch_pdl(s, l.grid, l.block, enum_generic_kernel<512, T0, C>, c, d, B, t, deltas);
+  }
+}
+
+// Plan::unary2 of the multi-kernel iteration: 4 instances per thread when B allows it and that
+// still leaves >= 16 warps per SM.
+template <bool T0>
+void launch_unary2(cudaStream_t s, const Plan& p, const Fused& c, int64_t B, float t,
+                   unsigned* deltas) {
+  if (p.unary2.count == 0) return;
+  ProfileScope ps(kProfEnumGeneric, s);
+  const Unary2Dev d{p.unary2.rec, p.unary2.count};
+  if (B % 4 == 0 && p.unary2.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32) {
+    const Launch2 l = launch2_x4(p.unary2.count, B, p.sm_count);
+    launch_pdl(s, l.grid, l.block, unary2_x4_kernel<T0>, c, d, t, deltas);
+  } else {
+    const Launch2 l = launch2(p.unary2.count, B, p.sm_count);
+    launch_pdl(s, l.grid, l.block, unary2_kernel<T0>, c, d, t, deltas);
   }
 }
 
@@ -1746,7 +1857,12 @@ void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool lo
       launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(2 + qi));
       if (tables != nullptr) tables += q.gemm_floats;
     }
-    launch_enum_generic<T0>(s, p, c, B, t, d);
+    if (p.unary2.count > 0) {
+      launch_unary2<T0>(s, p, c, B, t, d);
+      launch_enum_generic<T0>(s, p, c, B, t, d, &p.enum_generic_rest);
+    } else {
+      launch_enum_generic<T0>(s, p, c, B, t, d);
+    }
     launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d, site(2 + nq));
     launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d, site(3 + nq));
     launch_pool<T0>(s, p, c, B, t, 1, d);

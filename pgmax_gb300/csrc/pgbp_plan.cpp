@@ -543,6 +543,8 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
     std::vector<int32_t> g_fac;
     std::vector<int32_t> g_es, g_nes, g_eoff{0}, g_esz, g_eslot, g_evs, g_rb, g_ncfg, g_nv, g_cfg,
         g_les;
+    std::vector<char> g_u2;     // per generic factor: unary on a binary variable, configs (0), (1)
+    std::vector<int4> u2_rec;
     int max_es = 0;
     std::vector<int32_t> esz, estart;  // per factor, reused
     for (size_t k = 0; k < facs.size(); ++k) {
@@ -634,6 +636,13 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
         g_ncfg.push_back((int32_t)nc);
         g_nv.push_back(nv);
         g_cfg.push_back((int32_t)pot_first);
+        const bool u2 = nv == 1 && esz[0] == 2 && nc == 2 && les.size() == 2 && les[0] == 0 &&
+                        les[1] == 1;
+        g_u2.push_back(u2 ? 1 : 0);
+        if (u2) {
+          const int4 r = edge_rec(fb);
+          u2_rec.push_back(make_int4(r.x, r.y, r.z, (int32_t)pot_first));
+        }
       }
     }
     if (max_es > 512)
@@ -707,6 +716,50 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       g.cfg_begin = bd.upload(g_cfg);
       g.row_les = bd.upload(g_les);
       g.fac = bd.upload(g_fac);
+    }
+    if (!u2_rec.empty()) {
+      p.unary2.count = (int64_t)u2_rec.size();
+      p.unary2.rec = bd.upload(u2_rec);
+      // the other generic factors, in their order
+      std::vector<int32_t> r_es, r_nes, r_eoff{0}, r_esz, r_eslot, r_evs, r_rb, r_ncfg, r_nv, r_cfg,
+          r_les, r_fac;
+      int r_max = 0;
+      for (size_t i = 0; i < g_es.size(); ++i) {
+        if (g_u2[i]) continue;
+        r_es.push_back(g_es[i]);
+        r_nes.push_back(g_nes[i]);
+        r_max = std::max<int>(r_max, g_nes[i]);
+        for (int32_t j = g_eoff[i]; j < g_eoff[i + 1]; ++j) {
+          r_esz.push_back(g_esz[j]);
+          r_eslot.push_back(g_eslot[j]);
+          r_evs.push_back(g_evs[j]);
+        }
+        r_eoff.push_back((int32_t)r_esz.size());
+        r_rb.push_back((int32_t)r_les.size());
+        r_les.insert(r_les.end(), g_les.begin() + g_rb[i],
+                     g_les.begin() + g_rb[i] + (int64_t)g_ncfg[i] * g_nv[i]);
+        r_ncfg.push_back(g_ncfg[i]);
+        r_nv.push_back(g_nv[i]);
+        r_cfg.push_back(g_cfg[i]);
+        r_fac.push_back(g_fac[i]);
+      }
+      pgbp::EnumGeneric& r = p.enum_generic_rest;
+      r.count = (int64_t)r_es.size();
+      r.max_es = r_max;
+      if (r.count > 0) {
+        r.es_begin = bd.upload(r_es);
+        r.n_es = bd.upload(r_nes);
+        r.edge_off = bd.upload(r_eoff);
+        r.edge_size = bd.upload(r_esz);
+        r.edge_slot = bd.upload(r_eslot);
+        r.edge_vs = bd.upload(r_evs);
+        r.row_begin = bd.upload(r_rb);
+        r.n_cfg = bd.upload(r_ncfg);
+        r.n_vars = bd.upload(r_nv);
+        r.cfg_begin = bd.upload(r_cfg);
+        r.row_les = bd.upload(r_les);
+        r.fac = bd.upload(r_fac);
+      }
     }
     if (bd.err) return bail(bd.err);
   }
