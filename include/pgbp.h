@@ -293,13 +293,14 @@ int pgbp_argmax_rows(void* stream, int64_t rows, int64_t k, const float* in, int
  * paths and then, on the multi-kernel path, the kernel variants of each launch site (the binary
  * variable sums: 1 or 4 instances per thread; the other variable sums: per state or by
  * variable; each dense 2 x 2 pairwise bucket: 1 or 4 instances per thread; OR and AND: a thread
- * or a warp per factor). Those variants give bit-identical results. A site of shared K x K tables
+ * or a warp per factor; the generic EnumFactors: a thread per (factor, instance) or a CTA per
+ * factor staged in shared memory). Those variants give bit-identical results. A site of shared K x K tables
  * at temperature > 0 is not timed (the exp-domain tensor-core kernel, variant 1, agrees with the
  * direct kernel, variant 0, within float32 accuracy only) but may be set here. These calls export
  * and import the decision table so that a host can cache it across processes: sites are site[0]
  * the binary variable sums, site[1] the other variable sums, site[2 .. P + 1] the P pairwise
- * buckets in plan order, then OR, AND (num_sites = 4 + P); -1 = the built-in rule; path -1 = not
- * tuned. pgbp_plan_signature writes a string identifying the plan's structure
+ * buckets in plan order, then OR, AND, the generic EnumFactors (per-thread or staged kernel)
+ * (num_sites = 5 + P); -1 = the built-in rule; path -1 = not tuned. pgbp_plan_signature writes a string identifying the plan's structure
  * and the device's SM count: the key under which a table may be reused. */
 #define PGBP_TUNE_MAX_SITES 64
 typedef struct {
@@ -428,10 +429,15 @@ int pgbp_wait_timeouts(int64_t* count);
  *                                nothing in flight (tests the timeout path); 0: normal
  *   PGBP_DEBUG_LEGACY_MMA        1: shared 64 x 64 tables of a single instance run on the
  *                                warp-level mma.sync kernel instead of the tcgen05 one (for
- *                                comparison); 0: normal */
+ *                                comparison); 0: normal
+ *   PGBP_DEBUG_ENUM_KERNEL       generic EnumFactors (not dense pairwise) in run() and
+ *                                pgbp_factor_update: 1 = the per-thread kernel, 2 = the kernel
+ *                                staging each factor in shared memory (bit-identical results);
+ *                                0: the tuned choice, else the built-in rule */
 #define PGBP_DEBUG_WAIT_LIMIT_NS 1
 #define PGBP_DEBUG_SKIP_TABLE_COPY 2
 #define PGBP_DEBUG_LEGACY_MMA 3
+#define PGBP_DEBUG_ENUM_KERNEL 4
 int pgbp_debug_set(int knob, int64_t value);
 
 const char* pgbp_last_error(void);

@@ -60,6 +60,8 @@ int64_t expgemm_tc_table_floats(int K);
 struct EnumGeneric {
   int64_t count = 0;
   int max_es = 0;                 // largest number of edge states of one factor
+  int max_nv = 0;                 // largest number of variables of one factor
+  int64_t max_cfg = 0;            // largest number of configs of one factor
   int32_t* fac = nullptr;         // [count] factor index in the flat wiring
   int32_t* es_begin = nullptr;    // [count] absolute edge-state index
   int32_t* n_es = nullptr;        // [count]
@@ -72,6 +74,11 @@ struct EnumGeneric {
   int32_t* n_vars = nullptr;      // [count]
   int32_t* cfg_begin = nullptr;   // [count] absolute potential index
   int32_t* row_les = nullptr;     // [rows] edge state local to its factor
+  // configs by edge state: local edge state e of factor f is held by the local configs
+  // inv_cfg[inv_off[inv_begin[f] + e]] .. inv_cfg[inv_off[inv_begin[f] + e + 1] - 1], increasing
+  int32_t* inv_begin = nullptr;   // [count]
+  int32_t* inv_off = nullptr;     // [sum of (n_es + 1)] absolute positions in inv_cfg
+  int32_t* inv_cfg = nullptr;     // [rows]
 };
 
 // OR (off = +1) / AND (off = -1) factors: parents par_begin[f] .. par_begin[f + 1] - 1. Every edge
@@ -225,10 +232,15 @@ int take_plan_fault(const Plan& p);
 // Debug settings (pgbp_debug_set): the bounded waits' limit in ns (0 = the built-in 2 s),
 // whether the exp-domain kernels arm their table barrier without issuing the copy, so their wait
 // runs out with nothing in flight, and whether K = 64 at B = 1 runs the mma.sync kernel.
+// Launch sites the autotuner decides per (batch, temperature == 0), in the order of
+// pgbp_tuning_entry::site: binary sums, other sums, the pairwise buckets, OR, AND, generic Enum.
+inline int num_tune_sites(const Plan& p) { return 5 + (int)p.pairwise.size(); }
+
 struct DebugKnobs {
   unsigned long long wait_limit_ns = 0;
   int skip_table_copy = 0;
   int legacy_mma = 0;  // K = 64 at B = 1 on the mma.sync kernel instead of the tcgen05 one
+  int enum_kernel = 0;  // generic Enum factors: 0 = tuned / rule, 1 = per-thread, 2 = staged
 };
 DebugKnobs debug_knobs();
 
@@ -355,7 +367,24 @@ __device__ __forceinline__ void pdl_begin() {
 }
 
 // Launches `kernel` (which must begin with pdl_begin()) as a programmatic dependent of the
-// previous kernel in stream s.
+// previous kernel in stream s, with `smem` bytes of dynamic shared memory.
+template <class... KArgs, class... Args>
+void launch_pdl_smem(cudaStream_t s, dim3 grid, dim3 block, size_t smem,
+                     void (*kernel)(KArgs...), Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+// launch_pdl_smem without dynamic shared memory.
 template <class... KArgs, class... Args>
 void launch_pdl(cudaStream_t s, dim3 grid, dim3 block, void (*kernel)(KArgs...), Args... args) {
   cudaLaunchConfig_t cfg = {};

@@ -161,10 +161,23 @@ struct Fused {
     }
     for (int i = 0; i < k; ++i) vt[i] = vsum[(r.vs0 + i) * B + b] - old[i];
   }
+  // State i of what load gives, one state at a time.
+  __device__ __forceinline__ float old_at(const EdgeRef& r, int k, int i, int64_t b) const {
+    if (k == 2) {
+      float o0, o1;
+      decode2(cur[r.slot * B + b], o0, o1);
+      return i == 0 ? o0 : o1;
+    }
+    return cur[(r.slot + i) * B + b];
+  }
+  __device__ __forceinline__ float vt_at(const EdgeRef& r, int k, int i, int64_t b) const {
+    return vsum[(r.vs0 + i) * B + b] - old_at(r, k, i, b);
+  }
 
-  // bp.py:127-136 for one edge; outv(i) is the new factor-to-variable message of state i.
-  template <class F>
-  __device__ __forceinline__ void store(const EdgeRef& r, int k, const float* old, F outv,
+  // bp.py:127-136 for one edge; outv(i) is the new factor-to-variable message of state i, old[i]
+  // the current one (an array or an accessor).
+  template <class O, class F>
+  __device__ __forceinline__ void store(const EdgeRef& r, int k, const O& old, F outv,
                                         int64_t b, float& dmax) const {
     if (k == 2) {
       const float n0 = d * old[0] + omd * outv(0);
@@ -218,8 +231,12 @@ struct Update {
       vtof[i] = vt[b * vts + (r.es0 + i - base)];
     }
   }
-  template <class F>
-  __device__ __forceinline__ void store(const EdgeRef& r, int k, const float*, F outv, int64_t b,
+  __device__ __forceinline__ float old_at(const EdgeRef&, int, int, int64_t) const { return 0.0f; }
+  __device__ __forceinline__ float vt_at(const EdgeRef& r, int, int i, int64_t b) const {
+    return vt[b * vts + (r.es0 + i - base)];
+  }
+  template <class O, class F>
+  __device__ __forceinline__ void store(const EdgeRef& r, int k, const O&, F outv, int64_t b,
                                         float&) const {
     for (int i = 0; i < k; ++i) out[b * os + (r.es0 + i - base)] = outv(i);
   }
@@ -328,6 +345,9 @@ struct EnumGenericDev {
   const int32_t* __restrict__ cfg_begin;
   const int32_t* __restrict__ row_les;
   int64_t count;
+  const int32_t* __restrict__ inv_begin;
+  const int32_t* __restrict__ inv_off;
+  const int32_t* __restrict__ inv_cfg;
 };
 
 // pass_enum_fac_to_var_messages (enum.py:451-475) for an arbitrary config table: factor f,
@@ -394,6 +414,226 @@ __global__ void __launch_bounds__(256) enum_generic_kernel(C c, EnumGenericDev g
       enum_generic_unit<MAXES, T0>(c, g, f, l.b, t, dmax);
   }
   block_max_to(deltas, l, dmax);
+}
+
+// The current messages of one edge, read through the context state by state (the values its
+// load gives), for a store that takes them as old[i].
+template <class C>
+struct OldAt {
+  const C& c;
+  EdgeRef r;
+  int k;
+  int64_t b;
+  __device__ __forceinline__ float operator[](int i) const { return c.old_at(r, k, i, b); }
+};
+
+// Contexts with old_at / vt_at, which the staged kernel reads edges through.
+template <class C>
+struct HasStaged {
+  static constexpr bool value = false;
+};
+template <>
+struct HasStaged<Fused> {
+  static constexpr bool value = true;
+};
+template <>
+struct HasStaged<Update> {
+  static constexpr bool value = true;
+};
+
+// pass_enum_fac_to_var_messages (enum.py:451-475) for arbitrary config tables, staged in shared
+// memory: one CTA per (factor, group of ib instances), thread (item, j) with j = instance of
+// the group. Per factor, in shared memory:
+//   vt_s[e][j]  the variable-to-factor message of local edge state e
+//   mx_s[e][j]  the max of the config sums over the configs holding e; se_s[e][j] (T > 0) the
+//               sum of exp((sum - max) / t) over them
+//   rows_s      a tile of up to tk config rows (local edge states), copied from the table
+//   s_s[q][j]   the config sums of the tile
+// Per tile the config sums run with threads over (config, instance): the row's messages in
+// variable order, then the potential. The max over each edge state's configs then runs with
+// threads over (edge state, instance), along the factor's configs-by-edge-state list, whose
+// position per edge state carries from tile to tile in cur_s. At T > 0 a second pass over the
+// tiles sums the exponentials the same way. Each value goes through enum_generic_unit's
+// operations in the same order (sums in variable order, max and exp-sum in increasing config
+// order), so the two kernels give bit-identical messages.
+constexpr int kStagedThreads = 256;
+
+struct StagedShape {
+  int ib, tk;
+  size_t smem;
+};
+
+__host__ __device__ inline size_t staged_smem_bytes(int ib, int tk, int max_es, int max_nv, bool t0) {
+  const size_t floats = (size_t)max_es * ib * (t0 ? 2 : 3) + (size_t)tk * ib + kStagedThreads;
+  const size_t ints = (size_t)tk * max_nv + 2 * (size_t)max_es + (size_t)max_nv + 1;
+  return 4 * (floats + ints);
+}
+
+template <bool T0, class C>
+__global__ void __launch_bounds__(kStagedThreads) enum_staged_kernel(
+    C c, EnumGenericDev g, int64_t B, int ib, int tk, int max_es, int max_nv, float t,
+    unsigned* deltas) {
+  pdl_begin();
+  extern __shared__ float4 staged_smem4[];
+  float* vt_s = reinterpret_cast<float*>(staged_smem4);
+  float* mx_s = vt_s + max_es * ib;
+  float* se_s = mx_s + max_es * ib;  // T > 0 only
+  float* s_s = se_s + (T0 ? 0 : max_es * ib);
+  float* red = s_s + tk * ib;
+  int32_t* rows_s = reinterpret_cast<int32_t*>(red + kStagedThreads);
+  int32_t* cur_s = rows_s + tk * max_nv;  // [2][max_es] list positions, by tile parity
+  int32_t* pos_s = cur_s + 2 * max_es;    // [max_nv + 1] first local edge state of each edge
+  const int tid = threadIdx.x;
+  const int j = tid % ib, item0 = tid / ib, nitem = kStagedThreads / ib;
+  const int64_t b = (int64_t)blockIdx.x * ib + j;
+  const bool valid = b < B;  // instance 0 of every group is valid
+  float dmax = 0.0f;
+  for (int64_t f = blockIdx.y; f < g.count; f += gridDim.y) {
+    const int64_t e0 = g.es_begin[f];
+    const int nes = g.n_es[f], nv = g.n_vars[f], ncfg = g.n_cfg[f];
+    const int64_t rb = g.row_begin[f], k0 = g.cfg_begin[f];
+    const int ej0 = g.edge_off[f];
+    const int32_t* io = g.inv_off + g.inv_begin[f];
+    const int32_t* __restrict__ ic = g.inv_cfg;
+    __syncthreads();  // the previous factor is done with the shared arrays
+    if (tid == 0) {
+      int pos = 0;
+      for (int q = 0; q < nv; ++q) {
+        pos_s[q] = pos;
+        pos += g.edge_size[ej0 + q];
+      }
+      pos_s[nv] = pos;
+    }
+    __syncthreads();
+    for (int q = item0; q < nv; q += nitem) {
+      const int pos = pos_s[q], k = pos_s[q + 1] - pos;
+      const EdgeRef r{e0 + pos, g.edge_slot[ej0 + q], g.edge_vs[ej0 + q]};
+      for (int i = 0; i < k; ++i) {
+        vt_s[(pos + i) * ib + j] = valid ? c.vt_at(r, k, i, b) : 0.0f;
+        mx_s[(pos + i) * ib + j] = -INFINITY;
+        if (!T0) se_s[(pos + i) * ib + j] = 0.0f;
+      }
+    }
+    for (int pass = 0; pass < (T0 ? 1 : 2); ++pass) {
+      __syncthreads();  // messages in place; the previous pass is done with the lists
+      for (int e = tid; e < nes; e += kStagedThreads) cur_s[e] = io[e];
+      int par = 0;
+      for (int c0 = 0; c0 < ncfg; c0 += tk, par ^= 1) {
+        const int cn = min(tk, ncfg - c0), c1 = c0 + cn;
+        const bool last = c1 >= ncfg;
+        __syncthreads();  // positions set; the previous tile is done with rows_s and s_s
+        const int32_t* src = g.row_les + rb + (int64_t)c0 * nv;
+        for (int x = tid; x < cn * nv; x += kStagedThreads) rows_s[x] = __ldg(src + x);
+        __syncthreads();
+        if (valid) {
+          // four configs per step, their loads issued together; each sum keeps variable order
+          int q = item0;
+          for (; q + 3 * nitem < cn; q += 4 * nitem) {
+            const int32_t* row0 = rows_s + q * nv;
+            const int32_t* row1 = row0 + nitem * nv;
+            const int32_t* row2 = row1 + nitem * nv;
+            const int32_t* row3 = row2 + nitem * nv;
+            float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+            for (int i = 0; i < nv; ++i) {
+              const float x0 = vt_s[row0[i] * ib + j], x1 = vt_s[row1[i] * ib + j];
+              const float x2 = vt_s[row2[i] * ib + j], x3 = vt_s[row3[i] * ib + j];
+              s0 += x0;
+              s1 += x1;
+              s2 += x2;
+              s3 += x3;
+            }
+            const int64_t kq = k0 + c0 + q;
+            s0 = s0 + c.pot(kq, b);
+            s1 = s1 + c.pot(kq + nitem, b);
+            s2 = s2 + c.pot(kq + 2 * nitem, b);
+            s3 = s3 + c.pot(kq + 3 * nitem, b);
+            s_s[q * ib + j] = s0;
+            s_s[(q + nitem) * ib + j] = s1;
+            s_s[(q + 2 * nitem) * ib + j] = s2;
+            s_s[(q + 3 * nitem) * ib + j] = s3;
+          }
+          for (; q < cn; q += nitem) {
+            const int32_t* row = rows_s + q * nv;
+            float sum = 0.0f;
+            for (int i = 0; i < nv; ++i) sum += vt_s[row[i] * ib + j];
+            sum = sum + c.pot(k0 + c0 + q, b);
+            s_s[q * ib + j] = sum;
+          }
+        }
+        __syncthreads();
+        for (int e = item0; e < nes; e += nitem) {
+          const int p0 = cur_s[par * max_es + e];
+          int pe = io[e + 1];
+          if (!last) {  // the list's configs below c1: a binary search of the sorted list
+            int lo = p0, hi = pe;
+            while (lo < hi) {
+              const int mid = (lo + hi) >> 1;
+              if (__ldg(ic + mid) < c1) lo = mid + 1;
+              else hi = mid;
+            }
+            pe = lo;
+            if (j == 0) cur_s[(par ^ 1) * max_es + e] = pe;
+          }
+          if (!valid) continue;
+          const int x = e * ib + j;
+          // eight list entries per step: their loads issued together, folded in list order
+          if (pass == 0) {
+            float m = mx_s[x];
+            int p = p0;
+            for (; p + 8 <= pe; p += 8) {
+              float v[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) v[u] = s_s[(__ldg(ic + p + u) - c0) * ib + j];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) m = fmaxp(m, v[u]);
+            }
+            for (; p < pe; ++p) m = fmaxp(m, s_s[(__ldg(ic + p) - c0) * ib + j]);
+            mx_s[x] = m;
+          } else {
+            const float m = mx_s[x];
+            float se = se_s[x];
+            int p = p0;
+            for (; p + 8 <= pe; p += 8) {
+              float v[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) v[u] = s_s[(__ldg(ic + p + u) - c0) * ib + j];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) v[u] = expf(div_t(v[u] - m, t));
+#pragma unroll
+              for (int u = 0; u < 8; ++u) se += v[u];
+            }
+            for (; p < pe; ++p) se += expf(div_t(s_s[(__ldg(ic + p) - c0) * ib + j] - m, t));
+            se_s[x] = se;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      for (int q = item0; q < nv; q += nitem) {
+        const int pos = pos_s[q], k = pos_s[q + 1] - pos;
+        const EdgeRef r{e0 + pos, g.edge_slot[ej0 + q], g.edge_vs[ej0 + q]};
+        const OldAt<C> old{c, r, k, b};
+        const float* vq = vt_s + pos * ib + j;
+        const float* mq = mx_s + pos * ib + j;
+        if (T0) {
+          c.store(r, k, old, [&](int i) { return mq[i * ib] - vq[i * ib]; }, b, dmax);
+        } else {
+          const float* sq = se_s + pos * ib + j;
+          c.store(r, k, old, [&](int i) { return (t * logf(sq[i * ib]) + mq[i * ib]) - vq[i * ib]; },
+                  b, dmax);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  red[tid] = dmax;
+  __syncthreads();
+  if (tid < ib && valid && deltas != nullptr) {
+    float m = red[tid];
+    for (int q = 1; q < nitem; ++q) m = fmaxp(m, red[q * ib + tid]);
+    atomicMax(deltas + b, __float_as_uint(m));
+  }
 }
 
 // ----------------------------------------------------------------------------- OR / AND factors
@@ -1678,8 +1918,9 @@ PairwiseDev dev(const PairwiseBucket& q) {
   return PairwiseDev{q.rec, q.cfg_begin, q.count, q.n1, q.n2};
 }
 EnumGenericDev dev(const EnumGeneric& g) {
-  return EnumGenericDev{g.es_begin,  g.n_es,  g.edge_off, g.edge_size, g.edge_slot, g.edge_vs,
-                        g.row_begin, g.n_cfg, g.n_vars,   g.cfg_begin, g.row_les,   g.count};
+  return EnumGenericDev{g.es_begin,  g.n_es,    g.edge_off, g.edge_size, g.edge_slot,
+                        g.edge_vs,   g.row_begin, g.n_cfg,  g.n_vars,    g.cfg_begin,
+                        g.row_les,   g.count,   g.inv_begin, g.inv_off,  g.inv_cfg};
 }
 LogicalDev dev(const LogicalSet& g) {
   return LogicalDev{g.par_begin, g.par, g.child, g.count, g.off};
@@ -1707,12 +1948,58 @@ void launch_pairwise(cudaStream_t s, const Plan& p, const PairwiseBucket& q, con
   }
 }
 
+// Shape of the staged kernel for a set: instances per CTA (a power of two up to 32) and configs
+// per tile, within 48 KB of shared memory (four CTAs per SM).
+StagedShape staged_shape(const EnumGeneric& g, int64_t B, bool t0) {
+  const size_t budget = 48 * 1024;
+  int ib = 1;
+  while (ib * 2 <= std::min<int64_t>(B, 32)) ib *= 2;
+  while (ib > 1 && staged_smem_bytes(ib, kStagedThreads / ib, g.max_es, g.max_nv, t0) > budget)
+    ib /= 2;
+  const size_t fixed = staged_smem_bytes(ib, 0, g.max_es, g.max_nv, t0);
+  const size_t per = 4 * (size_t)(ib + g.max_nv);
+  int64_t tk = fixed < budget ? (int64_t)((budget - fixed) / per) : 1;
+  tk = std::max<int64_t>(1, std::min<int64_t>(tk, std::max<int64_t>(g.max_cfg, 1)));
+  return StagedShape{ib, (int)tk, staged_smem_bytes(ib, (int)tk, g.max_es, g.max_nv, t0)};
+}
+
+// The built-in rule between the two generic Enum kernels (the tuner times both on run()): the
+// staged one once a factor's table holds more than 128 (config, variable) entries or its
+// per-thread arrays would exceed 32 edge states. Measured per iteration (T = 0, B = 1 / 32 / 128):
+// 3,000 ternary 10-state factors with all 1,000 configs 0.80 / 0.69 / 1.60 ms per-thread against
+// 0.06 / 0.37 / 1.35 ms staged; 20,000 8-ary binary factors with 128 configs 0.31 / 0.67 / 2.46
+// against 0.22 / 0.40 / 1.52; 50,000 ternary 3-state factors with 14 configs 0.03 / 0.19 / 0.77
+// against 0.28 / 0.41 / 1.59 (a CTA per factor is too coarse for them).
+bool staged_rule(const EnumGeneric& g) { return g.max_cfg * g.max_nv > 128 || g.max_es > 32; }
+
+template <bool T0, class C>
+cudaError_t launch_staged(cudaStream_t s, const Plan& p, const EnumGeneric& g, const C& c,
+                          int64_t B, float t, unsigned* deltas) {
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      enum_staged_kernel<T0, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+  if (attr != cudaSuccess) return attr;
+  const StagedShape sh = staged_shape(g, B, T0);
+  const int64_t groups = (B + sh.ib - 1) / sh.ib;
+  const dim3 grid((unsigned)groups, (unsigned)std::min<int64_t>(g.count, 65535));
+  launch_pdl_smem(s, grid, dim3(kStagedThreads), sh.smem, enum_staged_kernel<T0, C>, c, dev(g), B,
+                  sh.ib, sh.tk, g.max_es, g.max_nv, t, deltas);
+  return cudaSuccess;
+}
+
+// variant: 0 = per-thread kernel, 1 = staged kernel (contexts with HasStaged), -1 = the rule;
+// the debug knob PGBP_DEBUG_ENUM_KERNEL overrides both.
 template <bool T0, class C>
 void launch_enum_generic(cudaStream_t s, const Plan& p, const C& c, int64_t B, float t,
-                         unsigned* deltas, const EnumGeneric* set = nullptr) {
+                         unsigned* deltas, const EnumGeneric* set = nullptr, int variant = -1) {
   const EnumGeneric& g = set != nullptr ? *set : p.enum_generic;
   if (g.count == 0) return;
   ProfileScope ps(kProfEnumGeneric, s);
+  if constexpr (HasStaged<C>::value) {
+    const int knob = debug_knobs().enum_kernel;
+    const bool staged = knob == 1 ? false : knob == 2 ? true : variant >= 0 ? variant == 1
+                                                                             : staged_rule(g);
+    if (staged && launch_staged<T0>(s, p, g, c, B, t, deltas) == cudaSuccess) return;
+  }
   const Launch2 l = launch2(g.count, B, p.sm_count);
   const EnumGenericDev d = dev(g);
   if (g.max_es <= 8) {
@@ -1835,7 +2122,13 @@ void launch_bucket(cudaStream_t s, const Plan& p, const PairwiseBucket& q, const
   }
 }
 
-int num_sites(const Plan& p) { return 4 + (int)p.pairwise.size(); }
+int num_sites(const Plan& p) { return num_tune_sites(p); }
+
+// The generic Enum set the multi-kernel iteration launches (the unary binary factors, when
+// present, run on their own kernel).
+const EnumGeneric& iterate_generic(const Plan& p) {
+  return p.unary2.count > 0 ? p.enum_generic_rest : p.enum_generic;
+}
 
 // sites: the tuned variant per launch site (tuned_sites' layout) or null for the built-in rules
 template <bool T0>
@@ -1857,12 +2150,8 @@ void iterate(cudaStream_t s, const Plan& p, int64_t B, Fused c, float t, bool lo
       launch_bucket<T0>(s, p, q, c, B, t, d, tables, site(2 + qi));
       if (tables != nullptr) tables += q.gemm_floats;
     }
-    if (p.unary2.count > 0) {
-      launch_unary2<T0>(s, p, c, B, t, d);
-      launch_enum_generic<T0>(s, p, c, B, t, d, &p.enum_generic_rest);
-    } else {
-      launch_enum_generic<T0>(s, p, c, B, t, d);
-    }
+    if (p.unary2.count > 0) launch_unary2<T0>(s, p, c, B, t, d);
+    launch_enum_generic<T0>(s, p, c, B, t, d, &iterate_generic(p), site(4 + nq));
     launch_logical<T0>(s, p, 0, c, B, t, low_t, 1, d, site(2 + nq));
     launch_logical<T0>(s, p, 1, c, B, t, low_t, 1, d, site(3 + nq));
     launch_pool<T0>(s, p, c, B, t, 1, d);
@@ -1944,6 +2233,10 @@ const int* tune_sites(const Plan& p, cudaStream_t s, int64_t B, Fused c, float t
         launch_logical<T0>(s, p, w, c, B, t, low_t, 1, dacc, v);
       });
   }
+  if (iterate_generic(p).count > 0)
+    choice[4 + nq] = pick(2, [&](int v) {
+      launch_enum_generic<T0>(s, p, c, B, t, dacc, &iterate_generic(p), v);
+    });
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *tuned_now = true;

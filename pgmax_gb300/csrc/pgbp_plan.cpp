@@ -194,6 +194,10 @@ int pgbp_debug_set(int knob, int64_t value) {
       if (value != 0 && value != 1) return fail(PGBP_ERR_INVALID_ARGUMENT, "expected 0 or 1");
       g_debug.legacy_mma = (int)value;
       return PGBP_OK;
+    case PGBP_DEBUG_ENUM_KERNEL:
+      if (value < 0 || value > 2) return fail(PGBP_ERR_INVALID_ARGUMENT, "expected 0, 1 or 2");
+      g_debug.enum_kernel = (int)value;
+      return PGBP_OK;
     default:
       return fail(PGBP_ERR_INVALID_ARGUMENT, "unknown debug knob %d", knob);
   }
@@ -700,66 +704,72 @@ int pgbp_plan_create(const pgbp_wiring_desc* d, int device, pgbp_plan** out) {
       p.num_enum_pairwise += q.count;
       p.pairwise.push_back(q);
     }
-    pgbp::EnumGeneric& g = p.enum_generic;
-    g.count = (int64_t)g_es.size();
-    g.max_es = max_es;
-    if (g.count > 0) {
-      g.es_begin = bd.upload(g_es);
-      g.n_es = bd.upload(g_nes);
-      g.edge_off = bd.upload(g_eoff);
-      g.edge_size = bd.upload(g_esz);
-      g.edge_slot = bd.upload(g_eslot);
-      g.edge_vs = bd.upload(g_evs);
-      g.row_begin = bd.upload(g_rb);
-      g.n_cfg = bd.upload(g_ncfg);
-      g.n_vars = bd.upload(g_nv);
-      g.cfg_begin = bd.upload(g_cfg);
-      g.row_les = bd.upload(g_les);
-      g.fac = bd.upload(g_fac);
-    }
+    // A generic set from the generic factors that `keep` selects, in their order, with each
+    // factor's configs listed by edge state for the staged kernel: local edge state e of factor
+    // f is held by configs inv_cfg[inv_off[inv_begin[f] + e]] .. inv_cfg[inv_off[inv_begin[f] +
+    // e + 1] - 1], local config indices in increasing order (the order of the reference's scatter
+    // of config sums onto edge states, enum.py:451-475).
+    auto build_generic = [&](pgbp::EnumGeneric& out, auto&& keep) {
+      std::vector<int32_t> o_es, o_nes, o_eoff{0}, o_esz, o_eslot, o_evs, o_rb, o_ncfg, o_nv,
+          o_cfg, o_les, o_fac, o_ib, o_io, o_ic;
+      std::vector<int32_t> cnt;
+      for (size_t i = 0; i < g_es.size(); ++i) {
+        if (!keep(i)) continue;
+        const int nes = g_nes[i], nv = g_nv[i];
+        const int64_t nc = g_ncfg[i];
+        o_es.push_back(g_es[i]);
+        o_nes.push_back(nes);
+        out.max_es = std::max(out.max_es, nes);
+        out.max_nv = std::max(out.max_nv, nv);
+        out.max_cfg = std::max<int64_t>(out.max_cfg, nc);
+        for (int32_t j = g_eoff[i]; j < g_eoff[i + 1]; ++j) {
+          o_esz.push_back(g_esz[j]);
+          o_eslot.push_back(g_eslot[j]);
+          o_evs.push_back(g_evs[j]);
+        }
+        o_eoff.push_back((int32_t)o_esz.size());
+        o_rb.push_back((int32_t)o_les.size());
+        const int32_t* les = g_les.data() + g_rb[i];
+        o_les.insert(o_les.end(), les, les + nc * nv);
+        o_ncfg.push_back((int32_t)nc);
+        o_nv.push_back(nv);
+        o_cfg.push_back(g_cfg[i]);
+        o_fac.push_back(g_fac[i]);
+        // inverse lists: counting sort of the (config, edge state) pairs by edge state
+        cnt.assign((size_t)nes + 1, 0);
+        for (int64_t r = 0; r < nc * nv; ++r) cnt[(size_t)les[r] + 1]++;
+        for (int e = 0; e < nes; ++e) cnt[(size_t)e + 1] += cnt[(size_t)e];
+        const int32_t base = (int32_t)o_ic.size();
+        o_ib.push_back((int32_t)o_io.size());
+        for (int e = 0; e <= nes; ++e) o_io.push_back(base + cnt[(size_t)e]);
+        o_ic.resize((size_t)base + (size_t)(nc * nv));
+        for (int64_t c = 0; c < nc; ++c)
+          for (int v = 0; v < nv; ++v) o_ic[(size_t)base + (size_t)cnt[(size_t)les[c * nv + v]]++] = (int32_t)c;
+      }
+      out.count = (int64_t)o_es.size();
+      if (out.count == 0) return;
+      out.es_begin = bd.upload(o_es);
+      out.n_es = bd.upload(o_nes);
+      out.edge_off = bd.upload(o_eoff);
+      out.edge_size = bd.upload(o_esz);
+      out.edge_slot = bd.upload(o_eslot);
+      out.edge_vs = bd.upload(o_evs);
+      out.row_begin = bd.upload(o_rb);
+      out.n_cfg = bd.upload(o_ncfg);
+      out.n_vars = bd.upload(o_nv);
+      out.cfg_begin = bd.upload(o_cfg);
+      out.row_les = bd.upload(o_les);
+      out.fac = bd.upload(o_fac);
+      out.inv_begin = bd.upload(o_ib);
+      out.inv_off = bd.upload(o_io);
+      out.inv_cfg = bd.upload(o_ic);
+    };
+    build_generic(p.enum_generic, [](size_t) { return true; });
     if (!u2_rec.empty()) {
       p.unary2.count = (int64_t)u2_rec.size();
       p.unary2.rec = bd.upload(u2_rec);
       // the other generic factors, in their order
-      std::vector<int32_t> r_es, r_nes, r_eoff{0}, r_esz, r_eslot, r_evs, r_rb, r_ncfg, r_nv, r_cfg,
-          r_les, r_fac;
-      int r_max = 0;
-      for (size_t i = 0; i < g_es.size(); ++i) {
-        if (g_u2[i]) continue;
-        r_es.push_back(g_es[i]);
-        r_nes.push_back(g_nes[i]);
-        r_max = std::max<int>(r_max, g_nes[i]);
-        for (int32_t j = g_eoff[i]; j < g_eoff[i + 1]; ++j) {
-          r_esz.push_back(g_esz[j]);
-          r_eslot.push_back(g_eslot[j]);
-          r_evs.push_back(g_evs[j]);
-        }
-        r_eoff.push_back((int32_t)r_esz.size());
-        r_rb.push_back((int32_t)r_les.size());
-        r_les.insert(r_les.end(), g_les.begin() + g_rb[i],
-                     g_les.begin() + g_rb[i] + (int64_t)g_ncfg[i] * g_nv[i]);
-        r_ncfg.push_back(g_ncfg[i]);
-        r_nv.push_back(g_nv[i]);
-        r_cfg.push_back(g_cfg[i]);
-        r_fac.push_back(g_fac[i]);
-      }
-      pgbp::EnumGeneric& r = p.enum_generic_rest;
-      r.count = (int64_t)r_es.size();
-      r.max_es = r_max;
-      if (r.count > 0) {
-        r.es_begin = bd.upload(r_es);
-        r.n_es = bd.upload(r_nes);
-        r.edge_off = bd.upload(r_eoff);
-        r.edge_size = bd.upload(r_esz);
-        r.edge_slot = bd.upload(r_eslot);
-        r.edge_vs = bd.upload(r_evs);
-        r.row_begin = bd.upload(r_rb);
-        r.n_cfg = bd.upload(r_ncfg);
-        r.n_vars = bd.upload(r_nv);
-        r.cfg_begin = bd.upload(r_cfg);
-        r.row_les = bd.upload(r_les);
-        r.fac = bd.upload(r_fac);
-      }
+      build_generic(p.enum_generic_rest, [&](size_t i) { return !g_u2[i]; });
     }
     if (bd.err) return bail(bd.err);
   }
@@ -1239,7 +1249,7 @@ int pgbp_plan_tuning_set(const pgbp_plan* plan, const pgbp_tuning_entry* entries
                          int64_t num_entries) {
   if (!plan || (num_entries > 0 && !entries)) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
   const pgbp::Plan& p = plan->p;
-  const int sites = 4 + (int)p.pairwise.size();
+  const int sites = pgbp::num_tune_sites(p);
   for (int64_t i = 0; i < num_entries; ++i) {
     const pgbp_tuning_entry& e = entries[i];
     if (e.batch <= 0 || e.path < -1 || e.path > 2 || (e.num_sites != 0 && e.num_sites != sites))

@@ -243,12 +243,15 @@ def wait_timeouts():
 DEBUG_WAIT_LIMIT_NS = 1
 DEBUG_SKIP_TABLE_COPY = 2
 DEBUG_LEGACY_MMA = 3
+DEBUG_ENUM_KERNEL = 4
 
 
 def debug_set(knob, value):
   """Process-wide debug setting (pgbp_debug_set): DEBUG_WAIT_LIMIT_NS (0 = the built-in 2 s),
   DEBUG_SKIP_TABLE_COPY (1 = the exp-domain kernels' table wait runs out with no copy issued) or
-  DEBUG_LEGACY_MMA (1 = shared 64 x 64 tables of one instance on the mma.sync kernel)."""
+  DEBUG_LEGACY_MMA (1 = shared 64 x 64 tables of one instance on the mma.sync kernel) or
+  DEBUG_ENUM_KERNEL (generic EnumFactors: 1 = per-thread kernel, 2 = staged kernel, 0 = tuned /
+  rule)."""
   check(load().pgbp_debug_set(int(knob), int(value)), "pgbp_debug_set")
 
 

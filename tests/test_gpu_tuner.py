@@ -55,10 +55,12 @@ def test_first_run_tunes_and_exports_the_sites():
   e = [x for x in entries if x["batch"] == 128 and x["temperature0"]]
   assert len(e) == 1
   sites = e[0]["sites"]
-  assert len(sites) == 4 + plan.info["num_pairwise_buckets"]
+  assert len(sites) == 5 + plan.info["num_pairwise_buckets"]
   assert sites[0] in (0, 1) and sites[2] in (0, 1)  # binary sums and the 2 x 2 bucket timed
   assert sites[1] == -1                             # no other variables
-  assert all(v == -1 for v in sites[3:])            # no other bucket, no OR / AND factors
+  # no other bucket, no OR / AND factors, no generic Enum factors beyond the unary biases (which
+  # run on their own kernel)
+  assert all(v == -1 for v in sites[3:])
 
 
 @pytest.mark.parametrize("temperature", [0.0, 1.0])
@@ -71,7 +73,7 @@ def test_every_variant_gives_identical_results(builder, kw, temperature):
   outs = []
   for forced in (0, 1):
     plan = _plan(w)
-    n = 4 + plan.info["num_pairwise_buckets"]
+    n = 5 + plan.info["num_pairwise_buckets"]
     plan.load_tuning([{"batch": 8, "temperature0": temperature == 0.0, "path": 0,
                        "sites": [forced] * n}])
     lp, ev, m = _inputs(plan, 8, 3)
@@ -90,7 +92,7 @@ def test_decisions_round_trip_and_json_cache(tmp_path, monkeypatch):
   lp, ev, m = _inputs(plan, 8, 1)
   plan.run(lp, ev, m, 3, 0.5, 0.0)
   first = plan.tuning()
-  assert first and all(len(e["sites"]) == 4 + plan.info["num_pairwise_buckets"] for e in first)
+  assert first and all(len(e["sites"]) == 5 + plan.info["num_pairwise_buckets"] for e in first)
   path = str(tmp_path / "tune.json")
   plan.save_tuning(path)
   table = json.load(open(path))
@@ -109,5 +111,5 @@ def test_entries_that_do_not_fit_the_plan_are_rejected():
   with pytest.raises(Exception, match="does not fit"):
     plan.load_tuning([{"batch": 4, "temperature0": True, "path": 0, "sites": [0, 1]}])
   with pytest.raises(Exception, match="out of range"):
-    n = 4 + plan.info["num_pairwise_buckets"]
+    n = 5 + plan.info["num_pairwise_buckets"]
     plan.load_tuning([{"batch": 4, "temperature0": True, "path": 0, "sites": [2] * n}])
