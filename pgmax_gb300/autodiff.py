@@ -11,8 +11,8 @@ respect to the log potentials). Here the same chain is differentiable in torch:
   the log potentials, the evidence and the initial messages.
 * `beliefs` is get_beliefs' flat scatter-add, whose backward is pgbp_beliefs_vjp (a gather).
 
-Graphs must consist of dense pairwise EnumFactors and the temperature must be > 0 (the adjoint's
-scope); anything else raises ValueError at backward time.
+Graphs must consist of EnumFactors (any config tables) and the temperature must be > 0 (the
+adjoint's scope); anything else raises ValueError at backward time.
 """
 
 from typing import Optional, Tuple

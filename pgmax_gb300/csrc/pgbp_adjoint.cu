@@ -1,5 +1,5 @@
 // Reverse mode of the damped BP iterations of run_with_diffs (pgmax/infer/bp.py:63-155) for graphs
-// whose factors are all dense pairwise EnumFactors, at temperature > 0: the hand-written adjoint
+// whose factors are all EnumFactors, at temperature > 0: the hand-written adjoint
 // behind differentiable BP (gradients of a loss on the final messages with respect to the log
 // potentials, the evidence and the initial messages).
 //
@@ -16,6 +16,11 @@
 //   gs_ij = gf1[i] p1_ij + gf2[j] p2_ij,  p1_ij = softmax_j(s_ij / T), p2_ij = softmax_i(s_ij / T)
 //   gvtof1[i] = sum_j gs_ij - gf1[i],  gvtof2[j] = sum_i gs_ij - gf2[j],  glp_ij += gs_ij
 //   gvsum[v] = sum_{e in v} gvtof[e],  gev[v] += gvsum[v]
+// For any other config table (generic EnumFactors) with config sums s_c = sum_{e in c} vtof[e] +
+// lp_c and f[e] = T log sum_{c holds e} exp((s_c - M_e) / T) + M_e - vtof[e]:
+//   gs_c = sum_{e in c} gf[e] p_e(c),  p_e(c) = exp((s_c - M_e) / T) / sum_{c' holds e} exp(...)
+//   gvtof[e] = sum_{c holds e} gs_c - gf[e],  glp_c += gs_c
+// (the pairwise formulas are this with c = (i, j)).
 //   g[e] (= dL/dm) = gdir[e] + gvsum[v(e)] - gvtof[e]
 // g is never stored: the next (earlier) step's factor kernel reads gdir, gvsum and gvtof of the
 // step after it and forms g for its own edges, so one backward step is two launches (factors,
@@ -138,16 +143,18 @@ __device__ __forceinline__ void pair_forward(Pair<M>& st, const int4 q, int n1, 
 }
 
 // Damping, normalisation and clipping of one edge with k <= M states (bp.py:127-133).
+// M = 0: k bounds the loops at run time (edges of any size).
 template <int M>
 __device__ __forceinline__ void edge_forward(const float* o, const float* f, int k, float d,
                                              float omd, float* __restrict__ out) {
-  constexpr int U = M <= 8 ? M : 1;
+  constexpr int U = M > 0 && M <= 8 ? M : 1;
+  const int n = M > 0 ? M : k;
   float mx = -INFINITY;
 #pragma unroll U
-  for (int s = 0; s < M; ++s)
+  for (int s = 0; s < n; ++s)
     if (s < k) mx = maxn(mx, d * o[s] + omd * f[s]);
 #pragma unroll U
-  for (int s = 0; s < M; ++s)
+  for (int s = 0; s < n; ++s)
     if (s < k) out[s] = maxn((d * o[s] + omd * f[s]) - mx, kMsgNegInf);
 }
 
@@ -157,11 +164,12 @@ template <int M>
 __device__ __forceinline__ void edge_backward(const float* o, const float* f, int k, float d,
                                               float omd, const float* g, float* gf,
                                               float* __restrict__ gdir) {
-  constexpr int U = M <= 8 ? M : 1;
+  constexpr int U = M > 0 && M <= 8 ? M : 1;
+  const int n = M > 0 ? M : k;
   int arg = 0;
   float nmax = d * o[0] + omd * f[0];
 #pragma unroll U
-  for (int s = 1; s < M; ++s)
+  for (int s = 1; s < n; ++s)
     if (s < k) {
       const float n = d * o[s] + omd * f[s];
       if (n > nmax) {
@@ -171,14 +179,14 @@ __device__ __forceinline__ void edge_backward(const float* o, const float* f, in
     }
   float gsum = 0.0f;
 #pragma unroll U
-  for (int s = 0; s < M; ++s)
+  for (int s = 0; s < n; ++s)
     if (s < k) {
       const float gy = ((d * o[s] + omd * f[s]) - nmax >= kMsgNegInf) ? g[s] : 0.0f;
       gf[s] = gy;
       gsum += gy;
     }
 #pragma unroll U
-  for (int s = 0; s < M; ++s)
+  for (int s = 0; s < n; ++s)
     if (s < k) {
       const float gn = gf[s] - (s == arg ? gsum : 0.0f);
       gf[s] = omd * gn;
@@ -294,6 +302,144 @@ __global__ void __launch_bounds__(256) pairwise_backward_kernel(PairArgs a, cons
   }
 }
 
+// Generic EnumFactors (Plan::enum_generic): a thread per (factor, instance), the factor's edge
+// states in per-thread arrays of MAXES entries.
+struct GenArgs {
+  const int32_t* __restrict__ es_begin;
+  const int32_t* __restrict__ n_es;
+  const int32_t* __restrict__ edge_off;
+  const int32_t* __restrict__ edge_size;
+  const int32_t* __restrict__ edge_vs;
+  const int32_t* __restrict__ row_begin;
+  const int32_t* __restrict__ n_cfg;
+  const int32_t* __restrict__ n_vars;
+  const int32_t* __restrict__ cfg_begin;
+  const int32_t* __restrict__ row_les;
+  int64_t count;
+  int64_t n_es_all, nvs, np_, B;
+  const float* __restrict__ lp;
+  int64_t lps;
+  float d, omd, t;
+};
+
+template <int MAXES>
+struct Gen {
+  float o[MAXES], v[MAXES], mx[MAXES], se[MAXES], f[MAXES];
+};
+
+// The factor's forward quantities for one instance (enum.py:451-475, the engine's operations in
+// its order: config sums in variable order, then max and exp-sum in increasing config order).
+template <int MAXES>
+__device__ __forceinline__ void gen_forward(Gen<MAXES>& st, const GenArgs& a, int64_t u,
+                                            const float* __restrict__ m,
+                                            const float* __restrict__ vsum,
+                                            const float* __restrict__ lpb) {
+  const int64_t e0 = a.es_begin[u];
+  const int n = a.n_es[u], nv = a.n_vars[u], ncfg = a.n_cfg[u];
+  const int32_t* rows0 = a.row_les + a.row_begin[u];
+  int pos = 0;
+  for (int j = a.edge_off[u]; j < a.edge_off[u + 1]; ++j) {
+    const int k = a.edge_size[j];
+    const int64_t vs0 = a.edge_vs[j];
+    for (int i = 0; i < k; ++i) {
+      st.o[pos + i] = m[e0 + pos + i];
+      st.v[pos + i] = vsum[vs0 + i] - st.o[pos + i];
+    }
+    pos += k;
+  }
+  for (int e = 0; e < n; ++e) {
+    st.mx[e] = -INFINITY;
+    st.se[e] = 0.0f;
+  }
+  for (int c = 0; c < ncfg; ++c) {
+    const int32_t* rows = rows0 + (int64_t)c * nv;
+    float sum = 0.0f;
+    for (int i = 0; i < nv; ++i) sum += st.v[rows[i]];
+    sum = sum + clip_lp(lpb[c]);
+    for (int i = 0; i < nv; ++i) st.mx[rows[i]] = maxn(st.mx[rows[i]], sum);
+  }
+  for (int c = 0; c < ncfg; ++c) {
+    const int32_t* rows = rows0 + (int64_t)c * nv;
+    float sum = 0.0f;
+    for (int i = 0; i < nv; ++i) sum += st.v[rows[i]];
+    sum = sum + clip_lp(lpb[c]);
+    for (int i = 0; i < nv; ++i) st.se[rows[i]] += expf(div_t(sum - st.mx[rows[i]], a.t));
+  }
+  for (int e = 0; e < n; ++e) st.f[e] = (a.t * logf(st.se[e]) + st.mx[e]) - st.v[e];
+}
+
+template <int MAXES>
+__global__ void __launch_bounds__(256) generic_forward_kernel(GenArgs a, const float* m,
+                                                              const float* vsum, float* out) {
+  pdl_begin();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count * a.B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / a.count, u = i % a.count;
+    Gen<MAXES> st;
+    gen_forward<MAXES>(st, a, u, m + b * a.n_es_all, vsum + b * a.nvs,
+                       a.lp + b * a.lps + a.cfg_begin[u]);
+    float* o = out + b * a.n_es_all + a.es_begin[u];
+    int pos = 0;
+    for (int j = a.edge_off[u]; j < a.edge_off[u + 1]; ++j) {
+      const int k = a.edge_size[j];
+      edge_forward<0>(st.o + pos, st.f + pos, k, a.d, a.omd, o + pos);
+      pos += k;
+    }
+  }
+}
+
+template <int MAXES>
+__global__ void __launch_bounds__(256) generic_backward_kernel(GenArgs a, const float* m,
+                                                               const float* vsum, GradIn gin,
+                                                               float* __restrict__ gdir,
+                                                               float* __restrict__ gvtof,
+                                                               float* __restrict__ glp) {
+  pdl_begin();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count * a.B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / a.count, u = i % a.count;
+    const int64_t k0 = a.cfg_begin[u];
+    const float* lpb = a.lp + b * a.lps + k0;
+    Gen<MAXES> st;
+    gen_forward<MAXES>(st, a, u, m + b * a.n_es_all, vsum + b * a.nvs, lpb);
+    const int64_t e0 = b * a.n_es_all + a.es_begin[u];
+    const int n = a.n_es[u], nv = a.n_vars[u], ncfg = a.n_cfg[u];
+    // g = dL/d(new messages) of the factor's edge states; gf = dL/df
+    float g[MAXES], gf[MAXES];
+    int pos = 0;
+    for (int j = a.edge_off[u]; j < a.edge_off[u + 1]; ++j) {
+      const int k = a.edge_size[j];
+      const int64_t vs0 = a.edge_vs[j];
+      for (int s = 0; s < k; ++s) {
+        const int64_t e = e0 + pos + s;
+        g[pos + s] = gin.gexp ? gin.gexp[e]
+                              : (gin.gdir[e] + gin.gvsum[b * a.nvs + vs0 + s]) - gin.gvtof[e];
+      }
+      edge_backward<0>(st.o + pos, st.f + pos, k, a.d, a.omd, g + pos, gf + pos, gdir + e0 + pos);
+      pos += k;
+    }
+    // g becomes the accumulator of dL/dvtof
+    for (int e = 0; e < n; ++e) g[e] = -gf[e];
+    const int32_t* rows0 = a.row_les + a.row_begin[u];
+    float* glpb = glp + b * a.np_ + k0;
+    for (int c = 0; c < ncfg; ++c) {
+      const int32_t* rows = rows0 + (int64_t)c * nv;
+      const float raw = lpb[c];
+      float sum = 0.0f;
+      for (int x = 0; x < nv; ++x) sum += st.v[rows[x]];
+      sum = sum + clip_lp(raw);
+      float gs = 0.0f;
+      for (int x = 0; x < nv; ++x) {
+        const int e = rows[x];
+        gs += gf[e] * (expf(div_t(sum - st.mx[e], a.t)) / st.se[e]);
+      }
+      for (int x = 0; x < nv; ++x) g[rows[x]] += gs;
+      if (raw >= -kLpClip && raw <= kLpClip) glpb[c] += gs;
+    }
+    for (int e = 0; e < n; ++e) gvtof[e0 + e] = g[e];
+  }
+}
+
 // gvsum[v] = sum_{e in v} gvtof[e]; gev[v] += gvsum[v].
 __global__ void __launch_bounds__(256) gvsum_kernel(const int32_t* __restrict__ vs_off,
                                                     const int32_t* __restrict__ vs_edges,
@@ -402,6 +548,56 @@ PairArgs pair_args(const Plan& p, const PairwiseBucket& q, int64_t B, const floa
                   p.num_potentials, B, lp, lps, d, omd, t};
 }
 
+GenArgs gen_args(const Plan& p, int64_t B, const float* lp, int64_t lps, float d, float omd,
+                 float t) {
+  const EnumGeneric& g = p.enum_generic;
+  return GenArgs{g.es_begin, g.n_es, g.edge_off, g.edge_size, g.edge_vs, g.row_begin, g.n_cfg,
+                 g.n_vars, g.cfg_begin, g.row_les, g.count, p.num_edge_states, p.num_var_states,
+                 p.num_potentials, B, lp, lps, d, omd, t};
+}
+
+// The generic factors' per-thread array size: the smallest of 8, 32, 128, 512 that holds the
+// largest factor's edge states.
+int gen_maxes(const Plan& p) {
+  const int m = p.enum_generic.max_es;
+  return m <= 8 ? 8 : m <= 32 ? 32 : m <= 128 ? 128 : 512;
+}
+
+void launch_generic_forward(const Plan& p, const GenArgs& a, cudaStream_t s, const float* m,
+                            const float* vsum, float* out) {
+  if (a.count == 0) return;
+  const dim3 grid = grid_for(a.count * a.B, p.sm_count);
+  switch (gen_maxes(p)) {
+    case 8: launch_pdl(s, grid, dim3(256), generic_forward_kernel<8>, a, m, vsum, out); break;
+    case 32: launch_pdl(s, grid, dim3(256), generic_forward_kernel<32>, a, m, vsum, out); break;
+    case 128: launch_pdl(s, grid, dim3(256), generic_forward_kernel<128>, a, m, vsum, out); break;
+    default: launch_pdl(s, grid, dim3(256), generic_forward_kernel<512>, a, m, vsum, out); break;
+  }
+}
+
+void launch_generic_backward(const Plan& p, const GenArgs& a, cudaStream_t s, const float* m,
+                             const float* vsum, const GradIn& gin, float* gdir, float* gvtof,
+                             float* glp) {
+  if (a.count == 0) return;
+  const dim3 grid = grid_for(a.count * a.B, p.sm_count);
+  switch (gen_maxes(p)) {
+    case 8:
+      launch_pdl(s, grid, dim3(256), generic_backward_kernel<8>, a, m, vsum, gin, gdir, gvtof, glp);
+      break;
+    case 32:
+      launch_pdl(s, grid, dim3(256), generic_backward_kernel<32>, a, m, vsum, gin, gdir, gvtof, glp);
+      break;
+    case 128:
+      launch_pdl(s, grid, dim3(256), generic_backward_kernel<128>, a, m, vsum, gin, gdir, gvtof,
+                 glp);
+      break;
+    default:
+      launch_pdl(s, grid, dim3(256), generic_backward_kernel<512>, a, m, vsum, gin, gdir, gvtof,
+                 glp);
+      break;
+  }
+}
+
 template <int M>
 void launch_forward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m, const float* vsum,
                       float* out) {
@@ -448,6 +644,7 @@ void recompute(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_
         default: launch_forward_m<64>(a, p.sm_count, s, mj, vj, next); break;
       }
     }
+    launch_generic_forward(p, gen_args(p, B, lp, lps, d, omd, t), s, mj, vj, next);
   }
 }
 
@@ -474,6 +671,8 @@ void backward_step(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
         break;
     }
   }
+  launch_generic_backward(p, gen_args(p, B, lp, lps, d, omd, t), s, m, vsum, gin, out.gdir,
+                          out.gvtof, glp);
   launch_pdl(s, grid_for(p.num_var_states * B, p.sm_count), dim3(256), gvsum_kernel, p.vs_off,
              p.vs_edges, p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
 }
@@ -499,10 +698,8 @@ cudaError_t aux_stream(int device, cudaStream_t* out) {
 const char* adjoint_unsupported(const Plan& p) {
   if (p.shared_potentials)
     return "the adjoint needs one potential table per factor; the plan shares tables";
-  if (p.enum_generic.count > 0)
-    return "the adjoint covers dense pairwise EnumFactors only; the graph has other EnumFactors";
   if (p.logical[0].count > 0 || p.logical[1].count > 0 || p.pool.count > 0)
-    return "the adjoint covers dense pairwise EnumFactors only; the graph has OR/AND/Pool factors";
+    return "the adjoint covers EnumFactors only; the graph has OR/AND/Pool factors";
   return "";
 }
 

@@ -156,9 +156,69 @@ def test_unsupported_graphs_and_temperature_raise():
   dd = _load("case_deconv_T1")
   p2 = _plan(dd)
   ck2 = torch.zeros((1, 1, p2.num_edge_states), device="cuda")
-  with pytest.raises(ValueError, match="dense pairwise"):
+  with pytest.raises(ValueError, match="EnumFactors only"):
     p2.run_vjp(dd["log_potentials"], dd["evidence"], ck2, 1,
                torch.zeros((1, p2.num_edge_states), device="cuda"), 0.5, 1.0, 1)
+
+
+def _generic_graph(states, arity, n_fac, keep, seed):
+  """A graph of higher-order EnumFactors (random variable sets and config subsets) as a fixture
+  dict: flat wiring, log potentials, zero evidence and messages."""
+  import itertools  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import factor, fgraph, infer, vgroup  # pylint: disable=g-import-not-at-top
+  rng = np.random.RandomState(seed)
+  n_vars = max(3 * arity, 8)
+  ns = np.array([states[i % len(states)] for i in range(n_vars)], dtype=np.int64)
+  var = vgroup.NDVarArray(num_states=ns, shape=(n_vars,))
+  fg = fgraph.FactorGraph(variable_groups=[var])
+  seen = set()
+  while len(seen) < n_fac:
+    vs = tuple(sorted(rng.choice(n_vars, size=arity, replace=False).tolist()))
+    if vs in seen:
+      continue
+    seen.add(vs)
+    allc = np.array(list(itertools.product(*[range(int(ns[v])) for v in vs])), dtype=np.int64)
+    if keep < 1.0:
+      sel = rng.rand(allc.shape[0]) < keep
+      sel[rng.randint(allc.shape[0])] = True
+      allc = allc[sel]
+    fg.add_factors(factor.EnumFactor(variables=[var[v] for v in vs], factor_configs=allc,
+                                     log_potentials=rng.normal(size=(allc.shape[0],))))
+  w = infer.InfererContext(fg.bp_state).flat_wiring()
+  w["num_variables"] = n_vars
+  nvs = int(np.asarray(w["var_states_for_edge_states"]).max()) + 1
+  nes = np.asarray(w["var_states_for_edge_states"]).shape[0]
+  return {"wiring": w, "log_potentials": np.asarray(fg.bp_state.log_potentials.value, np.float32),
+          "evidence": rng.normal(size=(nvs,)).astype(np.float32),
+          "ftov_msgs_in": np.zeros((nes,), np.float32)}
+
+
+# Higher-order and sparse config tables (the generic Enum adjoint kernels), and the RBM's
+# unary bias factors next to its pairwise ones, each at temperature > 0.
+GENERIC = {
+    "ternary_k3_dense": ((3,), 3, 10, 1.0),
+    "quaternary_mixed_sparse": ((2, 3, 4), 4, 12, 0.4),
+    "binary_6ary_half": ((2,), 6, 8, 0.5),
+}
+
+
+@pytest.mark.parametrize("temperature", [1.0, 0.6])
+@pytest.mark.parametrize("name", sorted(GENERIC) + ["case_rbm_s0"])
+def test_vjp_generic_enum_factors_match_float64_autograd(name, temperature):
+  torch = _torch()
+  d = _load(name) if name.startswith("case_") else _generic_graph(*GENERIC[name], seed=4)
+  plan = _plan(d)
+  B, iters, k = 3, 12, 4
+  lp, ev, m, w = _inputs(d, B, True, True, seed=9)
+  out, _, ck = plan.run_checkpointed(lp, ev, m, iters, 0.5, temperature, k)
+  g_lp, g_ev, g_m = plan.run_vjp(lp, ev, ck, iters, torch.as_tensor(w).cuda(), 0.5, temperature,
+                                 k, want_msgs_in=True)
+  torch.cuda.synchronize()
+  ref_out, (r_lp, r_ev, r_m) = _reference_grads(d, lp, ev, m, w, iters, 0.5, temperature)
+  np.testing.assert_allclose(out.cpu().numpy(), ref_out, atol=5e-5, rtol=0)
+  _close(g_lp.cpu().numpy(), r_lp, "g_log_potentials")
+  _close(g_ev.cpu().numpy(), r_ev, "g_evidence")
+  _close(g_m.cpu().numpy(), r_m, "g_msgs_in")
 
 
 def test_autograd_function_through_drop_in_api():
