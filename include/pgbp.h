@@ -291,8 +291,8 @@ int pgbp_argmax_rows(void* stream, int64_t rows, int64_t k, const float* in, int
 
 /* Autotuner decisions. pgbp_run times, once per (batch, temperature == 0), the eligible execution
  * paths and then, on the multi-kernel path, the kernel variants of each launch site (the binary
- * variable sums: 1 or 4 instances per thread; the other variable sums: per state or by
- * variable; each dense 2 x 2 pairwise bucket: 1 or 4 instances per thread; OR and AND: a thread
+ * variable sums: 1, 4 or 2 instances per thread, variants 0, 1, 2; the other variable sums: per
+ * state or by variable; each dense 2 x 2 pairwise bucket: 1 or 4 instances per thread; OR and AND: a thread
  * or a warp per factor; the generic EnumFactors: a thread per (factor, instance) or a CTA per
  * factor staged in shared memory). Those variants give bit-identical results. A site of shared K x K tables
  * at temperature > 0 is not timed (the exp-domain tensor-core kernel, variant 1, agrees with the

@@ -1447,6 +1447,48 @@ __global__ void __launch_bounds__(256) varsum_binary_x4_kernel(VarsumDev v, bool
   }
 }
 
+// Binary variable sums, 2 instances per thread (float2), sixteen slots in flight: half the
+// threads of the one-instance kernel, so a batch like the RBM's (1,284 variables x 128 instances)
+// fits in one wave of resident blocks instead of leaving its longest chains to a second one.
+__global__ void __launch_bounds__(256, 3) varsum_binary_x2_kernel(VarsumDev v, bool use_runs,
+                                                                  const float* __restrict__ msgs,
+                                                                  const float* __restrict__ ev,
+                                                                  int64_t evs, int64_t evb,
+                                                                  float* __restrict__ vsum,
+                                                                  int64_t B) {
+  pdl_begin();
+  const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (b >= B) return;
+  const int64_t u0 = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  const int64_t ustep = (int64_t)gridDim.y * blockDim.y;
+  const float* col = msgs + b;
+  for (int64_t u = u0; u < v.count; u += ustep) {
+    const int64_t v0 = v.vs[u];
+    float2 s0, s1;
+    if (evb == 0) {
+      const float e0 = ev[v0 * evs], e1 = ev[(v0 + 1) * evs];
+      s0 = make_float2(e0, e0);
+      s1 = make_float2(e1, e1);
+    } else {
+      s0 = *reinterpret_cast<const float2*>(ev + v0 * evs + b);
+      s1 = *reinterpret_cast<const float2*>(ev + (v0 + 1) * evs + b);
+    }
+    for_each_slot<16>(v, use_runs, u,
+                      [&](int64_t slot) { return *reinterpret_cast<const float2*>(col + slot * B); },
+                      [&](float2 c2) {
+                        float m0, m1;
+                        decode2(c2.x, m0, m1);
+                        s0.x += m0;
+                        s1.x += m1;
+                        decode2(c2.y, m0, m1);
+                        s0.y += m0;
+                        s1.y += m1;
+                      });
+    *reinterpret_cast<float2*>(vsum + v0 * B + b) = s0;
+    *reinterpret_cast<float2*>(vsum + (v0 + 1) * B + b) = s1;
+  }
+}
+
 // ----------------------------------------------------------------------------- small graphs
 // Graphs whose messages, variable sums and evidence fit in shared memory (Ising 50x50: 10,000
 // slots) run every iteration in one launch: one CTA per instance keeps its state on chip and
@@ -2074,10 +2116,15 @@ void launch_varsum(cudaStream_t s, const Plan& p, int64_t B, const float* cur, c
   ProfileScope ps(kProfVarsum, s);
   const VarsumSet& vb = p.varsum_binary;
   // 4 instances per thread only when that still leaves >= 16 warps per SM: the per-variable sums
-  // are serial chains, so latency is hidden by warps, not by the work inside one thread
+  // are serial chains, so latency is hidden by warps, not by the work inside one thread.
+  // vb_variant: 0 one instance per thread, 1 four, 2 two (B % 2 == 0); -1 the rule.
   const bool x4 = B % 4 == 0 && (vb_variant >= 0 ? vb_variant == 1
                                                  : vb.count * (B / 4) >= (int64_t)p.sm_count * 16 * 32);
-  if (vb.count > 0 && x4) {
+  if (vb.count > 0 && vb_variant == 2 && B % 2 == 0) {
+    const Launch2 l = launch2(vb.count, B / 2, p.sm_count);
+    launch_pdl(s, l.grid, l.block, varsum_binary_x2_kernel, dev(vb), vb.use_runs, cur, ev, evs, evb,
+               vsum, B);
+  } else if (vb.count > 0 && x4) {
     const Launch2 l = launch2_x4(vb.count, B, p.sm_count);
     launch_pdl(s, l.grid, l.block, varsum_binary_x4_kernel, dev(vb), vb.use_runs, cur, ev, evs, evb,
                vsum, B);
@@ -2209,8 +2256,14 @@ const int* tune_sites(const Plan& p, cudaStream_t s, int64_t B, Fused c, float t
     return best;
   };
   // the two variable-sum sites (binary, other) are timed with the other one's rule in place
-  if (p.varsum_binary.count > 0 && B % 4 == 0)
-    choice[0] = pick(2, [&](int v) { launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, v, -1); });
+  if (p.varsum_binary.count > 0 && B % 2 == 0) {
+    // one, two and (B % 4 == 0) four instances per thread
+    const int vb_variants[3] = {0, 2, 1};
+    const int k = pick(B % 4 == 0 ? 3 : 2, [&](int v) {
+      launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, vb_variants[v], -1);
+    });
+    choice[0] = k >= 0 ? vb_variants[k] : -1;
+  }
   if (p.varsum_other.byvar_groups > 0 && p.varsum_other.count > 0)
     choice[1] = pick(2, [&](int v) { launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum, -1, v); });
   launch_varsum(s, p, B, c.cur, ev, evs, evb, vsum);  // variable sums for the factor trials

@@ -1255,7 +1255,7 @@ int pgbp_plan_tuning_set(const pgbp_plan* plan, const pgbp_tuning_entry* entries
     if (e.batch <= 0 || e.path < -1 || e.path > 2 || (e.num_sites != 0 && e.num_sites != sites))
       return fail(PGBP_ERR_INVALID_ARGUMENT, "tuning entry %lld does not fit this plan", (long long)i);
     for (int k = 0; k < e.num_sites; ++k)
-      if (e.site[k] < -1 || e.site[k] > 1)
+      if (e.site[k] < -1 || e.site[k] > (k == 0 ? 2 : 1))
         return fail(PGBP_ERR_INVALID_ARGUMENT, "tuning entry %lld: variant out of range", (long long)i);
     if ((e.path == 1 && p.small_graph_smem == 0) || (e.path == 2 && p.cluster_size == 0))
       return fail(PGBP_ERR_INVALID_ARGUMENT, "tuning entry %lld: path not available", (long long)i);

@@ -56,7 +56,7 @@ def test_first_run_tunes_and_exports_the_sites():
   assert len(e) == 1
   sites = e[0]["sites"]
   assert len(sites) == 5 + plan.info["num_pairwise_buckets"]
-  assert sites[0] in (0, 1) and sites[2] in (0, 1)  # binary sums and the 2 x 2 bucket timed
+  assert sites[0] in (0, 1, 2) and sites[2] in (0, 1)  # binary sums and the 2 x 2 bucket timed
   assert sites[1] == -1                             # no other variables
   # no other bucket, no OR / AND factors, no generic Enum factors beyond the unary biases (which
   # run on their own kernel)
@@ -71,18 +71,21 @@ def test_every_variant_gives_identical_results(builder, kw, temperature):
   torch = _torch()
   w = _wiring(builder, **kw)
   outs = []
-  for forced in (0, 1):
+  # every site on variant 0, every site on variant 1, and the binary sums on variant 2 (two
+  # instances per thread) with the rest on 0
+  for forced in ((0, 0), (1, 1), (2, 0)):
     plan = _plan(w)
     n = 5 + plan.info["num_pairwise_buckets"]
     plan.load_tuning([{"batch": 8, "temperature0": temperature == 0.0, "path": 0,
-                       "sites": [forced] * n}])
+                       "sites": [forced[0]] + [forced[1]] * (n - 1)}])
     lp, ev, m = _inputs(plan, 8, 3)
     out, deltas = plan.run(lp, ev, m, 12, 0.5, temperature)
     outs.append((out, deltas))
   # bit patterns, so that NaN compares equal to NaN (random messages drive one deconvolution
   # instance to NaN at T = 1, in the float32 oracle as well)
   same = lambda a, b: torch.equal(a.contiguous().view(torch.int32), b.contiguous().view(torch.int32))
-  assert same(outs[0][0], outs[1][0]) and same(outs[0][1], outs[1][1])
+  for o in outs[1:]:
+    assert same(outs[0][0], o[0]) and same(outs[0][1], o[1])
 
 
 def test_decisions_round_trip_and_json_cache(tmp_path, monkeypatch):
