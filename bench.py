@@ -171,6 +171,155 @@ def run_ising(args):
   return 0
 
 
+ENUM_VARS, ENUM_K, ENUM_FACTORS, ENUM_B, ENUM_ITERS = 2000, 10, 3000, 128, 50
+
+
+def build_enum(seed=0):
+  """Higher-order EnumFactors: 3,000 ternary factors over random triples of 2,000 variables of 10
+  states, each with the full 1,000-config table (one shared config list, per-factor potentials
+  N(0, 1)); every variable also gets Gumbel evidence in the runs."""
+  import itertools  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import fgraph, fgroup, vgroup  # pylint: disable=g-import-not-at-top
+  rng = np.random.default_rng(seed)
+  var = vgroup.NDVarArray(num_states=ENUM_K, shape=(ENUM_VARS,))
+  fg = fgraph.FactorGraph(variable_groups=[var])
+  seen, triples = set(), []
+  while len(triples) < ENUM_FACTORS:
+    t = tuple(sorted(rng.choice(ENUM_VARS, size=3, replace=False).tolist()))
+    if t not in seen:
+      seen.add(t)
+      triples.append(t)
+  configs = np.array(list(itertools.product(range(ENUM_K), repeat=3)), dtype=np.int64)
+  fg.add_factors(fgroup.EnumFactorGroup(
+      variables_for_factors=[[var[i] for i in t] for t in triples], factor_configs=configs,
+      log_potentials=rng.normal(size=(ENUM_FACTORS, configs.shape[0])).astype(np.float32)))
+  return fg, var
+
+
+def run_enum(args):
+  """Perturb-and-MAP on a graph of higher-order EnumFactors (generic config tables, the staged or
+  per-thread generic kernel as the tuner picks): 128 samples, 50 iterations at T = 0 per step,
+  Gumbel noise generated on the GPU inside the run. Messages: 90,000 edge states x 128 samples
+  (46 MB) per buffer; the config rows and potentials (24 MB) are shared by the batch."""
+  import torch  # pylint: disable=g-import-not-at-top
+  from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
+  fg, var = build_enum()
+  bp = infer.BP(fg.bp_state)
+  base = bp.init()
+  dev = torch.device("cuda", 0)
+  stream = torch.cuda.current_stream(dev)
+  seeds = iter(range(1 << 40, 1 << 62))
+  map_h = torch.empty((ENUM_B, ENUM_VARS), dtype=torch.int32).pin_memory()
+  flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # larger than the 129 MB L2
+
+  def step():
+    out = bp.run_perturbed(base, ENUM_ITERS, next(seeds), ENUM_B, damping=0.5, temperature=0.0)
+    return infer.decode_map_states(bp.get_beliefs(out))
+
+  for _ in range(args.warmup):
+    step()
+  torch.cuda.synchronize()
+  s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  ms = 0.0
+  with ClockSampler(0) as clocks:
+    for _ in range(args.steps):
+      flush.zero_()
+      s0.record(stream)
+      step()
+      s1.record(stream)
+      torch.cuda.synchronize()
+      ms += s0.elapsed_time(s1)
+  # end to end: the MAP states of every sample copied to pinned host memory each step
+  e2e_ms = 0.0
+  for _ in range(args.steps):
+    flush.zero_()
+    s0.record(stream)
+    map_h.copy_(step()[var], non_blocking=True)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms += s0.elapsed_time(s1)
+  native.profile_read()
+  native.profile_enable(True)
+  for _ in range(args.steps):
+    step()
+  torch.cuda.synchronize()
+  native.profile_enable(False)
+  prof = native.profile_read()
+  plan = bp.context.plan
+  num_edges = 3 * ENUM_FACTORS
+  units = num_edges * ENUM_ITERS * ENUM_B * args.steps
+  n_es = plan.num_edge_states
+  gen_launches, gen_ms = prof["enum_generic"]
+  gen_launch_ms = gen_ms / max(gen_launches, 1)
+  # per launch: each (factor, instance) reads its 30 messages and 30 variable sums and writes 30
+  # messages; the config rows (3 int32 per config) and the potentials are read once
+  alg_bytes = ENUM_B * n_es * 4 * 3 + ENUM_FACTORS * 1000 * (3 * 4 + 4)
+  peak, peak_kind = peaks()
+  # shared-memory bound of the staged kernel: every (config, variable) pair read twice per
+  # (factor, instance), once for the config sums and once for the maxima, at 128 B per clock
+  # per SM (nominal) at the sampled SM clock
+  smem_bytes = 2 * ENUM_FACTORS * 1000 * 3 * ENUM_B * 4
+  csum = clocks.summary()
+  sm_mhz = csum.get("sm_mhz") or 2070
+  smem_peak_gbs = 128 * 152 * sm_mhz * 1e6 / 1e9
+  line = {
+      "metric": "edge-msg updates/s", "value": units / (ms / 1e3), "unit": "edge-msg updates/s",
+      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+      "data": "synthetic (seeded ternary 10-state tables N(0,1), Gumbel(0,1) noise on the GPU)",
+      "config": {"workload": "enum_ternary10_3000f_b128", "batch": ENUM_B,
+                 "num_iters": ENUM_ITERS, "temperature": 0.0, "damping": 0.5,
+                 "factors": ENUM_FACTORS, "configs_per_factor": 1000, "num_edges": num_edges,
+                 "edge_states": n_es, "l2": "flushed before every step (256 MB written)"},
+      "e2e": {"value": units / (e2e_ms / 1e3), "unit": "edge-msg updates/s",
+              "h2d_bytes_per_step": 0, "d2h_bytes_per_step": ENUM_B * ENUM_VARS * 4,
+              "noise": "Gumbel(0,1) generated on the GPU inside the run (pgbp_run_perturbed)"},
+      "gpu_launches": int(sum(v[0] for v in prof.values())),
+      "kernel_time_share": {k: v[1] / max(sum(x[1] for x in prof.values()), 1e-9)
+                            for k, v in prof.items() if v[0]},
+      "generic_kernel": _generic_site_choice(plan, ENUM_B),
+      "roofline": {"bound": "hbm", "kernel": "generic EnumFactor kernel",
+                   "achieved": alg_bytes / (gen_launch_ms / 1e3) / 1e9, "peak": peak,
+                   "unit": "GB/s", "frac": alg_bytes / (gen_launch_ms / 1e3) / 1e9 / peak,
+                   "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
+                   "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
+                   "launch_ms": gen_launch_ms,
+                   "note": "not HBM-bound: the config loops bound it (smem_estimate)"},
+      "smem_estimate": {"bytes_per_launch": smem_bytes,
+                        "peak_gbs_nominal": smem_peak_gbs,
+                        "frac": smem_bytes / (gen_launch_ms / 1e3) / 1e9 / smem_peak_gbs},
+      "clocks": csum,
+  }
+  if not args.no_cpu_baseline:
+    from oracle import oracle  # pylint: disable=g-import-not-at-top
+    w = oracle.Wiring(bp.context.flat_wiring())
+    lp = np.asarray(fg.fg_state.log_potentials, np.float32)
+    rng = np.random.default_rng(1)
+    nvs = fg.fg_state.num_var_states
+    n_cpu = 4
+    evs = rng.gumbel(size=(n_cpu, nvs)).astype(np.float32)
+    m0 = np.zeros((n_es,), np.float32)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.run_batch(w, lp, evs, m0, ENUM_ITERS, 0.5, 0.0, num_threads=threads)
+    dt = time.perf_counter() - t0
+    line["cpu_baseline"] = {"value": num_edges * ENUM_ITERS * n_cpu / dt,
+                            "unit": "edge-msg updates/s", "cores": min(threads, n_cpu),
+                            "kind": "port",
+                            "sample": f"{n_cpu} samples x {ENUM_ITERS} iterations, C oracle, "
+                                      f"{dt:.2f} s"}
+  print(json.dumps(line))
+  return 0
+
+
+def _generic_site_choice(plan, batch):
+  """The tuned generic-Enum kernel at this batch (T = 0): per-thread, staged or the rule."""
+  for e in plan.tuning():
+    if e["batch"] == batch and e["temperature0"] and e["sites"]:
+      return {0: "per-thread", 1: "staged", -1: "rule"}.get(e["sites"][-1], "rule")
+  return "rule"
+
+
 ADJ_N, ADJ_B, ADJ_ITERS, ADJ_CKPT, ADJ_FLIP = 64, 32, 100, 10, 0.1
 SDLP_TEMP, SDLP_ITERS = 1e-3, 200
 
@@ -1015,12 +1164,14 @@ def main():
   ap.add_argument("--exec-path", default="auto", choices=["auto", "multi", "small", "cluster"],
                   help="execution path of the ising workload (auto: timed choice)")
   ap.add_argument("--workload", default="rbm",
-                  choices=["rbm", "ising", "adjoint", "multigraph", "warmstart", "energy", "sdlp"],
+                  choices=["rbm", "ising", "adjoint", "multigraph", "warmstart", "energy", "sdlp",
+                           "enum"],
                   help="rbm: the headline RBM perturb-and-MAP batch (default); ising: the 50x50 "
                        "toroidal Ising configuration; adjoint: differentiable BP on 64x64 grids; "
                        "multigraph: the 256-graph uneven batch; warmstart: learned init vs "
                        "cold-start BP; energy: compute_energy of the RBM batch's decodings; "
-                       "sdlp: the smooth dual LP-MAP solver on the RBM batch")
+                       "sdlp: the smooth dual LP-MAP solver on the RBM batch; enum: "
+                       "perturb-and-MAP on 3,000 ternary 10-state EnumFactors")
   args = ap.parse_args()
   if args.warmup < 3:
     args.warmup = 3
@@ -1038,6 +1189,8 @@ def main():
     return run_energy(args)
   if args.workload == "sdlp":
     return run_sdlp(args)
+  if args.workload == "enum":
+    return run_enum(args)
 
   import torch  # pylint: disable=g-import-not-at-top
   from pgmax_gb300 import infer, native  # pylint: disable=g-import-not-at-top
