@@ -1273,7 +1273,9 @@ int pgbp_plan_tuning_set(const pgbp_plan* plan, const pgbp_tuning_entry* entries
 int pgbp_plan_signature(const pgbp_plan* plan, char* buf, size_t len) {
   if (!plan || !buf || len == 0) return fail(PGBP_ERR_INVALID_ARGUMENT, "null argument");
   const pgbp::Plan& p = plan->p;
-  std::string sig = "pgbp200|sm=" + std::to_string(p.sm_count) + "|es=" +
+  // "sites<n>": the layout of the decision table, so that tables of another layout are not found
+  std::string sig = "pgbp200|sites" + std::to_string(pgbp::num_tune_sites(p)) + "|sm=" +
+                    std::to_string(p.sm_count) + "|es=" +
                     std::to_string(p.num_edge_states) + "|vs=" + std::to_string(p.num_var_states) +
                     "|slots=" + std::to_string(p.num_slots) + "|vb=" +
                     std::to_string(p.varsum_binary.count) + "|vo=" +
