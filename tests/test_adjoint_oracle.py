@@ -82,3 +82,73 @@ def test_autograd_matches_central_differences(name, batched_lp):
           vals.append(float(_loss(g, *xs, iters, damping, temperature, labels_w)))
       fd = (vals[0] - vals[1]) / (2 * h)
       assert abs(fd - float(gx.reshape(-1)[idx])) <= 1e-6 * max(1.0, abs(fd)), (which, idx)
+
+
+# OR / AND / Pool factors (bp_torch.LogicalGraph): the forward against every reference fixture
+# of graphs with these factors, and autograd against central differences.
+LOGICAL = ["case_deconv_T1", "case_deconv_T0", "case_mixed_T1", "case_mixed_T0.3",
+           "case_mixed_T0.001", "case_mixed_T0", "case_mixed_iters0", "case_mixed_iters1"]
+
+
+@pytest.mark.parametrize("name", LOGICAL)
+def test_logical_forward_matches_reference_fixture(name):
+  d = _load(name)
+  g = bp_torch.LogicalGraph(d["wiring"])
+  f64 = lambda x: torch.as_tensor(np.asarray(x, dtype=np.float64))
+  with torch.no_grad():
+    out = g.run(f64(d["log_potentials"]), f64(d["evidence"]), f64(d["ftov_msgs_in"]),
+                int(d["num_iters"]), float(d["damping"]), float(d["temperature"]))
+  ref = d["ftov_msgs_out"]
+  fin = np.isfinite(ref)
+  np.testing.assert_array_equal(np.isfinite(out[0].numpy()), fin)
+  # float32 reference vs float64 restatement
+  np.testing.assert_allclose(out[0].numpy()[fin], ref[fin], atol=1e-5, rtol=0)
+
+
+def test_logical_graph_equals_enum_graph_on_enum_only_graphs():
+  d = _load("case_potts_K4")
+  f64 = lambda x: torch.as_tensor(np.asarray(x, dtype=np.float64))
+  args = (f64(d["log_potentials"]), f64(d["evidence"]), f64(d["ftov_msgs_in"]), 9, 0.5, 1.0)
+  with torch.no_grad():
+    a = bp_torch.EnumGraph(d["wiring"]).run(*args)
+    b = bp_torch.LogicalGraph(d["wiring"]).run(*args)
+  assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("name,temperature", [("case_mixed_T1", 1.0), ("case_mixed_T1", 0.7),
+                                              ("case_mixed_T1", 0.3), ("case_deconv_T1", 1.0)])
+def test_logical_autograd_matches_central_differences(name, temperature):
+  d = _load(name)
+  g = bp_torch.LogicalGraph(d["wiring"])
+  rng = np.random.default_rng(11)
+  B = 2
+  lp = np.asarray(d["log_potentials"], np.float64)
+  lp = np.stack([lp + 0.1 * rng.normal(size=lp.shape) for _ in range(B)])
+  ev = np.asarray(d["evidence"], np.float64)[None] + rng.normal(size=(B,) + d["evidence"].shape)
+  m = 0.3 * rng.normal(size=(B,) + d["ftov_msgs_in"].shape)
+  w = torch.as_tensor(rng.normal(size=(B,) + d["ftov_msgs_in"].shape))
+  iters, damping = 8, 0.5
+
+  def loss(*xs):
+    out = g.run(*xs, iters, damping, temperature)
+    return (torch.where(out > -1e30, out, torch.zeros_like(out)) * w).sum()
+
+  args = [torch.tensor(x, dtype=torch.float64, requires_grad=True) for x in (lp, ev, m)]
+  grads = torch.autograd.grad(loss(*args), args, allow_unused=True)
+  h = 1e-6
+  for which, (x, gx) in enumerate(zip(args, grads)):
+    flat = x.detach().reshape(-1)
+    gflat = gx.reshape(-1) if gx is not None else torch.zeros_like(flat)
+    assert torch.isfinite(gflat).all()
+    if flat.numel() == 0:  # the deconvolution graph has no potentials
+      continue
+    for idx in rng.choice(flat.numel(), size=6, replace=False):
+      vals = []
+      for sign in (1.0, -1.0):
+        xs = [a.detach().clone() for a in args]
+        xs[which].view(-1)[idx] += sign * h
+        with torch.no_grad():
+          vals.append(float(loss(*xs)))
+      fd = (vals[0] - vals[1]) / (2 * h)
+      assert abs(fd - float(gflat[idx])) <= 1e-5 * max(1.0, abs(fd)), (which, idx, fd,
+                                                                         float(gflat[idx]))
