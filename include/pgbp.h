@@ -234,8 +234,9 @@ int pgbp_run_checkpointed(const pgbp_plan* plan, void* stream, int64_t batch,
 /* Reverse mode of pgbp_run: the gradients that jax.grad gives through bp.run in the reference
  * (its learning example, examples/grid_mrf.ipynb cells 15-16, differentiates
  * pgmax/infer/bp.py:63-155 this way), computed by a hand-written adjoint instead of autodiff.
- * Covers graphs whose factors are all EnumFactors (dense pairwise and any other config table,
- * each with its own potentials), at temperature > 0 (else PGBP_ERR_UNSUPPORTED).
+ * Covers graphs of EnumFactors (dense pairwise and any other config table, each with its own
+ * potentials), OR and AND factors, at temperature > 0; Pool factors, shared tables or
+ * temperature 0 give PGBP_ERR_UNSUPPORTED.
  * checkpoints: those of pgbp_run_checkpointed with the same k = checkpoint_every (or, the same
  *   values, msgs_in followed by the msgs_out of pgbp_run called k iterations at a time). Each
  *   chunk is recomputed with the engine's arithmetic and walked backwards.

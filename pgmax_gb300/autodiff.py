@@ -11,8 +11,9 @@ respect to the log potentials). Here the same chain is differentiable in torch:
   the log potentials, the evidence and the initial messages.
 * `beliefs` is get_beliefs' flat scatter-add, whose backward is pgbp_beliefs_vjp (a gather).
 
-Graphs must consist of EnumFactors (any config tables) and the temperature must be > 0 (the
-adjoint's scope); anything else raises ValueError at backward time.
+Graphs must consist of EnumFactors (any config tables), OR and AND factors, and the temperature
+must be > 0 (the adjoint's scope); Pool factors or temperature 0 raise ValueError at backward
+time.
 """
 
 from typing import Optional, Tuple

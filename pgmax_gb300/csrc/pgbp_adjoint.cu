@@ -21,6 +21,13 @@
 //   gs_c = sum_{e in c} gf[e] p_e(c),  p_e(c) = exp((s_c - M_e) / T) / sum_{c' holds e} exp(...)
 //   gvtof[e] = sum_{c holds e} gs_c - gf[e],  glp_c += gs_c
 // (the pairwise formulas are this with c = (i, j)).
+// OR / AND factors (logical.py:645-779, normalize=True) are differentiated through their closed
+// form: parent differences, the factor sums FO = sum of the other-state messages and FX = sum of
+// logaddexp(rel, other), logaddexp / logminusexp of those, the temperature < 0.5 lower bounds
+// with the top two parent differences, and the single-parent rule. At logminusexp's eps cutoff
+// (which returns the constant -inf) and through a maximum the gradient follows the selected
+// branch; the derivative of logaddexp_t(a, b) is exp((a - l) / t), that of logminusexp_t(a, b)
+// is 1 / (1 - e) and -e / (1 - e) with e = exp((b - a) / t).
 //   g[e] (= dL/dm) = gdir[e] + gvsum[v(e)] - gvtof[e]
 // g is never stored: the next (earlier) step's factor kernel reads gdir, gvsum and gvtof of the
 // step after it and forms g for its own edges, so one backward step is two launches (factors,
@@ -440,6 +447,332 @@ __global__ void __launch_bounds__(256) generic_backward_kernel(GenArgs a, const 
   }
 }
 
+// ---- OR / AND factors (Plan::logical), a thread per (factor, instance)
+constexpr double kLowT = 0.5;  // TEMPERATURE_STABILITY_THRE, pgmax/factor/logical.py:33
+
+// update_utils.py:150-166, the engine's operations
+__device__ __forceinline__ float lae_t(float a, float b, float t) {
+  const float mx = maxn(a, b);
+  float mn;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(mn) : "f"(a), "f"(b));
+  return t * log1pf(expf(div_t(mn - mx, t))) + mx;
+}
+// update_utils.py:134-147 and 169-190 (both log1mexp branches evaluated, as jnp.where does)
+__device__ __forceinline__ float lme_t(float a, float b, float t, float eps) {
+  const float x = div_t(a - b, t);
+  const float u = logf(-expm1f(-x));
+  const float w = log1pf(-expf(-x));
+  const float v = t * ((x <= 0.693147182464599609375f) ? u : w) + a;
+  return (a >= b + eps) ? v : -INFINITY;
+}
+// Partial derivatives of lae_t (value l) and lme_t.
+__device__ __forceinline__ void d_lae(float a, float b, float l, float t, float& da, float& db) {
+  da = expf(div_t(a - l, t));
+  db = expf(div_t(b - l, t));
+}
+__device__ __forceinline__ void d_lme(float a, float b, float t, float eps, float& da, float& db) {
+  if (!(a >= b + eps)) {
+    da = 0.0f;
+    db = 0.0f;
+    return;
+  }
+  const float e = expf(div_t(b - a, t));
+  da = 1.0f / (1.0f - e);
+  db = -e / (1.0f - e);
+}
+
+struct LogArgs {
+  const int32_t* __restrict__ par_begin;
+  const int4* __restrict__ par;    // (first edge state, -, first variable state)
+  const int4* __restrict__ child;
+  int64_t count;
+  int rel;  // relevant state: 1 for OR, 0 for AND
+  int64_t n_es, nvs, B;
+  float d, omd, t;
+};
+
+// A binary edge's current messages and variable-to-factor messages (rel, other) in one instance.
+struct Bin {
+  float o[2];
+  float vr, vo;
+};
+
+__device__ __forceinline__ Bin load_bin(const int4 r, int rel, const float* __restrict__ m,
+                                        const float* __restrict__ vsum) {
+  Bin x;
+  x.o[0] = m[r.x];
+  x.o[1] = m[r.x + 1];
+  const float v0 = vsum[r.z] - x.o[0], v1 = vsum[r.z + 1] - x.o[1];
+  x.vr = rel ? v1 : v0;
+  x.vo = rel ? v0 : v1;
+  return x;
+}
+
+// The factor-level quantities of logical_unit (pgbp_kernels.cu), in its order of operations.
+struct LogFac {
+  int64_t p0, p1, arg, arg2;
+  float fs_oth, fs_x, max1, max2, c_rel, c_oth, ch_rel;
+  Bin c;
+  bool low, single;
+};
+
+__device__ __forceinline__ LogFac log_factor(const LogArgs& a, int64_t f, const float* m,
+                                             const float* vsum) {
+  LogFac q;
+  q.p0 = a.par_begin[f];
+  q.p1 = a.par_begin[f + 1];
+  q.low = (double)a.t < kLowT;
+  q.single = q.p1 - q.p0 == 1;
+  q.fs_oth = 0.0f;
+  q.fs_x = 0.0f;
+  q.max1 = -INFINITY;
+  for (int64_t i = q.p0; i < q.p1; ++i) {
+    const Bin x = load_bin(a.par[i], a.rel, m, vsum);
+    q.fs_oth += x.vo;
+    q.max1 = maxn(q.max1, x.vr - x.vo);
+    q.fs_x += lae_t(x.vr, x.vo, a.t);
+  }
+  q.arg = q.p1 - 1;
+  q.max2 = -INFINITY;
+  q.arg2 = -1;
+  {
+    int64_t last = -1;
+    for (int64_t i = q.p0; i < q.p1; ++i) {
+      const Bin x = load_bin(a.par[i], a.rel, m, vsum);
+      if (x.vr - x.vo == q.max1) last = i;
+    }
+    if (last >= 0) q.arg = last;
+    for (int64_t i = q.p0; i < q.p1; ++i) {
+      const Bin x = load_bin(a.par[i], a.rel, m, vsum);
+      const float w = i == q.arg ? -INFINITY : x.vr - x.vo;
+      q.max2 = maxn(q.max2, w);
+    }
+    for (int64_t i = q.p0; i < q.p1; ++i) {  // the last parent attaining max2
+      const Bin x = load_bin(a.par[i], a.rel, m, vsum);
+      if (i != q.arg && x.vr - x.vo == q.max2) q.arg2 = i;
+    }
+  }
+  q.c = load_bin(a.child[f], a.rel, m, vsum);
+  q.c_rel = q.c.vr;
+  q.c_oth = q.c.vo;
+  q.ch_rel = lme_t(q.fs_x, q.fs_oth, a.t, 1e-4f);
+  if (q.low) q.ch_rel = maxn(q.ch_rel, lae_t(q.fs_oth + q.max1, q.fs_oth + q.max2, a.t));
+  return q;
+}
+
+// Parent i's outputs (p_rel, p_oth) of logical_unit at T > 0.
+__device__ __forceinline__ void log_parent(const LogArgs& a, const LogFac& q, int64_t i,
+                                           const Bin& x, float& p_rel, float& p_oth) {
+  if (q.single) {
+    p_rel = q.c_rel;
+    p_oth = q.c_oth;
+    return;
+  }
+  const float lse = lae_t(x.vr, x.vo, a.t);
+  const float fs_lse_wo = q.fs_x - lse;
+  const float fs_oth_wo = q.fs_oth - x.vo;
+  p_rel = q.c_rel + fs_lse_wo;
+  const float opt1 = q.c_oth + fs_oth_wo;
+  const float opt2 = q.c_rel + fs_lse_wo;
+  const float opt3 = q.c_rel + fs_oth_wo;
+  p_oth = lme_t(lae_t(opt1, opt2, a.t), opt3, a.t, 1e-4f);
+  if (q.low) {
+    const float fsp = fs_oth_wo + (i == q.arg ? q.max2 : q.max1);
+    p_oth = maxn(p_oth, lae_t(opt1, q.c_rel + fsp, a.t));
+  }
+}
+
+__global__ void __launch_bounds__(256) logical_forward_kernel(LogArgs a, const float* m,
+                                                              const float* vsum, float* out) {
+  pdl_begin();
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < a.count * a.B;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = it / a.count, f = it % a.count;
+    const float* mb = m + b * a.n_es;
+    const float* vb = vsum + b * a.nvs;
+    float* ob = out + b * a.n_es;
+    const LogFac q = log_factor(a, f, mb, vb);
+    for (int64_t i = q.p0; i < q.p1; ++i) {
+      const int4 r = a.par[i];
+      const Bin x = load_bin(r, a.rel, mb, vb);
+      float p_rel, p_oth;
+      log_parent(a, q, i, x, p_rel, p_oth);
+      float fo[2];
+      fo[a.rel] = p_rel - p_oth;
+      fo[1 - a.rel] = 0.0f;
+      edge_forward<2>(x.o, fo, 2, a.d, a.omd, ob + r.x);
+    }
+    float fo[2];
+    fo[a.rel] = q.ch_rel - q.fs_oth;
+    fo[1 - a.rel] = 0.0f;
+    edge_forward<2>(q.c.o, fo, 2, a.d, a.omd, ob + a.child[f].x);
+  }
+}
+
+// dL/d(factor outputs) of a binary edge from the gradient of its next messages: g = gexp, or
+// gdir + gvsum[v] - gvtof of the step after; writes the damping path into gdir.
+__device__ __forceinline__ void edge_grad(const LogArgs& a, const GradIn& gin, int64_t b,
+                                          const int4 r, const Bin& x, const float* fo,
+                                          float* __restrict__ gdir, float* gf) {
+  const int64_t e = b * a.n_es + r.x;
+  float g[2];
+  for (int s = 0; s < 2; ++s)
+    g[s] = gin.gexp ? gin.gexp[e + s]
+                    : (gin.gdir[e + s] + gin.gvsum[b * a.nvs + r.z + s]) - gin.gvtof[e + s];
+  edge_backward<2>(x.o, fo, 2, a.d, a.omd, g, gf, gdir + e);
+}
+
+// The part of parent i's backward that involves its own outputs: from dPR = g, dPO = -g to the
+// factor-level and child gradients, and dA = dL/d(fs_x - lse_i), dO = dL/d(fs_oth - vo_i).
+struct ParentGrad {
+  float dA, dO, dcr, dco, dmax1, dmax2;
+};
+
+__device__ __forceinline__ ParentGrad parent_grad(const LogArgs& a, const LogFac& q, int64_t i,
+                                                  const Bin& x, float g) {
+  ParentGrad r{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  if (q.single) {
+    r.dcr = g;
+    r.dco = -g;
+    return r;
+  }
+  const float t = a.t;
+  float dPO = -g;
+  const float lse = lae_t(x.vr, x.vo, t);
+  const float A = q.fs_x - lse, O = q.fs_oth - x.vo;
+  const float o1 = q.c_oth + O, o2 = q.c_rel + A, o3 = q.c_rel + O;
+  const float qv = lae_t(o1, o2, t);
+  const float po = lme_t(qv, o3, t, 1e-4f);
+  if (q.low) {
+    const float M = i == q.arg ? q.max2 : q.max1;
+    const float lbx = q.c_rel + O + M;
+    const float lb = lae_t(o1, lbx, t);
+    if (lb > po) {
+      float s1, s2;
+      d_lae(o1, lbx, lb, t, s1, s2);
+      r.dco += dPO * s1;
+      r.dO += dPO * s1;
+      r.dcr += dPO * s2;
+      r.dO += dPO * s2;
+      if (i == q.arg) r.dmax2 += dPO * s2;
+      else r.dmax1 += dPO * s2;
+      dPO = 0.0f;
+    }
+  }
+  if (dPO != 0.0f) {
+    float pq, p3, s1, s2;
+    d_lme(qv, o3, t, 1e-4f, pq, p3);
+    const float dq = dPO * pq, do3 = dPO * p3;
+    d_lae(o1, o2, qv, t, s1, s2);
+    const float do1 = dq * s1, do2 = dq * s2;
+    r.dco += do1;
+    r.dO += do1;
+    r.dcr += do2;
+    r.dA += do2;
+    r.dcr += do3;
+    r.dO += do3;
+  }
+  r.dcr += g;  // p_rel = c_rel + A
+  r.dA += g;
+  return r;
+}
+
+__global__ void __launch_bounds__(256) logical_backward_kernel(LogArgs a, const float* m,
+                                                               const float* vsum, GradIn gin,
+                                                               float* __restrict__ gdir,
+                                                               float* __restrict__ gvtof) {
+  pdl_begin();
+  const int rel = a.rel, oth = 1 - a.rel;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < a.count * a.B;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = it / a.count, f = it % a.count;
+    const float* mb = m + b * a.n_es;
+    const float* vb = vsum + b * a.nvs;
+    const LogFac q = log_factor(a, f, mb, vb);
+    const float t = a.t;
+    // the child's output rel = ch_rel - fs_oth
+    float gc;
+    {
+      float fo[2], gf[2];
+      fo[rel] = q.ch_rel - q.fs_oth;
+      fo[oth] = 0.0f;
+      edge_grad(a, gin, b, a.child[f], q.c, fo, gdir, gf);
+      gc = gf[rel];
+    }
+    float dFX = 0.0f, dFO = -gc, dmax1 = 0.0f, dmax2 = 0.0f, dcr = 0.0f, dco = 0.0f;
+    {
+      float dCR = gc;
+      const float crl = lme_t(q.fs_x, q.fs_oth, t, 1e-4f);
+      if (q.low) {
+        const float xa = q.fs_oth + q.max1, xb = q.fs_oth + q.max2;
+        const float lbc = lae_t(xa, xb, t);
+        if (lbc > crl) {
+          float sa, sb;
+          d_lae(xa, xb, lbc, t, sa, sb);
+          dFO += dCR * (sa + sb);
+          dmax1 += dCR * sa;
+          dmax2 += dCR * sb;
+          dCR = 0.0f;
+        }
+      }
+      if (dCR != 0.0f) {
+        float pa, pb;
+        d_lme(q.fs_x, q.fs_oth, t, 1e-4f, pa, pb);
+        dFX += dCR * pa;
+        dFO += dCR * pb;
+      }
+    }
+    // parents, first pass: the factor-level sums of their gradients
+    for (int64_t i = q.p0; i < q.p1; ++i) {
+      const int4 r = a.par[i];
+      const Bin x = load_bin(r, rel, mb, vb);
+      float p_rel, p_oth, fo[2], gf[2];
+      log_parent(a, q, i, x, p_rel, p_oth);
+      fo[rel] = p_rel - p_oth;
+      fo[oth] = 0.0f;
+      edge_grad(a, gin, b, r, x, fo, gdir, gf);
+      const ParentGrad pg = parent_grad(a, q, i, x, gf[rel]);
+      dcr += pg.dcr;
+      dco += pg.dco;
+      dmax1 += pg.dmax1;
+      dmax2 += pg.dmax2;
+      dFX += pg.dA;
+      dFO += pg.dO;
+    }
+    // second pass: each parent's variable-to-factor gradients
+    for (int64_t i = q.p0; i < q.p1; ++i) {
+      const int4 r = a.par[i];
+      const Bin x = load_bin(r, rel, mb, vb);
+      float p_rel, p_oth, fo[2], gf[2];
+      log_parent(a, q, i, x, p_rel, p_oth);
+      fo[rel] = p_rel - p_oth;
+      fo[oth] = 0.0f;
+      edge_grad(a, gin, b, r, x, fo, gdir, gf);
+      const ParentGrad pg = parent_grad(a, q, i, x, gf[rel]);
+      const float dl = dFX - pg.dA;
+      float dvo = dFO - pg.dO, dvr = 0.0f;
+      float sr, so;
+      d_lae(x.vr, x.vo, lae_t(x.vr, x.vo, t), t, sr, so);
+      dvr += dl * sr;
+      dvo += dl * so;
+      if (i == q.arg) {
+        dvr += dmax1;
+        dvo -= dmax1;
+      }
+      if (i == q.arg2) {
+        dvr += dmax2;
+        dvo -= dmax2;
+      }
+      const int64_t e = b * a.n_es + r.x;
+      gvtof[e + rel] = dvr;
+      gvtof[e + oth] = dvo;
+    }
+    const int64_t ec = b * a.n_es + a.child[f].x;
+    gvtof[ec + rel] = dcr;
+    gvtof[ec + oth] = dco;
+  }
+}
+
 // gvsum[v] = sum_{e in v} gvtof[e]; gev[v] += gvsum[v].
 __global__ void __launch_bounds__(256) gvsum_kernel(const int32_t* __restrict__ vs_off,
                                                     const int32_t* __restrict__ vs_edges,
@@ -598,6 +931,12 @@ void launch_generic_backward(const Plan& p, const GenArgs& a, cudaStream_t s, co
   }
 }
 
+LogArgs log_args(const Plan& p, int w, int64_t B, float d, float omd, float t) {
+  const LogicalSet& g = p.logical[w];
+  return LogArgs{g.par_begin, g.par, g.child, g.count, g.off > 0 ? 1 : 0, p.num_edge_states,
+                 p.num_var_states, B, d, omd, t};
+}
+
 template <int M>
 void launch_forward_m(const PairArgs& a, int sm, cudaStream_t s, const float* m, const float* vsum,
                       float* out) {
@@ -645,6 +984,12 @@ void recompute(const Plan& p, cudaStream_t s, int64_t B, const float* lp, int64_
       }
     }
     launch_generic_forward(p, gen_args(p, B, lp, lps, d, omd, t), s, mj, vj, next);
+    for (int w = 0; w < 2; ++w) {
+      if (p.logical[w].count == 0) continue;
+      const LogArgs la = log_args(p, w, B, d, omd, t);
+      launch_pdl(s, grid_for(la.count * B, p.sm_count), dim3(256), logical_forward_kernel, la, mj,
+                 (const float*)vj, next);
+    }
   }
 }
 
@@ -673,6 +1018,12 @@ void backward_step(const Plan& p, cudaStream_t s, int64_t B, const float* lp, in
   }
   launch_generic_backward(p, gen_args(p, B, lp, lps, d, omd, t), s, m, vsum, gin, out.gdir,
                           out.gvtof, glp);
+  for (int w = 0; w < 2; ++w) {
+    if (p.logical[w].count == 0) continue;
+    const LogArgs la = log_args(p, w, B, d, omd, t);
+    launch_pdl(s, grid_for(la.count * B, p.sm_count), dim3(256), logical_backward_kernel, la, m,
+               vsum, gin, out.gdir, out.gvtof);
+  }
   launch_pdl(s, grid_for(p.num_var_states * B, p.sm_count), dim3(256), gvsum_kernel, p.vs_off,
              p.vs_edges, p.num_var_states, out.gvtof, p.num_edge_states, out.gvsum, gev, B);
 }
@@ -698,8 +1049,8 @@ cudaError_t aux_stream(int device, cudaStream_t* out) {
 const char* adjoint_unsupported(const Plan& p) {
   if (p.shared_potentials)
     return "the adjoint needs one potential table per factor; the plan shares tables";
-  if (p.logical[0].count > 0 || p.logical[1].count > 0 || p.pool.count > 0)
-    return "the adjoint covers EnumFactors only; the graph has OR/AND/Pool factors";
+  if (p.pool.count > 0)
+    return "the adjoint covers EnumFactors, OR and AND factors; the graph has Pool factors";
   return "";
 }
 

@@ -57,12 +57,13 @@ def _inputs(d, B, batched_lp, batched_ev, seed=0):
 
 def _reference_grads(d, lp, ev, m, w, iters, damping, temperature):
   torch = _torch()
-  g = bp_torch.EnumGraph(d["wiring"])
+  g = bp_torch.LogicalGraph(d["wiring"])  # equal to EnumGraph on Enum-only graphs
   args = [torch.tensor(np.asarray(x, np.float64), requires_grad=True) for x in (lp, ev, m)]
   out = g.run(*args, iters, damping, temperature)
   loss = (out * torch.as_tensor(w, dtype=torch.float64)).sum()
-  grads = torch.autograd.grad(loss, args)
-  return out.detach().numpy(), [x.numpy() for x in grads]
+  grads = torch.autograd.grad(loss, args, allow_unused=True)  # a graph may have no potentials
+  return out.detach().numpy(), [(torch.zeros_like(a) if x is None else x).detach().numpy()
+                                for a, x in zip(args, grads)]
 
 
 @pytest.mark.parametrize("name", ENUM_T_POS)
@@ -153,10 +154,10 @@ def test_unsupported_graphs_and_temperature_raise():
   _, _, ck = plan.run_checkpointed(lp, ev, m, 5, 0.5, 0.0, 2)
   with pytest.raises(ValueError, match="temperature > 0"):
     plan.run_vjp(lp, ev, ck, 5, torch.as_tensor(w).cuda(), 0.5, 0.0, 2)
-  dd = _load("case_deconv_T1")
+  dd = _load("case_mixed_T1")
   p2 = _plan(dd)
   ck2 = torch.zeros((1, 1, p2.num_edge_states), device="cuda")
-  with pytest.raises(ValueError, match="EnumFactors only"):
+  with pytest.raises(ValueError, match="Pool factors"):
     p2.run_vjp(dd["log_potentials"], dd["evidence"], ck2, 1,
                torch.zeros((1, p2.num_edge_states), device="cuda"), 0.5, 1.0, 1)
 
@@ -216,6 +217,58 @@ def test_vjp_generic_enum_factors_match_float64_autograd(name, temperature):
   torch.cuda.synchronize()
   ref_out, (r_lp, r_ev, r_m) = _reference_grads(d, lp, ev, m, w, iters, 0.5, temperature)
   np.testing.assert_allclose(out.cpu().numpy(), ref_out, atol=5e-5, rtol=0)
+  _close(g_lp.cpu().numpy(), r_lp, "g_log_potentials")
+  _close(g_ev.cpu().numpy(), r_ev, "g_evidence")
+  _close(g_m.cpu().numpy(), r_m, "g_msgs_in")
+
+
+def _logical_graph(seed):
+  """Binary variables with pairwise and ternary EnumFactors, OR and AND factors of 1 to 5
+  parents (the closed-form logical updates and their single-parent rule) as a fixture dict."""
+  from pgmax_gb300 import factor, fgraph, fgroup, infer, vgroup  # pylint: disable=g-import-not-at-top
+  rng = np.random.RandomState(seed)
+  n = 30
+  var = vgroup.NDVarArray(num_states=2, shape=(n,))
+  fg = fgraph.FactorGraph(variable_groups=[var])
+  fg.add_factors(fgroup.PairwiseFactorGroup(
+      variables_for_factors=[[var[i], var[i + 1]] for i in range(0, 10)],
+      log_potential_matrix=rng.normal(size=(10, 2, 2))))
+  fg.add_factors(factor.EnumFactor(variables=[var[0], var[5], var[9]],
+                                   factor_configs=np.array([[0, 0, 0], [1, 0, 1], [1, 1, 0],
+                                                            [0, 1, 1], [1, 1, 1]]),
+                                   log_potentials=rng.normal(size=(5,))))
+  fg.add_factors(fgroup.ORFactorGroup([[var[11], var[12], var[13]], [var[14], var[15]],
+                                       [var[16], var[17], var[18], var[19], var[20]],
+                                       [var[3], var[21]]]))
+  fg.add_factors(fgroup.ANDFactorGroup([[var[22], var[23], var[24]], [var[12], var[25]],
+                                        [var[26], var[27]]]))
+  fg.add_factors(factor.ANDFactor(variables=[var[7], var[28], var[29]]))
+  w = infer.InfererContext(fg.bp_state).flat_wiring()
+  w["num_variables"] = n
+  nvs = int(np.asarray(w["var_states_for_edge_states"]).max()) + 1
+  nes = np.asarray(w["var_states_for_edge_states"]).shape[0]
+  return {"wiring": w, "log_potentials": np.asarray(fg.bp_state.log_potentials.value, np.float32),
+          "evidence": rng.normal(size=(nvs,)).astype(np.float32),
+          "ftov_msgs_in": np.zeros((nes,), np.float32)}
+
+
+# OR / AND factors (the logical adjoint kernels), above and below the 0.5 temperature threshold
+# where the updates add their lower bounds. The deconvolution fixture is not a case here: on
+# these perturbed inputs its float32 forward already departs from the float64 one by up to
+# 2.5e-4 (T = 1) and 1.1e-3 (T = 0.3), the logminusexp cancellation of its 75-parent ORs.
+@pytest.mark.parametrize("temperature", [1.0, 0.3])
+def test_vjp_or_and_factors_match_float64_autograd(temperature):
+  torch = _torch()
+  d = _logical_graph(seed=2)
+  plan = _plan(d)
+  B, iters, k = 3, 10, 4
+  lp, ev, m, w = _inputs(d, B, True, True, seed=5)
+  out, _, ck = plan.run_checkpointed(lp, ev, m, iters, 0.5, temperature, k)
+  g_lp, g_ev, g_m = plan.run_vjp(lp, ev, ck, iters, torch.as_tensor(w).cuda(), 0.5, temperature,
+                                 k, want_msgs_in=True)
+  torch.cuda.synchronize()
+  ref_out, (r_lp, r_ev, r_m) = _reference_grads(d, lp, ev, m, w, iters, 0.5, temperature)
+  np.testing.assert_allclose(out.cpu().numpy(), ref_out, atol=1e-4, rtol=0)
   _close(g_lp.cpu().numpy(), r_lp, "g_log_potentials")
   _close(g_ev.cpu().numpy(), r_ev, "g_evidence")
   _close(g_m.cpu().numpy(), r_m, "g_msgs_in")
