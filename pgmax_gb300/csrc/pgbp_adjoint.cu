@@ -1,5 +1,5 @@
 // Reverse mode of the damped BP iterations of run_with_diffs (pgmax/infer/bp.py:63-155) for graphs
-// whose factors are all EnumFactors, at temperature > 0: the hand-written adjoint
+// of EnumFactors, OR and AND factors, at temperature > 0: the hand-written adjoint
 // behind differentiable BP (gradients of a loss on the final messages with respect to the log
 // potentials, the evidence and the initial messages).
 //
