@@ -42,3 +42,20 @@ def test_null_arguments_are_rejected_with_a_status():
   assert lib.pgbp_run(None, None, 1, None, 0, None, 0, None, 0, None, None, 1, 0.5, 0.0, None, 0) == 1
   assert lib.pgbp_workspace_size(None, 1, 1) == 0
   assert lib.pgbp_plan_destroy(None) == 0
+
+
+def test_debug_settings_validate_their_values():
+  """pgbp_debug_set needs no GPU: each knob accepts its documented range, rejects the rest with
+  status 1 (invalid argument), and 0 restores the default."""
+  lib = native.load()
+  for knob, good, bad in ((native.DEBUG_SKIP_TABLE_COPY, (0, 1), (2, -1)),
+                          (native.DEBUG_LEGACY_MMA, (0, 1), (2,)),
+                          (native.DEBUG_ENUM_KERNEL, (0, 1, 2), (3, -1)),
+                          (native.DEBUG_WAIT_LIMIT_NS, (0, 1000000), (-1, 10000000001))):
+    for v in good:
+      assert lib.pgbp_debug_set(knob, v) == 0, (knob, v)
+    for v in bad:
+      assert lib.pgbp_debug_set(knob, v) == 1, (knob, v)
+    assert lib.pgbp_debug_set(knob, 0) == 0
+  assert lib.pgbp_debug_set(99, 0) == 1
+  assert b"unknown debug knob" in lib.pgbp_last_error()
