@@ -152,3 +152,60 @@ def test_logical_autograd_matches_central_differences(name, temperature):
       fd = (vals[0] - vals[1]) / (2 * h)
       assert abs(fd - float(gflat[idx])) <= 1e-5 * max(1.0, abs(fd)), (which, idx, fd,
                                                                          float(gflat[idx]))
+
+
+def _closed_form_vjp_check(name, which, temperature):
+  """Per factor closed-form VJP (oracle/closed_form_vjp.py) against autograd of one update."""
+  from oracle import closed_form_vjp as cf  # pylint: disable=g-import-not-at-top
+  d = _load(name)
+  g = bp_torch.LogicalGraph(d["wiring"])
+  a0, b0 = g.msgs_ranges[1 + which]
+  n = b0 - a0
+  rng = np.random.default_rng(3 + which)
+  B = 2
+  vt = torch.tensor(rng.normal(size=(B, n)) * 2.0, dtype=torch.float64, requires_grad=True)
+  up = torch.tensor(rng.normal(size=(B, n)), dtype=torch.float64)
+  if which < 2:
+    out = g.logical_update(vt, which, temperature)
+  else:
+    out = g.pool_update(vt, temperature)
+  (want,) = torch.autograd.grad((out * up).sum(), vt)
+  got = np.zeros((B, n))
+  v, u = vt.detach().numpy(), up.numpy()
+  if which < 2:
+    pfi, pmi, ch, off, F = g.logical[which]
+    pfi, pmi, ch = pfi.numpy(), pmi.numpy(), ch.numpy()
+    for b in range(B):
+      for f in range(F):
+        idx = np.nonzero(pfi == f)[0]
+        dr, do, dcr, dco = cf.logical_factor_vjp(
+            [v[b, pmi[i] + off] for i in idx], [v[b, pmi[i]] for i in idx], v[b, ch[f] + off],
+            v[b, ch[f]], [u[b, pmi[i] + off] for i in idx], u[b, ch[f] + off], temperature)
+        for k, i in enumerate(idx):
+          got[b, pmi[i] + off] += dr[k]
+          got[b, pmi[i]] += do[k]
+        got[b, ch[f] + off] += dcr
+        got[b, ch[f]] += dco
+  else:
+    cfi, cmi, ind, F = g.pool
+    cfi, cmi, ind = cfi.numpy(), cmi.numpy(), ind.numpy()
+    for b in range(B):
+      for f in range(F):
+        idx = np.nonzero(cfi == f)[0]
+        dr, dz, dir_, diz = cf.pool_factor_vjp(
+            [v[b, cmi[i] + 1] for i in idx], [v[b, cmi[i]] for i in idx], v[b, ind[f] + 1],
+            v[b, ind[f]], [u[b, cmi[i] + 1] for i in idx], u[b, ind[f] + 1], temperature)
+        for k, i in enumerate(idx):
+          got[b, cmi[i] + 1] += dr[k]
+          got[b, cmi[i]] += dz[k]
+        got[b, ind[f] + 1] += dir_
+        got[b, ind[f]] += diz
+  np.testing.assert_allclose(got, want.numpy(), atol=1e-9, rtol=1e-9)
+
+
+@pytest.mark.parametrize("temperature", [1.0, 0.7, 0.3, 0.2])
+@pytest.mark.parametrize("name,which", [("case_mixed_T1", 0), ("case_mixed_T1", 1),
+                                        ("case_mixed_T1", 2), ("case_deconv_T1", 0),
+                                        ("case_deconv_T1", 1)])
+def test_closed_form_vjps_match_autograd(name, which, temperature):
+  _closed_form_vjp_check(name, which, temperature)
